@@ -1,0 +1,332 @@
+"""Benchmark: TDGL node-steps/s on the large single-domain workload.
+
+Workload (the metric's large single-domain configuration): Nx = Ny = 2049
+(Lx = Ly = 1024, dx = dy = 0.5), kappa = inf (A fixed in the Landau gauge
+Ax = -H*y, Ay = 0, H = 0.05), material tiling with circular holes of radius 4
+at seeded uniform positions covering >= 5% of the cells, random order parameter
+(seeded), TDGL dt = 0.1.  A step is one TDGL time step (one backward-Euler
+Jacobi solve) of the whole domain.  Synthetic, seeded inputs.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--dtype fp32|fp64] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Under torchrun each rank runs an independent
+replica on its own GPU (the single domain is not decomposed across GPUs).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SIDE = 2049
+DX = 0.5
+H_FIELD = 0.05
+DT = 0.1
+HOLE_R = 4.0
+HOLE_FRAC = 0.05
+METRIC = "TDGL node-steps/s (2049x2049, kappa=inf, 5% holes, dt=0.1)"
+
+
+def holes_mask(n_side, dx, radius, frac, seed):
+    """Cells (Nxc x Nyc, [i, j]) outside circular holes at uniform positions,
+    holes added until at least `frac` of the cells are removed."""
+    nc = n_side - 1
+    L = dx * (n_side - 1)
+    mt = np.ones((nc, nc), dtype=bool)
+    rng = np.random.default_rng(seed)
+    xc = (np.arange(nc) + 0.5) * dx
+    r_cells = int(np.ceil(radius / dx)) + 1
+    removed = 0
+    target = frac * nc * nc
+    while removed < target:
+        cx, cy = rng.random(2) * L
+        i0, j0 = int(cx / dx), int(cy / dx)
+        i_lo, i_hi = max(0, i0 - r_cells), min(nc, i0 + r_cells + 1)
+        j_lo, j_hi = max(0, j0 - r_cells), min(nc, j0 + r_cells + 1)
+        sub = (xc[i_lo:i_hi, None] - cx) ** 2 + (xc[None, j_lo:j_hi] - cy) ** 2 < radius * radius
+        before = mt[i_lo:i_hi, j_lo:j_hi].sum()
+        mt[i_lo:i_hi, j_lo:j_hi] &= ~sub
+        removed += before - mt[i_lo:i_hi, j_lo:j_hi].sum()
+    return mt
+
+
+def make_solver(n_side=N_SIDE, dtype=np.float32, seed=0, device=0):
+    from svirl_gb300 import GLSolver
+    mt = holes_mask(n_side, DX, HOLE_R, HOLE_FRAC, seed)
+    gl = GLSolver(Nx=n_side, Ny=n_side, dx=DX, dy=DX, order_parameter="random", random_seed=seed,
+                  gl_parameter=np.inf, homogeneous_external_field=H_FIELD, material_tiling=mt,
+                  dtype=dtype, device_id=device)
+    ya = gl.mesh.xy_a_grid[1]
+    gl.vars.vector_potential = ((-H_FIELD * ya).astype(dtype), np.zeros((n_side, n_side - 1), dtype=dtype))
+    return gl
+
+
+def make_oracle(n_side, seed=0):
+    """The same workload for the CPU oracle (FP64), on an n_side x n_side domain."""
+    from oracle import gl_oracle as O
+    from oracle import kernels_np as K
+    mt = holes_mask(n_side, DX, HOLE_R, HOLE_FRAC, seed)
+    g = K.Grid(n_side, n_side, DX, DX)
+    psi = O.random_order_parameter(g.N, 1.0, seed)
+    nm = O.node_mask(g, O.flatten_ij(mt)).reshape(-1)
+    ya = np.linspace(0.0, DX * (n_side - 1), n_side)
+    a = np.repeat((-H_FIELD * ya)[:, None], n_side - 1, axis=1).reshape(-1)  # a[j, i] = -H y_j
+    ab = np.concatenate([a, np.zeros(g.Nb)])
+    del nm
+    return O.GLOracle(n_side, n_side, DX, DX, psi, ab, mt=O.flatten_ij(mt), kappa=np.inf, H=H_FIELD, rand_t=seed)
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.tmp.flush()
+        self.tmp.seek(0)
+        rows = [r.strip().split(",") for r in self.tmp.read().strip().splitlines() if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for k, name in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# measurement helpers
+# ---------------------------------------------------------------------------
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(dtype_name):
+    """DRAM bytes per psi-sweep launch from the committed ncu summary (or None)."""
+    p = os.path.join(ROOT, "profiles", "psi_sweep_%s_2049.md" % dtype_name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(budget_s=20.0, n_side=257):
+    """The oracle (NumPy FP64, one thread) on a bounded sample of the workload."""
+    orc = make_oracle(n_side, seed=0)
+    t0 = time.perf_counter()
+    steps = 0
+    while time.perf_counter() - t0 < budget_s:
+        orc.td(dt=DT, Nt=1)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": n_side * n_side * steps / dt, "unit": "node-steps/s", "cores": 1, "kind": "port",
+            "sample": "oracle (NumPy FP64, 1 thread) on a %dx%d domain of the same workload, %d TD steps in %.1f s"
+                      % (n_side, n_side, steps, dt)}
+
+
+def _ref_worker(args):
+    n_side, seed, nsteps = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    orc = make_oracle(n_side, seed=seed)
+    t0 = time.perf_counter()
+    orc.td(dt=DT, Nt=nsteps)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    """The reference's computation on the host: the CPU oracle (the reference has
+    no CPU path of its own), on bounded samples of the workload, on all cores."""
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = len(os.sched_getaffinity(0))
+    # size the per-step sample so that the whole run stays within a few minutes
+    total = args.steps + args.warmup
+    n_side = 129 if total > 200 else 257
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_ref_worker, [(n_side, 100 + w, 1) for w in range(cores)])  # warm the workers
+        for _ in range(args.warmup):
+            pool.map(_ref_worker, [(n_side, 200 + w, 1) for w in range(cores)])
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            pool.map(_ref_worker, [(n_side, 300 + w, 1) for w in range(cores)])
+        wall = time.perf_counter() - t0
+    value = cores * n_side * n_side * args.steps / wall
+    line = {"metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": "tdgl_2049_kinf_holes5", "sample_domain": "%dx%d" % (n_side, n_side)},
+            "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": cores, "kind": "port",
+                             "sample": "%d independent %dx%d domains of the workload per step (one TD step each), "
+                                       "NumPy FP64 oracle, one process per core" % (cores, n_side, n_side)},
+            "e2e": {"value": value, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--dtype", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=N_SIDE)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    dtype = np.float32 if args.dtype == "fp32" else np.float64
+    gl = make_solver(args.size, dtype=dtype, seed=rank, device=local)
+    h = gl._h
+    N = args.size * args.size
+    h.td(DT, args.warmup, 0)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    st, ms = h.td_timed(DT, args.steps, 0)
+    clk = clocks.stop()
+    barrier()
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    sweeps = int(st.total_sweeps_psi)
+    value = world * N * args.steps / (ms * 1e-3)
+
+    # roofline of the dominant kernel (the psi Jacobi sweep), timed alone
+    sweep_ms = h.time_sweeps(0, 20)
+    bytes_per_node = (32 if dtype == np.float32 else 64) + 1   # psi^(k), rhs, 2 links, write; +1 B mask
+    alg_bytes = N * bytes_per_node
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
+
+    # end to end through the C ABI with pinned host buffers: H2D psi, one TD step, D2H psi
+    import torch
+    ctype = np.complex64 if dtype == np.float32 else np.complex128
+    pin_in = torch.empty(2 * N, dtype=torch.float32 if dtype == np.float32 else torch.float64, pin_memory=True)
+    pin_out = torch.empty_like(pin_in).pin_memory()
+    psi_in = pin_in.numpy().view(ctype)
+    psi_out = pin_out.numpy().view(ctype)
+    psi_in[:] = h.get_psi()
+    e2e_steps = max(10, min(args.steps // 10, 200))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h.set_psi(psi_in)
+        h.td(DT, 1, 0)
+        out = h.lib.glgpu_get_order_parameter(h.h, psi_out.ctypes.data_as(__import__("ctypes").c_void_p))
+        assert out == 0
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    e2e_value = world * N * e2e_steps / e2e_s
+
+    if rank == 0:
+        cpu = None if args.no_cpu_baseline else cpu_baseline()
+        launches = sweeps + 3 * args.steps + 2
+        line = {
+            "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if dtype == np.float32 else "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "tdgl_2049_kinf_holes5", "Nx": args.size, "Ny": args.size, "dx": DX,
+                       "kappa": "inf", "H": H_FIELD, "dt": DT, "hole_radius": HOLE_R, "hole_fraction": HOLE_FRAC,
+                       "parallelism": "replica per GPU" if world > 1 else "single GPU",
+                       "l2": "working set %.0f MB > 129 MB L2 (no flush between steps); sweep timing flushes L2"
+                             % (N * (3 * (8 if dtype == np.float32 else 16) + (8 if dtype == np.float32 else 16)) / 1e6),
+                       "mean_sweeps_per_step": sweeps / args.steps},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": ncu_traffic(args.dtype),
+                         "kernel": "k_psi_sweep", "bytes_per_launch": alg_bytes, "launch_ms": sweep_ms,
+                         "peak_kind": peak_kind},
+            "e2e": {"value": e2e_value, "unit": "node-steps/s",
+                    "h2d_bytes_per_step": int(psi_in.nbytes), "d2h_bytes_per_step": int(psi_out.nbytes),
+                    "how": "per step: H2D psi from pinned memory, glgpu_td (1 step), D2H psi, via the C ABI"},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    gl.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+/*
+ * libglgpu: GB300-native (sm_103a) 2D Ginzburg-Landau hot path behind a C ABI.
+ *
+ * Replaces the kernels that microsoft/svirl compiles at run time and looks up by
+ * name (svirl/parallel/startup.py:74-82, Startup.get_function), together with the
+ * host loops that drive them (svirl/solvers/td.py, svirl/solvers/cg.py,
+ * svirl/observables/observables.py).  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - dtype 4 = float32 (complex64 psi), 8 = float64 (complex128 psi), as the
+ *    reference's GLSolver(dtype=...) (svirl/__init__.py:65-71).
+ *  - Host buffers use the reference's flat layouts (svirl/storage/arrays.py:327-365):
+ *      psi: N = Nx*Ny complex values, n = i + Nx*j, interleaved (re, im);
+ *      A:   Nab reals, [a (i + (Nx-1)*j) | b (Na + i + Nx*j)];
+ *      material tiling: Nc = (Nx-1)*(Ny-1) bytes, cell i + (Nx-1)*j, 0 = not
+ *      superconducting; NULL = whole domain.
+ *  - Every call is synchronous with respect to the host unless stated otherwise,
+ *    runs on the handle's own CUDA stream, and returns GLGPU_OK (0) or a
+ *    negative GLGPU_E_* code; glgpu_last_error() gives the message.
+ *  - Device state is owned by the handle; host buffers are copied.  One handle
+ *    per host thread (thread-compatible, not thread-safe).
+ */
+#ifndef GLGPU_H
+#define GLGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GLGPU_OK 0
+#define GLGPU_E_ARG (-1)      /* bad argument (sizes, dtype, NULL) */
+#define GLGPU_E_CUDA (-2)     /* CUDA runtime error */
+#define GLGPU_E_OOM (-3)      /* device allocation failed */
+#define GLGPU_E_TIMEOUT (-4)  /* a device loop hit its iteration guard */
+#define GLGPU_E_NAN (-5)      /* NaN residual seen (state still updated like the reference) */
+#define GLGPU_E_NOROOT (-6)   /* no real non-negative line-search root */
+
+typedef struct glgpu_handle glgpu_handle;
+
+/* Geometry and precision: svirl/__init__.py:73-117 (Nx, Ny >= 4). */
+typedef struct {
+    int32_t Nx, Ny;
+    double dx, dy;
+    int32_t dtype;
+} glgpu_grid;
+
+/* Parameters: svirl/vars/params.py:47-118,270-325 and the stop criteria of
+ * svirl/__init__.py:147-151.  kappa <= 0 or inf means kappa = inf (A fixed). */
+typedef struct {
+    double kappa;           /* gl_parameter */
+    double sigma;           /* normal_conductivity */
+    double epsilon;         /* linear_coefficient (scalar) */
+    double H;               /* homogeneous_external_field */
+    double stop_psi;        /* stop_criterion_order_parameter (clamped like svirl/solvers/td.py:52-66) */
+    double stop_A;          /* stop_criterion_vector_potential */
+    double langevin_psi;    /* order_parameter_Langevin_coefficient */
+    double langevin_A;      /* vector_potential_Langevin_coefficient */
+    uint32_t rand_t;        /* Langevin time seed, svirl/solvers/td.py:35-37 */
+    int32_t pad_;
+} glgpu_params;
+
+/* Per-call TDGL statistics. */
+typedef struct {
+    int32_t steps;
+    int32_t max_sweeps_psi, max_sweeps_A;
+    int32_t last_sweeps_psi, last_sweeps_A;
+    int32_t nan_seen;
+    int64_t total_sweeps_psi, total_sweeps_A;
+    uint32_t rand_t;        /* Langevin seed after the call */
+    int32_t used_graph;     /* 1: device-side loop (CUDA graph), 0: host-driven loop */
+} glgpu_td_stats;
+
+/* --- lifetime: GLSolver construction / destruction (svirl/__init__.py:30-179,
+ *     svirl/parallel/startup.py:17-71) */
+int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out);
+int glgpu_destroy(glgpu_handle* h);
+const char* glgpu_last_error(const glgpu_handle* h);   /* h may be NULL: last create error */
+int glgpu_version(void);
+
+/* --- state and parameters (svirl/vars/vars.py:53-127, svirl/vars/params.py,
+ *     svirl/mesh/grid.py:102-127) */
+int glgpu_set_params(glgpu_handle* h, const glgpu_params* p);
+int glgpu_get_params(const glgpu_handle* h, glgpu_params* p);
+int glgpu_set_order_parameter(glgpu_handle* h, const void* psi);
+int glgpu_get_order_parameter(glgpu_handle* h, void* psi);
+int glgpu_set_vector_potential(glgpu_handle* h, const void* ab);
+int glgpu_get_vector_potential(glgpu_handle* h, void* ab);
+int glgpu_set_external_vector_potential(glgpu_handle* h, const void* abei);  /* NULL clears */
+int glgpu_set_material_tiling(glgpu_handle* h, const uint8_t* mt);          /* NULL = full domain */
+int glgpu_set_linear_coefficient_field(glgpu_handle* h, const void* eps);   /* N reals or NULL */
+
+/* --- TDGL: TD._solve (svirl/solvers/td.py:342-377); kernels
+ *     iterate_order_parameter_jacobi_step (svirl/cuda/td.h:4-133) and
+ *     iterate_vector_potential_jacobi_step (svirl/cuda/td.h:310-463).
+ *     eqn: 0 = both (td.py:342), 1 = order parameter only (td.py:337),
+ *     2 = vector potential only (td.py:444). */
+int glgpu_td(glgpu_handle* h, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats);
+int glgpu_set_use_graphs(glgpu_handle* h, int32_t enable);
+
+/* --- timing (CUDA events on the handle's stream; no counterpart in the reference,
+ *     which has no timing code: its profiler calls are commented out,
+ *     svirl/solvers/cg.py:473,546):
+ *   glgpu_td_timed:    glgpu_td, plus the device time of the whole TD run;
+ *   glgpu_time_sweeps: average device time of one Jacobi sweep kernel launch
+ *                      (which 0 = psi, 1 = A), L2 flushed before each launch;
+ *                      leaves the state at rest unchanged. */
+int glgpu_td_timed(glgpu_handle* h, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats, double* elapsed_ms);
+int glgpu_time_sweeps(glgpu_handle* h, int32_t which, int32_t nrep, double* avg_ms);
+
+/* --- observables (svirl/observables/observables.py:29-149) */
+int glgpu_free_energy(glgpu_handle* h, double* energy);          /* free_energy_pseudodensity + gsum, observables.h:250-362 */
+int glgpu_magnetic_field(glgpu_handle* h, void* B);              /* Nc reals, observables.h:4-37 */
+int glgpu_current_density(glgpu_handle* h, void* j);             /* Nab reals, observables.h:40-156 (kappa=inf: supercurrent) */
+int glgpu_supercurrent_density(glgpu_handle* h, void* js);       /* Nab reals, observables.h:159-235 */
+
+/* --- vortex detector (svirl/observables/vortex_detector.py:31-72): plaquette
+ *     winding scan on the GPU with a relaxed predicate; for each candidate cell
+ *     (sorted by cell index) `corners` receives 4 psi values (00, p0, pp, 0p;
+ *     complex in dtype) and 4 link values (a00, a0p, b00, bp0; dtype), so that
+ *     the caller can apply the reference's exact predicate and triangulation. */
+int glgpu_vortex_candidates(glgpu_handle* h, int32_t cap, int32_t* n_out, int32_t* cells, void* corners);
+
+/* --- modified nonlinear CG, one iteration in phases (svirl/solvers/cg.py:238-551):
+ *   glgpu_cg_reset_direction: dir.fill(0)                           (cg.py:264)
+ *   glgpu_cg_gradient:        dF/dpsi, dF/dA (cg.h:15-301) and, if
+ *                             compute_beta, Polak-Ribiere+ beta   (cg.py:422-449)
+ *   glgpu_cg_coefficients:    dir = beta*dir - g, then the 5 (kappa=inf) or 17
+ *                             line-search coefficients          (cg.h:314-731, cg.py:184-224,325-375)
+ *   glgpu_cg_update:          psi += a_psi dir_psi, A += a_A dir_A, then the
+ *                             free energy                       (cg.py:298-311,515-537) */
+int glgpu_cg_reset_direction(glgpu_handle* h);
+int glgpu_cg_gradient(glgpu_handle* h, int32_t compute_beta);
+int glgpu_cg_coefficients(glgpu_handle* h, double* c);            /* 5 or 17 doubles */
+int glgpu_cg_update(glgpu_handle* h, double alpha_psi, double alpha_A, double* energy);
+
+/* --- kernel-level test hooks used by the reference's tests
+ *     (CG._free_energy_jacobian_psi/_A, cg.py:112-181;
+ *      CG._free_energy_conjgrad_coef(_psi), cg.py:184-224,325-375) */
+int glgpu_jacobian(glgpu_handle* h, void* g_psi, void* g_A);       /* g_A may be NULL */
+int glgpu_conjgrad_coef(glgpu_handle* h, const void* dpsi, const void* dab, double* c);  /* dab NULL: 5 coefficients */
+
+/* --- FP64 vector sum in one launch (the reduction behind every energy/coefficient
+ *     sum), exposed as the reference's reduction test hook Reduction.gsum/gsum_v
+ *     (svirl/parallel/reduction.py:40-173,179-198).  x: n vectors of nv doubles
+ *     (nv = 1, 5 or 17), out: nv sums. */
+int glgpu_reduce_sum(glgpu_handle* h, const double* x, int64_t n, int32_t nv, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLGPU_H */

@@ -1,0 +1,353 @@
+// C ABI of libglgpu: handle lifetime, state and parameter transfer, and the
+// extern "C" wrappers of the TD / CG / observable entry points.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "glgpu_internal.h"
+
+using namespace glgpu;
+
+static thread_local std::string g_create_error;
+
+namespace glgpu {
+
+int set_error(glgpu_handle* h, int code, const std::string& msg) {
+    if (h) h->last_error = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+int cuda_check(glgpu_handle* h, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return GLGPU_OK;
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return set_error(h, GLGPU_E_OOM, m);
+    return set_error(h, GLGPU_E_CUDA, m);
+}
+
+size_t real_size(const glgpu_handle* h) { return (size_t)h->dtype; }
+
+static bool finite_kappa(const glgpu_params& p) { return p.kappa > 0.0 && !std::isinf(p.kappa); }
+
+void upload_inst(glgpu_handle* h) {
+    Inst I;
+    memset(&I, 0, sizeof(I));
+    I.g = h->g;
+    I.dt = 0.0;
+    I.epsilon = h->p.epsilon;
+    I.kappa2 = finite_kappa(h->p) ? h->p.kappa * h->p.kappa : -1.0;
+    I.rho = 1.0 / h->p.sigma;
+    I.H = h->p.H;
+    I.lang_psi = h->p.langevin_psi;
+    I.lang_A = h->p.langevin_A;
+    const double lo = h->dtype == 4 ? 1e-6 : 1e-12;  // svirl/solvers/td.py:52-66
+    I.stop_psi = h->p.stop_psi < lo ? lo : h->p.stop_psi;
+    I.stop_A = h->p.stop_A < lo ? lo : h->p.stop_A;
+    if (h->dtype == 4) {
+        I.stop_psi = (double)(float)I.stop_psi;
+        I.stop_A = (double)(float)I.stop_A;
+    }
+    for (int q = 0; q < 3; ++q) {
+        I.psi[q] = h->psi[q];
+        I.ab[q] = h->ab[q];
+    }
+    I.abei = h->abei;
+    I.mt = h->mt;
+    I.eps_sp = h->eps_sp;
+    I.U = h->U;
+    I.st = h->st;
+    I.tile0 = 0;
+    I.ntiles = h->ntiles;
+    I.solveA = finite_kappa(h->p) ? 1 : 0;
+    h->inst_h = I;
+    cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
+}
+
+}  // namespace glgpu
+
+static int check_handle(const glgpu_handle* h) { return h ? GLGPU_OK : GLGPU_E_ARG; }
+
+static void free_all(glgpu_handle* h) {
+    for (int q = 0; q < 3; ++q) {
+        if (h->psi[q]) cudaFree(h->psi[q]);
+        if (h->ab[q]) cudaFree(h->ab[q]);
+        if (h->td_exec[q]) cudaGraphExecDestroy(h->td_exec[q]);
+    }
+    for (int q = 0; q < 2; ++q) {
+        if (h->g_psi[q]) cudaFree(h->g_psi[q]);
+        if (h->g_A[q]) cudaFree(h->g_A[q]);
+        if (h->dir_psi[q]) cudaFree(h->dir_psi[q]);
+        if (h->dir_A[q]) cudaFree(h->dir_A[q]);
+    }
+    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->st, h->inst, h->tiles, h->loop, h->partials, h->counter,
+                    h->dscal, h->out, h->vort, h->vort_n, h->flush};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (h->hscal) cudaFreeHost(h->hscal);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+extern "C" {
+
+int glgpu_version(void) { return 10000; }
+
+const char* glgpu_last_error(const glgpu_handle* h) { return h ? h->last_error.c_str() : g_create_error.c_str(); }
+
+int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
+    if (!grid || !out) return set_error(nullptr, GLGPU_E_ARG, "glgpu_create: NULL argument");
+    *out = nullptr;
+    if (grid->Nx < 4 || grid->Ny < 4) return set_error(nullptr, GLGPU_E_ARG, "glgpu_create: Nx and Ny must be >= 4");
+    if (grid->dtype != 4 && grid->dtype != 8) return set_error(nullptr, GLGPU_E_ARG, "glgpu_create: dtype must be 4 or 8");
+    if (!(grid->dx > 0.0) || !(grid->dy > 0.0)) return set_error(nullptr, GLGPU_E_ARG, "glgpu_create: dx, dy must be > 0");
+    if ((long long)grid->Nx * grid->Ny > (1LL << 30)) return set_error(nullptr, GLGPU_E_ARG, "glgpu_create: grid too large");
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return set_error(nullptr, GLGPU_E_CUDA, std::string("glgpu_create: cudaSetDevice: ") + cudaGetErrorString(e));
+    glgpu_handle* h = new glgpu_handle();
+    h->device = device;
+    h->dtype = grid->dtype;
+    h->g = make_geo(grid->Nx, grid->Ny, grid->dx, grid->dy);
+    memset(&h->p, 0, sizeof(h->p));
+    h->p.kappa = INFINITY;
+    h->p.sigma = 1.0;
+    h->p.epsilon = 1.0;
+    h->p.stop_psi = 1e-6;
+    h->p.stop_A = 1e-6;
+    h->p.rand_t = 1;
+    const size_t rs = (size_t)h->dtype;
+    const size_t npsi = (size_t)h->g.N * 2 * rs, nab = (size_t)h->g.Nab * rs;
+    h->ntiles = blocks_for(h->g.N);
+    const int nblk = blocks_for(h->g.N);
+    bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (int q = 0; q < 3 && ok; ++q) ok = cudaMalloc(&h->psi[q], npsi) == cudaSuccess && cudaMalloc(&h->ab[q], nab) == cudaSuccess;
+    if (ok && h->dtype == 8) ok = cudaMalloc(&h->U, (size_t)h->g.Nab * 16) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->st, sizeof(InstState)) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->inst, sizeof(Inst)) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->tiles, sizeof(Tile) * (size_t)h->ntiles) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->loop, sizeof(LoopState)) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->partials, sizeof(double) * 17 * (size_t)nblk) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->counter, sizeof(unsigned) * 4) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->dscal, sizeof(double) * 32) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->out, nab > (size_t)h->g.Nxc * h->g.Nyc * rs ? nab : (size_t)h->g.Nxc * h->g.Nyc * rs) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->vort_n, sizeof(int)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&h->hscal, sizeof(double) * 32) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        free_all(h);
+        delete h;
+        return set_error(nullptr, GLGPU_E_OOM, "glgpu_create: device allocation failed");
+    }
+    std::vector<Tile> tiles(h->ntiles);
+    for (int k = 0; k < h->ntiles; ++k) tiles[k] = Tile{0, k * kThreads};
+    InstState st;
+    memset(&st, 0, sizeof(st));
+    st.rand_t = h->p.rand_t;
+    e = cudaMemcpyAsync(h->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->st, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->counter, 0, sizeof(unsigned) * 4, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->dscal, 0, sizeof(double) * 32, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->loop, 0, sizeof(LoopState), h->stream);
+    for (int q = 0; q < 3 && e == cudaSuccess; ++q) {
+        e = cudaMemsetAsync(h->psi[q], 0, npsi, h->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(h->ab[q], 0, nab, h->stream);
+    }
+    if (e == cudaSuccess) {
+        upload_inst(h);
+        e = cudaStreamSynchronize(h->stream);
+    }
+    if (e != cudaSuccess) {
+        std::string m = std::string("glgpu_create: ") + cudaGetErrorString(e);
+        free_all(h);
+        delete h;
+        return set_error(nullptr, GLGPU_E_CUDA, m);
+    }
+    *out = h;
+    return GLGPU_OK;
+}
+
+int glgpu_destroy(glgpu_handle* h) {
+    if (!h) return GLGPU_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return GLGPU_OK;
+}
+
+int glgpu_set_params(glgpu_handle* h, const glgpu_params* p) {
+    if (check_handle(h) || !p) return set_error(h, GLGPU_E_ARG, "set_params: NULL argument");
+    if (!(p->sigma > 0.0)) return set_error(h, GLGPU_E_ARG, "set_params: normal_conductivity must be > 0");
+    if (!(p->stop_psi > 0.0) || !(p->stop_A > 0.0)) return set_error(h, GLGPU_E_ARG, "set_params: stop criteria must be > 0");
+    const bool was_finite = finite_kappa(h->p), now_finite = finite_kappa(*p);
+    h->p = *p;
+    if (was_finite != now_finite) {
+        // the graph topology depends on kappa being finite
+        for (int q = 0; q < 3; ++q)
+            if (h->td_exec[q]) {
+                cudaGraphExecDestroy(h->td_exec[q]);
+                h->td_exec[q] = nullptr;
+            }
+    }
+    upload_inst(h);
+    cudaError_t e = cudaMemcpyAsync(&h->st->rand_t, &h->p.rand_t, sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return cuda_check(h, e, "set_params");
+}
+
+int glgpu_get_params(const glgpu_handle* h, glgpu_params* p) {
+    if (!h || !p) return GLGPU_E_ARG;
+    *p = h->p;
+    return GLGPU_OK;
+}
+
+static int h2d(glgpu_handle* h, void* dst, const void* src, size_t bytes, const char* what) {
+    if (!src) return set_error(h, GLGPU_E_ARG, std::string(what) + ": NULL buffer");
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return cuda_check(h, e, what);
+}
+
+static int d2h(glgpu_handle* h, void* dst, const void* src, size_t bytes, const char* what) {
+    if (!dst) return set_error(h, GLGPU_E_ARG, std::string(what) + ": NULL buffer");
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return cuda_check(h, e, what);
+}
+
+int glgpu_set_order_parameter(glgpu_handle* h, const void* psi) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return h2d(h, h->psi[0], psi, (size_t)h->g.N * 2 * real_size(h), "set_order_parameter");
+}
+
+int glgpu_get_order_parameter(glgpu_handle* h, void* psi) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return d2h(h, psi, h->psi[0], (size_t)h->g.N * 2 * real_size(h), "get_order_parameter");
+}
+
+int glgpu_set_vector_potential(glgpu_handle* h, const void* ab) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return h2d(h, h->ab[0], ab, (size_t)h->g.Nab * real_size(h), "set_vector_potential");
+}
+
+int glgpu_get_vector_potential(glgpu_handle* h, void* ab) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return d2h(h, ab, h->ab[0], (size_t)h->g.Nab * real_size(h), "get_vector_potential");
+}
+
+static int set_optional(glgpu_handle* h, void** slot, const void* src, size_t bytes, const char* what) {
+    if (!src) {
+        if (*slot) {
+            cudaStreamSynchronize(h->stream);
+            cudaFree(*slot);
+            *slot = nullptr;
+        }
+        upload_inst(h);
+        return cuda_check(h, cudaStreamSynchronize(h->stream), what);
+    }
+    if (!*slot && cudaMalloc(slot, bytes) != cudaSuccess) {
+        *slot = nullptr;
+        return set_error(h, GLGPU_E_OOM, std::string(what) + ": out of device memory");
+    }
+    upload_inst(h);
+    return h2d(h, *slot, src, bytes, what);
+}
+
+int glgpu_set_external_vector_potential(glgpu_handle* h, const void* abei) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return set_optional(h, &h->abei, abei, (size_t)h->g.Nab * real_size(h), "set_external_vector_potential");
+}
+
+int glgpu_set_material_tiling(glgpu_handle* h, const uint8_t* mt) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return set_optional(h, (void**)&h->mt, mt, (size_t)h->g.Nxc * h->g.Nyc, "set_material_tiling");
+}
+
+int glgpu_set_linear_coefficient_field(glgpu_handle* h, const void* eps) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return set_optional(h, &h->eps_sp, eps, (size_t)h->g.N * real_size(h), "set_linear_coefficient_field");
+}
+
+int glgpu_set_use_graphs(glgpu_handle* h, int32_t enable) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    h->use_graphs = enable != 0;
+    return GLGPU_OK;
+}
+
+int glgpu_td(glgpu_handle* h, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    cudaSetDevice(h->device);
+    return td_run(h, dt, Nt, eqn, stats, nullptr);
+}
+
+int glgpu_td_timed(glgpu_handle* h, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats, double* elapsed_ms) {
+    if (check_handle(h) || !elapsed_ms) return set_error(h, GLGPU_E_ARG, "td_timed: NULL argument");
+    cudaSetDevice(h->device);
+    return td_run(h, dt, Nt, eqn, stats, elapsed_ms);
+}
+
+int glgpu_time_sweeps(glgpu_handle* h, int32_t which, int32_t nrep, double* avg_ms) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    cudaSetDevice(h->device);
+    return time_sweeps(h, which, nrep, avg_ms);
+}
+
+int glgpu_free_energy(glgpu_handle* h, double* energy) {
+    if (check_handle(h) || !energy) return set_error(h, GLGPU_E_ARG, "free_energy: NULL argument");
+    return obs_free_energy(h, energy);
+}
+
+int glgpu_magnetic_field(glgpu_handle* h, void* B) {
+    if (check_handle(h) || !B) return set_error(h, GLGPU_E_ARG, "magnetic_field: NULL argument");
+    return obs_magnetic_field(h, B);
+}
+
+int glgpu_current_density(glgpu_handle* h, void* j) {
+    if (check_handle(h) || !j) return set_error(h, GLGPU_E_ARG, "current_density: NULL argument");
+    return obs_current_density(h, j);
+}
+
+int glgpu_supercurrent_density(glgpu_handle* h, void* js) {
+    if (check_handle(h) || !js) return set_error(h, GLGPU_E_ARG, "supercurrent_density: NULL argument");
+    return obs_supercurrent_density(h, js);
+}
+
+int glgpu_vortex_candidates(glgpu_handle* h, int32_t cap, int32_t* n_out, int32_t* cells, void* corners) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return obs_vortex_candidates(h, cap, n_out, cells, corners);
+}
+
+int glgpu_cg_reset_direction(glgpu_handle* h) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return cg_reset_direction(h);
+}
+
+int glgpu_cg_gradient(glgpu_handle* h, int32_t compute_beta) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return cg_gradient(h, compute_beta);
+}
+
+int glgpu_cg_coefficients(glgpu_handle* h, double* c) {
+    if (check_handle(h) || !c) return set_error(h, GLGPU_E_ARG, "cg_coefficients: NULL argument");
+    return cg_coefficients(h, c);
+}
+
+int glgpu_cg_update(glgpu_handle* h, double alpha_psi, double alpha_A, double* energy) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return cg_update(h, alpha_psi, alpha_A, energy);
+}
+
+int glgpu_jacobian(glgpu_handle* h, void* g_psi, void* g_A) {
+    if (check_handle(h) || !g_psi) return set_error(h, GLGPU_E_ARG, "jacobian: NULL argument");
+    return cg_read_gradient(h, g_psi, g_A);
+}
+
+int glgpu_conjgrad_coef(glgpu_handle* h, const void* dpsi, const void* dab, double* c) {
+    if (check_handle(h) || !dpsi || !c) return set_error(h, GLGPU_E_ARG, "conjgrad_coef: NULL argument");
+    return cg_coef_for(h, dpsi, dab, c);
+}
+
+int glgpu_reduce_sum(glgpu_handle* h, const double* x, int64_t n, int32_t nv, double* out) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    return reduce_sum(h, x, (long long)n, nv, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,222 @@
+// Shared device-side definitions of the GB300 GL solver (complex helpers, grid
+// geometry, cell flags, residual stop rule, FP64 block reductions).
+//
+// Layouts are the reference's (svirl/cuda/*.h): order parameter psi complex,
+// n = i + Nx*j; vector potential one real array [a | b] with
+// a[i + (Nx-1)*j] (x links) and b[Na + i + Nx*j] (y links); material tiling one
+// byte per cell i + (Nx-1)*j, NULL = whole domain superconducting.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace glgpu {
+
+constexpr int kThreads = 256;      // threads per CTA for all node kernels
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxSweeps = 1024;   // Jacobi cap per time step (svirl/solvers/td.py:164,274)
+constexpr int kLoopGuard = kMaxSweeps + 64;
+
+// ---------------------------------------------------------------------------
+// complex numbers as float2 / double2
+// ---------------------------------------------------------------------------
+template <typename T> struct C2T;
+template <> struct C2T<float> { using type = float2; };
+template <> struct C2T<double> { using type = double2; };
+template <typename T> using C2 = typename C2T<T>::type;
+
+template <typename T> __device__ __forceinline__ C2<T> cmk(T re, T im) { C2<T> z; z.x = re; z.y = im; return z; }
+#define GLGPU_COMPLEX_OPS(V, S)                                                                                 \
+    __device__ __forceinline__ V cadd(V a, V b) { V z; z.x = a.x + b.x; z.y = a.y + b.y; return z; }            \
+    __device__ __forceinline__ V csub(V a, V b) { V z; z.x = a.x - b.x; z.y = a.y - b.y; return z; }            \
+    __device__ __forceinline__ V cmul(V a, V b) { V z; z.x = a.x * b.x - a.y * b.y; z.y = a.x * b.y + a.y * b.x; return z; } \
+    __device__ __forceinline__ V cconj(V a) { V z; z.x = a.x; z.y = -a.y; return z; }                            \
+    __device__ __forceinline__ V cscale(S s, V a) { V z; z.x = s * a.x; z.y = s * a.y; return z; }              \
+    __device__ __forceinline__ S cabs2(V a) { return a.x * a.x + a.y * a.y; }
+GLGPU_COMPLEX_OPS(float2, float)
+GLGPU_COMPLEX_OPS(double2, double)
+#undef GLGPU_COMPLEX_OPS
+
+__device__ __forceinline__ void sincos_t(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_t(double x, double* s, double* c) { sincos(x, s, c); }
+
+// Link factor U(ph) = exp(-i ph) (svirl/cuda/common.h:28-33).
+template <typename T> __device__ __forceinline__ C2<T> link_U(T ph) {
+    T s, c;
+    sincos_t(ph, &s, &c);
+    return cmk<T>(c, -s);
+}
+
+// Im(conj(psi0) U(ph) psi1) (svirl/cuda/common.h:66-73).
+template <typename T> __device__ __forceinline__ T js_of(C2<T> p0, T ph, C2<T> p1) {
+    T s, c;
+    sincos_t(ph, &s, &c);
+    return (p0.x * p1.y - p0.y * p1.x) * c - (p0.x * p1.x + p0.y * p1.y) * s;
+}
+
+// |psi1 U(ph) - psi0|^2 (svirl/cuda/observables.h:238-247).
+template <typename T> __device__ __forceinline__ T g_grad(C2<T> p0, T ph, C2<T> p1) {
+    T s, c;
+    sincos_t(ph, &s, &c);
+    T re = p1.x * c + p1.y * s - p0.x;
+    T im = p1.y * c - p1.x * s - p0.y;
+    return re * re + im * im;
+}
+
+// psi1 U(ph) - psi0 (svirl/cuda/cg.h:304-311), with (s, c) = sincos(ph) given.
+template <typename T> __device__ __forceinline__ C2<T> grad_c_sc(C2<T> p0, T s, T c, C2<T> p1) {
+    return cmk<T>(p1.x * c + p1.y * s - p0.x, p1.y * c - p1.x * s - p0.y);
+}
+
+// ---------------------------------------------------------------------------
+// Langevin random numbers (svirl/cuda/common.h:36-63)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t rand_hash(uint32_t s) {
+    s = (s ^ 61u) ^ (s >> 16);
+    s *= 9u;
+    s = s ^ (s >> 4);
+    s *= 0x27d4eb2du;
+    s = s ^ (s >> 15);
+    return s;
+}
+template <typename T> __device__ __forceinline__ T rand_1(uint32_t n, uint32_t t) {
+    return T(0.00000000023283064365386962890625 * T(rand_hash(71u * n + 9887u * t)));
+}
+template <typename T> __device__ __forceinline__ T rand_2(uint32_t n, uint32_t t) {
+    return T(0.00000000023283064365386962890625 * T(rand_hash(73u * n + 9901u * t + 1u)));
+}
+
+// ---------------------------------------------------------------------------
+// geometry
+// ---------------------------------------------------------------------------
+struct Geo {
+    int Nx, Ny, Na, N, Nab, Nxc, Nyc;
+    double dx, dy;
+};
+
+__host__ __device__ inline Geo make_geo(int Nx, int Ny, double dx, double dy) {
+    Geo g;
+    g.Nx = Nx; g.Ny = Ny; g.Na = (Nx - 1) * Ny; g.N = Nx * Ny;
+    g.Nab = g.Na + Nx * (Ny - 1); g.Nxc = Nx - 1; g.Nyc = Ny - 1;
+    g.dx = dx; g.dy = dy;
+    return g;
+}
+
+// Cells around node (i, j): bit 0 = (i-1,j-1) "mm", 1 = (i-1,j) "mp",
+// 2 = (i,j-1) "pm", 3 = (i,j) "pp"; a bit is set when the cell exists and is in
+// material (svirl/cuda/td.h:129-138).
+__device__ __forceinline__ unsigned cell_bits(const Geo& g, const uint8_t* __restrict__ mt, int i, int j) {
+    bool mm = (i > 0) && (j > 0);
+    bool mp = (i > 0) && (j + 1 < g.Ny);
+    bool pm = (i + 1 < g.Nx) && (j > 0);
+    bool pp = (i + 1 < g.Nx) && (j + 1 < g.Ny);
+    if (mt != nullptr) {
+        if (mm) mm = mt[(i - 1) + g.Nxc * (j - 1)] != 0;
+        if (mp) mp = mt[(i - 1) + g.Nxc * j] != 0;
+        if (pm) pm = mt[i + g.Nxc * (j - 1)] != 0;
+        if (pp) pp = mt[i + g.Nxc * j] != 0;
+    }
+    return (mm ? 1u : 0u) | (mp ? 2u : 0u) | (pm ? 4u : 0u) | (pp ? 8u : 0u);
+}
+#define GL_MM(b) (((b) & 1u) != 0)
+#define GL_MP(b) (((b) & 2u) != 0)
+#define GL_PM(b) (((b) & 4u) != 0)
+#define GL_PP(b) (((b) & 8u) != 0)
+
+// ---------------------------------------------------------------------------
+// Jacobi stop rule (svirl/cuda/td.h:205-213, svirl/solvers/td.py:198-202):
+// per node code = int32(min(1e4*r/eps, 1e8)) in the kernel's precision, stop
+// when 1e-4*max(code) < 1, i.e. when the code of the largest residual is below
+// 10000 (the code is monotone in r, so the max residual decides).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool jacobi_converged(float r, double stop) {
+    float x = (float)((1.0e4 * (double)r) / (double)(float)stop);
+    if (x > 1.0e8) x = 1.0e8f;
+    return (int)x < 10000;
+}
+__device__ __forceinline__ bool jacobi_converged(double r, double stop) {
+    double x = (1.0e4 * r) / stop;
+    if (x > 1.0e8) x = 1.0e8;
+    return (int)x < 10000;
+}
+
+// Residuals are non-negative, so their IEEE bit patterns order like the values.
+__device__ __forceinline__ unsigned long long res_bits(float r) { return (unsigned long long)__float_as_uint(r); }
+__device__ __forceinline__ unsigned long long res_bits(double r) { return (unsigned long long)__double_as_longlong(r); }
+template <typename T> __device__ __forceinline__ T res_from_bits(unsigned long long b);
+template <> __device__ __forceinline__ float res_from_bits<float>(unsigned long long b) { return __uint_as_float((unsigned)b); }
+template <> __device__ __forceinline__ double res_from_bits<double>(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// ---------------------------------------------------------------------------
+// block reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int flat_tid() { return threadIdx.x + blockDim.x * threadIdx.y; }
+
+template <typename T> __device__ __forceinline__ T warp_max(T v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        T w = __shfl_down_sync(0xffffffffu, v, o);
+        v = v > w ? v : w;
+    }
+    return v;
+}
+
+// Sum NV doubles over the CTA; thread 0 gets the totals.  Fixed order: the
+// result is deterministic for a given launch shape.
+template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV]) {
+    __shared__ double sm[kWarps][NV];
+    const int tid = flat_tid(), lane = tid & 31, w = tid >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sm[w][k] = v[k];
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+            for (int q = 0; q < kWarps; ++q) s += sm[q][k];
+            v[k] = s;
+        }
+    }
+}
+
+// Grid-wide FP64 vector sum in one launch: every CTA stores its partials, the
+// last CTA to finish (ticket counter) adds the partials in block order and
+// writes NV results to out[] (scaled by `scale`).  `counter` must be 0 on entry
+// and is left 0.
+template <int NV>
+__device__ void grid_sum_finish(double (&v)[NV], double* __restrict__ partials, unsigned* counter,
+                                double* __restrict__ out, double scale) {
+    __shared__ bool last;
+    block_sum<NV>(v);
+    const int tid = flat_tid();
+    const int nblk = gridDim.x * gridDim.y;
+    const int bid = blockIdx.x + gridDim.x * blockIdx.y;
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) partials[(size_t)bid * NV + k] = v[k];
+        __threadfence();
+        unsigned t = atomicAdd(counter, 1u);
+        last = (t == (unsigned)nblk - 1u);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    for (int b = tid; b < nblk; b += blockDim.x * blockDim.y)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += ((volatile double*)partials)[(size_t)b * NV + k];
+    block_sum<NV>(acc);
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[k] = acc[k] * scale;
+        *counter = 0u;
+    }
+}
+
+}  // namespace glgpu

@@ -1,0 +1,145 @@
+// Internal structures of libglgpu: instance descriptors, device-side loop state,
+// the handle, and the host-side launch helpers shared by the translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "glgpu_common.cuh"
+#include "../../include/glgpu.h"
+
+namespace glgpu {
+
+// Device-resident state of one instance's Jacobi loops (updated by the kernels
+// themselves so that a whole TD run needs no host round trip).
+struct InstState {
+    unsigned long long res;   // max residual of the current sweep, as IEEE bits
+    unsigned blocks_done;     // CTAs of this instance finished in the current sweep
+    int sweep;                // sweeps done in the current Jacobi loop
+    int done;                 // current Jacobi loop finished
+    int rhs;                  // buffer index (0..2) of psi^(0) = right-hand side of the psi loop
+    int rhsA;                 // same for the A loop
+    uint32_t rand_t;          // Langevin time seed (svirl/solvers/td.py:35-37,204,313)
+    int nan_seen;             // a NaN residual was seen (the reference counts it as converged)
+    int last_sweeps_psi, last_sweeps_A, max_sweeps_psi, max_sweeps_A;
+    long long total_sweeps_psi, total_sweeps_A;
+    int steps;                // time steps done in the current call
+    int pad_;
+};
+
+// Everything a kernel needs to process one instance.  Lives in device memory,
+// one entry per instance of a batch (a single GLSolver is a batch of one).
+struct Inst {
+    Geo g;
+    double dt, epsilon, kappa2, rho, H;
+    double lang_psi, lang_A;
+    double stop_psi, stop_A;
+    void* psi[3];             // rotating TD buffers, psi[0] holds the state at rest
+    void* ab[3];              // rotating TD buffers, ab[0] holds the state at rest
+    const void* abei;         // external+irregular vector potential or NULL
+    const uint8_t* mt;        // material tiling (cells) or NULL
+    const void* eps_sp;       // spatial linear coefficient (nodes) or NULL
+    void* U;                  // FP64 link factors exp(-i d a), Nab complex
+    InstState* st;
+    int tile0, ntiles;        // this instance's range in the tile table
+    int solveA;               // finite kappa
+    int pad_;
+};
+
+// Global state of one batched Jacobi/time loop.
+struct LoopState {
+    int active;               // instances whose current Jacobi loop is not done
+    unsigned blocks_done;     // CTAs finished in the current launch
+    int launches;             // sweeps launched in the current Jacobi loop
+    int cont;                 // last decision of the Jacobi while loop
+    int step, Nt;             // time loop position / length
+    int err;                  // error bits (kErr*)
+    int ninst;
+};
+
+constexpr int kErrLoopGuard = 1;
+
+// A tile = 256 consecutive nodes of one instance.
+struct Tile {
+    int inst, n0;
+};
+
+}  // namespace glgpu
+
+// The opaque handle behind glgpu_handle*: one instance with its buffers.
+struct glgpu_handle {
+    int dtype;                   // 4 or 8
+    glgpu::Geo g;
+    glgpu_params p;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    // device buffers
+    void* psi[3] = {nullptr, nullptr, nullptr};
+    void* ab[3] = {nullptr, nullptr, nullptr};
+    void* abei = nullptr;
+    uint8_t* mt = nullptr;
+    void* eps_sp = nullptr;
+    void* U = nullptr;
+    glgpu::InstState* st = nullptr;
+    glgpu::Inst* inst = nullptr;        // device copy of the descriptor
+    glgpu::Inst inst_h;                 // host copy of the descriptor
+    glgpu::Tile* tiles = nullptr;
+    glgpu::LoopState* loop = nullptr;
+    int ntiles = 0;
+    // reductions / outputs
+    double* partials = nullptr;         // nblocks * 17 doubles
+    unsigned* counter = nullptr;        // ticket counter for grid_sum_finish
+    double* dscal = nullptr;            // device scalars: [0..16] coefficients, [20] energy, [24..27] beta sums, [28] beta_psi, [29] beta_A
+    void* out = nullptr;                // staging buffer for observables (Nab reals, Nc reals)
+    void* vort = nullptr;               // vortex candidates
+    int* vort_n = nullptr;
+    int vort_cap = 0;
+    // CG buffers (allocated on first use)
+    void* g_psi[2] = {nullptr, nullptr};
+    void* g_A[2] = {nullptr, nullptr};
+    void* dir_psi[2] = {nullptr, nullptr};
+    void* dir_A[2] = {nullptr, nullptr};
+    int cg_g = 0, cg_dir = 0;           // current index of g / dir
+    // TD graphs, one per equation mode
+    cudaGraphExec_t td_exec[3] = {nullptr, nullptr, nullptr};
+    bool td_graph_failed = false;
+    bool use_graphs = true;
+    std::string last_error;
+    void* flush = nullptr;              // L2 flush buffer for kernel timing
+    // host pinned staging for small results
+    double* hscal = nullptr;
+};
+
+namespace glgpu {
+
+int set_error(glgpu_handle* h, int code, const std::string& msg);
+int cuda_check(glgpu_handle* h, cudaError_t e, const char* what);
+void upload_inst(glgpu_handle* h);
+size_t real_size(const glgpu_handle* h);
+
+// td.cu
+int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms);
+int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms);
+// obs.cu
+int obs_free_energy(glgpu_handle* h, double* out);
+int obs_magnetic_field(glgpu_handle* h, void* host_out);
+int obs_current_density(glgpu_handle* h, void* host_out);
+int obs_supercurrent_density(glgpu_handle* h, void* host_out);
+int obs_vortex_candidates(glgpu_handle* h, int cap, int* n_out, int32_t* cells, void* corners);
+int reduce_sum(glgpu_handle* h, const double* x, long long n, int nv, double* out);
+// cg.cu
+int cg_ensure(glgpu_handle* h);
+int cg_reset_direction(glgpu_handle* h);
+int cg_gradient(glgpu_handle* h, int compute_beta);
+int cg_coefficients(glgpu_handle* h, double* c_out);
+int cg_update(glgpu_handle* h, double alpha_psi, double alpha_A, double* energy_out);
+int cg_read_gradient(glgpu_handle* h, void* gpsi_host, void* gA_host);
+int cg_coef_for(glgpu_handle* h, const void* dpsi_host, const void* dab_host, double* c_out);
+
+inline int blocks_for(long long n) { return (int)((n + kThreads - 1) / kThreads); }
+
+}  // namespace glgpu

@@ -1,0 +1,350 @@
+// Observables of one GL instance: free energy (one launch, FP64 accumulation,
+// deterministic last-CTA finish), magnetic field, total current and supercurrent
+// densities, and the plaquette-winding vortex candidate scan.
+//
+// Reference: svirl/cuda/observables.h:4-362, svirl/observables/observables.py:29-149,
+// svirl/observables/vortex_detector.py:31-72.
+#include "glgpu_internal.h"
+
+namespace glgpu {
+
+// Du discretisation weights (svirl/cuda/observables.h:294-299).
+template <typename T> struct DuW {
+    T r_m0, r_p0, r_0m, r_0p, g;
+};
+template <typename T> __device__ __forceinline__ DuW<T> du_weights(unsigned cb) {
+    DuW<T> w;
+    const T mm = GL_MM(cb) ? T(1) : T(0), mp = GL_MP(cb) ? T(1) : T(0);
+    const T pm = GL_PM(cb) ? T(1) : T(0), pp = GL_PP(cb) ? T(1) : T(0);
+    w.r_m0 = T(0.5) * (mm + mp);
+    w.r_p0 = T(0.5) * (pm + pp);
+    w.r_0m = T(0.5) * (mm + pm);
+    w.r_0p = T(0.5) * (mp + pp);
+    w.g = T(0.25) * (w.r_m0 + w.r_p0 + w.r_0m + w.r_0p);
+    return w;
+}
+
+template <typename T> __device__ __forceinline__ T link_phase(const T* abei, const T* ab, int n) {
+    T p = T(0);
+    if (abei) p += abei[n];
+    if (ab) p += ab[n];
+    return p;
+}
+
+// curl of one link field on cell (i, j): idx*(b[i+1,j]-b[i,j]) - idy*(a[i,j+1]-a[i,j]).
+template <typename T> __device__ __forceinline__ T cell_curl(const Geo& g, const T* A, int i, int j, T idx, T idy) {
+    const int Nxa = g.Nx - 1;
+    return idx * (A[g.Na + (i + 1) + g.Nx * j] - A[g.Na + i + g.Nx * j]) - idy * (A[i + Nxa * (j + 1)] - A[i + Nxa * j]);
+}
+
+// Free-energy pseudo-density at node n before the dx*dy factor
+// (svirl/cuda/observables.h:276-356).
+template <typename T>
+__device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H,
+                                            const uint8_t* mt, const C2<T>* psi, const T* abei, const T* ab, int n) {
+    const int i = n % g.Nx, j = n / g.Nx;
+    const unsigned cb = cell_bits(g, mt, i, j);
+    const T dx = (T)g.dx, dy = (T)g.dy, idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
+    const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy));
+    T e = T(0);
+    if (cb) {
+        const DuW<T> w = du_weights<T>(cb);
+        const C2<T> p00 = psi[n];
+        const T p2 = cabs2(p00);
+        const T eps = eps_sp ? eps_sp[n] : eps0;
+        e += w.g * (T(0.5) * p2 - eps) * p2;
+        if (GL_PM(cb) || GL_PP(cb)) {
+            T ph = link_phase(abei, ab, i + (g.Nx - 1) * j);
+            e += w.r_p0 * idx2 * g_grad<T>(p00, dx * ph, psi[n + 1]);
+        }
+        if (GL_MP(cb) || GL_PP(cb)) {
+            T ph = link_phase(abei, ab, g.Na + i + g.Nx * j);
+            e += w.r_0p * idy2 * g_grad<T>(p00, dy * ph, psi[n + g.Nx]);
+        }
+    }
+    if (kappa2 > T(0) && i < g.Nxc && j < g.Nyc) {
+        T dB = -H;
+        if (abei) dB += cell_curl(g, abei, i, j, idx, idy);
+        if (ab) dB += cell_curl(g, ab, i, j, idx, idy);
+        e += kappa2 * dB * dB;
+    }
+    return e;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_energy(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const uint8_t* mt,
+         const C2<T>* __restrict__ psi, const T* abei, const T* ab, double* partials, unsigned* counter, double* out) {
+    const int n = blockIdx.x * kThreads + threadIdx.x;
+    double v[1] = {0.0};
+    if (n < g.N) v[0] = (double)energy_density<T>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, mt, psi, abei, ab, n);
+    grid_sum_finish<1>(v, partials, counter, out, g.dx * g.dy);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_magnetic_field(Geo g, const T* abei, const T* ab, T* B) {
+    const int n = blockIdx.x * kThreads + threadIdx.x;
+    if (n >= g.Nxc * g.Nyc) return;
+    const int i = n % g.Nxc, j = n / g.Nxc;
+    const T idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
+    T b = T(0);
+    if (abei) b += cell_curl(g, abei, i, j, idx, idy);
+    if (ab) b += cell_curl(g, ab, i, j, idx, idy);
+    B[n] = b;
+}
+
+// kappa^2 curl curl A on the link starting at node (i, j) along x (xdir) or y,
+// with the reference's boundary treatment (svirl/cuda/observables.h:66-155,
+// svirl/cuda/cg.h:174-300).  abei_nb_scale_dd: the external part's neighbour
+// terms carry dd/dd (current) or 1 (gradient); both are 1.
+template <typename T>
+__device__ __forceinline__ T curlcurl_link(const Geo& g, const T* abei, const T* ab, T H, int i, int j, bool xdir) {
+    const int Nxa = g.Nx - 1, Na = g.Na, Nx = g.Nx;
+    const T idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
+    const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy)), idxy = T(1.0 / (g.dx * g.dy));
+    T c = T(0), dd = T(1);
+    if (xdir) {
+        const int n = i + Nxa * j;
+        if (j == 0) { c -= T(2) * H * idy; dd = T(2); }
+        else if (j + 1 == g.Ny) { c += T(2) * H * idy; dd = T(2); }
+        if (abei) c += T(2) / dd * idy2 * abei[n];
+        if (ab) c += T(2) * idy2 * ab[n];
+        if (j > 0) {
+            if (abei) c += (-idy2 * abei[i + Nxa * (j - 1)] + idxy * abei[Na + i + Nx * (j - 1)] - idxy * abei[Na + i + 1 + Nx * (j - 1)]);
+            if (ab) c += dd * (-idy2 * ab[i + Nxa * (j - 1)] + idxy * ab[Na + i + Nx * (j - 1)] - idxy * ab[Na + i + 1 + Nx * (j - 1)]);
+        }
+        if (j + 1 < g.Ny) {
+            if (abei) c += (-idy2 * abei[i + Nxa * (j + 1)] - idxy * abei[Na + i + Nx * j] + idxy * abei[Na + i + 1 + Nx * j]);
+            if (ab) c += dd * (-idy2 * ab[i + Nxa * (j + 1)] - idxy * ab[Na + i + Nx * j] + idxy * ab[Na + i + 1 + Nx * j]);
+        }
+    } else {
+        const int n = Na + i + Nx * j;
+        if (i == 0) { c += T(2) * H * idx; dd = T(2); }
+        else if (i + 1 == g.Nx) { c -= T(2) * H * idx; dd = T(2); }
+        if (abei) c += T(2) / dd * idx2 * abei[n];
+        if (ab) c += T(2) * idx2 * ab[n];
+        if (i > 0) {
+            if (abei) c += (-idx2 * abei[Na + (i - 1) + Nx * j] + idxy * abei[(i - 1) + Nxa * j] - idxy * abei[(i - 1) + Nxa * (j + 1)]);
+            if (ab) c += dd * (-idx2 * ab[Na + (i - 1) + Nx * j] + idxy * ab[(i - 1) + Nxa * j] - idxy * ab[(i - 1) + Nxa * (j + 1)]);
+        }
+        if (i + 1 < g.Nx) {
+            if (abei) c += (-idx2 * abei[Na + (i + 1) + Nx * j] - idxy * abei[i + Nxa * j] + idxy * abei[i + Nxa * (j + 1)]);
+            if (ab) c += dd * (-idx2 * ab[Na + (i + 1) + Nx * j] - idxy * ab[i + Nxa * j] + idxy * ab[i + Nxa * (j + 1)]);
+        }
+    }
+    return c;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_current_density(Geo g, double kappa2, double H, const T* abei, const T* ab, T* out) {
+    const int n = blockIdx.x * kThreads + threadIdx.x;
+    if (n >= g.N) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    if (i < g.Nx - 1) out[i + (g.Nx - 1) * j] = (T)kappa2 * curlcurl_link<T>(g, abei, ab, (T)H, i, j, true);
+    if (j < g.Ny - 1) out[g.Na + i + g.Nx * j] = (T)kappa2 * curlcurl_link<T>(g, abei, ab, (T)H, i, j, false);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_supercurrent_density(Geo g, const uint8_t* mt, const C2<T>* __restrict__ psi, const T* abei, const T* ab, T* out) {
+    const int n = blockIdx.x * kThreads + threadIdx.x;
+    if (n >= g.N) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    const unsigned cb = cell_bits(g, mt, i, j);
+    const C2<T> p0 = psi[n];
+    if (i < g.Nx - 1) {
+        const int na = i + (g.Nx - 1) * j;
+        T jl = T(0);
+        if (GL_PM(cb) || GL_PP(cb)) {
+            const T r = T(0.5) * ((GL_PM(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));
+            jl = r * T(1.0 / g.dx) * js_of<T>(p0, (T)g.dx * link_phase(abei, ab, na), psi[n + 1]);
+        }
+        out[na] = jl;
+    }
+    if (j < g.Ny - 1) {
+        const int nb = g.Na + i + g.Nx * j;
+        T jl = T(0);
+        if (GL_MP(cb) || GL_PP(cb)) {
+            const T r = T(0.5) * ((GL_MP(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));
+            jl = r * T(1.0 / g.dy) * js_of<T>(p0, (T)g.dy * link_phase(abei, ab, nb), psi[n + g.Nx]);
+        }
+        out[nb] = jl;
+    }
+}
+
+// Plaquette winding per cell in FP64 (svirl/observables/vortex_detector.py:55-72)
+// with a relaxed predicate (|v| > 0.45 and |v - round(v)| < 0.15), so the exact
+// predicate, applied afterwards to the copied corner data, selects a subset.
+__device__ __forceinline__ double pmod(double x, double m) { return x - floor(x / m) * m; }
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_vortex_scan(Geo g, double H, const C2<T>* __restrict__ psi, const T* __restrict__ ab, int cap,
+              int* count, int* cells, T* corners) {
+    const int n = blockIdx.x * kThreads + threadIdx.x;
+    if (n >= g.Nxc * g.Nyc) return;
+    const int i = n % g.Nxc, j = n / g.Nxc;
+    const int Nxa = g.Nx - 1;
+    const C2<T> p00 = psi[i + g.Nx * j], pp0 = psi[i + 1 + g.Nx * j];
+    const C2<T> ppp = psi[i + 1 + g.Nx * (j + 1)], p0p = psi[i + g.Nx * (j + 1)];
+    const T a00 = ab[i + Nxa * j], a0p = ab[i + Nxa * (j + 1)];
+    const T b00 = ab[g.Na + i + g.Nx * j], bp0 = ab[g.Na + i + 1 + g.Nx * j];
+    const double t00 = atan2((double)p00.y, (double)p00.x), tp0 = atan2((double)pp0.y, (double)pp0.x);
+    const double tpp = atan2((double)ppp.y, (double)ppp.x), t0p = atan2((double)p0p.y, (double)p0p.x);
+    const double pi = 3.141592653589793, tp = 2.0 * pi;
+    const double v = -(0.5 / pi) * (pmod(tp0 - t00 - g.dx * (double)a00 + pi, tp) + pmod(tpp - tp0 - g.dy * (double)bp0 + pi, tp)
+                                    + pmod(t0p - tpp + g.dx * (double)a0p + pi, tp) + pmod(t00 - t0p + g.dy * (double)b00 + pi, tp)
+                                    - 4.0 * pi + g.dx * g.dy * H);
+    if (fabs(v) > 0.45 && fabs(v - rint(v)) < 0.15) {
+        int k = atomicAdd(count, 1);
+        if (k < cap) {
+            cells[k] = n;
+            T* c = corners + (size_t)k * 12;
+            c[0] = p00.x; c[1] = p00.y; c[2] = pp0.x; c[3] = pp0.y;
+            c[4] = ppp.x; c[5] = ppp.y; c[6] = p0p.x; c[7] = p0p.y;
+            c[8] = a00; c[9] = a0p; c[10] = b00; c[11] = bp0;
+        }
+    }
+}
+
+// Grid-stride FP64 sum of n vectors of NV doubles.
+template <int NV>
+__global__ void __launch_bounds__(kThreads)
+k_vsum(const double* __restrict__ x, long long n, double* partials, unsigned* counter, double* out) {
+    double v[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = 0.0;
+    for (long long m = (long long)blockIdx.x * kThreads + threadIdx.x; m < n; m += (long long)gridDim.x * kThreads)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] += x[m * NV + k];
+    grid_sum_finish<NV>(v, partials, counter, out, 1.0);
+}
+
+// ---------------------------------------------------------------------------
+// host entry points
+// ---------------------------------------------------------------------------
+
+int reduce_sum(glgpu_handle* h, const double* x, long long n, int nv, double* out) {
+    if (!x || !out || n < 0 || !(nv == 1 || nv == 5 || nv == 17)) return set_error(h, GLGPU_E_ARG, "reduce_sum: bad arguments");
+    double* dx = nullptr;
+    const size_t bytes = (size_t)(n > 0 ? n : 1) * nv * sizeof(double);
+    if (cudaMalloc(&dx, bytes) != cudaSuccess) return set_error(h, GLGPU_E_OOM, "reduce_sum: out of device memory");
+    cudaError_t e = n > 0 ? cudaMemcpyAsync(dx, x, (size_t)n * nv * sizeof(double), cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
+    long long nb = (n + kThreads - 1) / kThreads;
+    int grid = (int)(nb < 1 ? 1 : (nb > h->ntiles ? h->ntiles : nb));
+    if (e == cudaSuccess) {
+        if (nv == 1) k_vsum<1><<<grid, kThreads, 0, h->stream>>>(dx, n, h->partials, h->counter, h->dscal + 0);
+        else if (nv == 5) k_vsum<5><<<grid, kThreads, 0, h->stream>>>(dx, n, h->partials, h->counter, h->dscal + 0);
+        else k_vsum<17><<<grid, kThreads, 0, h->stream>>>(dx, n, h->partials, h->counter, h->dscal + 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->hscal, h->dscal, nv * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(dx);
+    if (e != cudaSuccess) return cuda_check(h, e, "reduce_sum");
+    for (int k = 0; k < nv; ++k) out[k] = h->hscal[k];
+    return GLGPU_OK;
+}
+
+static inline bool finite_kappa(const glgpu_handle* h) { return h->p.kappa > 0.0 && !std::isinf(h->p.kappa); }
+static inline double kappa2_of(const glgpu_handle* h) { return finite_kappa(h) ? h->p.kappa * h->p.kappa : -1.0; }
+
+int obs_free_energy_device(glgpu_handle* h) {
+    const int nb = blocks_for(h->g.N);
+    if (h->dtype == 8)
+        k_energy<double><<<nb, kThreads, 0, h->stream>>>(h->g, kappa2_of(h), h->p.epsilon, (const double*)h->eps_sp, h->p.H, h->mt,
+                                                        (const double2*)h->psi[0], (const double*)h->abei, (const double*)h->ab[0],
+                                                        h->partials, h->counter, h->dscal + 20);
+    else
+        k_energy<float><<<nb, kThreads, 0, h->stream>>>(h->g, kappa2_of(h), h->p.epsilon, (const float*)h->eps_sp, h->p.H, h->mt,
+                                                       (const float2*)h->psi[0], (const float*)h->abei, (const float*)h->ab[0],
+                                                       h->partials, h->counter, h->dscal + 20);
+    return cuda_check(h, cudaGetLastError(), "free_energy launch");
+}
+
+int obs_free_energy(glgpu_handle* h, double* out) {
+    int rc = obs_free_energy_device(h);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(h->hscal + 20, h->dscal + 20, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "free_energy");
+    *out = h->hscal[20];
+    return GLGPU_OK;
+}
+
+static int copy_out(glgpu_handle* h, void* host, size_t bytes, const char* what) {
+    cudaError_t e = cudaMemcpyAsync(host, h->out, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return cuda_check(h, e, what);
+}
+
+int obs_magnetic_field(glgpu_handle* h, void* host_out) {
+    const int nc = h->g.Nxc * h->g.Nyc;
+    if (h->dtype == 8)
+        k_magnetic_field<double><<<blocks_for(nc), kThreads, 0, h->stream>>>(h->g, (const double*)h->abei, (const double*)h->ab[0], (double*)h->out);
+    else
+        k_magnetic_field<float><<<blocks_for(nc), kThreads, 0, h->stream>>>(h->g, (const float*)h->abei, (const float*)h->ab[0], (float*)h->out);
+    return copy_out(h, host_out, (size_t)nc * real_size(h), "magnetic_field");
+}
+
+int obs_supercurrent_density(glgpu_handle* h, void* host_out) {
+    if (h->dtype == 8)
+        k_supercurrent_density<double><<<blocks_for(h->g.N), kThreads, 0, h->stream>>>(h->g, h->mt, (const double2*)h->psi[0],
+                                                                                      (const double*)h->abei, (const double*)h->ab[0], (double*)h->out);
+    else
+        k_supercurrent_density<float><<<blocks_for(h->g.N), kThreads, 0, h->stream>>>(h->g, h->mt, (const float2*)h->psi[0],
+                                                                                     (const float*)h->abei, (const float*)h->ab[0], (float*)h->out);
+    return copy_out(h, host_out, (size_t)h->g.Nab * real_size(h), "supercurrent_density");
+}
+
+int obs_current_density(glgpu_handle* h, void* host_out) {
+    if (!finite_kappa(h)) return obs_supercurrent_density(h, host_out);  // observables.py:89-90
+    if (h->dtype == 8)
+        k_current_density<double><<<blocks_for(h->g.N), kThreads, 0, h->stream>>>(h->g, kappa2_of(h), h->p.H, (const double*)h->abei,
+                                                                                 (const double*)h->ab[0], (double*)h->out);
+    else
+        k_current_density<float><<<blocks_for(h->g.N), kThreads, 0, h->stream>>>(h->g, kappa2_of(h), h->p.H, (const float*)h->abei,
+                                                                                (const float*)h->ab[0], (float*)h->out);
+    return copy_out(h, host_out, (size_t)h->g.Nab * real_size(h), "current_density");
+}
+
+int obs_vortex_candidates(glgpu_handle* h, int cap, int* n_out, int32_t* cells, void* corners) {
+    if (cap < 0 || !n_out) return set_error(h, GLGPU_E_ARG, "vortex_candidates: bad arguments");
+    if (cap > h->vort_cap) {
+        if (h->vort) cudaFree(h->vort);
+        h->vort = nullptr;
+        h->vort_cap = 0;
+        size_t bytes = (size_t)cap * (sizeof(int) + 12 * real_size(h));
+        if (cudaMalloc(&h->vort, bytes) != cudaSuccess) return set_error(h, GLGPU_E_OOM, "vortex_candidates: out of memory");
+        h->vort_cap = cap;
+    }
+    cudaError_t e = cudaMemsetAsync(h->vort_n, 0, sizeof(int), h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "vortex_candidates");
+    const int nc = h->g.Nxc * h->g.Nyc;
+    int* dcells = (int*)h->vort;
+    void* dcorn = (char*)h->vort + (size_t)h->vort_cap * sizeof(int);
+    if (h->dtype == 8)
+        k_vortex_scan<double><<<blocks_for(nc), kThreads, 0, h->stream>>>(h->g, h->p.H, (const double2*)h->psi[0], (const double*)h->ab[0],
+                                                                         cap, h->vort_n, dcells, (double*)dcorn);
+    else
+        k_vortex_scan<float><<<blocks_for(nc), kThreads, 0, h->stream>>>(h->g, h->p.H, (const float2*)h->psi[0], (const float*)h->ab[0],
+                                                                        cap, h->vort_n, dcells, (float*)dcorn);
+    int cnt = 0;
+    e = cudaMemcpyAsync(&cnt, h->vort_n, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "vortex_candidates");
+    *n_out = cnt;
+    const int m = cnt < cap ? cnt : cap;
+    if (m > 0) {
+        if (cells) e = cudaMemcpyAsync(cells, dcells, (size_t)m * sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess && corners)
+            e = cudaMemcpyAsync(corners, dcorn, (size_t)m * 12 * real_size(h), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return cuda_check(h, e, "vortex_candidates copy");
+    }
+    return GLGPU_OK;
+}
+
+}  // namespace glgpu

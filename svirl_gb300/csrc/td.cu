@@ -1,0 +1,700 @@
+// TDGL time stepping on the GPU: the Jacobi sweeps of the backward-Euler psi step
+// and of the A step, and the time/Jacobi loops themselves, which run entirely on
+// the device (a CUDA graph with nested conditional WHILE nodes; the sweep kernel
+// that finishes last decides whether the loop continues).
+//
+// Reference: svirl/cuda/td.h:4-133 (psi sweep), td.h:310-463 (A sweep),
+// svirl/solvers/td.py:157-218,252-325,342-377 (host loops, stop rule, swaps).
+//
+// Buffer rotation.  The reference copies psi into a separate right-hand-side
+// buffer each step and ping-pongs psi/psi_next.  Here three buffers rotate:
+// psi^(0) (the right-hand side) stays in buffer R, and sweep k reads psi^(k) and
+// writes psi^(k+1), with psi^(k) in buffer (R+1+((k-1)&1))%3 for k>=1.  No copy
+// is needed, and the values are those of the reference.  For A the same
+// rotation also reproduces the reference's aliasing of the supercurrent
+// argument (svirl/solvers/td.py:266,303): sweep k sees A^(2*floor(k/2)), which is
+// buffer R for k<2 and (R+2)%3 afterwards; in odd sweeps that buffer is also the
+// destination, read and then written by the same thread, as in the reference.
+// The Langevin noise of sweep 0 (td.h:147-151,451-454) is recomputed in every
+// sweep from its hash instead of being stored into the right-hand side.
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+
+#include "glgpu_internal.h"
+
+namespace glgpu {
+
+__device__ __forceinline__ int buf_of(int R, int k) { return k == 0 ? R : (R + 1 + ((k - 1) & 1)) % 3; }
+
+// Called by the last CTA of a launch: decide whether the Jacobi while loop goes on.
+__device__ void finish_launch(LoopState* loop, cudaGraphConditionalHandle cond, int use_cond) {
+    __threadfence();
+    loop->blocks_done = 0u;
+    int L = loop->launches + 1;
+    loop->launches = L;
+    int act = atomicAdd(&loop->active, 0);
+    int cont = act > 0 ? 1 : 0;
+    if (cont && L >= kLoopGuard) {
+        cont = 0;
+        loop->err |= kErrLoopGuard;
+    }
+    loop->cont = cont;
+    if (use_cond) cudaGraphSetConditional(cond, (unsigned)cont);
+}
+
+template <typename T>
+__device__ void finish_instance(const Inst& I, LoopState* loop, int k, bool is_psi) {
+    InstState* st = I.st;
+    __threadfence();
+    unsigned long long b = atomicExch(&st->res, 0ull);
+    T r = res_from_bits<T>(b);
+    bool conv = jacobi_converged(r, is_psi ? I.stop_psi : I.stop_A);
+    int s = k + 1;
+    st->sweep = s;
+    st->blocks_done = 0u;
+    if (conv || s >= kMaxSweeps) {
+        st->done = 1;
+        if (is_psi) {
+            st->rhs = buf_of(st->rhs, s);
+            st->last_sweeps_psi = s;
+            st->total_sweeps_psi += s;
+            if (s > st->max_sweeps_psi) st->max_sweeps_psi = s;
+        } else {
+            st->rhsA = buf_of(st->rhsA, s);
+            st->last_sweeps_A = s;
+            st->total_sweeps_A += s;
+            if (s > st->max_sweeps_A) st->max_sweeps_A = s;
+        }
+        atomicSub(&loop->active, 1);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T block_max_res(T v, bool nan) {
+    __shared__ T sm[kWarps];
+    __shared__ int snan;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) snan = 0;
+    v = warp_max(v);
+    __syncthreads();
+    if (nan) snan = 1;
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    if (tid == 0) {
+        for (int q = 1; q < kWarps; ++q) v = v > sm[q] ? v : sm[q];
+        if (snan) v = -v - T(1);  // flag NaN in the sign: residuals are >= 0
+    }
+    return v;
+}
+
+// One Jacobi sweep of the psi step for every tile of every active instance
+// (svirl/cuda/td.h:4-133, Winecki-Adams link weights td.h:159-163).
+// PRE_U: link factors precomputed per time step (FP64); otherwise they are
+// evaluated in place (FP32).
+template <typename T, bool PRE_U>
+__global__ void __launch_bounds__(kThreads)
+k_psi_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopState* loop,
+            cudaGraphConditionalHandle cond, int use_cond) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    InstState* st = I.st;
+    const int tid = threadIdx.x;
+    __shared__ int s_skip, s_k, s_R, s_RA;
+    __shared__ uint32_t s_rt;
+    if (tid == 0) {
+        s_skip = *(volatile int*)&st->done;
+        s_k = *(volatile int*)&st->sweep;
+        s_R = *(volatile int*)&st->rhs;
+        s_RA = *(volatile int*)&st->rhsA;
+        s_rt = *(volatile uint32_t*)&st->rand_t;
+    }
+    __syncthreads();
+    if (!s_skip) {
+        const int k = s_k, R = s_R;
+        const C2<T>* cur = (const C2<T>*)I.psi[buf_of(R, k)];
+        const C2<T>* rhs = (const C2<T>*)I.psi[R];
+        C2<T>* __restrict__ nxt = (C2<T>*)I.psi[(R + 1 + (k & 1)) % 3];
+        const Geo g = I.g;
+        const int n = t.n0 + tid;
+        T res = T(0);
+        bool nan = false;
+        if (n < g.N) {
+            const int i = n % g.Nx, j = n / g.Nx;
+            const unsigned cb = cell_bits(g, I.mt, i, j);
+            const C2<T> p00 = cur[n];
+            C2<T> out = cmk<T>(T(0), T(0));
+            if (cb) {
+                C2<T> r = rhs[n];
+                if (I.lang_psi > 1.0e-32) {
+                    const T lc = (T)I.lang_psi;
+                    r.x += lc * T(rand_1<T>((uint32_t)n, s_rt) - 0.5);
+                    r.y += lc * T(rand_2<T>((uint32_t)n, s_rt) - 0.5);
+                }
+                const T eps = I.eps_sp ? ((const T*)I.eps_sp)[n] : (T)I.epsilon;
+                const bool rm0 = GL_MM(cb) || GL_MP(cb), rp0 = GL_PM(cb) || GL_PP(cb);
+                const bool r0m = GL_MM(cb) || GL_PM(cb), r0p = GL_MP(cb) || GL_PP(cb);
+                const T dx = (T)g.dx, dy = (T)g.dy;
+                const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy));
+                C2<T> sx = cmk<T>(T(0), T(0)), sy = cmk<T>(T(0), T(0));
+                if (PRE_U) {
+                    const C2<T>* __restrict__ Ul = (const C2<T>*)I.U;
+                    if (rm0) sx = cadd(sx, cmul(cconj(Ul[(i - 1) + (g.Nx - 1) * j]), cur[n - 1]));
+                    if (rp0) sx = cadd(sx, cmul(Ul[i + (g.Nx - 1) * j], cur[n + 1]));
+                    if (r0m) sy = cadd(sy, cmul(cconj(Ul[g.Na + i + g.Nx * (j - 1)]), cur[n - g.Nx]));
+                    if (r0p) sy = cadd(sy, cmul(Ul[g.Na + i + g.Nx * j], cur[n + g.Nx]));
+                } else {
+                    const T* __restrict__ A = (const T*)I.ab[s_RA];
+                    if (rm0) sx = cadd(sx, cmul(link_U<T>(-dx * A[(i - 1) + (g.Nx - 1) * j]), cur[n - 1]));
+                    if (rp0) sx = cadd(sx, cmul(link_U<T>(dx * A[i + (g.Nx - 1) * j]), cur[n + 1]));
+                    if (r0m) sy = cadd(sy, cmul(link_U<T>(-dy * A[g.Na + i + g.Nx * (j - 1)]), cur[n - g.Nx]));
+                    if (r0p) sy = cadd(sy, cmul(link_U<T>(dy * A[g.Na + i + g.Nx * j]), cur[n + g.Nx]));
+                }
+                const T dt = (T)I.dt;
+                const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
+                const T diag = T(1) + dt * (r.x * r.x + r.y * r.y - eps + (idx2 * wx + idy2 * wy));
+                const T inv = T(1) / diag;
+                out.x = (r.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
+                out.y = (r.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
+            }
+            nxt[n] = out;
+            T dr = fabs(out.x - p00.x), di = fabs(out.y - p00.y);
+            res = dr > di ? dr : di;
+            if (!(dr == dr) || !(di == di)) {  // NaN: counts as 0 like the reference's int conversion
+                nan = true;
+                res = (dr == dr) ? dr : ((di == di) ? di : T(0));
+            }
+        }
+        T bmax = block_max_res<T>(res, nan);
+        if (tid == 0) {
+            if (bmax < T(0)) {
+                atomicOr(&st->nan_seen, 1);
+                bmax = -(bmax + T(1));
+            }
+            atomicMax(&st->res, res_bits(bmax));
+            __threadfence();
+            unsigned prev = atomicAdd(&st->blocks_done, 1u);
+            if (prev == (unsigned)I.ntiles - 1u) finish_instance<T>(I, loop, k, true);
+        }
+    }
+    if (tid == 0) {
+        __threadfence();
+        unsigned gdone = atomicAdd(&loop->blocks_done, 1u);
+        if (gdone == gridDim.x - 1u) finish_launch(loop, cond, use_cond);
+    }
+}
+
+// One Jacobi sweep of the A step (svirl/cuda/td.h:310-463): each thread owns the
+// x link and the y link that start at its node.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopState* loop,
+          cudaGraphConditionalHandle cond, int use_cond) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    InstState* st = I.st;
+    const int tid = threadIdx.x;
+    __shared__ int s_skip, s_k, s_R, s_P;
+    __shared__ uint32_t s_rt;
+    if (tid == 0) {
+        s_skip = *(volatile int*)&st->done;
+        s_k = *(volatile int*)&st->sweep;
+        s_R = *(volatile int*)&st->rhsA;
+        s_P = *(volatile int*)&st->rhs;
+        s_rt = *(volatile uint32_t*)&st->rand_t;
+    }
+    __syncthreads();
+    if (!s_skip) {
+        const int k = s_k, R = s_R;
+        const T* cur = (const T*)I.ab[buf_of(R, k)];
+        const T* rhs = (const T*)I.ab[R];
+        const T* abi = (const T*)I.ab[k < 2 ? R : (R + 2) % 3];
+        T* nxt = (T*)I.ab[(R + 1 + (k & 1)) % 3];
+        const C2<T>* __restrict__ psi = (const C2<T>*)I.psi[s_P];
+        const Geo g = I.g;
+        const int n = t.n0 + tid;
+        T res = T(0);
+        bool nan = false;
+        if (n < g.N) {
+            const int i = n % g.Nx, j = n / g.Nx;
+            const int Nxa = g.Nx - 1, Na = g.Na;
+            const bool has_a = i < g.Nx - 1, has_b = j < g.Ny - 1;
+            const int na = i + Nxa * j, nb = Na + i + g.Nx * j;
+            // read the supercurrent phases before anything is stored (aliasing, see top)
+            const T ph_a = has_a ? abi[na] : T(0);
+            const T ph_b = has_b ? abi[nb] : T(0);
+            const unsigned cb = cell_bits(g, I.mt, i, j);
+            const C2<T> psi0 = psi[n];
+            const T dx = (T)g.dx, dy = (T)g.dy;
+            const T idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
+            const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy)), idxy = T(1.0 / (g.dx * g.dy));
+            const T k2 = (T)I.kappa2, H = (T)I.H;
+            const T dt_rho = (T)I.dt * (T)I.rho;
+            const T dt_rho_k2 = dt_rho * k2;
+            const T lc = (T)I.lang_A;
+            const bool lang = I.lang_A > 1.0e-32;
+            T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
+            if (has_a) {
+                T r = rhs[na];
+                if (lang) r += lc * T(rand_1<T>((uint32_t)na, s_rt) - 0.5);
+                T rh = T(0), dd = T(1);
+                if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
+                else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
+                T jl = T(0);
+                if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
+                T nbs = T(0);
+                if (j > 0) nbs += idy2 * cur[i + Nxa * (j - 1)] - idxy * cur[Na + i + g.Nx * (j - 1)] + idxy * cur[Na + i + 1 + g.Nx * (j - 1)];
+                if (j < g.Ny - 1) nbs += idy2 * cur[i + Nxa * (j + 1)] + idxy * cur[Na + i + g.Nx * j] - idxy * cur[Na + i + 1 + g.Nx * j];
+                va = (r + dt_rho * (jl + rh) + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idy2);
+                ca = cur[na];
+            }
+            if (has_b) {
+                T r = rhs[nb];
+                if (lang) r += lc * T(rand_2<T>((uint32_t)nb, s_rt) - 0.5);
+                T rh = T(0), dd = T(1);
+                if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
+                else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
+                T jl = T(0);
+                if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
+                T nbs = T(0);
+                if (i > 0) nbs += idx2 * cur[Na + (i - 1) + g.Nx * j] - idxy * cur[(i - 1) + Nxa * j] + idxy * cur[(i - 1) + Nxa * (j + 1)];
+                if (i < g.Nx - 1) nbs += idx2 * cur[Na + (i + 1) + g.Nx * j] + idxy * cur[i + Nxa * j] - idxy * cur[i + Nxa * (j + 1)];
+                vb = (r + dt_rho * (jl + rh) + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idx2);
+                cbv = cur[nb];
+            }
+            if (has_a) {
+                nxt[na] = va;
+                T d = fabs(va - ca);
+                if (d == d) res = d; else nan = true;
+            }
+            if (has_b) {
+                nxt[nb] = vb;
+                T d = fabs(vb - cbv);
+                if (d == d) { if (d > res) res = d; } else nan = true;
+            }
+        }
+        T bmax = block_max_res<T>(res, nan);
+        if (tid == 0) {
+            if (bmax < T(0)) {
+                atomicOr(&st->nan_seen, 1);
+                bmax = -(bmax + T(1));
+            }
+            atomicMax(&st->res, res_bits(bmax));
+            __threadfence();
+            unsigned prev = atomicAdd(&st->blocks_done, 1u);
+            if (prev == (unsigned)I.ntiles - 1u) finish_instance<T>(I, loop, k, false);
+        }
+    }
+    if (tid == 0) {
+        __threadfence();
+        unsigned gdone = atomicAdd(&loop->blocks_done, 1u);
+        if (gdone == gridDim.x - 1u) finish_launch(loop, cond, use_cond);
+    }
+}
+
+// FP64 link factors U = exp(-i d a) of the current A, once per time step
+// (A is fixed during the psi Jacobi loop).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const Geo g = I.g;
+    const int n = t.n0 + threadIdx.x;
+    if (n >= g.N) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    const T* A = (const T*)I.ab[*(volatile int*)&I.st->rhsA];
+    C2<T>* U = (C2<T>*)I.U;
+    if (i < g.Nx - 1) {
+        int na = i + (g.Nx - 1) * j;
+        U[na] = link_U<T>((T)g.dx * A[na]);
+    }
+    if (j < g.Ny - 1) {
+        int nb = g.Na + i + g.Nx * j;
+        U[nb] = link_U<T>((T)g.dy * A[nb]);
+    }
+}
+
+// Start of a Jacobi loop: reset the per-instance loop state and the while
+// condition.  which: 0 = psi loop, 1 = A loop.
+__global__ void k_loop_begin(const Inst* __restrict__ insts, int ninst, LoopState* loop,
+                             cudaGraphConditionalHandle cond, int use_cond) {
+    for (int q = threadIdx.x; q < ninst; q += blockDim.x) {
+        InstState* st = insts[q].st;
+        st->sweep = 0;
+        st->done = 0;
+        st->blocks_done = 0u;
+        st->res = 0ull;
+    }
+    if (threadIdx.x == 0) {
+        loop->active = ninst;
+        loop->launches = 0;
+        loop->blocks_done = 0u;
+        loop->cont = 1;
+        if (use_cond) cudaGraphSetConditional(cond, 1u);
+    }
+}
+
+// End of a Jacobi loop: advance the Langevin seed (td.py:204,313).
+__global__ void k_loop_end(const Inst* __restrict__ insts, int ninst) {
+    for (int q = threadIdx.x; q < ninst; q += blockDim.x) insts[q].st->rand_t += 1u;
+}
+
+// End of a time step: count it and decide whether the time loop goes on.
+__global__ void k_step_end(const Inst* __restrict__ insts, int ninst, LoopState* loop,
+                           cudaGraphConditionalHandle cond, int use_cond) {
+    for (int q = threadIdx.x; q < ninst; q += blockDim.x) insts[q].st->steps += 1;
+    if (threadIdx.x == 0) {
+        int s = loop->step + 1;
+        loop->step = s;
+        if (use_cond) cudaGraphSetConditional(cond, s < loop->Nt ? 1u : 0u);
+    }
+}
+
+// After a TD call: move psi and A back into buffer 0.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_canonical_copy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const Geo g = I.g;
+    const int n = t.n0 + threadIdx.x;
+    if (n >= g.N) return;
+    const int R = *(volatile int*)&I.st->rhs, RA = *(volatile int*)&I.st->rhsA;
+    if (R != 0) ((C2<T>*)I.psi[0])[n] = ((const C2<T>*)I.psi[R])[n];
+    if (RA != 0) {
+        const int i = n % g.Nx, j = n / g.Nx;
+        if (i < g.Nx - 1) { int na = i + (g.Nx - 1) * j; ((T*)I.ab[0])[na] = ((const T*)I.ab[RA])[na]; }
+        if (j < g.Ny - 1) { int nb = g.Na + i + g.Nx * j; ((T*)I.ab[0])[nb] = ((const T*)I.ab[RA])[nb]; }
+    }
+}
+
+__global__ void k_canonical_reset(const Inst* __restrict__ insts, int ninst) {
+    for (int q = threadIdx.x; q < ninst; q += blockDim.x) {
+        insts[q].st->rhs = 0;
+        insts[q].st->rhsA = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+struct TDLaunch {
+    const Inst* insts;
+    const Tile* tiles;
+    LoopState* loop;
+    int ninst, ntiles, dtype;
+    bool solveA, pre_u;
+};
+
+static void* psi_sweep_fn(int dtype) {
+    return dtype == 8 ? (void*)k_psi_sweep<double, true> : (void*)k_psi_sweep<float, false>;
+}
+static void* A_sweep_fn(int dtype) {
+    return dtype == 8 ? (void*)k_A_sweep<double> : (void*)k_A_sweep<float>;
+}
+
+static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
+                              void* fn, dim3 grid, dim3 block, void** args) {
+    cudaKernelNodeParams p;
+    memset(&p, 0, sizeof(p));
+    p.func = fn;
+    p.gridDim = grid;
+    p.blockDim = block;
+    p.sharedMemBytes = 0;
+    p.kernelParams = args;
+    p.extra = nullptr;
+    return cudaGraphAddKernelNode(node, g, deps, ndeps, &p);
+}
+
+static cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
+                             cudaGraphConditionalHandle h, cudaGraph_t* body) {
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaError_t e = cudaGraphAddNode(node, g, deps, nullptr, ndeps, &p);
+    if (e == cudaSuccess) *body = p.conditional.phGraph_out[0];
+    return e;
+}
+
+#define GCHK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { err = e_; goto fail; } } while (0)
+
+// Build the whole TD run as one graph:
+//   [U once (FP64, kappa=inf)] -> WHILE(step < Nt) {
+//       [U (FP64, finite kappa)] -> loop_begin -> WHILE(active) { psi sweep } -> loop_end
+//       -> loop_begin -> WHILE(active) { A sweep } -> loop_end -> step_end }
+//   -> canonical copy -> canonical reset
+static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* exec) {
+    cudaError_t err = cudaSuccess;
+    cudaGraph_t top = nullptr, obody = nullptr, pbody = nullptr, abody = nullptr;
+    cudaGraphConditionalHandle hout, hpsi = 0, hA = 0;
+    cudaGraphNode_t n_pre = nullptr, n_out = nullptr, n_cc = nullptr, n_cr = nullptr, prev = nullptr, nd;
+    const bool do_psi = eqn != 2, do_A = (eqn != 1) && L.solveA;
+    int one = 1;
+    const dim3 gt(L.ntiles), bt(kThreads), g1(1), b1(32);
+    Inst const* insts = L.insts;
+    Tile const* tiles = L.tiles;
+    LoopState* loop = L.loop;
+    int ninst = L.ninst;
+
+    GCHK(cudaGraphCreate(&top, 0));
+    GCHK(cudaGraphConditionalHandleCreate(&hout, top, 1, cudaGraphCondAssignDefault));
+    if (do_psi && L.pre_u && !L.solveA) {
+        void* a[] = {&insts, &tiles};
+        GCHK(add_kernel(top, &n_pre, nullptr, 0, (void*)k_link_U<double>, gt, bt, a));
+    }
+    GCHK(add_while(top, &n_out, n_pre ? &n_pre : nullptr, n_pre ? 1 : 0, hout, &obody));
+    if (do_psi) {
+        GCHK(cudaGraphConditionalHandleCreate(&hpsi, obody, 1, cudaGraphCondAssignDefault));
+        if (L.pre_u && L.solveA) {
+            void* a[] = {&insts, &tiles};
+            GCHK(add_kernel(obody, &nd, nullptr, 0, (void*)k_link_U<double>, gt, bt, a));
+            prev = nd;
+        }
+        {
+            void* a[] = {&insts, &ninst, &loop, &hpsi, &one};
+            GCHK(add_kernel(obody, &nd, prev ? &prev : nullptr, prev ? 1 : 0, (void*)k_loop_begin, g1, b1, a));
+            prev = nd;
+        }
+        GCHK(add_while(obody, &nd, &prev, 1, hpsi, &pbody));
+        prev = nd;
+        {
+            cudaGraphNode_t sw;
+            void* a[] = {&insts, &tiles, &loop, &hpsi, &one};
+            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype), gt, bt, a));
+        }
+        {
+            void* a[] = {&insts, &ninst};
+            GCHK(add_kernel(obody, &nd, &prev, 1, (void*)k_loop_end, g1, b1, a));
+            prev = nd;
+        }
+    }
+    if (do_A) {
+        GCHK(cudaGraphConditionalHandleCreate(&hA, obody, 1, cudaGraphCondAssignDefault));
+        {
+            void* a[] = {&insts, &ninst, &loop, &hA, &one};
+            GCHK(add_kernel(obody, &nd, prev ? &prev : nullptr, prev ? 1 : 0, (void*)k_loop_begin, g1, b1, a));
+            prev = nd;
+        }
+        GCHK(add_while(obody, &nd, &prev, 1, hA, &abody));
+        prev = nd;
+        {
+            cudaGraphNode_t sw;
+            void* a[] = {&insts, &tiles, &loop, &hA, &one};
+            GCHK(add_kernel(abody, &sw, nullptr, 0, A_sweep_fn(L.dtype), gt, bt, a));
+        }
+        {
+            void* a[] = {&insts, &ninst};
+            GCHK(add_kernel(obody, &nd, &prev, 1, (void*)k_loop_end, g1, b1, a));
+            prev = nd;
+        }
+    }
+    {
+        void* a[] = {&insts, &ninst, &loop, &hout, &one};
+        GCHK(add_kernel(obody, &nd, prev ? &prev : nullptr, prev ? 1 : 0, (void*)k_step_end, g1, b1, a));
+    }
+    {
+        void* a[] = {&insts, &tiles};
+        void* fn = L.dtype == 8 ? (void*)k_canonical_copy<double> : (void*)k_canonical_copy<float>;
+        GCHK(add_kernel(top, &n_cc, &n_out, 1, fn, gt, bt, a));
+        void* b[] = {&insts, &ninst};
+        GCHK(add_kernel(top, &n_cr, &n_cc, 1, (void*)k_canonical_reset, g1, b1, b));
+    }
+    GCHK(cudaGraphInstantiate(exec, top, 0));
+    cudaGraphDestroy(top);
+    return cudaSuccess;
+fail:
+    if (top) cudaGraphDestroy(top);
+    *exec = nullptr;
+    return err;
+}
+
+// Host-driven fallback: the same kernels, the loop decided on the host after
+// each chunk of sweeps (sweeps of finished instances are no-ops).
+static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_t s) {
+    const bool do_psi = eqn != 2, do_A = (eqn != 1) && L.solveA;
+    const int chunk = 4;
+    cudaGraphConditionalHandle none = 0;
+    int cont = 1;
+    if (do_psi && L.pre_u && !L.solveA) k_link_U<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    for (int step = 0; step < Nt; ++step) {
+        for (int part = 0; part < 2; ++part) {
+            if (part == 0 && !do_psi) continue;
+            if (part == 1 && !do_A) continue;
+            if (part == 0 && L.pre_u && L.solveA) k_link_U<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+            k_loop_begin<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0);
+            for (;;) {
+                for (int c = 0; c < chunk; ++c) {
+                    if (part == 0) {
+                        if (L.dtype == 8) k_psi_sweep<double, true><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
+                        else k_psi_sweep<float, false><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
+                    } else {
+                        if (L.dtype == 8) k_A_sweep<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
+                        else k_A_sweep<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
+                    }
+                }
+                cudaError_t e = cudaMemcpyAsync(&cont, &L.loop->cont, sizeof(int), cudaMemcpyDeviceToHost, s);
+                if (e != cudaSuccess) return e;
+                e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess) return e;
+                if (!cont) break;
+            }
+            k_loop_end<<<1, 32, 0, s>>>(L.insts, L.ninst);
+        }
+        k_step_end<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0);
+    }
+    if (L.dtype == 8) k_canonical_copy<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    else k_canonical_copy<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    k_canonical_reset<<<1, 32, 0, s>>>(L.insts, L.ninst);
+    return cudaGetLastError();
+}
+
+// Prepare one timed sweep: Jacobi sweep index k (k >= 1 reads a psi^(k) buffer
+// distinct from the right-hand side, as in a typical sweep), loop not done.
+__global__ void k_bench_prep(const Inst* __restrict__ insts, int ninst, LoopState* loop, int k) {
+    for (int q = threadIdx.x; q < ninst; q += blockDim.x) {
+        InstState* st = insts[q].st;
+        st->sweep = k;
+        st->done = 0;
+        st->blocks_done = 0u;
+        st->res = 0ull;
+    }
+    if (threadIdx.x == 0) {
+        loop->active = ninst;
+        loop->launches = 0;
+        loop->blocks_done = 0u;
+        loop->cont = 1;
+    }
+}
+
+int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
+    if (nrep < 1 || which < 0 || which > 1 || !avg_ms) return set_error(h, GLGPU_E_ARG, "time_sweeps: bad arguments");
+    const bool solveA = h->p.kappa > 0.0 && !std::isinf(h->p.kappa);
+    if (which == 1 && !solveA) return set_error(h, GLGPU_E_ARG, "time_sweeps: A sweeps need a finite kappa");
+    const size_t flush_bytes = (size_t)256 << 20;  // > 129 MB of L2
+    if (!h->flush && cudaMalloc(&h->flush, flush_bytes) != cudaSuccess) return set_error(h, GLGPU_E_OOM, "time_sweeps: flush buffer");
+    h->inst_h.dt = h->inst_h.dt > 0.0 ? h->inst_h.dt : 0.1;
+    cudaError_t e = cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "time_sweeps");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaGraphConditionalHandle none = 0;
+    if (h->dtype == 8) k_link_U<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles);
+    double total = 0.0;
+    for (int r = 0; r < nrep && e == cudaSuccess; ++r) {
+        cudaMemsetAsync(h->flush, r & 0xff, flush_bytes, h->stream);
+        k_bench_prep<<<1, 32, 0, h->stream>>>(h->inst, 1, h->loop, 1);
+        cudaEventRecord(e0, h->stream);
+        if (which == 0) {
+            if (h->dtype == 8) k_psi_sweep<double, true><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+            else k_psi_sweep<float, false><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+        } else {
+            if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+            else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+        }
+        cudaEventRecord(e1, h->stream);
+        e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        total += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // leave the loop state as a finished loop; the state at rest (buffer 0) was not written
+    k_canonical_reset<<<1, 32, 0, h->stream>>>(h->inst, 1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "time_sweeps");
+    *avg_ms = total / nrep;
+    return GLGPU_OK;
+}
+
+int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms) {
+    if (eqn < 0 || eqn > 2 || Nt < 0) return set_error(h, GLGPU_E_ARG, "glgpu_td: bad eqn or Nt");
+    const bool solveA = h->p.kappa > 0.0 && !std::isinf(h->p.kappa);
+    // dt of the order-parameter iterator; the A kernel also receives it (td.py:278)
+    {
+        cudaError_t e = cudaMemsetAsync(&h->st->nan_seen, 0, offsetof(InstState, pad_) - offsetof(InstState, nan_seen), h->stream);
+        if (e != cudaSuccess) return cuda_check(h, e, "td: reset counters");
+        h->inst_h.dt = dt;
+        e = cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
+        if (e != cudaSuccess) return cuda_check(h, e, "td: write descriptor");
+    }
+    TDLaunch L;
+    L.insts = h->inst; L.tiles = h->tiles; L.loop = h->loop; L.ninst = 1; L.ntiles = h->ntiles;
+    L.dtype = h->dtype; L.solveA = solveA; L.pre_u = (h->dtype == 8);
+    int used_graph = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (elapsed_ms) {
+        *elapsed_ms = 0.0;
+        cudaEventCreate(&ev0);
+        cudaEventCreate(&ev1);
+    }
+    if (Nt > 0) {
+        LoopState ls;
+        memset(&ls, 0, sizeof(ls));
+        ls.Nt = Nt;
+        ls.ninst = 1;
+        cudaError_t e = cudaMemcpyAsync(h->loop, &ls, sizeof(ls), cudaMemcpyHostToDevice, h->stream);
+        if (e != cudaSuccess) return cuda_check(h, e, "td: loop state");
+        const int gi = eqn * 1;  // graph slot per eqn (solveA is fixed by the descriptor's kappa)
+        if (h->use_graphs && !h->td_graph_failed) {
+            if (h->td_exec[gi] == nullptr) {
+                e = build_td_graph(L, eqn, &h->td_exec[gi]);
+                if (e != cudaSuccess) {
+                    h->td_graph_failed = true;
+                    cudaGetLastError();
+                }
+            }
+            if (h->td_exec[gi] != nullptr) {
+                if (ev0) cudaEventRecord(ev0, h->stream);
+                e = cudaGraphLaunch(h->td_exec[gi], h->stream);
+                if (e != cudaSuccess) return cuda_check(h, e, "td: graph launch");
+                used_graph = 1;
+            }
+        }
+        if (!used_graph) {
+            if (ev0) cudaEventRecord(ev0, h->stream);
+            e = run_host_loop(L, eqn, Nt, h->stream);
+            if (e != cudaSuccess) return cuda_check(h, e, "td: host loop");
+        }
+        if (ev1) cudaEventRecord(ev1, h->stream);
+    }
+    InstState hs;
+    LoopState hl;
+    cudaError_t e = cudaMemcpyAsync(&hs, h->st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hl, h->loop, sizeof(hl), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "td: run");
+    if (ev0) {
+        float ms = 0.f;
+        if (Nt > 0 && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) *elapsed_ms = ms;
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+    }
+    h->p.rand_t = hs.rand_t;
+    if (stats) {
+        stats->steps = Nt > 0 ? hl.step : 0;
+        stats->max_sweeps_psi = hs.max_sweeps_psi;
+        stats->max_sweeps_A = hs.max_sweeps_A;
+        stats->last_sweeps_psi = hs.last_sweeps_psi;
+        stats->last_sweeps_A = hs.last_sweeps_A;
+        stats->nan_seen = hs.nan_seen;
+        stats->total_sweeps_psi = hs.total_sweeps_psi;
+        stats->total_sweeps_A = hs.total_sweeps_A;
+        stats->rand_t = hs.rand_t;
+        stats->used_graph = used_graph;
+    }
+    if (Nt > 0 && (hl.err & kErrLoopGuard)) return set_error(h, GLGPU_E_TIMEOUT, "td: Jacobi loop guard reached");
+    if (hs.nan_seen) {
+        set_error(h, GLGPU_E_NAN, "td: NaN residual (the state was updated as the reference does)");
+        return GLGPU_E_NAN;
+    }
+    return GLGPU_OK;
+}
+
+}  // namespace glgpu
