@@ -58,6 +58,7 @@ void upload_inst(glgpu_handle* h) {
     I.st = h->st;
     I.tile0 = 0;
     I.ntiles = h->ntiles;
+    I.nitems = h->nitems;
     I.solveA = finite_kappa(h->p) ? 1 : 0;
     h->inst_h = I;
     cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
@@ -79,7 +80,7 @@ static void free_all(glgpu_handle* h) {
         if (h->dir_psi[q]) cudaFree(h->dir_psi[q]);
         if (h->dir_A[q]) cudaFree(h->dir_A[q]);
     }
-    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->st, h->inst, h->tiles, h->loop, h->partials, h->counter,
+    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->st, h->inst, h->tiles, h->items, h->loop, h->partials, h->counter,
                     h->dscal, h->out, h->vort, h->vort_n, h->flush};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -123,6 +124,9 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     ok = ok && cudaMalloc(&h->st, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->inst, sizeof(Inst)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->tiles, sizeof(Tile) * (size_t)h->ntiles) == cudaSuccess;
+    const int nstrips = (h->g.Nx + 31) / 32, nrows = (h->g.Ny + kStripRows - 1) / kStripRows;
+    h->nitems = nstrips * nrows;
+    ok = ok && cudaMalloc(&h->items, sizeof(Item) * (size_t)h->nitems) == cudaSuccess;
     ok = ok && cudaMalloc(&h->loop, sizeof(LoopState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->partials, sizeof(double) * 17 * (size_t)nblk) == cudaSuccess;
     ok = ok && cudaMalloc(&h->counter, sizeof(unsigned) * 4) == cudaSuccess;
@@ -138,10 +142,17 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     }
     std::vector<Tile> tiles(h->ntiles);
     for (int k = 0; k < h->ntiles; ++k) tiles[k] = Tile{0, k * kThreads};
+    // items row-block major, so that concurrently running warps share halo rows in L2
+    std::vector<Item> items;
+    items.reserve(h->nitems);
+    for (int r = 0; r < nrows; ++r)
+        for (int s = 0; s < nstrips; ++s) items.push_back(Item{0, 32 * s, kStripRows * r, 0});
+    h->psi_grid = psi_sweep_grid(h->dtype, h->nitems);
     InstState st;
     memset(&st, 0, sizeof(st));
     st.rand_t = h->p.rand_t;
     e = cudaMemcpyAsync(h->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->items, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->st, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->counter, 0, sizeof(unsigned) * 4, h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->dscal, 0, sizeof(double) * 32, h->stream);

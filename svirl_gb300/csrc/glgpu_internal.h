@@ -46,6 +46,7 @@ struct Inst {
     void* U;                  // FP64 link factors exp(-i d a), Nab complex
     InstState* st;
     int tile0, ntiles;        // this instance's range in the tile table
+    int nitems;               // number of warp-strip items of this instance
     int solveA;               // finite kappa
     int pad_;
 };
@@ -68,6 +69,13 @@ struct Tile {
     int inst, n0;
 };
 
+// Work item of the warp-strip psi sweep: 32 columns (x0..x0+31) by kStripRows
+// rows (j0..) of one instance, processed by one warp.
+constexpr int kStripRows = 8;
+struct Item {
+    int inst, x0, j0, pad;
+};
+
 }  // namespace glgpu
 
 // The opaque handle behind glgpu_handle*: one instance with its buffers.
@@ -88,6 +96,9 @@ struct glgpu_handle {
     glgpu::Inst* inst = nullptr;        // device copy of the descriptor
     glgpu::Inst inst_h;                 // host copy of the descriptor
     glgpu::Tile* tiles = nullptr;
+    glgpu::Item* items = nullptr;
+    int nitems = 0;
+    int psi_grid = 0;                   // CTAs of the persistent psi sweep
     glgpu::LoopState* loop = nullptr;
     int ntiles = 0;
     // reductions / outputs
@@ -124,6 +135,7 @@ size_t real_size(const glgpu_handle* h);
 // td.cu
 int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms);
 int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms);
+int psi_sweep_grid(int dtype, int nitems);
 // obs.cu
 int obs_free_energy(glgpu_handle* h, double* out);
 int obs_magnetic_field(glgpu_handle* h, void* host_out);

@@ -89,96 +89,171 @@ __device__ __forceinline__ T block_max_res(T v, bool nan) {
     return v;
 }
 
-// One Jacobi sweep of the psi step for every tile of every active instance
-// (svirl/cuda/td.h:4-133, Winecki-Adams link weights td.h:159-163).
-// PRE_U: link factors precomputed per time step (FP64); otherwise they are
-// evaluated in place (FP32).
+// Residual bookkeeping of one warp for the instance it is working on: the warp
+// max goes to the instance with one atomic, and the warp that completes the
+// instance's last item closes that instance's sweep.
+template <typename T>
+__device__ __forceinline__ void warp_flush(const Inst* insts, int inst, int k, T wmax, bool wnan, int count,
+                                           LoopState* loop) {
+    const unsigned full = 0xffffffffu;
+    T m = warp_max(wmax);
+    const bool anynan = __any_sync(full, wnan);
+    if ((threadIdx.x & 31) == 0 && count > 0) {
+        const Inst& I = insts[inst];
+        InstState* st = I.st;
+        if (anynan) atomicOr(&st->nan_seen, 1);
+        atomicMax(&st->res, res_bits(m));
+        __threadfence();
+        unsigned prev = atomicAdd(&st->blocks_done, (unsigned)count);
+        if (prev + (unsigned)count == (unsigned)I.nitems) finish_instance<T>(I, loop, k, true);
+    }
+}
+
+template <typename T> __device__ __forceinline__ C2<T> shfl_up_c(C2<T> v, int d) {
+    return cmk<T>(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+}
+template <typename T> __device__ __forceinline__ C2<T> shfl_down_c(C2<T> v, int d) {
+    return cmk<T>(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+
+// Link factor exp(-i d a) of link index l: evaluated in place (FP32) or read
+// from the per-step table (FP64).
+template <typename T, bool PRE_U>
+__device__ __forceinline__ C2<T> link_factor(const T* A, const C2<T>* U, int l, T d) {
+    if (PRE_U) return U[l];
+    return link_U<T>(d * A[l]);
+}
+
+__device__ __forceinline__ bool cell_in(const Geo& g, const uint8_t* mt, int ci, int cj) {
+    if (ci < 0 || cj < 0 || ci >= g.Nxc || cj >= g.Nyc) return false;
+    return mt == nullptr || mt[ci + g.Nxc * cj] != 0;
+}
+
+// One Jacobi sweep of the psi step (svirl/cuda/td.h:4-133, Winecki-Adams link
+// weights td.h:159-163) over every active instance.  A warp owns a strip of 32
+// columns and kStripRows rows: it walks down the rows keeping psi(j-1), psi(j),
+// psi(j+1), the y link below and the cells below in registers, and takes the
+// x neighbours, the x link on the left and the cell on the left from the
+// neighbouring lane, so each node loads psi, rhs, its two links and its cell
+// once and evaluates one x-link and one y-link factor.  Persistent grid: warps
+// stride over the item table.  PRE_U: link factors from the per-step table
+// (FP64); otherwise evaluated in place (FP32).
 template <typename T, bool PRE_U>
 __global__ void __launch_bounds__(kThreads)
-k_psi_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopState* loop,
+k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
             cudaGraphConditionalHandle cond, int use_cond) {
-    const Tile t = tiles[blockIdx.x];
-    const Inst& I = insts[t.inst];
-    InstState* st = I.st;
-    const int tid = threadIdx.x;
-    __shared__ int s_skip, s_k, s_R, s_RA;
-    __shared__ uint32_t s_rt;
-    if (tid == 0) {
-        s_skip = *(volatile int*)&st->done;
-        s_k = *(volatile int*)&st->sweep;
-        s_R = *(volatile int*)&st->rhs;
-        s_RA = *(volatile int*)&st->rhsA;
-        s_rt = *(volatile uint32_t*)&st->rand_t;
-    }
-    __syncthreads();
-    if (!s_skip) {
-        const int k = s_k, R = s_R;
-        const C2<T>* cur = (const C2<T>*)I.psi[buf_of(R, k)];
-        const C2<T>* rhs = (const C2<T>*)I.psi[R];
-        C2<T>* __restrict__ nxt = (C2<T>*)I.psi[(R + 1 + (k & 1)) % 3];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
+    int cur_inst = -1, k = 0, count = 0, done = 1;
+    T wmax = T(0);
+    bool wnan = false;
+    // per-instance values, refreshed when the warp moves to another instance
+    const C2<T>* cur = nullptr;
+    const C2<T>* rhs = nullptr;
+    C2<T>* nxt = nullptr;
+    const T* A = nullptr;
+    const C2<T>* U = nullptr;
+    uint32_t rt = 0;
+    for (int it = gw; it < nitems; it += nw) {
+        const Item w = items[it];
+        if (w.inst != cur_inst) {
+            if (cur_inst >= 0 && !done) warp_flush<T>(insts, cur_inst, k, wmax, wnan, count, loop);
+            cur_inst = w.inst;
+            const InstState* st = insts[cur_inst].st;
+            done = *(volatile const int*)&st->done;
+            k = *(volatile const int*)&st->sweep;
+            const int R = *(volatile const int*)&st->rhs, RA = *(volatile const int*)&st->rhsA;
+            rt = *(volatile const uint32_t*)&st->rand_t;
+            const Inst& I = insts[cur_inst];
+            cur = (const C2<T>*)I.psi[buf_of(R, k)];
+            rhs = (const C2<T>*)I.psi[R];
+            nxt = (C2<T>*)I.psi[(R + 1 + (k & 1)) % 3];
+            A = (const T*)I.ab[RA];
+            U = (const C2<T>*)I.U;
+            wmax = T(0);
+            wnan = false;
+            count = 0;
+        }
+        if (done) continue;
+        const Inst& I = insts[cur_inst];
         const Geo g = I.g;
-        const int n = t.n0 + tid;
-        T res = T(0);
-        bool nan = false;
-        if (n < g.N) {
-            const int i = n % g.Nx, j = n / g.Nx;
-            const unsigned cb = cell_bits(g, I.mt, i, j);
-            const C2<T> p00 = cur[n];
-            C2<T> out = cmk<T>(T(0), T(0));
-            if (cb) {
-                C2<T> r = rhs[n];
-                if (I.lang_psi > 1.0e-32) {
-                    const T lc = (T)I.lang_psi;
-                    r.x += lc * T(rand_1<T>((uint32_t)n, s_rt) - 0.5);
-                    r.y += lc * T(rand_2<T>((uint32_t)n, s_rt) - 0.5);
+        const uint8_t* mt = I.mt;
+        const T* eps_sp = (const T*)I.eps_sp;
+        const T dt = (T)I.dt, eps0 = (T)I.epsilon, dx = (T)g.dx, dy = (T)g.dy;
+        const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy));
+        const bool lang = I.lang_psi > 1.0e-32;
+        const T lc = (T)I.lang_psi;
+        const int Nx = g.Nx, Nxa = g.Nx - 1;
+        const int i = w.x0 + lane;
+        const bool vi = i < Nx;
+        const int j0 = w.j0, jend = min(j0 + kStripRows, g.Ny);
+        const C2<T> z = cmk<T>(T(0), T(0));
+        // state carried down the strip
+        C2<T> p_prev = (vi && j0 > 0) ? cur[i + Nx * (j0 - 1)] : z;
+        C2<T> p_c = vi ? cur[i + Nx * j0] : z;
+        C2<T> ub_down = (vi && j0 > 0 && j0 - 1 < g.Ny - 1) ? link_factor<T, PRE_U>(A, U, g.Na + i + Nx * (j0 - 1), dy) : z;
+        bool c_pm = vi && cell_in(g, mt, i, j0 - 1);       // cell (i, j-1)
+        bool c_mm = vi && cell_in(g, mt, i - 1, j0 - 1);   // cell (i-1, j-1)
+        for (int j = j0; j < jend; ++j) {
+            const int n = i + Nx * j;
+            const C2<T> p_next = (vi && j + 1 < g.Ny) ? cur[n + Nx] : z;
+            // x neighbours and x links from the neighbouring lanes
+            C2<T> p_left = shfl_up_c<T>(p_c, 1), p_right = shfl_down_c<T>(p_c, 1);
+            const C2<T> ua = (vi && i < Nx - 1) ? link_factor<T, PRE_U>(A, U, i + Nxa * j, dx) : z;
+            C2<T> ua_left = shfl_up_c<T>(ua, 1);
+            const bool c_pp = vi && cell_in(g, mt, i, j);
+            bool c_mp = __shfl_up_sync(full, c_pp, 1);
+            if (lane == 0) {
+                p_left = (vi && i > 0) ? cur[n - 1] : z;
+                ua_left = (vi && i > 0) ? link_factor<T, PRE_U>(A, U, (i - 1) + Nxa * j, dx) : z;
+                c_mp = vi && cell_in(g, mt, i - 1, j);
+            }
+            if (lane == 31) p_right = (vi && i + 1 < Nx) ? cur[n + 1] : z;
+            const C2<T> ub = (vi && j < g.Ny - 1) ? link_factor<T, PRE_U>(A, U, g.Na + i + Nx * j, dy) : z;
+            if (vi) {
+                const bool mm = c_mm, mp = c_mp, pm = c_pm, pp = c_pp;
+                const C2<T> p00 = p_c;
+                C2<T> out = z;
+                if (mm || mp || pm || pp) {
+                    C2<T> r = rhs[n];
+                    if (lang) {
+                        r.x += lc * T(rand_1<T>((uint32_t)n, rt) - 0.5);
+                        r.y += lc * T(rand_2<T>((uint32_t)n, rt) - 0.5);
+                    }
+                    const T eps = eps_sp ? eps_sp[n] : eps0;
+                    const bool rm0 = mm || mp, rp0 = pm || pp, r0m = mm || pm, r0p = mp || pp;
+                    C2<T> sx = z, sy = z;
+                    if (rm0) sx = cadd(sx, cmul(cconj(ua_left), p_left));
+                    if (rp0) sx = cadd(sx, cmul(ua, p_right));
+                    if (r0m) sy = cadd(sy, cmul(cconj(ub_down), p_prev));
+                    if (r0p) sy = cadd(sy, cmul(ub, p_next));
+                    const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
+                    const T diag = T(1) + dt * (r.x * r.x + r.y * r.y - eps + (idx2 * wx + idy2 * wy));
+                    const T inv = T(1) / diag;
+                    out.x = (r.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
+                    out.y = (r.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
                 }
-                const T eps = I.eps_sp ? ((const T*)I.eps_sp)[n] : (T)I.epsilon;
-                const bool rm0 = GL_MM(cb) || GL_MP(cb), rp0 = GL_PM(cb) || GL_PP(cb);
-                const bool r0m = GL_MM(cb) || GL_PM(cb), r0p = GL_MP(cb) || GL_PP(cb);
-                const T dx = (T)g.dx, dy = (T)g.dy;
-                const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy));
-                C2<T> sx = cmk<T>(T(0), T(0)), sy = cmk<T>(T(0), T(0));
-                if (PRE_U) {
-                    const C2<T>* __restrict__ Ul = (const C2<T>*)I.U;
-                    if (rm0) sx = cadd(sx, cmul(cconj(Ul[(i - 1) + (g.Nx - 1) * j]), cur[n - 1]));
-                    if (rp0) sx = cadd(sx, cmul(Ul[i + (g.Nx - 1) * j], cur[n + 1]));
-                    if (r0m) sy = cadd(sy, cmul(cconj(Ul[g.Na + i + g.Nx * (j - 1)]), cur[n - g.Nx]));
-                    if (r0p) sy = cadd(sy, cmul(Ul[g.Na + i + g.Nx * j], cur[n + g.Nx]));
-                } else {
-                    const T* __restrict__ A = (const T*)I.ab[s_RA];
-                    if (rm0) sx = cadd(sx, cmul(link_U<T>(-dx * A[(i - 1) + (g.Nx - 1) * j]), cur[n - 1]));
-                    if (rp0) sx = cadd(sx, cmul(link_U<T>(dx * A[i + (g.Nx - 1) * j]), cur[n + 1]));
-                    if (r0m) sy = cadd(sy, cmul(link_U<T>(-dy * A[g.Na + i + g.Nx * (j - 1)]), cur[n - g.Nx]));
-                    if (r0p) sy = cadd(sy, cmul(link_U<T>(dy * A[g.Na + i + g.Nx * j]), cur[n + g.Nx]));
+                nxt[n] = out;
+                const T dr = fabs(out.x - p00.x), di = fabs(out.y - p00.y);
+                T res = dr > di ? dr : di;
+                if (!(dr == dr) || !(di == di)) {  // NaN counts as 0, like the reference's int conversion
+                    wnan = true;
+                    res = (dr == dr) ? dr : ((di == di) ? di : T(0));
                 }
-                const T dt = (T)I.dt;
-                const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
-                const T diag = T(1) + dt * (r.x * r.x + r.y * r.y - eps + (idx2 * wx + idy2 * wy));
-                const T inv = T(1) / diag;
-                out.x = (r.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
-                out.y = (r.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
+                wmax = res > wmax ? res : wmax;
             }
-            nxt[n] = out;
-            T dr = fabs(out.x - p00.x), di = fabs(out.y - p00.y);
-            res = dr > di ? dr : di;
-            if (!(dr == dr) || !(di == di)) {  // NaN: counts as 0 like the reference's int conversion
-                nan = true;
-                res = (dr == dr) ? dr : ((di == di) ? di : T(0));
-            }
+            p_prev = p_c;
+            p_c = p_next;
+            ub_down = ub;
+            c_pm = c_pp;
+            c_mm = c_mp;
         }
-        T bmax = block_max_res<T>(res, nan);
-        if (tid == 0) {
-            if (bmax < T(0)) {
-                atomicOr(&st->nan_seen, 1);
-                bmax = -(bmax + T(1));
-            }
-            atomicMax(&st->res, res_bits(bmax));
-            __threadfence();
-            unsigned prev = atomicAdd(&st->blocks_done, 1u);
-            if (prev == (unsigned)I.ntiles - 1u) finish_instance<T>(I, loop, k, true);
-        }
+        ++count;
     }
-    if (tid == 0) {
+    if (cur_inst >= 0 && !done) warp_flush<T>(insts, cur_inst, k, wmax, wnan, count, loop);
+    __syncthreads();
+    if (threadIdx.x == 0) {
         __threadfence();
         unsigned gdone = atomicAdd(&loop->blocks_done, 1u);
         if (gdone == gridDim.x - 1u) finish_launch(loop, cond, use_cond);
@@ -384,8 +459,9 @@ __global__ void k_canonical_reset(const Inst* __restrict__ insts, int ninst) {
 struct TDLaunch {
     const Inst* insts;
     const Tile* tiles;
+    const Item* items;
     LoopState* loop;
-    int ninst, ntiles, dtype;
+    int ninst, ntiles, nitems, psi_grid, dtype;
     bool solveA, pre_u;
 };
 
@@ -464,8 +540,10 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         prev = nd;
         {
             cudaGraphNode_t sw;
-            void* a[] = {&insts, &tiles, &loop, &hpsi, &one};
-            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype), gt, bt, a));
+            Item const* items = L.items;
+            int nitems = L.nitems;
+            void* a[] = {&insts, &items, &nitems, &loop, &hpsi, &one};
+            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype), dim3(L.psi_grid), bt, a));
         }
         {
             void* a[] = {&insts, &ninst};
@@ -530,8 +608,8 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
             for (;;) {
                 for (int c = 0; c < chunk; ++c) {
                     if (part == 0) {
-                        if (L.dtype == 8) k_psi_sweep<double, true><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
-                        else k_psi_sweep<float, false><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
+                        if (L.dtype == 8) k_psi_sweep<double, true><<<L.psi_grid, kThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
+                        else k_psi_sweep<float, false><<<L.psi_grid, kThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
                     } else {
                         if (L.dtype == 8) k_A_sweep<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
                         else k_A_sweep<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
@@ -591,8 +669,8 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
         k_bench_prep<<<1, 32, 0, h->stream>>>(h->inst, 1, h->loop, 1);
         cudaEventRecord(e0, h->stream);
         if (which == 0) {
-            if (h->dtype == 8) k_psi_sweep<double, true><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
-            else k_psi_sweep<float, false><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+            if (h->dtype == 8) k_psi_sweep<double, true><<<h->psi_grid, kThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
+            else k_psi_sweep<float, false><<<h->psi_grid, kThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
         } else {
             if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
             else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
@@ -613,6 +691,19 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     return GLGPU_OK;
 }
 
+// CTAs of the persistent psi sweep: all SMs at full occupancy, or fewer if
+// there are fewer items than warps.
+int psi_sweep_grid(int dtype, int nitems) {
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void* fn = psi_sweep_fn(dtype);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    const int need = (nitems + kWarps - 1) / kWarps;
+    const int full = sms * per_sm;
+    return need < full ? (need > 0 ? need : 1) : full;
+}
+
 int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms) {
     if (eqn < 0 || eqn > 2 || Nt < 0) return set_error(h, GLGPU_E_ARG, "glgpu_td: bad eqn or Nt");
     const bool solveA = h->p.kappa > 0.0 && !std::isinf(h->p.kappa);
@@ -626,6 +717,7 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     }
     TDLaunch L;
     L.insts = h->inst; L.tiles = h->tiles; L.loop = h->loop; L.ninst = 1; L.ntiles = h->ntiles;
+    L.items = h->items; L.nitems = h->nitems; L.psi_grid = h->psi_grid;
     L.dtype = h->dtype; L.solveA = solveA; L.pre_u = (h->dtype == 8);
     int used_graph = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
