@@ -147,6 +147,21 @@ int glgpu_conjgrad_coef(glgpu_handle* h, const void* dpsi, const void* dab, doub
  *     (nv = 1, 5 or 17), out: nv sums. */
 int glgpu_reduce_sum(glgpu_handle* h, const double* x, int64_t n, int32_t nv, double* out);
 
+/* --- free energy of a caller-owned state with no allocation by the library.
+ *     No counterpart in the reference (its gsum allocates work arrays,
+ *     svirl/parallel/reduction.py:165-172).  For callers that must not let a
+ *     library call cudaMalloc (their own allocator or a fixed pre-sized arena owns
+ *     the device memory).  psi, ab, abei (nullable), mt (nullable) and energy
+ *     (one double) are DEVICE pointers on the current device; stream may be NULL.
+ *     Asynchronous: *energy is written when the stream reaches the kernel.  The
+ *     reduction scratch is a static 256 KB device array in the library (held by
+ *     every GPU that loads it until exit), so grids are limited to 8,388,608
+ *     nodes (larger ones: GLGPU_E_ARG).  The first call on a device looks the
+ *     array up (cudaGetSymbolAddress); make that first call before any stream
+ *     capture.  All calls share the array: calls that overlap on the GPU race. */
+int glgpu_free_energy_noalloc(const glgpu_grid* grid, const glgpu_params* params, const void* psi, const void* ab,
+                              const void* abei, const uint8_t* mt, double* energy, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

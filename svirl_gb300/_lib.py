@@ -74,6 +74,7 @@ _SIGNATURES = {
     "glgpu_jacobian": (C.c_int, [_H, _P, _P]),
     "glgpu_conjgrad_coef": (C.c_int, [_H, _P, _P, _P]),
     "glgpu_reduce_sum": (C.c_int, [_H, _P, C.c_int64, C.c_int32, _P]),
+    "glgpu_free_energy_noalloc": (C.c_int, [C.POINTER(Grid), C.POINTER(Params), _P, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

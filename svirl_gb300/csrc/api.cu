@@ -356,6 +356,11 @@ int glgpu_conjgrad_coef(glgpu_handle* h, const void* dpsi, const void* dab, doub
     return cg_coef_for(h, dpsi, dab, c);
 }
 
+int glgpu_free_energy_noalloc(const glgpu_grid* grid, const glgpu_params* params, const void* psi, const void* ab,
+                              const void* abei, const uint8_t* mt, double* energy, void* stream) {
+    return free_energy_noalloc(grid, params, psi, ab, abei, mt, energy, (cudaStream_t)stream);
+}
+
 int glgpu_reduce_sum(glgpu_handle* h, const double* x, int64_t n, int32_t nv, double* out) {
     if (check_handle(h)) return GLGPU_E_ARG;
     return reduce_sum(h, x, (long long)n, nv, out);

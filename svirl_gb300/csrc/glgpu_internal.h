@@ -143,6 +143,8 @@ int obs_current_density(glgpu_handle* h, void* host_out);
 int obs_supercurrent_density(glgpu_handle* h, void* host_out);
 int obs_vortex_candidates(glgpu_handle* h, int cap, int* n_out, int32_t* cells, void* corners);
 int reduce_sum(glgpu_handle* h, const double* x, long long n, int nv, double* out);
+int free_energy_noalloc(const glgpu_grid* grid, const glgpu_params* p, const void* psi, const void* ab,
+                        const void* abei, const uint8_t* mt, double* energy, cudaStream_t stream);
 // cg.cu
 int cg_ensure(glgpu_handle* h);
 int cg_reset_direction(glgpu_handle* h);

@@ -4,6 +4,9 @@
 //
 // Reference: svirl/cuda/observables.h:4-362, svirl/observables/observables.py:29-149,
 // svirl/observables/vortex_detector.py:31-72.
+#include <mutex>
+#include <string>
+
 #include "glgpu_internal.h"
 
 namespace glgpu {
@@ -225,6 +228,82 @@ k_vsum(const double* __restrict__ x, long long n, double* partials, unsigned* co
 // ---------------------------------------------------------------------------
 // host entry points
 // ---------------------------------------------------------------------------
+
+// ---------------------------------------------------------------------------
+// Free energy with no allocation by the library (glgpu_free_energy_noalloc).
+//
+// For callers that cannot let a library call cudaMalloc: a host process whose
+// own allocator owns the device memory (a framework's caching allocator, a
+// pre-sized arena under a fixed memory budget), or a plugin that must not
+// allocate behind its host's back.  The caller passes the state and the output
+// as device pointers; the reduction's scratch (one partial sum per CTA and the
+// last-CTA ticket counter) lives in the static array below, which every GPU that
+// loads libglgpu.so holds until the process exits: 32769 doubles = 256 KB + 8 B.
+// Grids up to kNoAllocMaxNodes nodes fit; larger grids are rejected.
+// ---------------------------------------------------------------------------
+constexpr long long kNoAllocMaxNodes = 1LL << 23;                       // 8,388,608 nodes
+constexpr int kNoAllocMaxBlocks = (int)(kNoAllocMaxNodes / kThreads);   // 32,768 CTAs
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxBlocks + 1];  // partials, then the counter
+
+// Device address of g_noalloc_scratch for each device (host code cannot use the
+// symbol itself: on the host it names a stand-in, not device memory).  Filled on
+// the first call made with that device current.
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_addr[256] = {nullptr};
+
+static double* noalloc_scratch(int dev, std::string* why) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (dev < 0 || dev >= 256) {
+        *why = "device ordinal out of range";
+        return nullptr;
+    }
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            *why = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+            return nullptr;
+        }
+        g_noalloc_addr[dev] = (double*)p;
+    }
+    return g_noalloc_addr[dev];
+}
+
+int free_energy_noalloc(const glgpu_grid* grid, const glgpu_params* p, const void* psi, const void* ab,
+                        const void* abei, const uint8_t* mt, double* energy, cudaStream_t stream) {
+    if (!grid || !p || !psi || !energy) return set_error(nullptr, GLGPU_E_ARG, "glgpu_free_energy_noalloc: NULL argument");
+    if (grid->Nx < 4 || grid->Ny < 4 || (grid->dtype != 4 && grid->dtype != 8) || !(grid->dx > 0.0) || !(grid->dy > 0.0))
+        return set_error(nullptr, GLGPU_E_ARG, "glgpu_free_energy_noalloc: bad grid (Nx, Ny >= 4, dtype 4 or 8, dx, dy > 0)");
+    const long long n = (long long)grid->Nx * grid->Ny;
+    if (n > kNoAllocMaxNodes)
+        return set_error(nullptr, GLGPU_E_ARG,
+                         "glgpu_free_energy_noalloc: " + std::to_string(n) + " nodes exceed the static scratch's maximum of " +
+                             std::to_string(kNoAllocMaxNodes) + " nodes; use glgpu_free_energy on a handle");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(nullptr, GLGPU_E_CUDA, std::string("glgpu_free_energy_noalloc: ") + cudaGetErrorString(e));
+    std::string why;
+    double* scratch = noalloc_scratch(dev, &why);
+    if (!scratch) return set_error(nullptr, GLGPU_E_CUDA, "glgpu_free_energy_noalloc: " + why);
+    unsigned* counter = (unsigned*)(scratch + kNoAllocMaxBlocks);
+    const Geo g = make_geo(grid->Nx, grid->Ny, grid->dx, grid->dy);
+    const bool finite = p->kappa > 0.0 && !std::isinf(p->kappa);
+    const double k2 = finite ? p->kappa * p->kappa : -1.0;
+    // the ticket counter must start at zero; the last call may have been interrupted
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned), stream);
+    if (e == cudaSuccess) {
+        const int nb = blocks_for(n);
+        if (grid->dtype == 8)
+            k_energy<double><<<nb, kThreads, 0, stream>>>(g, k2, p->epsilon, nullptr, p->H, mt, (const double2*)psi,
+                                                         (const double*)abei, (const double*)ab, scratch, counter, energy);
+        else
+            k_energy<float><<<nb, kThreads, 0, stream>>>(g, k2, p->epsilon, nullptr, p->H, mt, (const float2*)psi,
+                                                        (const float*)abei, (const float*)ab, scratch, counter, energy);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return set_error(nullptr, GLGPU_E_CUDA, std::string("glgpu_free_energy_noalloc: ") + cudaGetErrorString(e));
+    return GLGPU_OK;
+}
 
 int reduce_sum(glgpu_handle* h, const double* x, long long n, int nv, double* out) {
     if (!x || !out || n < 0 || !(nv == 1 || nv == 5 || nv == 17)) return set_error(h, GLGPU_E_ARG, "reduce_sum: bad arguments");
