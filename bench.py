@@ -231,6 +231,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, default=N_SIDE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="host-driven Jacobi loop (same kernels); ncu cannot profile kernels inside conditional graphs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -250,6 +252,8 @@ def main():
     dtype = np.float32 if args.dtype == "fp32" else np.float64
     gl = make_solver(args.size, dtype=dtype, seed=rank, device=local)
     h = gl._h
+    if args.no_graphs:
+        h.set_use_graphs(False)
     N = args.size * args.size
     h.td(DT, args.warmup, 0)
 
@@ -273,7 +277,8 @@ def main():
 
     # roofline of the dominant kernel (the psi Jacobi sweep), timed alone
     sweep_ms = h.time_sweeps(0, 20)
-    bytes_per_node = (32 if dtype == np.float32 else 64) + 1   # psi^(k), rhs, 2 links, write; +1 B mask
+    # per node: psi^(k), rhs, the two link factors of the step's table, write; +1 B link-weight code
+    bytes_per_node = (40 if dtype == np.float32 else 80) + 1
     alg_bytes = N * bytes_per_node
     peak, peak_kind = peaks()
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9

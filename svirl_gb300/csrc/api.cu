@@ -55,11 +55,22 @@ void upload_inst(glgpu_handle* h) {
     I.mt = h->mt;
     I.eps_sp = h->eps_sp;
     I.U = h->U;
+    I.code = h->code;
     I.st = h->st;
     I.tile0 = 0;
     I.ntiles = h->ntiles;
     I.nitems = h->nitems;
     I.solveA = finite_kappa(h->p) ? 1 : 0;
+    I.fepsilon = (float)I.epsilon;
+    I.fkappa2 = (float)I.kappa2;
+    I.frho = (float)I.rho;
+    I.fH = (float)I.H;
+    I.flang_psi = (float)I.lang_psi;
+    I.flang_A = (float)I.lang_A;
+    I.lang_psi_on = (h->dtype == 4 ? (double)I.flang_psi : I.lang_psi) > 1.0e-32 ? 1 : 0;
+    I.lang_A_on = (h->dtype == 4 ? (double)I.flang_A : I.lang_A) > 1.0e-32 ? 1 : 0;
+    I.dt = h->inst_h.dt;
+    I.fdt = (float)I.dt;
     h->inst_h = I;
     cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
 }
@@ -80,7 +91,7 @@ static void free_all(glgpu_handle* h) {
         if (h->dir_psi[q]) cudaFree(h->dir_psi[q]);
         if (h->dir_A[q]) cudaFree(h->dir_A[q]);
     }
-    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->st, h->inst, h->tiles, h->items, h->loop, h->partials, h->counter,
+    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->code, h->st, h->inst, h->tiles, h->items, h->loop, h->partials, h->counter,
                     h->dscal, h->out, h->vort, h->vort_n, h->flush};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -120,11 +131,12 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     const int nblk = blocks_for(h->g.N);
     bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int q = 0; q < 3 && ok; ++q) ok = cudaMalloc(&h->psi[q], npsi) == cudaSuccess && cudaMalloc(&h->ab[q], nab) == cudaSuccess;
-    if (ok && h->dtype == 8) ok = cudaMalloc(&h->U, (size_t)h->g.Nab * 16) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->U, (size_t)h->g.Nab * 2 * rs) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->code, (size_t)h->g.N) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->inst, sizeof(Inst)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->tiles, sizeof(Tile) * (size_t)h->ntiles) == cudaSuccess;
-    const int nstrips = (h->g.Nx + 31) / 32, nrows = (h->g.Ny + kStripRows - 1) / kStripRows;
+    const int nstrips = (h->g.Nx + kStripCols - 1) / kStripCols, nrows = (h->g.Ny + kStripRows - 1) / kStripRows;
     h->nitems = nstrips * nrows;
     ok = ok && cudaMalloc(&h->items, sizeof(Item) * (size_t)h->nitems) == cudaSuccess;
     ok = ok && cudaMalloc(&h->loop, sizeof(LoopState)) == cudaSuccess;
@@ -146,7 +158,7 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     std::vector<Item> items;
     items.reserve(h->nitems);
     for (int r = 0; r < nrows; ++r)
-        for (int s = 0; s < nstrips; ++s) items.push_back(Item{0, 32 * s, kStripRows * r, 0});
+        for (int s = 0; s < nstrips; ++s) items.push_back(Item{0, kStripCols * s, kStripRows * r, 0});
     h->psi_grid = psi_sweep_grid(h->dtype, h->nitems);
     InstState st;
     memset(&st, 0, sizeof(st));

@@ -43,8 +43,8 @@ template <typename T> __device__ __forceinline__ C2<T> gjac(C2<T> p0, T ph, C2<T
 template <typename T>
 __device__ __forceinline__ T curlcurl_grad(const Geo& g, const T* abei, const T* ab, T H, int i, int j, bool xdir) {
     const int Nxa = g.Nx - 1, Na = g.Na, Nx = g.Nx;
-    const T idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
-    const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy)), idxy = T(1.0 / (g.dx * g.dy));
+    const T idx = GT(g, idx), idy = GT(g, idy);
+    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
     T c = T(0), dd = T(1);
     if (xdir) {
         const int n = i + Nxa * j;
@@ -91,8 +91,8 @@ k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const ui
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, mt, i, j);
-        const T dx = (T)g.dx, dy = (T)g.dy, idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
-        const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy));
+        const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
+        const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
         const C2<T> p0 = psi[n];
         C2<T> gj = cmk<T>(T(0), T(0));
         if (cb) {
@@ -190,8 +190,8 @@ k_cg_dir_coef(Geo g, double kappa2, double eps0, const T* eps_sp, double H, cons
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, mt, i, j);
-        const T dx = (T)g.dx, dy = (T)g.dy, idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
-        const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy));
+        const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
+        const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
         const C2<T> d0 = dpsi(n);
         if (dir_mode) dN[n] = d0;
         if (NV == 17 && dir_mode) {
@@ -277,7 +277,7 @@ k_cg_dir_coef(Geo g, double kappa2, double eps0, const T* eps_sp, double H, cons
             }
         }
     }
-    grid_sum_finish<NV>(c, partials, counter, dscal, g.dx * g.dy);
+    grid_sum_finish<NV>(c, partials, counter, dscal, g.dxdy);
 }
 
 template <typename T>

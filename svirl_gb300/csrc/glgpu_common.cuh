@@ -79,19 +79,26 @@ __device__ __forceinline__ uint32_t rand_hash(uint32_t s) {
     s = s ^ (s >> 15);
     return s;
 }
+// 2^-32 * hash: the scale is a power of two, so the product in T is exact and
+// equals the reference's double product rounded to T.
 template <typename T> __device__ __forceinline__ T rand_1(uint32_t n, uint32_t t) {
-    return T(0.00000000023283064365386962890625 * T(rand_hash(71u * n + 9887u * t)));
+    return T(rand_hash(71u * n + 9887u * t)) * T(2.3283064365386962890625e-10);
 }
 template <typename T> __device__ __forceinline__ T rand_2(uint32_t n, uint32_t t) {
-    return T(0.00000000023283064365386962890625 * T(rand_hash(73u * n + 9901u * t + 1u)));
+    return T(rand_hash(73u * n + 9901u * t + 1u)) * T(2.3283064365386962890625e-10);
 }
 
 // ---------------------------------------------------------------------------
 // geometry
 // ---------------------------------------------------------------------------
+// Grid geometry with its derived constants precomputed on the host in double
+// and rounded once to float (as the reference bakes 1.0/(dx*dx) etc. into its
+// kernels at compile time): FP32 kernels then execute no FP64 instruction,
+// which matters on GB300 where the FP64 pipe is a small fraction of FP32.
 struct Geo {
     int Nx, Ny, Na, N, Nab, Nxc, Nyc;
-    double dx, dy;
+    double dx, dy, idx, idy, idx2, idy2, idxy, dxdy;
+    float fdx, fdy, fidx, fidy, fidx2, fidy2, fidxy, fdxdy;
 };
 
 __host__ __device__ inline Geo make_geo(int Nx, int Ny, double dx, double dy) {
@@ -99,8 +106,19 @@ __host__ __device__ inline Geo make_geo(int Nx, int Ny, double dx, double dy) {
     g.Nx = Nx; g.Ny = Ny; g.Na = (Nx - 1) * Ny; g.N = Nx * Ny;
     g.Nab = g.Na + Nx * (Ny - 1); g.Nxc = Nx - 1; g.Nyc = Ny - 1;
     g.dx = dx; g.dy = dy;
+    g.idx = 1.0 / dx; g.idy = 1.0 / dy;
+    g.idx2 = 1.0 / (dx * dx); g.idy2 = 1.0 / (dy * dy); g.idxy = 1.0 / (dx * dy);
+    g.dxdy = dx * dy;
+    g.fdx = (float)dx; g.fdy = (float)dy; g.fidx = (float)g.idx; g.fidy = (float)g.idy;
+    g.fidx2 = (float)g.idx2; g.fidy2 = (float)g.idy2; g.fidxy = (float)g.idxy; g.fdxdy = (float)g.dxdy;
     return g;
 }
+
+// The T-precision copy of a constant stored in both precisions.
+template <typename T> __host__ __device__ __forceinline__ T gsel(double d, float f);
+template <> __host__ __device__ __forceinline__ float gsel<float>(double, float f) { return f; }
+template <> __host__ __device__ __forceinline__ double gsel<double>(double d, float) { return d; }
+#define GT(g, name) gsel<T>((g).name, (g).f##name)
 
 // Cells around node (i, j): bit 0 = (i-1,j-1) "mm", 1 = (i-1,j) "mp",
 // 2 = (i,j-1) "pm", 3 = (i,j) "pp"; a bit is set when the cell exists and is in

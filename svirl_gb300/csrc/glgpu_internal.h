@@ -38,12 +38,15 @@ struct Inst {
     double dt, epsilon, kappa2, rho, H;
     double lang_psi, lang_A;
     double stop_psi, stop_A;
+    float fdt, fepsilon, fkappa2, frho, fH, flang_psi, flang_A, pad_f;  // the same, rounded to float
+    int lang_psi_on, lang_A_on;  // Langevin coefficient (in the solver's precision) > 1e-32 (td.h:147,451)
     void* psi[3];             // rotating TD buffers, psi[0] holds the state at rest
     void* ab[3];              // rotating TD buffers, ab[0] holds the state at rest
     const void* abei;         // external+irregular vector potential or NULL
     const uint8_t* mt;        // material tiling (cells) or NULL
     const void* eps_sp;       // spatial linear coefficient (nodes) or NULL
-    void* U;                  // FP64 link factors exp(-i d a), Nab complex
+    void* U;                  // link factors exp(-i d a) of the psi loop, Nab complex
+    uint8_t* code;            // per-node link-weight bits of the psi loop, N bytes
     InstState* st;
     int tile0, ntiles;        // this instance's range in the tile table
     int nitems;               // number of warp-strip items of this instance
@@ -69,9 +72,10 @@ struct Tile {
     int inst, n0;
 };
 
-// Work item of the warp-strip psi sweep: 32 columns (x0..x0+31) by kStripRows
-// rows (j0..) of one instance, processed by one warp.
+// Work item of the warp-strip psi sweep: kStripCols output columns (x0..) by
+// kStripRows rows (j0..) of one instance, processed by one warp.
 constexpr int kStripRows = 8;
+constexpr int kStripCols = 30;
 struct Item {
     int inst, x0, j0, pad;
 };
@@ -92,6 +96,7 @@ struct glgpu_handle {
     uint8_t* mt = nullptr;
     void* eps_sp = nullptr;
     void* U = nullptr;
+    uint8_t* code = nullptr;
     glgpu::InstState* st = nullptr;
     glgpu::Inst* inst = nullptr;        // device copy of the descriptor
     glgpu::Inst inst_h;                 // host copy of the descriptor

@@ -47,8 +47,8 @@ __device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, cons
                                             const uint8_t* mt, const C2<T>* psi, const T* abei, const T* ab, int n) {
     const int i = n % g.Nx, j = n / g.Nx;
     const unsigned cb = cell_bits(g, mt, i, j);
-    const T dx = (T)g.dx, dy = (T)g.dy, idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
-    const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy));
+    const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
+    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
     T e = T(0);
     if (cb) {
         const DuW<T> w = du_weights<T>(cb);
@@ -81,7 +81,7 @@ k_energy(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const uin
     const int n = blockIdx.x * kThreads + threadIdx.x;
     double v[1] = {0.0};
     if (n < g.N) v[0] = (double)energy_density<T>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, mt, psi, abei, ab, n);
-    grid_sum_finish<1>(v, partials, counter, out, g.dx * g.dy);
+    grid_sum_finish<1>(v, partials, counter, out, g.dxdy);
 }
 
 template <typename T>
@@ -90,7 +90,7 @@ k_magnetic_field(Geo g, const T* abei, const T* ab, T* B) {
     const int n = blockIdx.x * kThreads + threadIdx.x;
     if (n >= g.Nxc * g.Nyc) return;
     const int i = n % g.Nxc, j = n / g.Nxc;
-    const T idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
+    const T idx = GT(g, idx), idy = GT(g, idy);
     T b = T(0);
     if (abei) b += cell_curl(g, abei, i, j, idx, idy);
     if (ab) b += cell_curl(g, ab, i, j, idx, idy);
@@ -104,8 +104,8 @@ k_magnetic_field(Geo g, const T* abei, const T* ab, T* B) {
 template <typename T>
 __device__ __forceinline__ T curlcurl_link(const Geo& g, const T* abei, const T* ab, T H, int i, int j, bool xdir) {
     const int Nxa = g.Nx - 1, Na = g.Na, Nx = g.Nx;
-    const T idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
-    const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy)), idxy = T(1.0 / (g.dx * g.dy));
+    const T idx = GT(g, idx), idy = GT(g, idy);
+    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
     T c = T(0), dd = T(1);
     if (xdir) {
         const int n = i + Nxa * j;
@@ -162,7 +162,7 @@ k_supercurrent_density(Geo g, const uint8_t* mt, const C2<T>* __restrict__ psi, 
         T jl = T(0);
         if (GL_PM(cb) || GL_PP(cb)) {
             const T r = T(0.5) * ((GL_PM(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));
-            jl = r * T(1.0 / g.dx) * js_of<T>(p0, (T)g.dx * link_phase(abei, ab, na), psi[n + 1]);
+            jl = r * GT(g, idx) * js_of<T>(p0, GT(g, dx) * link_phase(abei, ab, na), psi[n + 1]);
         }
         out[na] = jl;
     }
@@ -171,7 +171,7 @@ k_supercurrent_density(Geo g, const uint8_t* mt, const C2<T>* __restrict__ psi, 
         T jl = T(0);
         if (GL_MP(cb) || GL_PP(cb)) {
             const T r = T(0.5) * ((GL_MP(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));
-            jl = r * T(1.0 / g.dy) * js_of<T>(p0, (T)g.dy * link_phase(abei, ab, nb), psi[n + g.Nx]);
+            jl = r * GT(g, idy) * js_of<T>(p0, GT(g, dy) * link_phase(abei, ab, nb), psi[n + g.Nx]);
         }
         out[nb] = jl;
     }

@@ -116,33 +116,20 @@ template <typename T> __device__ __forceinline__ C2<T> shfl_down_c(C2<T> v, int 
     return cmk<T>(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
 }
 
-// Link factor exp(-i d a) of link index l: evaluated in place (FP32) or read
-// from the per-step table (FP64).
-template <typename T, bool PRE_U>
-__device__ __forceinline__ C2<T> link_factor(const T* A, const C2<T>* U, int l, T d) {
-    if (PRE_U) return U[l];
-    return link_U<T>(d * A[l]);
-}
-
-__device__ __forceinline__ bool cell_in(const Geo& g, const uint8_t* mt, int ci, int cj) {
-    if (ci < 0 || cj < 0 || ci >= g.Nxc || cj >= g.Nyc) return false;
-    return mt == nullptr || mt[ci + g.Nxc * cj] != 0;
-}
-
 // One Jacobi sweep of the psi step (svirl/cuda/td.h:4-133, Winecki-Adams link
-// weights td.h:159-163) over every active instance.  A warp owns a strip of 32
-// columns and kStripRows rows: it walks down the rows keeping psi(j-1), psi(j),
-// psi(j+1), the y link below and the cells below in registers, and takes the
-// x neighbours, the x link on the left and the cell on the left from the
-// neighbouring lane, so each node loads psi, rhs, its two links and its cell
-// once and evaluates one x-link and one y-link factor.  Persistent grid: warps
-// stride over the item table.  PRE_U: link factors from the per-step table
-// (FP64); otherwise evaluated in place (FP32).
-template <typename T, bool PRE_U>
+// weights td.h:159-163) over every active instance, reading the per-step tables
+// of k_link_U (link factors U and link-weight codes), so the sweep itself does no
+// transcendental math and no mask logic.  A warp owns a strip of kStripCols = 30
+// output columns plus one halo column on each side (lanes 0 and 31) and
+// kStripRows rows: it walks down the rows keeping psi(j-1), psi(j), psi(j+1) and
+// the y link below in registers and takes the x neighbours and the x link on its
+// left from the adjacent lanes, so each node loads psi, rhs, its two link factors
+// and its code once.  The row walk is unrolled with every load issued ahead of
+// its use.  Persistent grid: warps stride over the item table.
+template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
             cudaGraphConditionalHandle cond, int use_cond) {
-    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
     int cur_inst = -1, k = 0, count = 0, done = 1;
@@ -152,8 +139,8 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
     const C2<T>* cur = nullptr;
     const C2<T>* rhs = nullptr;
     C2<T>* nxt = nullptr;
-    const T* A = nullptr;
     const C2<T>* U = nullptr;
+    const uint8_t* code = nullptr;
     uint32_t rt = 0;
     for (int it = gw; it < nitems; it += nw) {
         const Item w = items[it];
@@ -163,14 +150,14 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             const InstState* st = insts[cur_inst].st;
             done = *(volatile const int*)&st->done;
             k = *(volatile const int*)&st->sweep;
-            const int R = *(volatile const int*)&st->rhs, RA = *(volatile const int*)&st->rhsA;
+            const int R = *(volatile const int*)&st->rhs;
             rt = *(volatile const uint32_t*)&st->rand_t;
             const Inst& I = insts[cur_inst];
             cur = (const C2<T>*)I.psi[buf_of(R, k)];
             rhs = (const C2<T>*)I.psi[R];
             nxt = (C2<T>*)I.psi[(R + 1 + (k & 1)) % 3];
-            A = (const T*)I.ab[RA];
             U = (const C2<T>*)I.U;
+            code = I.code;
             wmax = T(0);
             wnan = false;
             count = 0;
@@ -178,64 +165,77 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
         if (done) continue;
         const Inst& I = insts[cur_inst];
         const Geo g = I.g;
-        const uint8_t* mt = I.mt;
         const T* eps_sp = (const T*)I.eps_sp;
-        const T dt = (T)I.dt, eps0 = (T)I.epsilon, dx = (T)g.dx, dy = (T)g.dy;
-        const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy));
-        const bool lang = I.lang_psi > 1.0e-32;
-        const T lc = (T)I.lang_psi;
-        const int Nx = g.Nx, Nxa = g.Nx - 1;
-        const int i = w.x0 + lane;
-        const bool vi = i < Nx;
-        const int j0 = w.j0, jend = min(j0 + kStripRows, g.Ny);
+        const T dt = gsel<T>(I.dt, I.fdt), eps0 = gsel<T>(I.epsilon, I.fepsilon);
+        const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
+        const bool lang = I.lang_psi_on != 0;
+        const T lc = gsel<T>(I.lang_psi, I.flang_psi);
+        const int Nx = g.Nx, Ny = g.Ny, Nxa = g.Nx - 1, Na = g.Na;
+        // lane L holds column x0 - 1 + L: lanes 0 and 31 only supply the neighbours
+        // (halo lanes), lanes 1..30 produce the strip's 30 output columns
+        const int i = w.x0 - 1 + lane;
+        const bool in_x = i >= 0 && i < Nx;
+        const bool out_lane = lane >= 1 && lane <= 30 && in_x;
+        const int j0 = w.j0;
         const C2<T> z = cmk<T>(T(0), T(0));
-        // state carried down the strip
-        C2<T> p_prev = (vi && j0 > 0) ? cur[i + Nx * (j0 - 1)] : z;
-        C2<T> p_c = vi ? cur[i + Nx * j0] : z;
-        C2<T> ub_down = (vi && j0 > 0 && j0 - 1 < g.Ny - 1) ? link_factor<T, PRE_U>(A, U, g.Na + i + Nx * (j0 - 1), dy) : z;
-        bool c_pm = vi && cell_in(g, mt, i, j0 - 1);       // cell (i, j-1)
-        bool c_mm = vi && cell_in(g, mt, i - 1, j0 - 1);   // cell (i-1, j-1)
-        for (int j = j0; j < jend; ++j) {
+        C2<T> p_prev = (in_x && j0 > 0) ? __ldg(&cur[i + Nx * (j0 - 1)]) : z;
+        C2<T> p_c = in_x ? __ldg(&cur[i + Nx * j0]) : z;
+        C2<T> ub_down = (out_lane && j0 > 0) ? __ldg(&U[Na + i + Nx * (j0 - 1)]) : z;
+        // software pipeline: the loads of row r+1 are issued before row r is computed
+        struct Row {
+            C2<T> p_next, ua, ub, rr;
+            T eps;
+            unsigned cd;
+        };
+        auto load_row = [&](int r) -> Row {
+            Row q;
+            const int j = j0 + r;
             const int n = i + Nx * j;
-            const C2<T> p_next = (vi && j + 1 < g.Ny) ? cur[n + Nx] : z;
-            // x neighbours and x links from the neighbouring lanes
-            C2<T> p_left = shfl_up_c<T>(p_c, 1), p_right = shfl_down_c<T>(p_c, 1);
-            const C2<T> ua = (vi && i < Nx - 1) ? link_factor<T, PRE_U>(A, U, i + Nxa * j, dx) : z;
-            C2<T> ua_left = shfl_up_c<T>(ua, 1);
-            const bool c_pp = vi && cell_in(g, mt, i, j);
-            bool c_mp = __shfl_up_sync(full, c_pp, 1);
-            if (lane == 0) {
-                p_left = (vi && i > 0) ? cur[n - 1] : z;
-                ua_left = (vi && i > 0) ? link_factor<T, PRE_U>(A, U, (i - 1) + Nxa * j, dx) : z;
-                c_mp = vi && cell_in(g, mt, i - 1, j);
-            }
-            if (lane == 31) p_right = (vi && i + 1 < Nx) ? cur[n + 1] : z;
-            const C2<T> ub = (vi && j < g.Ny - 1) ? link_factor<T, PRE_U>(A, U, g.Na + i + Nx * j, dy) : z;
-            if (vi) {
-                const bool mm = c_mm, mp = c_mp, pm = c_pm, pp = c_pp;
-                const C2<T> p00 = p_c;
+            const bool ld = in_x && j < Ny, ldo = out_lane && j < Ny;
+            q.p_next = (ld && j + 1 < Ny) ? __ldg(&cur[n + Nx]) : z;
+            q.ua = (ld && i < Nx - 1) ? __ldg(&U[i + Nxa * j]) : z;
+            q.ub = (ldo && j < Ny - 1) ? __ldg(&U[Na + n]) : z;
+            q.cd = ldo ? (unsigned)__ldg(&code[n]) : 0u;
+            q.rr = ldo ? __ldg(&rhs[n]) : z;
+            q.eps = (ldo && eps_sp) ? __ldg(&eps_sp[n]) : eps0;
+            return q;
+        };
+        Row nx = load_row(0);
+#pragma unroll
+        for (int r = 0; r < kStripRows; ++r) {
+            const Row cu = nx;
+            if (r + 1 < kStripRows) nx = load_row(r + 1);
+            const int j = j0 + r;
+            const int n = i + Nx * j;
+            const bool ldo = out_lane && j < Ny;
+            const C2<T> p_next = cu.p_next, ua = cu.ua, ub = cu.ub, rr = cu.rr;
+            const unsigned cd = cu.cd;
+            const T eps = cu.eps;
+            // x neighbours and the x link on the left from the adjacent lanes
+            const C2<T> p_left = shfl_up_c<T>(p_c, 1), p_right = shfl_down_c<T>(p_c, 1);
+            const C2<T> ua_left = shfl_up_c<T>(ua, 1);
+            if (ldo) {
                 C2<T> out = z;
-                if (mm || mp || pm || pp) {
-                    C2<T> r = rhs[n];
+                if (cd & 3u) {  // a node with a material cell has a left or a right link
+                    C2<T> rq = rr;
                     if (lang) {
-                        r.x += lc * T(rand_1<T>((uint32_t)n, rt) - 0.5);
-                        r.y += lc * T(rand_2<T>((uint32_t)n, rt) - 0.5);
+                        rq.x += lc * (rand_1<T>((uint32_t)n, rt) - T(0.5));
+                        rq.y += lc * (rand_2<T>((uint32_t)n, rt) - T(0.5));
                     }
-                    const T eps = eps_sp ? eps_sp[n] : eps0;
-                    const bool rm0 = mm || mp, rp0 = pm || pp, r0m = mm || pm, r0p = mp || pp;
+                    const bool rm0 = cd & 1u, rp0 = cd & 2u, r0m = cd & 4u, r0p = cd & 8u;
                     C2<T> sx = z, sy = z;
                     if (rm0) sx = cadd(sx, cmul(cconj(ua_left), p_left));
                     if (rp0) sx = cadd(sx, cmul(ua, p_right));
                     if (r0m) sy = cadd(sy, cmul(cconj(ub_down), p_prev));
                     if (r0p) sy = cadd(sy, cmul(ub, p_next));
                     const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
-                    const T diag = T(1) + dt * (r.x * r.x + r.y * r.y - eps + (idx2 * wx + idy2 * wy));
+                    const T diag = T(1) + dt * (rq.x * rq.x + rq.y * rq.y - eps + (idx2 * wx + idy2 * wy));
                     const T inv = T(1) / diag;
-                    out.x = (r.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
-                    out.y = (r.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
+                    out.x = (rq.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
+                    out.y = (rq.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
                 }
                 nxt[n] = out;
-                const T dr = fabs(out.x - p00.x), di = fabs(out.y - p00.y);
+                const T dr = fabs(out.x - p_c.x), di = fabs(out.y - p_c.y);
                 T res = dr > di ? dr : di;
                 if (!(dr == dr) || !(di == di)) {  // NaN counts as 0, like the reference's int conversion
                     wnan = true;
@@ -246,8 +246,6 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             p_prev = p_c;
             p_c = p_next;
             ub_down = ub;
-            c_pm = c_pp;
-            c_mm = c_mp;
         }
         ++count;
     }
@@ -301,18 +299,18 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
             const T ph_b = has_b ? abi[nb] : T(0);
             const unsigned cb = cell_bits(g, I.mt, i, j);
             const C2<T> psi0 = psi[n];
-            const T dx = (T)g.dx, dy = (T)g.dy;
-            const T idx = T(1.0 / g.dx), idy = T(1.0 / g.dy);
-            const T idx2 = T(1.0 / (g.dx * g.dx)), idy2 = T(1.0 / (g.dy * g.dy)), idxy = T(1.0 / (g.dx * g.dy));
-            const T k2 = (T)I.kappa2, H = (T)I.H;
-            const T dt_rho = (T)I.dt * (T)I.rho;
+            const T dx = GT(g, dx), dy = GT(g, dy);
+            const T idx = GT(g, idx), idy = GT(g, idy);
+            const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
+            const T k2 = gsel<T>(I.kappa2, I.fkappa2), H = gsel<T>(I.H, I.fH);
+            const T dt_rho = gsel<T>(I.dt, I.fdt) * gsel<T>(I.rho, I.frho);
             const T dt_rho_k2 = dt_rho * k2;
-            const T lc = (T)I.lang_A;
-            const bool lang = I.lang_A > 1.0e-32;
+            const T lc = gsel<T>(I.lang_A, I.flang_A);
+            const bool lang = I.lang_A_on != 0;
             T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
             if (has_a) {
                 T r = rhs[na];
-                if (lang) r += lc * T(rand_1<T>((uint32_t)na, s_rt) - 0.5);
+                if (lang) r += lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5));
                 T rh = T(0), dd = T(1);
                 if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
                 else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
@@ -326,7 +324,7 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
             }
             if (has_b) {
                 T r = rhs[nb];
-                if (lang) r += lc * T(rand_2<T>((uint32_t)nb, s_rt) - 0.5);
+                if (lang) r += lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5));
                 T rh = T(0), dd = T(1);
                 if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
                 else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
@@ -368,8 +366,10 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
     }
 }
 
-// FP64 link factors U = exp(-i d a) of the current A, once per time step
-// (A is fixed during the psi Jacobi loop).
+// Per-step tables of the psi Jacobi loop, during which A is fixed: the link
+// factors U = exp(-i d a) of the current A, and per node the Winecki-Adams
+// link weights as a bit code (bit 0: left link r_m0, 1: right r_p0, 2: lower
+// r_0m, 3: upper r_0p; a node is updated iff it has a left or a right link).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
@@ -379,15 +379,19 @@ k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
     const int n = t.n0 + threadIdx.x;
     if (n >= g.N) return;
     const int i = n % g.Nx, j = n / g.Nx;
+    const unsigned cb = cell_bits(g, I.mt, i, j);
+    const unsigned rm0 = (GL_MM(cb) || GL_MP(cb)) ? 1u : 0u, rp0 = (GL_PM(cb) || GL_PP(cb)) ? 1u : 0u;
+    const unsigned r0m = (GL_MM(cb) || GL_PM(cb)) ? 1u : 0u, r0p = (GL_MP(cb) || GL_PP(cb)) ? 1u : 0u;
+    I.code[n] = (uint8_t)(rm0 | (rp0 << 1) | (r0m << 2) | (r0p << 3));
     const T* A = (const T*)I.ab[*(volatile int*)&I.st->rhsA];
     C2<T>* U = (C2<T>*)I.U;
     if (i < g.Nx - 1) {
         int na = i + (g.Nx - 1) * j;
-        U[na] = link_U<T>((T)g.dx * A[na]);
+        U[na] = link_U<T>(GT(g, dx) * A[na]);
     }
     if (j < g.Ny - 1) {
         int nb = g.Na + i + g.Nx * j;
-        U[nb] = link_U<T>((T)g.dy * A[nb]);
+        U[nb] = link_U<T>(GT(g, dy) * A[nb]);
     }
 }
 
@@ -466,7 +470,7 @@ struct TDLaunch {
 };
 
 static void* psi_sweep_fn(int dtype) {
-    return dtype == 8 ? (void*)k_psi_sweep<double, true> : (void*)k_psi_sweep<float, false>;
+    return dtype == 8 ? (void*)k_psi_sweep<double> : (void*)k_psi_sweep<float>;
 }
 static void* A_sweep_fn(int dtype) {
     return dtype == 8 ? (void*)k_A_sweep<double> : (void*)k_A_sweep<float>;
@@ -521,14 +525,14 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
     GCHK(cudaGraphConditionalHandleCreate(&hout, top, 1, cudaGraphCondAssignDefault));
     if (do_psi && L.pre_u && !L.solveA) {
         void* a[] = {&insts, &tiles};
-        GCHK(add_kernel(top, &n_pre, nullptr, 0, (void*)k_link_U<double>, gt, bt, a));
+        GCHK(add_kernel(top, &n_pre, nullptr, 0, (L.dtype == 8 ? (void*)k_link_U<double> : (void*)k_link_U<float>), gt, bt, a));
     }
     GCHK(add_while(top, &n_out, n_pre ? &n_pre : nullptr, n_pre ? 1 : 0, hout, &obody));
     if (do_psi) {
         GCHK(cudaGraphConditionalHandleCreate(&hpsi, obody, 1, cudaGraphCondAssignDefault));
         if (L.pre_u && L.solveA) {
             void* a[] = {&insts, &tiles};
-            GCHK(add_kernel(obody, &nd, nullptr, 0, (void*)k_link_U<double>, gt, bt, a));
+            GCHK(add_kernel(obody, &nd, nullptr, 0, (L.dtype == 8 ? (void*)k_link_U<double> : (void*)k_link_U<float>), gt, bt, a));
             prev = nd;
         }
         {
@@ -591,6 +595,11 @@ fail:
     return err;
 }
 
+static void launch_link_U(const TDLaunch& L, cudaStream_t s) {
+    if (L.dtype == 8) k_link_U<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    else k_link_U<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+}
+
 // Host-driven fallback: the same kernels, the loop decided on the host after
 // each chunk of sweeps (sweeps of finished instances are no-ops).
 static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_t s) {
@@ -598,18 +607,18 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
     const int chunk = 4;
     cudaGraphConditionalHandle none = 0;
     int cont = 1;
-    if (do_psi && L.pre_u && !L.solveA) k_link_U<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    if (do_psi && !L.solveA) launch_link_U(L, s);
     for (int step = 0; step < Nt; ++step) {
         for (int part = 0; part < 2; ++part) {
             if (part == 0 && !do_psi) continue;
             if (part == 1 && !do_A) continue;
-            if (part == 0 && L.pre_u && L.solveA) k_link_U<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+            if (part == 0 && L.solveA) launch_link_U(L, s);
             k_loop_begin<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0);
             for (;;) {
                 for (int c = 0; c < chunk; ++c) {
                     if (part == 0) {
-                        if (L.dtype == 8) k_psi_sweep<double, true><<<L.psi_grid, kThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
-                        else k_psi_sweep<float, false><<<L.psi_grid, kThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
+                        if (L.dtype == 8) k_psi_sweep<double><<<L.psi_grid, kThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
+                        else k_psi_sweep<float><<<L.psi_grid, kThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
                     } else {
                         if (L.dtype == 8) k_A_sweep<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
                         else k_A_sweep<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
@@ -656,6 +665,7 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     const size_t flush_bytes = (size_t)256 << 20;  // > 129 MB of L2
     if (!h->flush && cudaMalloc(&h->flush, flush_bytes) != cudaSuccess) return set_error(h, GLGPU_E_OOM, "time_sweeps: flush buffer");
     h->inst_h.dt = h->inst_h.dt > 0.0 ? h->inst_h.dt : 0.1;
+    h->inst_h.fdt = (float)h->inst_h.dt;
     cudaError_t e = cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return cuda_check(h, e, "time_sweeps");
     cudaEvent_t e0, e1;
@@ -663,14 +673,15 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     cudaEventCreate(&e1);
     cudaGraphConditionalHandle none = 0;
     if (h->dtype == 8) k_link_U<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles);
+    else k_link_U<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles);
     double total = 0.0;
     for (int r = 0; r < nrep && e == cudaSuccess; ++r) {
         cudaMemsetAsync(h->flush, r & 0xff, flush_bytes, h->stream);
         k_bench_prep<<<1, 32, 0, h->stream>>>(h->inst, 1, h->loop, 1);
         cudaEventRecord(e0, h->stream);
         if (which == 0) {
-            if (h->dtype == 8) k_psi_sweep<double, true><<<h->psi_grid, kThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
-            else k_psi_sweep<float, false><<<h->psi_grid, kThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
+            if (h->dtype == 8) k_psi_sweep<double><<<h->psi_grid, kThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
+            else k_psi_sweep<float><<<h->psi_grid, kThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
         } else {
             if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
             else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
@@ -712,13 +723,14 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
         cudaError_t e = cudaMemsetAsync(&h->st->nan_seen, 0, offsetof(InstState, pad_) - offsetof(InstState, nan_seen), h->stream);
         if (e != cudaSuccess) return cuda_check(h, e, "td: reset counters");
         h->inst_h.dt = dt;
+        h->inst_h.fdt = (float)dt;
         e = cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
         if (e != cudaSuccess) return cuda_check(h, e, "td: write descriptor");
     }
     TDLaunch L;
     L.insts = h->inst; L.tiles = h->tiles; L.loop = h->loop; L.ninst = 1; L.ntiles = h->ntiles;
     L.items = h->items; L.nitems = h->nitems; L.psi_grid = h->psi_grid;
-    L.dtype = h->dtype; L.solveA = solveA; L.pre_u = (h->dtype == 8);
+    L.dtype = h->dtype; L.solveA = solveA; L.pre_u = true;
     int used_graph = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (elapsed_ms) {
