@@ -147,6 +147,19 @@ int glgpu_conjgrad_coef(glgpu_handle* h, const void* dpsi, const void* dab, doub
  *     (nv = 1, 5 or 17), out: nv sums. */
 int glgpu_reduce_sum(glgpu_handle* h, const double* x, int64_t n, int32_t nv, double* out);
 
+/* --- batches: several instances (any sizes and parameters; one dtype, one
+ *     device) advanced by one device-side TD loop.  No counterpart in the
+ *     reference, which runs one solver per process (svirl/config.py); each
+ *     instance follows TD._solve (svirl/solvers/td.py:342-377) with its own
+ *     Jacobi stop rule, exactly as if it ran alone.  The batch references the
+ *     handles (it does not own them); their state is read and written in place. */
+typedef struct glgpu_batch glgpu_batch;
+int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** out);
+int glgpu_batch_destroy(glgpu_batch* b);
+const char* glgpu_batch_last_error(const glgpu_batch* b);
+int glgpu_batch_td(glgpu_batch* b, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats, double* elapsed_ms);
+int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable);
+
 /* --- free energy of a caller-owned state with no allocation by the library.
  *     No counterpart in the reference (its gsum allocates work arrays,
  *     svirl/parallel/reduction.py:165-172).  For callers that must not let a

@@ -75,6 +75,11 @@ _SIGNATURES = {
     "glgpu_conjgrad_coef": (C.c_int, [_H, _P, _P, _P]),
     "glgpu_reduce_sum": (C.c_int, [_H, _P, C.c_int64, C.c_int32, _P]),
     "glgpu_free_energy_noalloc": (C.c_int, [C.POINTER(Grid), C.POINTER(Params), _P, _P, _P, _P, _P, _P]),
+    "glgpu_batch_create": (C.c_int, [C.POINTER(_H), C.c_int32, C.POINTER(_H)]),
+    "glgpu_batch_destroy": (C.c_int, [_H]),
+    "glgpu_batch_last_error": (C.c_char_p, [_H]),
+    "glgpu_batch_td": (C.c_int, [_H, C.c_double, C.c_int32, C.c_int32, C.POINTER(TDStats), C.POINTER(C.c_double)]),
+    "glgpu_batch_set_use_graphs": (C.c_int, [_H, C.c_int32]),
 }
 
 _lib = None

@@ -1,0 +1,93 @@
+"""Batched engine: many GL instances of uneven sizes advanced together on one GPU.
+
+    from svirl_gb300 import GLSolver
+    from svirl_gb300.batch import GLBatch
+    solvers = [GLSolver(...), GLSolver(...), ...]      # any sizes / parameters, one dtype
+    batch = GLBatch(solvers)
+    stats = batch.td(dt=0.1, Nt=2000)                  # one device-side loop for all
+    batch.cg(n_iter=1000, gtol=1e-8)                   # device CG, every instance at once
+
+The TD call runs every instance's time loop and Jacobi loops inside one CUDA
+graph launch: one sweep launch covers all instances (concatenated item tables,
+per-instance descriptors), each instance keeps the reference's own Jacobi stop
+rule and buffer bookkeeping, so each ends in exactly the state it reaches when
+run alone.  The reference has no batched mode (one solver per process).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+
+class GLBatch:
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        if not self.solvers:
+            raise ValueError("GLBatch needs at least one solver")
+        dt = {s.cfg.dtype for s in self.solvers}
+        if len(dt) != 1:
+            raise ValueError("all solvers of a batch must have the same dtype")
+        self.lib = _lib.load()
+        n = len(self.solvers)
+        arr = (C.c_void_p * n)(*[s._h.h.value for s in self.solvers])
+        b = C.c_void_p()
+        rc = self.lib.glgpu_batch_create(arr, n, C.byref(b))
+        if rc != 0:
+            raise _lib.GLGPUError("glgpu_batch_create failed (%d): %s" % (rc, self.lib.glgpu_last_error(None).decode()))
+        self.b = b
+        self.last_stats = None
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.glgpu_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc == 0:
+            return
+        msg = self.lib.glgpu_batch_last_error(self.b)
+        msg = msg.decode() if msg else ""
+        if rc == _lib.GLGPU_E_NAN:
+            import warnings
+            warnings.warn("glgpu: %s: %s" % (what, msg), RuntimeWarning, stacklevel=3)
+            return
+        raise _lib.GLGPUError("glgpu error %d in %s: %s" % (rc, what, msg))
+
+    def set_use_graphs(self, enable):
+        self._check(self.lib.glgpu_batch_set_use_graphs(self.b, 1 if enable else 0), "set_use_graphs")
+
+    def td(self, dt=0.1, Nt=1000, eqn=None, timed=False):
+        """``solve.td(dt, Nt, eqn=eqn)`` of every solver, in one device loop."""
+        code = {None: 0, "order_parameter": 1, "vector_potential": 2}[eqn]
+        for s in self.solvers:
+            s.solve._init_td()
+            td = s.solve._td
+            if eqn in (None, "order_parameter"):
+                td._set_iterator_options("order_parameter", Nt, dt, None)
+            if eqn in (None, "vector_potential"):
+                td._set_iterator_options("vector_potential", Nt, dt, None)
+            if eqn == "vector_potential" and td.dt is None:
+                raise TypeError("vector-potential steps use the order-parameter dt, which is not set yet")
+        dt_used = self.solvers[0].solve._td.dt
+        st = _lib.TDStats()
+        ms = C.c_double()
+        self._check(self.lib.glgpu_batch_td(self.b, float(dt_used), int(Nt), code, C.byref(st), C.byref(ms)), "batch_td")
+        for s in self.solvers:
+            s.solve.vortices_detected = False
+        self.last_stats = st
+        return (st, ms.value) if timed else st
+
+    def free_energies(self):
+        return np.array([s.observables.free_energy for s in self.solvers])
+
+    def cg(self, n_iter=1000, **kw):
+        """``solve.cg(n_iter)`` of every solver (reference algorithm, host line search)."""
+        for s in self.solvers:
+            s.solve.cg(n_iter=n_iter)

@@ -27,6 +27,11 @@ int cuda_check(glgpu_handle* h, cudaError_t e, const char* what) {
 
 size_t real_size(const glgpu_handle* h) { return (size_t)h->dtype; }
 
+int batch_error(glgpu_batch* b, int code, const std::string& msg) {
+    if (b) b->last_error = msg;
+    return code;
+}
+
 static bool finite_kappa(const glgpu_params& p) { return p.kappa > 0.0 && !std::isinf(p.kappa); }
 
 void upload_inst(glgpu_handle* h) {
@@ -83,8 +88,10 @@ static void free_all(glgpu_handle* h) {
     for (int q = 0; q < 3; ++q) {
         if (h->psi[q]) cudaFree(h->psi[q]);
         if (h->ab[q]) cudaFree(h->ab[q]);
-        if (h->td_exec[q]) cudaGraphExecDestroy(h->td_exec[q]);
     }
+    for (int q = 0; q < 6; ++q)
+        if (h->td_exec[q]) cudaGraphExecDestroy(h->td_exec[q]);
+    if (h->st_gather) cudaFree(h->st_gather);
     for (int q = 0; q < 2; ++q) {
         if (h->g_psi[q]) cudaFree(h->g_psi[q]);
         if (h->g_A[q]) cudaFree(h->g_A[q]);
@@ -134,6 +141,7 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     ok = ok && cudaMalloc(&h->U, (size_t)h->g.Nab * 2 * rs) == cudaSuccess;
     ok = ok && cudaMalloc(&h->code, (size_t)h->g.N) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st, sizeof(InstState)) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->st_gather, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->inst, sizeof(Inst)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->tiles, sizeof(Tile) * (size_t)h->ntiles) == cudaSuccess;
     const int nstrips = (h->g.Nx + kStripCols - 1) / kStripCols, nrows = (h->g.Ny + kStripRows - 1) / kStripRows;
@@ -202,14 +210,8 @@ int glgpu_set_params(glgpu_handle* h, const glgpu_params* p) {
     if (!(p->stop_psi > 0.0) || !(p->stop_A > 0.0)) return set_error(h, GLGPU_E_ARG, "set_params: stop criteria must be > 0");
     const bool was_finite = finite_kappa(h->p), now_finite = finite_kappa(*p);
     h->p = *p;
-    if (was_finite != now_finite) {
-        // the graph topology depends on kappa being finite
-        for (int q = 0; q < 3; ++q)
-            if (h->td_exec[q]) {
-                cudaGraphExecDestroy(h->td_exec[q]);
-                h->td_exec[q] = nullptr;
-            }
-    }
+    (void)was_finite;  // the TD graphs are kept per (equation mode, kappa finite)
+    (void)now_finite;
     upload_inst(h);
     cudaError_t e = cudaMemcpyAsync(&h->st->rand_t, &h->p.rand_t, sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -366,6 +368,82 @@ int glgpu_jacobian(glgpu_handle* h, void* g_psi, void* g_A) {
 int glgpu_conjgrad_coef(glgpu_handle* h, const void* dpsi, const void* dab, double* c) {
     if (check_handle(h) || !dpsi || !c) return set_error(h, GLGPU_E_ARG, "conjgrad_coef: NULL argument");
     return cg_coef_for(h, dpsi, dab, c);
+}
+
+int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** out) {
+    if (!handles || !out || n < 1) return set_error(nullptr, GLGPU_E_ARG, "glgpu_batch_create: bad arguments");
+    *out = nullptr;
+    for (int q = 0; q < n; ++q) {
+        if (!handles[q]) return set_error(nullptr, GLGPU_E_ARG, "glgpu_batch_create: NULL handle");
+        if (handles[q]->dtype != handles[0]->dtype || handles[q]->device != handles[0]->device)
+            return set_error(nullptr, GLGPU_E_ARG, "glgpu_batch_create: handles differ in dtype or device");
+        for (int r = 0; r < q; ++r)
+            if (handles[r] == handles[q]) return set_error(nullptr, GLGPU_E_ARG, "glgpu_batch_create: repeated handle");
+    }
+    glgpu_batch* b = new glgpu_batch();
+    b->dtype = handles[0]->dtype;
+    b->device = handles[0]->device;
+    b->ninst = n;
+    b->hs.assign(handles, handles + n);
+    cudaSetDevice(b->device);
+    std::vector<Tile> tiles;
+    std::vector<Item> items;
+    for (int q = 0; q < n; ++q) {
+        const Geo& g = handles[q]->g;
+        for (int k = 0; k < handles[q]->ntiles; ++k) tiles.push_back(Tile{q, k * kThreads});
+        const int nstrips = (g.Nx + kStripCols - 1) / kStripCols, nrows = (g.Ny + kStripRows - 1) / kStripRows;
+        for (int r = 0; r < nrows; ++r)
+            for (int s = 0; s < nstrips; ++s) items.push_back(Item{q, kStripCols * s, kStripRows * r, 0});
+    }
+    b->ntiles = (int)tiles.size();
+    b->nitems = (int)items.size();
+    b->psi_grid = psi_sweep_grid(b->dtype, b->nitems);
+    b->gather_h.resize(n);
+    bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaMalloc(&b->insts, sizeof(Inst) * (size_t)n) == cudaSuccess;
+    ok = ok && cudaMalloc(&b->gather, sizeof(InstState) * (size_t)n) == cudaSuccess;
+    ok = ok && cudaMalloc(&b->tiles, sizeof(Tile) * tiles.size()) == cudaSuccess;
+    ok = ok && cudaMalloc(&b->items, sizeof(Item) * items.size()) == cudaSuccess;
+    ok = ok && cudaMalloc(&b->loop, sizeof(LoopState)) == cudaSuccess;
+    cudaError_t e = ok ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->items, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+        glgpu_batch_destroy(b);
+        return set_error(nullptr, e == cudaErrorMemoryAllocation ? GLGPU_E_OOM : GLGPU_E_CUDA,
+                         std::string("glgpu_batch_create: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return GLGPU_OK;
+}
+
+int glgpu_batch_destroy(glgpu_batch* b) {
+    if (!b) return GLGPU_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (int q = 0; q < 6; ++q)
+        if (b->td_exec[q]) cudaGraphExecDestroy(b->td_exec[q]);
+    void* ptrs[] = {b->insts, b->gather, b->tiles, b->items, b->loop};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return GLGPU_OK;
+}
+
+const char* glgpu_batch_last_error(const glgpu_batch* b) { return b ? b->last_error.c_str() : g_create_error.c_str(); }
+
+int glgpu_batch_td(glgpu_batch* b, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats, double* elapsed_ms) {
+    if (!b) return GLGPU_E_ARG;
+    cudaSetDevice(b->device);
+    return batch_td(b, dt, Nt, eqn, stats, elapsed_ms);
+}
+
+int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable) {
+    if (!b) return GLGPU_E_ARG;
+    b->use_graphs = enable != 0;
+    return GLGPU_OK;
 }
 
 int glgpu_free_energy_noalloc(const glgpu_grid* grid, const glgpu_params* params, const void* psi, const void* ab,

@@ -120,8 +120,9 @@ struct glgpu_handle {
     void* dir_psi[2] = {nullptr, nullptr};
     void* dir_A[2] = {nullptr, nullptr};
     int cg_g = 0, cg_dir = 0;           // current index of g / dir
-    // TD graphs, one per equation mode
-    cudaGraphExec_t td_exec[3] = {nullptr, nullptr, nullptr};
+    // TD graphs, one per (equation mode, kappa finite)
+    cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    glgpu::InstState* st_gather = nullptr;  // device copy target of the loop state
     bool td_graph_failed = false;
     bool use_graphs = true;
     std::string last_error;
@@ -130,8 +131,30 @@ struct glgpu_handle {
     double* hscal = nullptr;
 };
 
+// A batch: several handles (instances of any sizes and parameters, one dtype,
+// one device) advanced together.  Their descriptors, item and tile tables are
+// concatenated, so one sweep launch covers every instance and each instance
+// keeps its own Jacobi stop rule.
+struct glgpu_batch {
+    int dtype = 4, device = 0, ninst = 0;
+    std::vector<glgpu_handle*> hs;
+    cudaStream_t stream = nullptr;
+    glgpu::Inst* insts = nullptr;
+    glgpu::Tile* tiles = nullptr;
+    glgpu::Item* items = nullptr;
+    glgpu::LoopState* loop = nullptr;
+    glgpu::InstState* gather = nullptr;
+    std::vector<glgpu::InstState> gather_h;
+    int ntiles = 0, nitems = 0, psi_grid = 0;
+    cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool td_graph_failed = false, use_graphs = true;
+    std::string last_error;
+};
+
 namespace glgpu {
 
+int batch_error(glgpu_batch* b, int code, const std::string& msg);
+int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms);
 int set_error(glgpu_handle* h, int code, const std::string& msg);
 int cuda_check(glgpu_handle* h, cudaError_t e, const char* what);
 void upload_inst(glgpu_handle* h);

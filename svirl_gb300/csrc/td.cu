@@ -372,9 +372,10 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
 // r_0m, 3: upper r_0p; a node is updated iff it has a left or a right link).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int only_solveA) {
     const Tile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
+    if (only_solveA && !I.solveA) return;  // A of a kappa=inf instance does not change
     const Geo g = I.g;
     const int n = t.n0 + threadIdx.x;
     if (n >= g.N) return;
@@ -396,28 +397,35 @@ k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
 }
 
 // Start of a Jacobi loop: reset the per-instance loop state and the while
-// condition.  which: 0 = psi loop, 1 = A loop.
+// condition.  which: 0 = psi loop, 1 = A loop; kappa=inf instances have no A loop
+// (svirl/solvers/td.py:476).
 __global__ void k_loop_begin(const Inst* __restrict__ insts, int ninst, LoopState* loop,
-                             cudaGraphConditionalHandle cond, int use_cond) {
+                             cudaGraphConditionalHandle cond, int use_cond, int which) {
+    int active = 0;
     for (int q = threadIdx.x; q < ninst; q += blockDim.x) {
         InstState* st = insts[q].st;
+        const bool part = which == 0 || insts[q].solveA;
         st->sweep = 0;
-        st->done = 0;
+        st->done = part ? 0 : 1;
         st->blocks_done = 0u;
         st->res = 0ull;
+        active += part ? 1 : 0;
     }
+    for (int o = 16; o > 0; o >>= 1) active += __shfl_down_sync(0xffffffffu, active, o);
     if (threadIdx.x == 0) {
-        loop->active = ninst;
+        loop->active = active;
         loop->launches = 0;
         loop->blocks_done = 0u;
-        loop->cont = 1;
-        if (use_cond) cudaGraphSetConditional(cond, 1u);
+        loop->cont = active > 0 ? 1 : 0;
+        if (use_cond) cudaGraphSetConditional(cond, active > 0 ? 1u : 0u);
     }
 }
 
-// End of a Jacobi loop: advance the Langevin seed (td.py:204,313).
-__global__ void k_loop_end(const Inst* __restrict__ insts, int ninst) {
-    for (int q = threadIdx.x; q < ninst; q += blockDim.x) insts[q].st->rand_t += 1u;
+// End of a Jacobi loop: advance the Langevin seed of the instances that ran it
+// (td.py:204,313).
+__global__ void k_loop_end(const Inst* __restrict__ insts, int ninst, int which) {
+    for (int q = threadIdx.x; q < ninst; q += blockDim.x)
+        if (which == 0 || insts[q].solveA) insts[q].st->rand_t += 1u;
 }
 
 // End of a time step: count it and decide whether the time loop goes on.
@@ -466,7 +474,7 @@ struct TDLaunch {
     const Item* items;
     LoopState* loop;
     int ninst, ntiles, nitems, psi_grid, dtype;
-    bool solveA, pre_u;
+    bool any_solveA;
 };
 
 static void* psi_sweep_fn(int dtype) {
@@ -474,6 +482,9 @@ static void* psi_sweep_fn(int dtype) {
 }
 static void* A_sweep_fn(int dtype) {
     return dtype == 8 ? (void*)k_A_sweep<double> : (void*)k_A_sweep<float>;
+}
+static void* link_fn(int dtype) {
+    return dtype == 8 ? (void*)k_link_U<double> : (void*)k_link_U<float>;
 }
 
 static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
@@ -503,40 +514,41 @@ static cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, const cudaGra
 
 #define GCHK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { err = e_; goto fail; } } while (0)
 
-// Build the whole TD run as one graph:
-//   [U once (FP64, kappa=inf)] -> WHILE(step < Nt) {
-//       [U (FP64, finite kappa)] -> loop_begin -> WHILE(active) { psi sweep } -> loop_end
-//       -> loop_begin -> WHILE(active) { A sweep } -> loop_end -> step_end }
+// Build the whole TD run of all instances as one graph:
+//   [tables, all instances] -> WHILE(step < Nt) {
+//       [tables, finite-kappa instances] -> loop_begin(psi) -> WHILE(active) { psi sweep } -> loop_end(psi)
+//       -> loop_begin(A) -> WHILE(active) { A sweep } -> loop_end(A) -> step_end }
 //   -> canonical copy -> canonical reset
 static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* exec) {
     cudaError_t err = cudaSuccess;
     cudaGraph_t top = nullptr, obody = nullptr, pbody = nullptr, abody = nullptr;
     cudaGraphConditionalHandle hout, hpsi = 0, hA = 0;
     cudaGraphNode_t n_pre = nullptr, n_out = nullptr, n_cc = nullptr, n_cr = nullptr, prev = nullptr, nd;
-    const bool do_psi = eqn != 2, do_A = (eqn != 1) && L.solveA;
-    int one = 1;
+    const bool do_psi = eqn != 2, do_A = (eqn != 1) && L.any_solveA;
+    int zero = 0, one = 1;
     const dim3 gt(L.ntiles), bt(kThreads), g1(1), b1(32);
     Inst const* insts = L.insts;
     Tile const* tiles = L.tiles;
+    Item const* items = L.items;
     LoopState* loop = L.loop;
-    int ninst = L.ninst;
+    int ninst = L.ninst, nitems = L.nitems;
 
     GCHK(cudaGraphCreate(&top, 0));
     GCHK(cudaGraphConditionalHandleCreate(&hout, top, 1, cudaGraphCondAssignDefault));
-    if (do_psi && L.pre_u && !L.solveA) {
-        void* a[] = {&insts, &tiles};
-        GCHK(add_kernel(top, &n_pre, nullptr, 0, (L.dtype == 8 ? (void*)k_link_U<double> : (void*)k_link_U<float>), gt, bt, a));
+    if (do_psi) {
+        void* a[] = {&insts, &tiles, &zero};
+        GCHK(add_kernel(top, &n_pre, nullptr, 0, link_fn(L.dtype), gt, bt, a));
     }
     GCHK(add_while(top, &n_out, n_pre ? &n_pre : nullptr, n_pre ? 1 : 0, hout, &obody));
     if (do_psi) {
         GCHK(cudaGraphConditionalHandleCreate(&hpsi, obody, 1, cudaGraphCondAssignDefault));
-        if (L.pre_u && L.solveA) {
-            void* a[] = {&insts, &tiles};
-            GCHK(add_kernel(obody, &nd, nullptr, 0, (L.dtype == 8 ? (void*)k_link_U<double> : (void*)k_link_U<float>), gt, bt, a));
+        if (L.any_solveA) {
+            void* a[] = {&insts, &tiles, &one};
+            GCHK(add_kernel(obody, &nd, nullptr, 0, link_fn(L.dtype), gt, bt, a));
             prev = nd;
         }
         {
-            void* a[] = {&insts, &ninst, &loop, &hpsi, &one};
+            void* a[] = {&insts, &ninst, &loop, &hpsi, &one, &zero};
             GCHK(add_kernel(obody, &nd, prev ? &prev : nullptr, prev ? 1 : 0, (void*)k_loop_begin, g1, b1, a));
             prev = nd;
         }
@@ -544,13 +556,11 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         prev = nd;
         {
             cudaGraphNode_t sw;
-            Item const* items = L.items;
-            int nitems = L.nitems;
             void* a[] = {&insts, &items, &nitems, &loop, &hpsi, &one};
             GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype), dim3(L.psi_grid), bt, a));
         }
         {
-            void* a[] = {&insts, &ninst};
+            void* a[] = {&insts, &ninst, &zero};
             GCHK(add_kernel(obody, &nd, &prev, 1, (void*)k_loop_end, g1, b1, a));
             prev = nd;
         }
@@ -558,7 +568,7 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
     if (do_A) {
         GCHK(cudaGraphConditionalHandleCreate(&hA, obody, 1, cudaGraphCondAssignDefault));
         {
-            void* a[] = {&insts, &ninst, &loop, &hA, &one};
+            void* a[] = {&insts, &ninst, &loop, &hA, &one, &one};
             GCHK(add_kernel(obody, &nd, prev ? &prev : nullptr, prev ? 1 : 0, (void*)k_loop_begin, g1, b1, a));
             prev = nd;
         }
@@ -570,7 +580,7 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
             GCHK(add_kernel(abody, &sw, nullptr, 0, A_sweep_fn(L.dtype), gt, bt, a));
         }
         {
-            void* a[] = {&insts, &ninst};
+            void* a[] = {&insts, &ninst, &one};
             GCHK(add_kernel(obody, &nd, &prev, 1, (void*)k_loop_end, g1, b1, a));
             prev = nd;
         }
@@ -595,25 +605,25 @@ fail:
     return err;
 }
 
-static void launch_link_U(const TDLaunch& L, cudaStream_t s) {
-    if (L.dtype == 8) k_link_U<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
-    else k_link_U<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+static void launch_link_U(const TDLaunch& L, int only_solveA, cudaStream_t s) {
+    if (L.dtype == 8) k_link_U<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, only_solveA);
+    else k_link_U<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, only_solveA);
 }
 
 // Host-driven fallback: the same kernels, the loop decided on the host after
 // each chunk of sweeps (sweeps of finished instances are no-ops).
 static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_t s) {
-    const bool do_psi = eqn != 2, do_A = (eqn != 1) && L.solveA;
+    const bool do_psi = eqn != 2, do_A = (eqn != 1) && L.any_solveA;
     const int chunk = 4;
     cudaGraphConditionalHandle none = 0;
     int cont = 1;
-    if (do_psi && !L.solveA) launch_link_U(L, s);
+    if (do_psi) launch_link_U(L, 0, s);
     for (int step = 0; step < Nt; ++step) {
         for (int part = 0; part < 2; ++part) {
             if (part == 0 && !do_psi) continue;
             if (part == 1 && !do_A) continue;
-            if (part == 0 && L.solveA) launch_link_U(L, s);
-            k_loop_begin<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0);
+            if (part == 0 && L.any_solveA) launch_link_U(L, 1, s);
+            k_loop_begin<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0, part);
             for (;;) {
                 for (int c = 0; c < chunk; ++c) {
                     if (part == 0) {
@@ -630,7 +640,7 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
                 if (e != cudaSuccess) return e;
                 if (!cont) break;
             }
-            k_loop_end<<<1, 32, 0, s>>>(L.insts, L.ninst);
+            k_loop_end<<<1, 32, 0, s>>>(L.insts, L.ninst, part);
         }
         k_step_end<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0);
     }
@@ -658,6 +668,22 @@ __global__ void k_bench_prep(const Inst* __restrict__ insts, int ninst, LoopStat
     }
 }
 
+// Per-call counters of every instance back to zero.
+__global__ void k_reset_counters(const Inst* __restrict__ insts, int ninst) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ninst; q += gridDim.x * blockDim.x) {
+        InstState* st = insts[q].st;
+        st->nan_seen = 0;
+        st->last_sweeps_psi = st->last_sweeps_A = st->max_sweeps_psi = st->max_sweeps_A = 0;
+        st->total_sweeps_psi = st->total_sweeps_A = 0;
+        st->steps = 0;
+    }
+}
+
+// The instances' loop states gathered into one array (one copy to the host).
+__global__ void k_gather_states(const Inst* __restrict__ insts, int ninst, InstState* out) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ninst; q += gridDim.x * blockDim.x) out[q] = *insts[q].st;
+}
+
 int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     if (nrep < 1 || which < 0 || which > 1 || !avg_ms) return set_error(h, GLGPU_E_ARG, "time_sweeps: bad arguments");
     const bool solveA = h->p.kappa > 0.0 && !std::isinf(h->p.kappa);
@@ -672,8 +698,8 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaGraphConditionalHandle none = 0;
-    if (h->dtype == 8) k_link_U<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles);
-    else k_link_U<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles);
+    if (h->dtype == 8) k_link_U<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, 0);
+    else k_link_U<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, 0);
     double total = 0.0;
     for (int r = 0; r < nrep && e == cudaSuccess; ++r) {
         cudaMemsetAsync(h->flush, r & 0xff, flush_bytes, h->stream);
@@ -715,89 +741,140 @@ int psi_sweep_grid(int dtype, int nitems) {
     return need < full ? (need > 0 ? need : 1) : full;
 }
 
-int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms) {
-    if (eqn < 0 || eqn > 2 || Nt < 0) return set_error(h, GLGPU_E_ARG, "glgpu_td: bad eqn or Nt");
-    const bool solveA = h->p.kappa > 0.0 && !std::isinf(h->p.kappa);
-    // dt of the order-parameter iterator; the A kernel also receives it (td.py:278)
-    {
-        cudaError_t e = cudaMemsetAsync(&h->st->nan_seen, 0, offsetof(InstState, pad_) - offsetof(InstState, nan_seen), h->stream);
-        if (e != cudaSuccess) return cuda_check(h, e, "td: reset counters");
-        h->inst_h.dt = dt;
-        h->inst_h.fdt = (float)dt;
-        e = cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
-        if (e != cudaSuccess) return cuda_check(h, e, "td: write descriptor");
-    }
-    TDLaunch L;
-    L.insts = h->inst; L.tiles = h->tiles; L.loop = h->loop; L.ninst = 1; L.ntiles = h->ntiles;
-    L.items = h->items; L.nitems = h->nitems; L.psi_grid = h->psi_grid;
-    L.dtype = h->dtype; L.solveA = solveA; L.pre_u = true;
-    int used_graph = 0;
+struct TDOutcome {
+    cudaError_t err;
+    int used_graph, loop_err, steps;
+    float ms;
+};
+
+// One TD call over the instances of L: per-call counters reset, the graph (built
+// once per eqn mode and kappa mix) or the host-driven loop, then the instances'
+// loop states gathered to the host.
+static TDOutcome td_core(cudaStream_t s, const TDLaunch& L, int Nt, int eqn, cudaGraphExec_t* execs, bool* graph_failed,
+                         bool use_graphs, bool timed, InstState* gather_dev, InstState* gather_host) {
+    TDOutcome o = {cudaSuccess, 0, 0, 0, 0.f};
+    k_reset_counters<<<(L.ninst + 127) / 128, 128, 0, s>>>(L.insts, L.ninst);
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    if (elapsed_ms) {
-        *elapsed_ms = 0.0;
+    if (timed) {
         cudaEventCreate(&ev0);
         cudaEventCreate(&ev1);
     }
+    LoopState hl;
+    memset(&hl, 0, sizeof(hl));
     if (Nt > 0) {
         LoopState ls;
         memset(&ls, 0, sizeof(ls));
         ls.Nt = Nt;
-        ls.ninst = 1;
-        cudaError_t e = cudaMemcpyAsync(h->loop, &ls, sizeof(ls), cudaMemcpyHostToDevice, h->stream);
-        if (e != cudaSuccess) return cuda_check(h, e, "td: loop state");
-        const int gi = eqn * 1;  // graph slot per eqn (solveA is fixed by the descriptor's kappa)
-        if (h->use_graphs && !h->td_graph_failed) {
-            if (h->td_exec[gi] == nullptr) {
-                e = build_td_graph(L, eqn, &h->td_exec[gi]);
-                if (e != cudaSuccess) {
-                    h->td_graph_failed = true;
+        ls.ninst = L.ninst;
+        o.err = cudaMemcpyAsync(L.loop, &ls, sizeof(ls), cudaMemcpyHostToDevice, s);
+        if (o.err != cudaSuccess) return o;
+        const int slot = eqn * 2 + (L.any_solveA ? 1 : 0);
+        if (use_graphs && !*graph_failed) {
+            if (execs[slot] == nullptr) {
+                if (build_td_graph(L, eqn, &execs[slot]) != cudaSuccess) {
+                    *graph_failed = true;
                     cudaGetLastError();
                 }
             }
-            if (h->td_exec[gi] != nullptr) {
-                if (ev0) cudaEventRecord(ev0, h->stream);
-                e = cudaGraphLaunch(h->td_exec[gi], h->stream);
-                if (e != cudaSuccess) return cuda_check(h, e, "td: graph launch");
-                used_graph = 1;
+            if (execs[slot] != nullptr) {
+                if (ev0) cudaEventRecord(ev0, s);
+                o.err = cudaGraphLaunch(execs[slot], s);
+                if (o.err != cudaSuccess) return o;
+                o.used_graph = 1;
             }
         }
-        if (!used_graph) {
-            if (ev0) cudaEventRecord(ev0, h->stream);
-            e = run_host_loop(L, eqn, Nt, h->stream);
-            if (e != cudaSuccess) return cuda_check(h, e, "td: host loop");
+        if (!o.used_graph) {
+            if (ev0) cudaEventRecord(ev0, s);
+            o.err = run_host_loop(L, eqn, Nt, s);
+            if (o.err != cudaSuccess) return o;
         }
-        if (ev1) cudaEventRecord(ev1, h->stream);
+        if (ev1) cudaEventRecord(ev1, s);
     }
-    InstState hs;
-    LoopState hl;
-    cudaError_t e = cudaMemcpyAsync(&hs, h->st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&hl, h->loop, sizeof(hl), cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    if (e != cudaSuccess) return cuda_check(h, e, "td: run");
+    k_gather_states<<<(L.ninst + 127) / 128, 128, 0, s>>>(L.insts, L.ninst, gather_dev);
+    o.err = cudaMemcpyAsync(gather_host, gather_dev, sizeof(InstState) * (size_t)L.ninst, cudaMemcpyDeviceToHost, s);
+    if (o.err == cudaSuccess) o.err = cudaMemcpyAsync(&hl, L.loop, sizeof(hl), cudaMemcpyDeviceToHost, s);
+    if (o.err == cudaSuccess) o.err = cudaStreamSynchronize(s);
     if (ev0) {
-        float ms = 0.f;
-        if (Nt > 0 && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) *elapsed_ms = ms;
+        if (o.err == cudaSuccess && Nt > 0) cudaEventElapsedTime(&o.ms, ev0, ev1);
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);
     }
+    o.loop_err = Nt > 0 ? hl.err : 0;
+    o.steps = Nt > 0 ? hl.step : 0;
+    return o;
+}
+
+static void fill_stats(glgpu_td_stats* stats, const InstState* hs, int n, const TDOutcome& o) {
+    if (!stats) return;
+    memset(stats, 0, sizeof(*stats));
+    stats->steps = o.steps;
+    stats->used_graph = o.used_graph;
+    for (int q = 0; q < n; ++q) {
+        const InstState& s = hs[q];
+        if (s.max_sweeps_psi > stats->max_sweeps_psi) stats->max_sweeps_psi = s.max_sweeps_psi;
+        if (s.max_sweeps_A > stats->max_sweeps_A) stats->max_sweeps_A = s.max_sweeps_A;
+        stats->last_sweeps_psi = s.last_sweeps_psi;
+        stats->last_sweeps_A = s.last_sweeps_A;
+        stats->nan_seen |= s.nan_seen;
+        stats->total_sweeps_psi += s.total_sweeps_psi;
+        stats->total_sweeps_A += s.total_sweeps_A;
+        stats->rand_t = s.rand_t;
+    }
+}
+
+int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms) {
+    if (eqn < 0 || eqn > 2 || Nt < 0) return set_error(h, GLGPU_E_ARG, "glgpu_td: bad eqn or Nt");
+    // dt of the order-parameter iterator; the A kernel also receives it (td.py:278)
+    h->inst_h.dt = dt;
+    h->inst_h.fdt = (float)dt;
+    cudaError_t e = cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "td: write descriptor");
+    TDLaunch L;
+    L.insts = h->inst; L.tiles = h->tiles; L.items = h->items; L.loop = h->loop;
+    L.ninst = 1; L.ntiles = h->ntiles; L.nitems = h->nitems; L.psi_grid = h->psi_grid; L.dtype = h->dtype;
+    L.any_solveA = h->inst_h.solveA != 0;
+    InstState hs;
+    TDOutcome o = td_core(h->stream, L, Nt, eqn, h->td_exec, &h->td_graph_failed, h->use_graphs, elapsed_ms != nullptr,
+                          h->st_gather, &hs);
+    if (o.err != cudaSuccess) return cuda_check(h, o.err, "td");
+    if (elapsed_ms) *elapsed_ms = o.ms;
     h->p.rand_t = hs.rand_t;
-    if (stats) {
-        stats->steps = Nt > 0 ? hl.step : 0;
-        stats->max_sweeps_psi = hs.max_sweeps_psi;
-        stats->max_sweeps_A = hs.max_sweeps_A;
-        stats->last_sweeps_psi = hs.last_sweeps_psi;
-        stats->last_sweeps_A = hs.last_sweeps_A;
-        stats->nan_seen = hs.nan_seen;
-        stats->total_sweeps_psi = hs.total_sweeps_psi;
-        stats->total_sweeps_A = hs.total_sweeps_A;
-        stats->rand_t = hs.rand_t;
-        stats->used_graph = used_graph;
+    fill_stats(stats, &hs, 1, o);
+    if (o.loop_err & kErrLoopGuard) return set_error(h, GLGPU_E_TIMEOUT, "td: Jacobi loop guard reached");
+    if (hs.nan_seen) return set_error(h, GLGPU_E_NAN, "td: NaN residual (the state was updated as the reference does)");
+    return GLGPU_OK;
+}
+
+int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms) {
+    if (eqn < 0 || eqn > 2 || Nt < 0) return batch_error(b, GLGPU_E_ARG, "batch_td: bad eqn or Nt");
+    std::vector<Inst> insts(b->ninst);
+    bool any_solveA = false;
+    for (int q = 0; q < b->ninst; ++q) {
+        glgpu_handle* h = b->hs[q];
+        cudaStreamSynchronize(h->stream);
+        h->inst_h.dt = dt;
+        h->inst_h.fdt = (float)dt;
+        insts[q] = h->inst_h;
+        any_solveA = any_solveA || h->inst_h.solveA != 0;
     }
-    if (Nt > 0 && (hl.err & kErrLoopGuard)) return set_error(h, GLGPU_E_TIMEOUT, "td: Jacobi loop guard reached");
-    if (hs.nan_seen) {
-        set_error(h, GLGPU_E_NAN, "td: NaN residual (the state was updated as the reference does)");
-        return GLGPU_E_NAN;
+    cudaError_t e = cudaMemcpyAsync(b->insts, insts.data(), sizeof(Inst) * insts.size(), cudaMemcpyHostToDevice, b->stream);
+    if (e != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_td: ") + cudaGetErrorString(e));
+    TDLaunch L;
+    L.insts = b->insts; L.tiles = b->tiles; L.items = b->items; L.loop = b->loop;
+    L.ninst = b->ninst; L.ntiles = b->ntiles; L.nitems = b->nitems; L.psi_grid = b->psi_grid; L.dtype = b->dtype;
+    L.any_solveA = any_solveA;
+    TDOutcome o = td_core(b->stream, L, Nt, eqn, b->td_exec, &b->td_graph_failed, b->use_graphs, elapsed_ms != nullptr,
+                          b->gather, b->gather_h.data());
+    if (o.err != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_td: ") + cudaGetErrorString(o.err));
+    if (elapsed_ms) *elapsed_ms = o.ms;
+    int nan = 0;
+    for (int q = 0; q < b->ninst; ++q) {
+        b->hs[q]->p.rand_t = b->gather_h[q].rand_t;
+        nan |= b->gather_h[q].nan_seen;
     }
+    fill_stats(stats, b->gather_h.data(), b->ninst, o);
+    if (o.loop_err & kErrLoopGuard) return batch_error(b, GLGPU_E_TIMEOUT, "batch_td: Jacobi loop guard reached");
+    if (nan) return batch_error(b, GLGPU_E_NAN, "batch_td: NaN residual in at least one instance");
     return GLGPU_OK;
 }
 
