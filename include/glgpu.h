@@ -159,6 +159,21 @@ int glgpu_batch_destroy(glgpu_batch* b);
 const char* glgpu_batch_last_error(const glgpu_batch* b);
 int glgpu_batch_td(glgpu_batch* b, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats, double* elapsed_ms);
 int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable);
+/* Free-energy minimisation of every instance of the batch with the step
+ * length, beta and stop test decided on the device (one graph launch for the
+ * whole run).  No counterpart in the reference; each instance follows the
+ * Polak-Ribiere+ CG of svirl/solvers/cg.py:238-318 (kappa = inf) and
+ * cg.py:452-544 (finite kappa) from a zero direction, with alpha chosen as the
+ * smallest non-negative stationary point of the quartic (kappa = inf) or by a
+ * damped Newton descent of the (alpha_psi, alpha_A) polynomial from (0, 0)
+ * (finite kappa) instead of numpy roots / scipy BFGS on the host.  Stops per
+ * instance after n_iter updates, when |E_k/E_{k-1} - 1| < rtol (cg.py:315-318),
+ * or when |grad F| <= gtol |grad F of the first iteration| (gtol = 0: off).
+ * Per-instance outputs (each may be NULL): iterations done, final energy,
+ * final |grad F| relative to the first, status (1 gradient stop, 2 energy stop,
+ * 3 n_iter reached, -1 no descent step; then GLGPU_E_NOROOT is returned). */
+int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t* iters, double* energies,
+                   double* grad_rel, int32_t* status, double* elapsed_ms);
 
 /* --- free energy of a caller-owned state with no allocation by the library.
  *     No counterpart in the reference (its gsum allocates work arrays,

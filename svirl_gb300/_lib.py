@@ -80,6 +80,8 @@ _SIGNATURES = {
     "glgpu_batch_last_error": (C.c_char_p, [_H]),
     "glgpu_batch_td": (C.c_int, [_H, C.c_double, C.c_int32, C.c_int32, C.POINTER(TDStats), C.POINTER(C.c_double)]),
     "glgpu_batch_set_use_graphs": (C.c_int, [_H, C.c_int32]),
+    "glgpu_batch_cg": (C.c_int, [_H, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
 }
 
 _lib = None

@@ -5,7 +5,7 @@
     solvers = [GLSolver(...), GLSolver(...), ...]      # any sizes / parameters, one dtype
     batch = GLBatch(solvers)
     stats = batch.td(dt=0.1, Nt=2000)                  # one device-side loop for all
-    batch.cg(n_iter=1000, gtol=1e-8)                   # device CG, every instance at once
+    batch.cg(n_iter=1000, gtol=1e-6)                   # device CG, every instance at once
 
 The TD call runs every instance's time loop and Jacobi loops inside one CUDA
 graph launch: one sweep launch covers all instances (concatenated item tables,
@@ -87,7 +87,40 @@ class GLBatch:
     def free_energies(self):
         return np.array([s.observables.free_energy for s in self.solvers])
 
-    def cg(self, n_iter=1000, **kw):
-        """``solve.cg(n_iter)`` of every solver (reference algorithm, host line search)."""
+    def cg(self, n_iter=1000, rtol=None, gtol=0.0, mode="device", timed=False):
+        """Free-energy minimisation of every solver.
+
+        ``mode="device"``: one graph launch runs the CG of all instances; beta,
+        the step lengths and the stop test are decided on the device (see
+        ``glgpu_batch_cg``).  Stops per instance after ``n_iter`` updates, on the
+        reference's energy-ratio test with ``rtol`` (default: the first
+        solver's ``convergence_rtol``) or when the gradient norm falls below
+        ``gtol`` times its first value.  Returns a dict of per-instance arrays
+        ``iters``, ``energy``, ``grad_rel``, ``status`` (and ``ms`` if ``timed``).
+
+        ``mode="reference"``: ``solve.cg(n_iter)`` of each solver in turn, the
+        reference's decisions taken on the host."""
+        if mode == "reference":
+            for s in self.solvers:
+                s.solve.cg(n_iter=n_iter)
+            return None
+        if mode != "device":
+            raise ValueError("mode must be 'device' or 'reference'")
+        if rtol is None:
+            rtol = self.solvers[0].cfg.convergence_rtol
+        n = len(self.solvers)
+        iters = (C.c_int32 * n)()
+        energy = (C.c_double * n)()
+        grad_rel = (C.c_double * n)()
+        status = (C.c_int32 * n)()
+        ms = C.c_double()
+        rc = self.lib.glgpu_batch_cg(self.b, int(n_iter), float(rtol), float(gtol), iters, energy, grad_rel, status,
+                                     C.byref(ms))
         for s in self.solvers:
-            s.solve.cg(n_iter=n_iter)
+            s.solve.vortices_detected = False
+        self._check(rc, "batch_cg")
+        out = {"iters": np.array(iters[:], dtype=np.int32), "energy": np.array(energy[:]),
+               "grad_rel": np.array(grad_rel[:]), "status": np.array(status[:], dtype=np.int32)}
+        if timed:
+            out["ms"] = ms.value
+        return out

@@ -62,6 +62,13 @@ void upload_inst(glgpu_handle* h) {
     I.U = h->U;
     I.code = h->code;
     I.st = h->st;
+    I.cg = h->cgst;
+    for (int q = 0; q < 2; ++q) {
+        I.gpsi[q] = h->g_psi[q];
+        I.gA[q] = h->g_A[q];
+        I.dpsi[q] = h->dir_psi[q];
+        I.dA[q] = h->dir_A[q];
+    }
     I.tile0 = 0;
     I.ntiles = h->ntiles;
     I.nitems = h->nitems;
@@ -92,6 +99,7 @@ static void free_all(glgpu_handle* h) {
     for (int q = 0; q < 6; ++q)
         if (h->td_exec[q]) cudaGraphExecDestroy(h->td_exec[q]);
     if (h->st_gather) cudaFree(h->st_gather);
+    if (h->cgst) cudaFree(h->cgst);
     for (int q = 0; q < 2; ++q) {
         if (h->g_psi[q]) cudaFree(h->g_psi[q]);
         if (h->g_A[q]) cudaFree(h->g_A[q]);
@@ -424,7 +432,8 @@ int glgpu_batch_destroy(glgpu_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (int q = 0; q < 6; ++q)
         if (b->td_exec[q]) cudaGraphExecDestroy(b->td_exec[q]);
-    void* ptrs[] = {b->insts, b->gather, b->tiles, b->items, b->loop};
+    if (b->cg_exec) cudaGraphExecDestroy(b->cg_exec);
+    void* ptrs[] = {b->insts, b->gather, b->tiles, b->items, b->loop, b->cg_partials, b->cg_loop};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -438,6 +447,13 @@ int glgpu_batch_td(glgpu_batch* b, double dt, int32_t Nt, int32_t eqn, glgpu_td_
     if (!b) return GLGPU_E_ARG;
     cudaSetDevice(b->device);
     return batch_td(b, dt, Nt, eqn, stats, elapsed_ms);
+}
+
+int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t* iters, double* energies,
+                   double* grad_rel, int32_t* status, double* elapsed_ms) {
+    if (!b) return GLGPU_E_ARG;
+    cudaSetDevice(b->device);
+    return batch_cg(b, n_iter, rtol, gtol, iters, energies, grad_rel, status, elapsed_ms);
 }
 
 int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable) {

@@ -1,116 +1,34 @@
 // Modified nonlinear conjugate gradient of the GL free energy, in fused phases:
 //   k_cg_grad:      dF/dpsi and dF/dA (svirl/cuda/cg.h:15-301) plus the four
-//                   Polak-Ribiere sums and beta = max(num/den, 0)
-//                   (svirl/solvers/cg.py:422-449, svirl/cuda/utils.h:12-70,139-146);
+//                   Polak-Ribiere sums (svirl/cuda/utils.h:12-70);
+//   k_cg_beta:      beta = max(num/den, 0) (svirl/solvers/cg.py:422-449,
+//                   svirl/cuda/utils.h:139-146);
 //   k_cg_dir_coef:  dir = beta*dir - g (svirl/cuda/utils.h:96-114) and the 5 or 17
 //                   line-search coefficients (svirl/cuda/cg.h:314-731) in one pass,
 //                   neighbour directions recomputed in registers;
 //   k_cg_update:    psi += a_psi dir, A += a_A dir_A (svirl/cuda/utils.h:73-92).
-// All sums accumulate in FP64 and finish in the launch's last CTA.
+// All sums accumulate in FP64 and finish in the launch's last CTA.  These are
+// the single-instance kernels of the reference-decision CG (step length chosen
+// on the host); the batched device CG is in cgb.cu.
 #include "glgpu_internal.h"
+#include "glgpu_phys.cuh"
 
 namespace glgpu {
 
-template <typename T> struct DuW2 {
-    T r_m0, r_p0, r_0m, r_0p, g;
-};
-template <typename T> __device__ __forceinline__ DuW2<T> du_w(unsigned cb) {
-    DuW2<T> w;
-    const T mm = GL_MM(cb) ? T(1) : T(0), mp = GL_MP(cb) ? T(1) : T(0);
-    const T pm = GL_PM(cb) ? T(1) : T(0), pp = GL_PP(cb) ? T(1) : T(0);
-    w.r_m0 = T(0.5) * (mm + mp);
-    w.r_p0 = T(0.5) * (pm + pp);
-    w.r_0m = T(0.5) * (mm + pm);
-    w.r_0p = T(0.5) * (mp + pp);
-    w.g = T(0.25) * (w.r_m0 + w.r_p0 + w.r_0m + w.r_0p);
-    return w;
-}
-
-template <typename T> __device__ __forceinline__ T lphase(const T* abei, const T* ab, int n) {
-    T p = T(0);
-    if (abei) p += abei[n];
-    if (ab) p += ab[n];
-    return p;
-}
-
-// 2 (psi0 - psi1 U(ph)) (svirl/cuda/cg.h:4-12)
-template <typename T> __device__ __forceinline__ C2<T> gjac(C2<T> p0, T ph, C2<T> p1) {
-    T s, c;
-    sincos_t(ph, &s, &c);
-    return cmk<T>(T(2) * (p0.x - (p1.x * c + p1.y * s)), T(2) * (p0.y - (p1.y * c - p1.x * s)));
-}
-
-template <typename T>
-__device__ __forceinline__ T curlcurl_grad(const Geo& g, const T* abei, const T* ab, T H, int i, int j, bool xdir) {
-    const int Nxa = g.Nx - 1, Na = g.Na, Nx = g.Nx;
-    const T idx = GT(g, idx), idy = GT(g, idy);
-    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
-    T c = T(0), dd = T(1);
-    if (xdir) {
-        const int n = i + Nxa * j;
-        if (j == 0) { c -= T(2) * H * idy; dd = T(2); }
-        else if (j + 1 == g.Ny) { c += T(2) * H * idy; dd = T(2); }
-        if (abei) c += T(2) / dd * idy2 * abei[n];
-        if (ab) c += T(2) * idy2 * ab[n];
-        if (j > 0) {
-            if (abei) c += (-idy2 * abei[i + Nxa * (j - 1)] + idxy * abei[Na + i + Nx * (j - 1)] - idxy * abei[Na + i + 1 + Nx * (j - 1)]);
-            if (ab) c += dd * (-idy2 * ab[i + Nxa * (j - 1)] + idxy * ab[Na + i + Nx * (j - 1)] - idxy * ab[Na + i + 1 + Nx * (j - 1)]);
-        }
-        if (j + 1 < g.Ny) {
-            if (abei) c += (-idy2 * abei[i + Nxa * (j + 1)] - idxy * abei[Na + i + Nx * j] + idxy * abei[Na + i + 1 + Nx * j]);
-            if (ab) c += dd * (-idy2 * ab[i + Nxa * (j + 1)] - idxy * ab[Na + i + Nx * j] + idxy * ab[Na + i + 1 + Nx * j]);
-        }
-    } else {
-        const int n = Na + i + Nx * j;
-        if (i == 0) { c += T(2) * H * idx; dd = T(2); }
-        else if (i + 1 == g.Nx) { c -= T(2) * H * idx; dd = T(2); }
-        if (abei) c += T(2) / dd * idx2 * abei[n];
-        if (ab) c += T(2) * idx2 * ab[n];
-        if (i > 0) {
-            if (abei) c += (-idx2 * abei[Na + (i - 1) + Nx * j] + idxy * abei[(i - 1) + Nxa * j] - idxy * abei[(i - 1) + Nxa * (j + 1)]);
-            if (ab) c += dd * (-idx2 * ab[Na + (i - 1) + Nx * j] + idxy * ab[(i - 1) + Nxa * j] - idxy * ab[(i - 1) + Nxa * (j + 1)]);
-        }
-        if (i + 1 < g.Nx) {
-            if (abei) c += (-idx2 * abei[Na + (i + 1) + Nx * j] - idxy * abei[i + Nxa * j] + idxy * abei[i + Nxa * (j + 1)]);
-            if (ab) c += dd * (-idx2 * ab[Na + (i + 1) + Nx * j] - idxy * ab[i + Nxa * j] + idxy * ab[i + Nxa * (j + 1)]);
-        }
-    }
-    return c;
-}
-
 // Gradient at node n (psi part) and its two links (A part), plus the four
-// Polak-Ribiere sums.  beta_mode: 0 = gradient only, 1 = also update beta.
+// Polak-Ribiere sums.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const uint8_t* mt,
           const C2<T>* __restrict__ psi, const T* abei, const T* ab,
           C2<T>* __restrict__ gpsi, T* __restrict__ gA, const C2<T>* __restrict__ gpsi_prev, const T* __restrict__ gA_prev,
-          int solveA, int beta_mode, double* partials, unsigned* counter, double* dscal) {
+          int solveA, double* partials, unsigned* counter, double* dscal) {
     const int n = blockIdx.x * kThreads + threadIdx.x;
     double v[4] = {0.0, 0.0, 0.0, 0.0};
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, mt, i, j);
-        const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
-        const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
-        const C2<T> p0 = psi[n];
-        C2<T> gj = cmk<T>(T(0), T(0));
-        if (cb) {
-            const DuW2<T> w = du_w<T>(cb);
-            const T eps = eps_sp ? eps_sp[n] : (T)eps0;
-            const T p = p0.x * p0.x + p0.y * p0.y - eps;
-            gj = cadd(gj, cscale(T(2) * w.g * p, p0));
-            if (GL_MM(cb) || GL_MP(cb))
-                gj = cadd(gj, cscale(w.r_m0 * idx2, gjac<T>(p0, -dx * lphase(abei, ab, (i - 1) + (g.Nx - 1) * j), psi[n - 1])));
-            if (GL_PM(cb) || GL_PP(cb))
-                gj = cadd(gj, cscale(w.r_p0 * idx2, gjac<T>(p0, dx * lphase(abei, ab, i + (g.Nx - 1) * j), psi[n + 1])));
-            if (GL_MM(cb) || GL_PM(cb))
-                gj = cadd(gj, cscale(w.r_0m * idy2, gjac<T>(p0, -dy * lphase(abei, ab, g.Na + i + g.Nx * (j - 1)), psi[n - g.Nx])));
-            if (GL_MP(cb) || GL_PP(cb))
-                gj = cadd(gj, cscale(w.r_0p * idy2, gjac<T>(p0, dy * lphase(abei, ab, g.Na + i + g.Nx * j), psi[n + g.Nx])));
-        }
-        const T dxdy = dx * dy;
-        const C2<T> G = cscale(dxdy, gj);
+        const C2<T> G = grad_psi_node<T>(g, (T)eps0, eps_sp, psi, abei, ab, n, i, j, cb);
         gpsi[n] = G;
         const C2<T> Gp = gpsi_prev[n];
         v[0] = (double)(G.x * (G.x - Gp.x) + G.y * (G.y - Gp.y));
@@ -119,12 +37,7 @@ k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const ui
             const T k2 = (T)kappa2, Hh = (T)H;
             if (i < g.Nx - 1) {
                 const int na = i + (g.Nx - 1) * j;
-                T c = k2 * curlcurl_grad<T>(g, abei, ab, Hh, i, j, true);
-                if (GL_PM(cb) || GL_PP(cb)) {
-                    const T r = T(0.5) * ((GL_PM(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));
-                    c += -r * idx * js_of<T>(p0, dx * lphase(abei, ab, na), psi[n + 1]);
-                }
-                const T Ga = T(2) * dxdy * c;
+                const T Ga = grad_A_link<T>(g, k2, Hh, psi, abei, ab, n, i, j, cb, true);
                 gA[na] = Ga;
                 const T Gpa = gA_prev[na];
                 v[2] += (double)(Ga * (Ga - Gpa));
@@ -132,12 +45,7 @@ k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const ui
             }
             if (j < g.Ny - 1) {
                 const int nb = g.Na + i + g.Nx * j;
-                T c = k2 * curlcurl_grad<T>(g, abei, ab, Hh, i, j, false);
-                if (GL_MP(cb) || GL_PP(cb)) {
-                    const T r = T(0.5) * ((GL_MP(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));
-                    c += -r * idy * js_of<T>(p0, dy * lphase(abei, ab, nb), psi[n + g.Nx]);
-                }
-                const T Gb = T(2) * dxdy * c;
+                const T Gb = grad_A_link<T>(g, k2, Hh, psi, abei, ab, n, i, j, cb, false);
                 gA[nb] = Gb;
                 const T Gpb = gA_prev[nb];
                 v[2] += (double)(Gb * (Gb - Gpb));
@@ -190,92 +98,14 @@ k_cg_dir_coef(Geo g, double kappa2, double eps0, const T* eps_sp, double H, cons
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, mt, i, j);
-        const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
-        const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
-        const C2<T> d0 = dpsi(n);
-        if (dir_mode) dN[n] = d0;
-        if (NV == 17 && dir_mode) {
-            if (i < g.Nx - 1) { int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
-            if (j < g.Ny - 1) { int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
-        }
-        if (cb) {
-            const DuW2<T> w = du_w<T>(cb);
-            const C2<T> p0 = psi[n];
-            const T eps = eps_sp ? eps_sp[n] : (T)eps0;
-            const T p2 = cabs2(p0), d2 = cabs2(d0);
-            const T tw = T(2) * (p0.x * d0.x + p0.y * d0.y);
-            const T k00 = w.g * (T(0.5) * p2 - eps) * p2;
-            const T k10 = w.g * tw * (p2 - eps);
-            const T k20 = w.g * (-eps * d2 + T(0.5) * tw * tw + p2 * d2);
-            const T k30 = w.g * tw * d2;
-            const T k40 = w.g * T(0.5) * d2 * d2;
-            if (NV == 5) {
-                c[0] += k00; c[1] += k10; c[2] += k20; c[3] += k30; c[4] += k40;
-            } else {
-                c[0] += k00; c[5] += k10; c[10] += k20; c[15] += k30; c[16] += k40;
-            }
-#pragma unroll
-            for (int dir = 0; dir < 2; ++dir) {
-                const bool on = dir == 0 ? (GL_PM(cb) || GL_PP(cb)) : (GL_MP(cb) || GL_PP(cb));
-                if (!on) continue;
-                const int nl = dir == 0 ? i + (g.Nx - 1) * j : g.Na + i + g.Nx * j;
-                const int m1 = dir == 0 ? n + 1 : n + g.Nx;
-                const T d = dir == 0 ? dx : dy;
-                const T wr = (dir == 0 ? w.r_p0 : w.r_0p) * (dir == 0 ? idx2 : idy2);
-                T ph = T(0);
-                if (abei) ph += d * abei[nl];
-                if (ab) ph += d * ab[nl];
-                const C2<T> p1 = psi[m1], d1 = dpsi(m1);
-                T s, cs;
-                sincos_t(ph, &s, &cs);
-                const C2<T> gp = grad_c_sc<T>(p0, s, cs, p1), gd = grad_c_sc<T>(d0, s, cs, d1);
-                const T gg_p = gp.x * gp.x + gp.y * gp.y;
-                const T gg_d = gd.x * gd.x + gd.y * gd.y;
-                const T zr = gp.x * gd.x + gp.y * gd.y;   // Re(conj(gp) * gd)
-                if (NV == 5) {
-                    c[2] += wr * gg_d;
-                    c[1] += wr * T(2) * zr;
-                    c[0] += wr * gg_p;
-                } else {
-                    c[0] += wr * gg_p;
-                    c[5] += wr * T(2) * zr;
-                    c[10] += wr * gg_d;
-                    const T dph = d * dA(nl);
-                    const T dph2 = dph * dph;
-                    // U(-ph) = (cos ph, sin ph)
-                    const C2<T> Um = cmk<T>(cs, s);
-                    const C2<T> z1 = cmul(cmul(p0, Um), cconj(p1));
-                    const C2<T> z2 = cadd(cmul(cmul(p0, Um), cconj(d1)), cmul(cmul(d0, Um), cconj(p1)));
-                    const C2<T> z3 = cmul(cmul(d0, Um), cconj(d1));
-                    const C2<T> zz[3] = {z1, z2, z3};
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        const int b = 1 + 5 * q;
-                        c[b + 0] += wr * T(2) * zz[q].y * dph;
-                        c[b + 1] += wr * zz[q].x * dph2;
-                        c[b + 2] += -wr / T(3) * zz[q].y * dph2 * dph;
-                        c[b + 3] += -wr / T(12) * zz[q].x * dph2 * dph2;
-                    }
-                }
+        if (dir_mode) {
+            dN[n] = dpsi(n);
+            if (NV == 17) {
+                if (i < g.Nx - 1) { int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
+                if (j < g.Ny - 1) { int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
             }
         }
-        if (kappa2 > 0.0 && i < g.Nxc && j < g.Nyc) {
-            const int Nxa = g.Nx - 1;
-            const int ia00 = i + Nxa * j, ia0p = i + Nxa * (j + 1), ib00 = g.Na + i + g.Nx * j, ibp0 = g.Na + i + 1 + g.Nx * j;
-            const T k2 = (T)kappa2;
-            if (NV == 5) {
-                const T dB = idx * (ab[ibp0] - ab[ib00]) - idy * (ab[ia0p] - ab[ia00]) - (T)H;
-                c[0] += k2 * dB * dB;
-            } else {
-                const T a00 = lphase(abei, ab, ia00), a0p = lphase(abei, ab, ia0p);
-                const T b00 = lphase(abei, ab, ib00), bp0 = lphase(abei, ab, ibp0);
-                const T BH = idx * (bp0 - b00) - idy * (a0p - a00) - (T)H;
-                const T dB = idx * (dA(ibp0) - dA(ib00)) - idy * (dA(ia0p) - dA(ia00));
-                c[0] += k2 * BH * BH;
-                c[1] += k2 * T(2) * BH * dB;
-                c[2] += k2 * dB * dB;
-            }
-        }
+        coef_node<T, NV>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, psi, abei, ab, n, i, j, cb, dpsi, dA, c);
     }
     grid_sum_finish<NV>(c, partials, counter, dscal, g.dxdy);
 }
@@ -320,9 +150,12 @@ int cg_ensure(glgpu_handle* h) {
         cudaMemsetAsync(h->dir_A[q], 0, ab, h->stream);
     }
     cudaMemsetAsync(h->dscal + 28, 0, 2 * sizeof(double), h->stream);  // beta = 0
+    if (cudaMalloc(&h->cgst, sizeof(CGState)) != cudaSuccess) return set_error(h, GLGPU_E_OOM, "cg: out of device memory");
+    cudaMemsetAsync(h->cgst, 0, sizeof(CGState), h->stream);
     h->cg_g = 0;
     h->cg_dir = 0;
-    return cuda_check(h, cudaGetLastError(), "cg_ensure");
+    upload_inst(h);  // the descriptor carries the CG buffers
+    return cuda_check(h, cudaStreamSynchronize(h->stream), "cg_ensure");
 }
 
 int cg_reset_direction(glgpu_handle* h) {
@@ -336,7 +169,7 @@ static void launch_grad(glgpu_handle* h, int out_idx, int beta) {
     const int prev = 1 - out_idx;
     k_cg_grad<T><<<blocks_for(h->g.N), kThreads, 0, h->stream>>>(
         h->g, k2(h), h->p.epsilon, (const T*)h->eps_sp, h->p.H, h->mt, (const C2<T>*)h->psi[0], (const T*)h->abei, (const T*)h->ab[0],
-        (C2<T>*)h->g_psi[out_idx], (T*)h->g_A[out_idx], (const C2<T>*)h->g_psi[prev], (const T*)h->g_A[prev], fk(h) ? 1 : 0, beta,
+        (C2<T>*)h->g_psi[out_idx], (T*)h->g_A[out_idx], (const C2<T>*)h->g_psi[prev], (const T*)h->g_A[prev], fk(h) ? 1 : 0,
         h->partials, h->counter, h->dscal);
     if (beta) k_cg_beta<T><<<1, 32, 0, h->stream>>>(h->dscal, fk(h) ? 1 : 0);
 }

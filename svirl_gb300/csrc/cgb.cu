@@ -1,0 +1,665 @@
+// Batched device-side CG: every instance of a batch minimises its free energy
+// with the modified nonlinear CG of svirl/solvers/cg.py (Polak-Ribiere+ beta,
+// exact quartic line search in psi / quartic-in-psi, 4th-order-in-A polynomial
+// for (alpha_psi, alpha_A)), with the step length, beta and the stop test decided
+// on the device, so a whole CG run is one CUDA-graph launch for all instances.
+//
+// Per iteration: tile kernels (256 nodes of one instance per CTA) write per-tile
+// FP64 partial sums; one warp per instance then adds its tiles' partials in tile
+// order (deterministic) and takes the scalar decisions:
+//   kb_grad -> kb_inst_beta -> kb_dir_coef -> kb_inst_alpha -> kb_update ->
+//   kb_energy -> kb_inst_stop (sets the WHILE condition).
+// alpha: kappa = inf, the smallest non-negative real root of dP/dalpha (the
+// reference uses numpy polyroots, svirl/solvers/cg.py:227-235); finite kappa, a
+// damped Newton descent of the 2-D polynomial from (0, 0) (the reference uses
+// scipy BFGS from (0, 0), cg.py:378-419).  Stop: the reference's energy-ratio
+// test (cg.py:315-318,541-544) or |grad F| <= gtol |grad F at the first iteration|.
+// A call starts from a zero direction and beta = 0.
+#include <cmath>
+#include <cstring>
+
+#include "glgpu_internal.h"
+#include "glgpu_phys.cuh"
+
+namespace glgpu {
+
+constexpr int kPart = 17;  // doubles of per-tile partials
+
+struct CGLoop {
+    int active;
+    int iters;     // loop iterations done in this call
+    int n_iter;
+    int pad_;
+    double rtol, gtol;
+};
+
+template <typename T>
+__device__ __forceinline__ void store_partials(const double* v, int nv, double* out) {
+    for (int k = 0; k < nv; ++k) out[k] = v[k];
+}
+
+// gradient (new buffer), Polak-Ribiere sums and |g|^2 per tile
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const CGState* cs = I.cg;
+    if (*(volatile const int*)&cs->done) return;
+    const Geo g = I.g;
+    const int gi = cs->gi;
+    const C2<T>* psi = (const C2<T>*)I.psi[0];
+    const T* ab = (const T*)I.ab[0];
+    const T* abei = (const T*)I.abei;
+    C2<T>* G = (C2<T>*)I.gpsi[1 - gi];
+    const C2<T>* Gp = (const C2<T>*)I.gpsi[gi];
+    T* GA = (T*)I.gA[1 - gi];
+    const T* GAp = (const T*)I.gA[gi];
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const int n = t.n0 + threadIdx.x;
+    if (n < g.N) {
+        const int i = n % g.Nx, j = n / g.Nx;
+        const unsigned cb = cell_bits(g, I.mt, i, j);
+        const C2<T> gv = grad_psi_node<T>(g, gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp, psi, abei, ab, n, i, j, cb);
+        G[n] = gv;
+        const C2<T> gp = Gp[n];
+        v[0] = (double)(gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y));
+        v[1] = (double)(gp.x * gp.x + gp.y * gp.y);
+        v[4] = (double)(gv.x * gv.x + gv.y * gv.y);
+        if (I.solveA) {
+            const T k2 = gsel<T>(I.kappa2, I.fkappa2), H = gsel<T>(I.H, I.fH);
+            for (int dir = 0; dir < 2; ++dir) {
+                const bool has = dir == 0 ? (i < g.Nx - 1) : (j < g.Ny - 1);
+                if (!has) continue;
+                const int l = dir == 0 ? i + (g.Nx - 1) * j : g.Na + i + g.Nx * j;
+                const T ga = grad_A_link<T>(g, k2, H, psi, abei, ab, n, i, j, cb, dir == 0);
+                GA[l] = ga;
+                const T gap = GAp[l];
+                v[2] += (double)(ga * (ga - gap));
+                v[3] += (double)(gap * gap);
+                v[4] += (double)(ga * ga);
+            }
+        }
+    }
+    block_sum<5>(v);
+    if (threadIdx.x == 0) store_partials<T>(v, 5, partials + (size_t)blockIdx.x * kPart);
+}
+
+// Sum of component k of the partials of instance I's tiles, in tile order, by one warp.
+__device__ __forceinline__ double warp_tile_sum(const double* partials, int tile0, int ntiles, int k) {
+    const int lane = threadIdx.x & 31;
+    double s = 0.0;
+    for (int q = lane; q < ntiles; q += 32) s += partials[(size_t)(tile0 + q) * kPart + k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    return __shfl_sync(0xffffffffu, s, 0);
+}
+
+// beta (Polak-Ribiere+, cg.py:422-449) and the gradient-norm stop, one warp per instance
+__global__ void __launch_bounds__(128)
+kb_inst_beta(const Inst* __restrict__ insts, int ninst, const double* __restrict__ partials,
+                             CGLoop* loop) {
+    const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= ninst) return;
+    const Inst& I = insts[q];
+    CGState* cs = I.cg;
+    if (cs->done) return;
+    double v[5];
+    for (int k = 0; k < 5; ++k) v[k] = warp_tile_sum(partials, I.tile0, I.ntiles, k);
+    if ((threadIdx.x & 31) != 0) return;
+    if (cs->iter > 0) {
+        cs->beta_psi = fmax(v[0] / v[1], 0.0);
+        cs->beta_A = I.solveA ? fmax(v[2] / v[3], 0.0) : 0.0;
+    } else {
+        cs->beta_psi = 0.0;
+        cs->beta_A = 0.0;
+        cs->g2_0 = v[4];
+    }
+    cs->g2 = v[4];
+    cs->gi = 1 - cs->gi;
+    if (cs->iter > 0 && !(v[4] > loop->gtol * loop->gtol * cs->g2_0)) {
+        cs->done = 1;
+        cs->status = 1;
+        atomicSub(&loop->active, 1);
+    }
+}
+
+// new direction (written) and the per-tile line-search coefficient partials
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const CGState* cs = I.cg;
+    if (*(volatile const int*)&cs->done) return;
+    const Geo g = I.g;
+    const int gi = cs->gi, di = cs->di;
+    const T bp = (T)cs->beta_psi, bA = (T)cs->beta_A;
+    const C2<T>* psi = (const C2<T>*)I.psi[0];
+    const T* ab = (const T*)I.ab[0];
+    const T* abei = (const T*)I.abei;
+    const C2<T>* G = (const C2<T>*)I.gpsi[gi];
+    const T* GA = (const T*)I.gA[gi];
+    const C2<T>* dO = (const C2<T>*)I.dpsi[di];
+    const T* dAO = (const T*)I.dA[di];
+    C2<T>* dN = (C2<T>*)I.dpsi[1 - di];
+    T* dAN = (T*)I.dA[1 - di];
+    auto dpsi = [&](int m) -> C2<T> {
+        const C2<T> o = dO[m], gg = G[m];
+        return cmk<T>(bp * o.x - gg.x, bp * o.y - gg.y);
+    };
+    auto dA = [&](int m) -> T { return bA * dAO[m] - GA[m]; };
+    double c[17];
+#pragma unroll
+    for (int k = 0; k < 17; ++k) c[k] = 0.0;
+    const int n = t.n0 + threadIdx.x;
+    if (n < g.N) {
+        const int i = n % g.Nx, j = n / g.Nx;
+        const unsigned cb = cell_bits(g, I.mt, i, j);
+        dN[n] = dpsi(n);
+        const T eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
+        if (I.solveA) {
+            if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
+            if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
+            coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, n, i, j, cb,
+                             dpsi, dA, c);
+        } else {
+            double c5[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+            coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, n, i, j, cb, dpsi, dA, c5);
+            c[0] = c5[0]; c[5] = c5[1]; c[10] = c5[2]; c[15] = c5[3]; c[16] = c5[4];
+        }
+    }
+    block_sum<17>(c);
+    if (threadIdx.x == 0) store_partials<T>(c, 17, partials + (size_t)blockIdx.x * kPart);
+}
+
+// Real roots of d0 + d1 a + d2 a^2 + d3 a^3; returns the smallest root >= 0 or -1.
+__device__ double smallest_nonneg_root_cubic(double d0, double d1, double d2, double d3) {
+    double roots[3];
+    int nr = 0;
+    const double scale = fabs(d0) + fabs(d1) + fabs(d2) + fabs(d3);
+    if (!(scale > 0.0)) return -1.0;
+    if (fabs(d3) <= 1e-14 * scale) {
+        if (fabs(d2) <= 1e-14 * scale) {
+            if (d1 != 0.0) roots[nr++] = -d0 / d1;
+        } else {
+            const double disc = d1 * d1 - 4.0 * d2 * d0;
+            if (disc >= 0.0) {
+                const double s = sqrt(disc);
+                const double qq = -0.5 * (d1 + (d1 >= 0.0 ? s : -s));
+                if (qq != 0.0) roots[nr++] = d0 / qq;
+                roots[nr++] = qq / d2;
+            }
+        }
+    } else {
+        const double a = d2 / d3, b = d1 / d3, c = d0 / d3;
+        const double p = b - a * a / 3.0, qv = 2.0 * a * a * a / 27.0 - a * b / 3.0 + c;
+        const double disc = 0.25 * qv * qv + p * p * p / 27.0;
+        if (disc > 0.0) {
+            const double s = sqrt(disc);
+            roots[nr++] = cbrt(-0.5 * qv + s) + cbrt(-0.5 * qv - s) - a / 3.0;
+        } else {
+            const double r = 2.0 * sqrt(-p / 3.0);
+            double arg = r != 0.0 ? 3.0 * qv / (p * r) : 0.0;
+            arg = fmax(-1.0, fmin(1.0, arg));
+            const double phi = acos(arg);
+            for (int k = 0; k < 3; ++k) roots[nr++] = r * cos((phi - 2.0 * 3.141592653589793 * k) / 3.0) - a / 3.0;
+        }
+    }
+    double best = -1.0;
+    for (int k = 0; k < nr; ++k) {
+        double x = roots[k];
+        for (int it = 0; it < 3; ++it) {  // Newton polish on the cubic
+            const double f = ((d3 * x + d2) * x + d1) * x + d0, df = (3.0 * d3 * x + 2.0 * d2) * x + d1;
+            if (df != 0.0) x -= f / df;
+        }
+        if (x >= 0.0 && (best < 0.0 || x < best)) best = x;
+    }
+    return best;
+}
+
+// F(a, b) = sum c[i][j] a^i b^j for the 17-coefficient layout, with its
+// gradient and Hessian.
+__device__ void poly2(const double* c17, double a, double b, double* F, double* Fa, double* Fb, double* Faa,
+                      double* Fab, double* Fbb) {
+    double cc[5][5];
+    for (int i = 0; i < 5; ++i)
+        for (int j = 0; j < 5; ++j) cc[i][j] = 0.0;
+    for (int j = 0; j < 5; ++j) {
+        cc[0][j] = c17[j];
+        cc[1][j] = c17[5 + j];
+        cc[2][j] = c17[10 + j];
+    }
+    cc[3][0] = c17[15];
+    cc[4][0] = c17[16];
+    double ap[5] = {1, a, a * a, a * a * a, a * a * a * a}, bp[5] = {1, b, b * b, b * b * b, b * b * b * b};
+    double f = 0, fa = 0, fb = 0, faa = 0, fab = 0, fbb = 0;
+    for (int i = 0; i < 5; ++i)
+        for (int j = 0; j < 5; ++j) {
+            const double w = cc[i][j];
+            if (w == 0.0) continue;
+            f += w * ap[i] * bp[j];
+            if (i >= 1) fa += w * i * ap[i - 1] * bp[j];
+            if (j >= 1) fb += w * j * ap[i] * bp[j - 1];
+            if (i >= 2) faa += w * i * (i - 1) * ap[i - 2] * bp[j];
+            if (i >= 1 && j >= 1) fab += w * i * j * ap[i - 1] * bp[j - 1];
+            if (j >= 2) fbb += w * j * (j - 1) * ap[i] * bp[j - 2];
+        }
+    *F = f; *Fa = fa; *Fb = fb; *Faa = faa; *Fab = fab; *Fbb = fbb;
+}
+
+// local minimum of the 2-D polynomial reached by descent from (0, 0)
+__device__ bool minimise_poly2(const double* c17, double* a_out, double* b_out) {
+    double a = 0.0, b = 0.0;
+    double F, Fa, Fb, Faa, Fab, Fbb;
+    poly2(c17, a, b, &F, &Fa, &Fb, &Faa, &Fab, &Fbb);
+    const double g0 = sqrt(Fa * Fa + Fb * Fb);
+    for (int it = 0; it < 60; ++it) {
+        const double gn = sqrt(Fa * Fa + Fb * Fb);
+        if (!(gn > 1e-14 * (g0 + 1e-300))) break;
+        double sa, sb;
+        const double det = Faa * Fbb - Fab * Fab;
+        if (Faa > 0.0 && det > 0.0) {
+            sa = -(Fbb * Fa - Fab * Fb) / det;
+            sb = -(-Fab * Fa + Faa * Fb) / det;
+        } else {
+            const double h = fabs(Faa) + fabs(Fbb) + 1e-300;
+            sa = -Fa / h;
+            sb = -Fb / h;
+        }
+        double t = 1.0, Fn, Fna, Fnb, Fnaa, Fnab, Fnbb;
+        const double slope = Fa * sa + Fb * sb;
+        bool moved = false;
+        for (int ls = 0; ls < 60; ++ls) {
+            poly2(c17, a + t * sa, b + t * sb, &Fn, &Fna, &Fnb, &Fnaa, &Fnab, &Fnbb);
+            if (Fn <= F + 1e-4 * t * slope) {
+                moved = true;
+                break;
+            }
+            t *= 0.5;
+        }
+        if (!moved) break;
+        a += t * sa;
+        b += t * sb;
+        F = Fn; Fa = Fna; Fb = Fnb; Faa = Fnaa; Fab = Fnab; Fbb = Fnbb;
+        if (fabs(t * sa) + fabs(t * sb) <= 1e-15 * (1.0 + fabs(a) + fabs(b))) break;
+    }
+    *a_out = a;
+    *b_out = b;
+    return isfinite(a) && isfinite(b);
+}
+
+// coefficients of each instance and its step lengths, one warp per instance
+__global__ void __launch_bounds__(128)
+kb_inst_alpha(const Inst* __restrict__ insts, int ninst, const double* __restrict__ partials,
+                              CGLoop* loop) {
+    const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= ninst) return;
+    const Inst& I = insts[q];
+    CGState* cs = I.cg;
+    if (cs->done) return;
+    double c[17];
+    for (int k = 0; k < 17; ++k) c[k] = warp_tile_sum(partials, I.tile0, I.ntiles, k) * I.g.dxdy;
+    if ((threadIdx.x & 31) != 0) return;
+    for (int k = 0; k < 17; ++k) cs->c[k] = c[k];
+    bool ok;
+    if (I.solveA) {
+        ok = minimise_poly2(c, &cs->alpha_psi, &cs->alpha_A);
+    } else {
+        const double a = smallest_nonneg_root_cubic(c[5], 2.0 * c[10], 3.0 * c[15], 4.0 * c[16]);
+        ok = a >= 0.0;
+        cs->alpha_psi = a;
+        cs->alpha_A = 0.0;
+    }
+    cs->di = 1 - cs->di;  // the new direction is now current
+    if (!ok) {
+        cs->done = 1;
+        cs->status = -1;
+        atomicSub(&loop->active, 1);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+kb_update(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const CGState* cs = I.cg;
+    if (*(volatile const int*)&cs->done) return;
+    const Geo g = I.g;
+    const int n = t.n0 + threadIdx.x;
+    if (n >= g.N) return;
+    const T ap = (T)cs->alpha_psi, aA = (T)cs->alpha_A;
+    C2<T>* psi = (C2<T>*)I.psi[0];
+    const C2<T> d = ((const C2<T>*)I.dpsi[cs->di])[n];
+    C2<T> p = psi[n];
+    p.x = ap * d.x + p.x;
+    p.y = ap * d.y + p.y;
+    psi[n] = p;
+    if (I.solveA) {
+        T* ab = (T*)I.ab[0];
+        const T* dA = (const T*)I.dA[cs->di];
+        const int i = n % g.Nx, j = n / g.Nx;
+        if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; ab[na] = aA * dA[na] + ab[na]; }
+        if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; ab[nb] = aA * dA[nb] + ab[nb]; }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials, int all) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    if (!all && *(volatile const int*)&I.cg->done) return;
+    const Geo g = I.g;
+    double v[1] = {0.0};
+    const int n = t.n0 + threadIdx.x;
+    if (n < g.N)
+        v[0] = (double)energy_density<T>(g, gsel<T>(I.kappa2, I.fkappa2), gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp,
+                                         gsel<T>(I.H, I.fH), I.mt, (const C2<T>*)I.psi[0], (const T*)I.abei,
+                                         (const T*)I.ab[0], n);
+    block_sum<1>(v);
+    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kPart] = v[0];
+}
+
+// energies, the energy-ratio stop, the iteration cap, and the WHILE condition
+// (one CTA for the whole batch).
+__global__ void __launch_bounds__(1024)
+kb_inst_stop(const Inst* __restrict__ insts, int ninst, const double* __restrict__ partials,
+                             CGLoop* loop, cudaGraphConditionalHandle cond, int use_cond) {
+    const int nw = blockDim.x >> 5;
+    for (int q = threadIdx.x >> 5; q < ninst; q += nw) {
+        const Inst& I = insts[q];
+        CGState* cs = I.cg;
+        if (cs->done) continue;
+        const double E = warp_tile_sum(partials, I.tile0, I.ntiles, 0) * I.g.dxdy;
+        if ((threadIdx.x & 31) != 0) continue;
+        cs->E_prev = cs->E;
+        cs->E = E;
+        const int it = cs->iter;
+        cs->iter = it + 1;
+        if (it > 0 && fabs(E / cs->E_prev - 1.0) < loop->rtol) {
+            cs->done = 1;
+            cs->status = 2;
+            atomicSub(&loop->active, 1);
+        } else if (cs->iter >= loop->n_iter) {
+            cs->done = 1;
+            cs->status = 3;
+            atomicSub(&loop->active, 1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const int iters = loop->iters + 1;
+        loop->iters = iters;
+        const int act = atomicAdd(&loop->active, 0);
+        const unsigned go = (act > 0 && iters < loop->n_iter + 2) ? 1u : 0u;
+        if (use_cond) cudaGraphSetConditional(cond, go);
+        loop->pad_ = (int)go;
+    }
+}
+
+// start of a CG call: zero direction, beta = 0, counters; energy of the start state
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+kb_zero_dir(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const Geo g = I.g;
+    const int n = t.n0 + threadIdx.x;
+    if (n >= g.N) return;
+    ((C2<T>*)I.dpsi[0])[n] = cmk<T>(T(0), T(0));
+    ((C2<T>*)I.gpsi[0])[n] = cmk<T>(T(0), T(0));
+    const int i = n % g.Nx, j = n / g.Nx;
+    if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; ((T*)I.dA[0])[na] = T(0); ((T*)I.gA[0])[na] = T(0); }
+    if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; ((T*)I.dA[0])[nb] = T(0); ((T*)I.gA[0])[nb] = T(0); }
+}
+
+__global__ void __launch_bounds__(1024)
+kb_init(const Inst* __restrict__ insts, int ninst, const double* __restrict__ partials, CGLoop* loop,
+                        cudaGraphConditionalHandle cond, int use_cond) {
+    const int nw = blockDim.x >> 5;
+    for (int q = threadIdx.x >> 5; q < ninst; q += nw) {
+        const Inst& I = insts[q];
+        const double E = warp_tile_sum(partials, I.tile0, I.ntiles, 0) * I.g.dxdy;
+        if ((threadIdx.x & 31) != 0) continue;
+        CGState* cs = I.cg;
+        cs->beta_psi = cs->beta_A = 0.0;
+        cs->alpha_psi = cs->alpha_A = 0.0;
+        cs->E = E;
+        cs->E_prev = E;
+        cs->g2 = cs->g2_0 = 0.0;
+        cs->iter = 0;
+        cs->done = 0;
+        cs->gi = 0;
+        cs->di = 0;
+        cs->status = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        loop->active = ninst;
+        loop->iters = 0;
+        const unsigned go = (ninst > 0 && loop->n_iter > 0) ? 1u : 0u;
+        if (use_cond) cudaGraphSetConditional(cond, go);
+        loop->pad_ = (int)go;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+struct CGLaunch {
+    const Inst* insts;
+    const Tile* tiles;
+    double* partials;
+    CGLoop* loop;
+    int ninst, ntiles, dtype;
+};
+
+static void* fn_grad(int dt) { return dt == 8 ? (void*)kb_grad<double> : (void*)kb_grad<float>; }
+static void* fn_dir_coef(int dt) { return dt == 8 ? (void*)kb_dir_coef<double> : (void*)kb_dir_coef<float>; }
+static void* fn_update(int dt) { return dt == 8 ? (void*)kb_update<double> : (void*)kb_update<float>; }
+static void* fn_energy(int dt) { return dt == 8 ? (void*)kb_energy<double> : (void*)kb_energy<float>; }
+static void* fn_zero_dir(int dt) { return dt == 8 ? (void*)kb_zero_dir<double> : (void*)kb_zero_dir<float>; }
+
+static inline int warp_blocks(int ninst) { return (ninst + 3) / 4; }  // 4 warps of 32 per CTA
+
+// Host-driven loop body (the graph holds the same launches).
+static cudaError_t cg_launch_body(const CGLaunch& L, cudaStream_t s) {
+    const cudaGraphConditionalHandle none = 0;
+    const int wb = warp_blocks(L.ninst);
+    if (L.dtype == 8) kb_grad<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
+    else kb_grad<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
+    kb_inst_beta<<<wb, 128, 0, s>>>(L.insts, L.ninst, L.partials, L.loop);
+    if (L.dtype == 8) kb_dir_coef<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
+    else kb_dir_coef<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
+    kb_inst_alpha<<<wb, 128, 0, s>>>(L.insts, L.ninst, L.partials, L.loop);
+    if (L.dtype == 8) kb_update<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    else kb_update<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    if (L.dtype == 8) kb_energy<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, 0);
+    else kb_energy<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, 0);
+    kb_inst_stop<<<1, 1024, 0, s>>>(L.insts, L.ninst, L.partials, L.loop, none, 0);
+    return cudaGetLastError();
+}
+
+static cudaError_t cg_launch_prologue(const CGLaunch& L, cudaStream_t s) {
+    const cudaGraphConditionalHandle none = 0;
+    if (L.dtype == 8) kb_zero_dir<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    else kb_zero_dir<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    if (L.dtype == 8) kb_energy<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, 1);
+    else kb_energy<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, 1);
+    kb_init<<<1, 1024, 0, s>>>(L.insts, L.ninst, L.partials, L.loop, none, 0);
+    return cudaGetLastError();
+}
+
+#define GCHK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { err = e_; goto fail; } } while (0)
+
+// The whole CG run of all instances as one graph:
+//   zero_dir -> energy -> init -> WHILE(active) {
+//       grad -> beta -> dir_coef -> alpha -> update -> energy -> stop }
+static cudaError_t build_cg_graph(const CGLaunch& L, cudaGraphExec_t* exec) {
+    cudaError_t err = cudaSuccess;
+    cudaGraph_t top = nullptr, body = nullptr;
+    cudaGraphConditionalHandle h;
+    cudaGraphNode_t prev = nullptr, nd;
+    int zero = 0, one = 1;
+    const dim3 gt(L.ntiles), bt(kThreads), gw(warp_blocks(L.ninst)), bw(128), g1(1), b1(1024);
+    const Inst* insts = L.insts;
+    const Tile* tiles = L.tiles;
+    double* partials = L.partials;
+    CGLoop* loop = L.loop;
+    int ninst = L.ninst;
+
+    GCHK(cudaGraphCreate(&top, 0));
+    GCHK(cudaGraphConditionalHandleCreate(&h, top, 0, cudaGraphCondAssignDefault));
+    {
+        void* a[] = {&insts, &tiles};
+        GCHK(add_kernel(top, &nd, nullptr, 0, fn_zero_dir(L.dtype), gt, bt, a));
+        prev = nd;
+    }
+    {
+        void* a[] = {&insts, &tiles, &partials, &one};
+        GCHK(add_kernel(top, &nd, &prev, 1, fn_energy(L.dtype), gt, bt, a));
+        prev = nd;
+    }
+    {
+        void* a[] = {&insts, &ninst, &partials, &loop, &h, &one};
+        GCHK(add_kernel(top, &nd, &prev, 1, (void*)kb_init, g1, b1, a));
+        prev = nd;
+    }
+    GCHK(add_while(top, &nd, &prev, 1, h, &body));
+    prev = nullptr;
+    {
+        void* a[] = {&insts, &tiles, &partials};
+        GCHK(add_kernel(body, &nd, nullptr, 0, fn_grad(L.dtype), gt, bt, a));
+        prev = nd;
+    }
+    {
+        void* a[] = {&insts, &ninst, &partials, &loop};
+        GCHK(add_kernel(body, &nd, &prev, 1, (void*)kb_inst_beta, gw, bw, a));
+        prev = nd;
+    }
+    {
+        void* a[] = {&insts, &tiles, &partials};
+        GCHK(add_kernel(body, &nd, &prev, 1, fn_dir_coef(L.dtype), gt, bt, a));
+        prev = nd;
+    }
+    {
+        void* a[] = {&insts, &ninst, &partials, &loop};
+        GCHK(add_kernel(body, &nd, &prev, 1, (void*)kb_inst_alpha, gw, bw, a));
+        prev = nd;
+    }
+    {
+        void* a[] = {&insts, &tiles};
+        GCHK(add_kernel(body, &nd, &prev, 1, fn_update(L.dtype), gt, bt, a));
+        prev = nd;
+    }
+    {
+        void* a[] = {&insts, &tiles, &partials, &zero};
+        GCHK(add_kernel(body, &nd, &prev, 1, fn_energy(L.dtype), gt, bt, a));
+        prev = nd;
+    }
+    {
+        void* a[] = {&insts, &ninst, &partials, &loop, &h, &one};
+        GCHK(add_kernel(body, &nd, &prev, 1, (void*)kb_inst_stop, g1, b1, a));
+    }
+    GCHK(cudaGraphInstantiate(exec, top, 0));
+    cudaGraphDestroy(top);
+    return cudaSuccess;
+fail:
+    if (top) cudaGraphDestroy(top);
+    *exec = nullptr;
+    return err;
+}
+#undef GCHK
+
+int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int32_t* iters, double* energies, double* grad_rel,
+             int32_t* status, double* elapsed_ms) {
+    if (n_iter < 0 || !(rtol >= 0.0) || !(gtol >= 0.0)) return batch_error(b, GLGPU_E_ARG, "batch_cg: bad n_iter, rtol or gtol");
+    std::vector<Inst> insts(b->ninst);
+    int tile0 = 0;
+    for (int q = 0; q < b->ninst; ++q) {
+        glgpu_handle* h = b->hs[q];
+        const int rc = cg_ensure(h);
+        if (rc) return batch_error(b, rc, "batch_cg: " + h->last_error);
+        cudaStreamSynchronize(h->stream);
+        insts[q] = h->inst_h;
+        insts[q].tile0 = tile0;  // the batch's tile table lists the instances' tiles in order
+        tile0 += h->ntiles;
+    }
+    if (!b->cg_partials && cudaMalloc(&b->cg_partials, sizeof(double) * kPart * (size_t)b->ntiles) != cudaSuccess)
+        return batch_error(b, GLGPU_E_OOM, "batch_cg: out of device memory");
+    if (!b->cg_loop && cudaMalloc(&b->cg_loop, sizeof(CGLoop)) != cudaSuccess)
+        return batch_error(b, GLGPU_E_OOM, "batch_cg: out of device memory");
+    cudaStream_t s = b->stream;
+    CGLoop lp;
+    memset(&lp, 0, sizeof(lp));
+    lp.n_iter = n_iter;
+    lp.rtol = rtol;
+    lp.gtol = gtol;
+    cudaError_t e = cudaMemcpyAsync(b->insts, insts.data(), sizeof(Inst) * insts.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->cg_loop, &lp, sizeof(lp), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_cg: ") + cudaGetErrorString(e));
+    CGLaunch L;
+    L.insts = b->insts;
+    L.tiles = b->tiles;
+    L.partials = b->cg_partials;
+    L.loop = (CGLoop*)b->cg_loop;
+    L.ninst = b->ninst;
+    L.ntiles = b->ntiles;
+    L.dtype = b->dtype;
+    if (b->use_graphs && !b->cg_graph_failed && !b->cg_exec && build_cg_graph(L, &b->cg_exec) != cudaSuccess) {
+        b->cg_graph_failed = true;
+        cudaGetLastError();
+    }
+    const bool graph = b->use_graphs && b->cg_exec != nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (elapsed_ms) {
+        cudaEventCreate(&ev0);
+        cudaEventCreate(&ev1);
+        cudaEventRecord(ev0, s);
+    }
+    if (graph) {
+        e = cudaGraphLaunch(b->cg_exec, s);
+    } else {
+        e = cg_launch_prologue(L, s);
+        int* go_h = nullptr;
+        if (e == cudaSuccess) e = cudaMallocHost(&go_h, sizeof(int));
+        for (int it = 0; e == cudaSuccess && it < n_iter + 1; ++it) {
+            *go_h = 0;
+            e = cudaMemcpyAsync(go_h, &L.loop->pad_, sizeof(int), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess || !*go_h) break;
+            e = cg_launch_body(L, s);
+        }
+        if (go_h) cudaFreeHost(go_h);
+    }
+    if (elapsed_ms) cudaEventRecord(ev1, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (elapsed_ms) {
+        float ms = 0.f;
+        if (e == cudaSuccess) cudaEventElapsedTime(&ms, ev0, ev1);
+        *elapsed_ms = ms;
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+    }
+    if (e != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_cg: ") + cudaGetErrorString(e));
+    int nfail = 0;
+    for (int q = 0; q < b->ninst; ++q) {
+        CGState cs;
+        e = cudaMemcpy(&cs, b->hs[q]->cgst, sizeof(cs), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_cg: ") + cudaGetErrorString(e));
+        if (iters) iters[q] = cs.iter;
+        if (energies) energies[q] = cs.E;
+        if (grad_rel) grad_rel[q] = cs.g2_0 > 0.0 ? std::sqrt(cs.g2 / cs.g2_0) : 0.0;
+        if (status) status[q] = cs.status;
+        if (cs.status < 0) ++nfail;
+    }
+    if (nfail)
+        return batch_error(b, GLGPU_E_NOROOT, "batch_cg: no descent step for " + std::to_string(nfail) + " instance(s)");
+    return GLGPU_OK;
+}
+
+}  // namespace glgpu

@@ -31,6 +31,18 @@ struct InstState {
     int pad_;
 };
 
+// Device-resident state of one instance in the batched device CG.
+struct CGState {
+    double beta_psi, beta_A;
+    double c[17];             // line-search coefficients of the current iteration
+    double alpha_psi, alpha_A;
+    double E, E_prev;         // energy after the last / the previous update
+    double g2, g2_0;          // |gradient|^2 now and at the first iteration
+    int iter, done, gi, di;   // iterations done, finished, current gradient / direction buffer
+    int status;               // 0 ok, 1 gradient-norm stop, 2 energy stop, 3 n_iter, -1 no step found
+    int pad_[3];
+};
+
 // Everything a kernel needs to process one instance.  Lives in device memory,
 // one entry per instance of a batch (a single GLSolver is a batch of one).
 struct Inst {
@@ -48,6 +60,11 @@ struct Inst {
     void* U;                  // link factors exp(-i d a) of the psi loop, Nab complex
     uint8_t* code;            // per-node link-weight bits of the psi loop, N bytes
     InstState* st;
+    CGState* cg;              // batched device CG state (NULL until used)
+    void* gpsi[2];            // CG gradient buffers (psi part, A part) and directions
+    void* gA[2];
+    void* dpsi[2];
+    void* dA[2];
     int tile0, ntiles;        // this instance's range in the tile table
     int nitems;               // number of warp-strip items of this instance
     int solveA;               // finite kappa
@@ -120,6 +137,7 @@ struct glgpu_handle {
     void* dir_psi[2] = {nullptr, nullptr};
     void* dir_A[2] = {nullptr, nullptr};
     int cg_g = 0, cg_dir = 0;           // current index of g / dir
+    glgpu::CGState* cgst = nullptr;     // batched device CG state
     // TD graphs, one per (equation mode, kappa finite)
     cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     glgpu::InstState* st_gather = nullptr;  // device copy target of the loop state
@@ -148,6 +166,11 @@ struct glgpu_batch {
     int ntiles = 0, nitems = 0, psi_grid = 0;
     cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool td_graph_failed = false, use_graphs = true;
+    // batched device CG (allocated on first use)
+    double* cg_partials = nullptr;       // ntiles * 17 doubles
+    void* cg_loop = nullptr;             // CGLoop
+    cudaGraphExec_t cg_exec = nullptr;
+    bool cg_graph_failed = false;
     std::string last_error;
 };
 
@@ -181,6 +204,14 @@ int cg_coefficients(glgpu_handle* h, double* c_out);
 int cg_update(glgpu_handle* h, double alpha_psi, double alpha_A, double* energy_out);
 int cg_read_gradient(glgpu_handle* h, void* gpsi_host, void* gA_host);
 int cg_coef_for(glgpu_handle* h, const void* dpsi_host, const void* dab_host, double* c_out);
+// cgb.cu
+int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int32_t* iters, double* energies, double* grad_rel,
+             int32_t* status, double* elapsed_ms);
+// td.cu graph helpers
+cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps, void* fn, dim3 grid,
+                       dim3 block, void** args);
+cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
+                      cudaGraphConditionalHandle h, cudaGraph_t* body);
 
 inline int blocks_for(long long n) { return (int)((n + kThreads - 1) / kThreads); }
 

@@ -8,71 +8,9 @@
 #include <string>
 
 #include "glgpu_internal.h"
+#include "glgpu_phys.cuh"
 
 namespace glgpu {
-
-// Du discretisation weights (svirl/cuda/observables.h:294-299).
-template <typename T> struct DuW {
-    T r_m0, r_p0, r_0m, r_0p, g;
-};
-template <typename T> __device__ __forceinline__ DuW<T> du_weights(unsigned cb) {
-    DuW<T> w;
-    const T mm = GL_MM(cb) ? T(1) : T(0), mp = GL_MP(cb) ? T(1) : T(0);
-    const T pm = GL_PM(cb) ? T(1) : T(0), pp = GL_PP(cb) ? T(1) : T(0);
-    w.r_m0 = T(0.5) * (mm + mp);
-    w.r_p0 = T(0.5) * (pm + pp);
-    w.r_0m = T(0.5) * (mm + pm);
-    w.r_0p = T(0.5) * (mp + pp);
-    w.g = T(0.25) * (w.r_m0 + w.r_p0 + w.r_0m + w.r_0p);
-    return w;
-}
-
-template <typename T> __device__ __forceinline__ T link_phase(const T* abei, const T* ab, int n) {
-    T p = T(0);
-    if (abei) p += abei[n];
-    if (ab) p += ab[n];
-    return p;
-}
-
-// curl of one link field on cell (i, j): idx*(b[i+1,j]-b[i,j]) - idy*(a[i,j+1]-a[i,j]).
-template <typename T> __device__ __forceinline__ T cell_curl(const Geo& g, const T* A, int i, int j, T idx, T idy) {
-    const int Nxa = g.Nx - 1;
-    return idx * (A[g.Na + (i + 1) + g.Nx * j] - A[g.Na + i + g.Nx * j]) - idy * (A[i + Nxa * (j + 1)] - A[i + Nxa * j]);
-}
-
-// Free-energy pseudo-density at node n before the dx*dy factor
-// (svirl/cuda/observables.h:276-356).
-template <typename T>
-__device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H,
-                                            const uint8_t* mt, const C2<T>* psi, const T* abei, const T* ab, int n) {
-    const int i = n % g.Nx, j = n / g.Nx;
-    const unsigned cb = cell_bits(g, mt, i, j);
-    const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
-    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
-    T e = T(0);
-    if (cb) {
-        const DuW<T> w = du_weights<T>(cb);
-        const C2<T> p00 = psi[n];
-        const T p2 = cabs2(p00);
-        const T eps = eps_sp ? eps_sp[n] : eps0;
-        e += w.g * (T(0.5) * p2 - eps) * p2;
-        if (GL_PM(cb) || GL_PP(cb)) {
-            T ph = link_phase(abei, ab, i + (g.Nx - 1) * j);
-            e += w.r_p0 * idx2 * g_grad<T>(p00, dx * ph, psi[n + 1]);
-        }
-        if (GL_MP(cb) || GL_PP(cb)) {
-            T ph = link_phase(abei, ab, g.Na + i + g.Nx * j);
-            e += w.r_0p * idy2 * g_grad<T>(p00, dy * ph, psi[n + g.Nx]);
-        }
-    }
-    if (kappa2 > T(0) && i < g.Nxc && j < g.Nyc) {
-        T dB = -H;
-        if (abei) dB += cell_curl(g, abei, i, j, idx, idy);
-        if (ab) dB += cell_curl(g, ab, i, j, idx, idy);
-        e += kappa2 * dB * dB;
-    }
-    return e;
-}
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -95,48 +33,6 @@ k_magnetic_field(Geo g, const T* abei, const T* ab, T* B) {
     if (abei) b += cell_curl(g, abei, i, j, idx, idy);
     if (ab) b += cell_curl(g, ab, i, j, idx, idy);
     B[n] = b;
-}
-
-// kappa^2 curl curl A on the link starting at node (i, j) along x (xdir) or y,
-// with the reference's boundary treatment (svirl/cuda/observables.h:66-155,
-// svirl/cuda/cg.h:174-300).  abei_nb_scale_dd: the external part's neighbour
-// terms carry dd/dd (current) or 1 (gradient); both are 1.
-template <typename T>
-__device__ __forceinline__ T curlcurl_link(const Geo& g, const T* abei, const T* ab, T H, int i, int j, bool xdir) {
-    const int Nxa = g.Nx - 1, Na = g.Na, Nx = g.Nx;
-    const T idx = GT(g, idx), idy = GT(g, idy);
-    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
-    T c = T(0), dd = T(1);
-    if (xdir) {
-        const int n = i + Nxa * j;
-        if (j == 0) { c -= T(2) * H * idy; dd = T(2); }
-        else if (j + 1 == g.Ny) { c += T(2) * H * idy; dd = T(2); }
-        if (abei) c += T(2) / dd * idy2 * abei[n];
-        if (ab) c += T(2) * idy2 * ab[n];
-        if (j > 0) {
-            if (abei) c += (-idy2 * abei[i + Nxa * (j - 1)] + idxy * abei[Na + i + Nx * (j - 1)] - idxy * abei[Na + i + 1 + Nx * (j - 1)]);
-            if (ab) c += dd * (-idy2 * ab[i + Nxa * (j - 1)] + idxy * ab[Na + i + Nx * (j - 1)] - idxy * ab[Na + i + 1 + Nx * (j - 1)]);
-        }
-        if (j + 1 < g.Ny) {
-            if (abei) c += (-idy2 * abei[i + Nxa * (j + 1)] - idxy * abei[Na + i + Nx * j] + idxy * abei[Na + i + 1 + Nx * j]);
-            if (ab) c += dd * (-idy2 * ab[i + Nxa * (j + 1)] - idxy * ab[Na + i + Nx * j] + idxy * ab[Na + i + 1 + Nx * j]);
-        }
-    } else {
-        const int n = Na + i + Nx * j;
-        if (i == 0) { c += T(2) * H * idx; dd = T(2); }
-        else if (i + 1 == g.Nx) { c -= T(2) * H * idx; dd = T(2); }
-        if (abei) c += T(2) / dd * idx2 * abei[n];
-        if (ab) c += T(2) * idx2 * ab[n];
-        if (i > 0) {
-            if (abei) c += (-idx2 * abei[Na + (i - 1) + Nx * j] + idxy * abei[(i - 1) + Nxa * j] - idxy * abei[(i - 1) + Nxa * (j + 1)]);
-            if (ab) c += dd * (-idx2 * ab[Na + (i - 1) + Nx * j] + idxy * ab[(i - 1) + Nxa * j] - idxy * ab[(i - 1) + Nxa * (j + 1)]);
-        }
-        if (i + 1 < g.Nx) {
-            if (abei) c += (-idx2 * abei[Na + (i + 1) + Nx * j] - idxy * abei[i + Nxa * j] + idxy * abei[i + Nxa * (j + 1)]);
-            if (ab) c += dd * (-idx2 * ab[Na + (i + 1) + Nx * j] - idxy * ab[i + Nxa * j] + idxy * ab[i + Nxa * (j + 1)]);
-        }
-    }
-    return c;
 }
 
 template <typename T>

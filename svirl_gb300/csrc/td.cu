@@ -487,7 +487,7 @@ static void* link_fn(int dtype) {
     return dtype == 8 ? (void*)k_link_U<double> : (void*)k_link_U<float>;
 }
 
-static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
+cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
                               void* fn, dim3 grid, dim3 block, void** args) {
     cudaKernelNodeParams p;
     memset(&p, 0, sizeof(p));
@@ -500,7 +500,7 @@ static cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGr
     return cudaGraphAddKernelNode(node, g, deps, ndeps, &p);
 }
 
-static cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
+cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
                              cudaGraphConditionalHandle h, cudaGraph_t* body) {
     cudaGraphNodeParams p = {};
     p.type = cudaGraphNodeTypeConditional;
