@@ -152,18 +152,23 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(dtype_name):
-    """DRAM bytes per psi-sweep launch from the committed ncu summary (or None)."""
+def ncu_traffic(dtype_name, fuse):
+    """DRAM bytes per psi-sweep launch from the committed ncu summary of the same
+    kernel build (same sweeps per launch), or None."""
     p = os.path.join(ROOT, "profiles", "psi_sweep_%s_2049.md" % dtype_name)
     if not os.path.exists(p):
         return None
+    vals = {}
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
+        if ":" in line and line.split(":", 1)[0] in ("traffic_bytes_per_launch", "sweeps_per_launch"):
+            k, v = line.split(":", 1)
             try:
-                return float(line.split(":", 1)[1].strip())
+                vals[k] = float(v.strip())
             except ValueError:
                 return None
-    return None
+    if int(vals.get("sweeps_per_launch", 1)) != fuse:
+        return None
+    return vals.get("traffic_bytes_per_launch")
 
 
 def cpu_baseline(budget_s=20.0, n_side=257):
@@ -275,11 +280,14 @@ def main():
     sweeps = int(st.total_sweeps_psi)
     value = world * N * args.steps / (ms * 1e-3)
 
-    # roofline of the dominant kernel (the psi Jacobi sweep), timed alone
+    # roofline of the dominant kernel (the psi Jacobi sweep), timed alone.  One
+    # launch does `fuse` sweeps.  Algorithmic bytes per node-sweep: read psi^(k),
+    # the right-hand side and two link values of A, write psi^(k+1) (32 B FP32,
+    # 64 B FP64), +1 B for the material mask.
+    fuse = int(h.lib.glgpu_psi_sweeps_per_launch())
     sweep_ms = h.time_sweeps(0, 20)
-    # per node: psi^(k), rhs, the two link factors of the step's table, write; +1 B link-weight code
-    bytes_per_node = (40 if dtype == np.float32 else 80) + 1
-    alg_bytes = N * bytes_per_node
+    bytes_per_node_sweep = (32 if dtype == np.float32 else 64) + 1
+    alg_bytes = N * bytes_per_node_sweep * fuse
     peak, peak_kind = peaks()
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
 
@@ -305,7 +313,9 @@ def main():
 
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_baseline()
-        launches = sweeps + 3 * args.steps + 2
+        # sweep launches counted on the device, plus per step the link table, the
+        # loop begin/end and step-end kernels, plus the final copy and reset
+        launches = int(st.sweep_launches) + 4 * args.steps + 3
         line = {
             "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -317,9 +327,10 @@ def main():
                              % (N * (3 * (8 if dtype == np.float32 else 16) + (8 if dtype == np.float32 else 16)) / 1e6),
                        "mean_sweeps_per_step": sweeps / args.steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": ncu_traffic(args.dtype),
-                         "kernel": "k_psi_sweep", "bytes_per_launch": alg_bytes, "launch_ms": sweep_ms,
-                         "peak_kind": peak_kind},
+                         "frac": achieved / peak, "traffic": ncu_traffic(args.dtype, fuse),
+                         "kernel": "k_psi_sweep", "sweeps_per_launch": fuse,
+                         "bytes_per_node_sweep": bytes_per_node_sweep, "bytes_per_launch": alg_bytes,
+                         "launch_ms": sweep_ms, "peak_kind": peak_kind},
             "e2e": {"value": e2e_value, "unit": "node-steps/s",
                     "h2d_bytes_per_step": int(psi_in.nbytes), "d2h_bytes_per_step": int(psi_out.nbytes),
                     "how": "per step: H2D psi from pinned memory, glgpu_td (1 step), D2H psi, via the C ABI"},

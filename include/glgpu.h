@@ -70,6 +70,7 @@ typedef struct {
     int64_t total_sweeps_psi, total_sweeps_A;
     uint32_t rand_t;        /* Langevin seed after the call */
     int32_t used_graph;     /* 1: device-side loop (CUDA graph), 0: host-driven loop */
+    int64_t sweep_launches; /* Jacobi sweep kernel launches (psi and A) */
 } glgpu_td_stats;
 
 /* --- lifetime: GLSolver construction / destruction (svirl/__init__.py:30-179,
@@ -78,6 +79,10 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out);
 int glgpu_destroy(glgpu_handle* h);
 const char* glgpu_last_error(const glgpu_handle* h);   /* h may be NULL: last create error */
 int glgpu_version(void);
+/* Jacobi sweeps of the psi step done by one launch of the psi sweep kernel
+ * (temporal blocking; every sweep is still written, so the loop stops exactly
+ * where the reference's one-sweep-per-launch loop stops). */
+int glgpu_psi_sweeps_per_launch(void);
 
 /* --- state and parameters (svirl/vars/vars.py:53-127, svirl/vars/params.py,
  *     svirl/mesh/grid.py:102-127) */
@@ -171,9 +176,14 @@ int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable);
  * or when |grad F| <= gtol |grad F of the first iteration| (gtol = 0: off).
  * Per-instance outputs (each may be NULL): iterations done, final energy,
  * final |grad F| relative to the first, status (1 gradient stop, 2 energy stop,
- * 3 n_iter reached, -1 no descent step; then GLGPU_E_NOROOT is returned). */
-int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t* iters, double* energies,
-                   double* grad_rel, int32_t* status, double* elapsed_ms);
+ * 3 n_iter reached, -1 no descent step; then GLGPU_E_NOROOT is returned).
+ * flags: GLGPU_CG_EXACT_BOUNDARY makes dF/dA the exact derivative of the free
+ * energy on the boundary links too; the reference's formula (cg.h:174-300)
+ * doubles the H and A terms there, so its gradient does not vanish at the
+ * energy minimum and the gradient-norm stop cannot be met at finite kappa. */
+#define GLGPU_CG_EXACT_BOUNDARY 1
+int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t flags, int32_t* iters,
+                   double* energies, double* grad_rel, int32_t* status, double* elapsed_ms);
 
 /* --- free energy of a caller-owned state with no allocation by the library.
  *     No counterpart in the reference (its gsum allocates work arrays,

@@ -473,6 +473,29 @@ def free_energy_jacobian_A(g, kappa2, H, mt, psi, abei, ab):
     return np.concatenate([(s * ca).reshape(-1), (s * cb).reshape(-1)])
 
 
+def free_energy_jacobian_A_exact(g, kappa2, H, mt, psi, abei, ab):
+    """The exact derivative of ``free_energy`` with respect to A.  Not in the
+    reference: its dF/dA (``svirl/cuda/cg.h:124-301``, above) doubles the H and A
+    terms of the magnetic part on the boundary links, which belong to one cell
+    only.  Here the magnetic part is assembled cell by cell from
+    d/dA kappa^2 dx dy (curl A - H)^2; the supercurrent part is the reference's."""
+    r = -H * np.ones((g.Nyc, g.Nxc))
+    if abei is not None:
+        r = r + _curl(g, abei)
+    if ab is not None:
+        r = r + _curl(g, ab)
+    ca = np.zeros((g.Nya, g.Nxa))
+    cb = np.zeros((g.Nyb, g.Nxb))
+    ca[:-1, :] += g.idy * r   # link a(i, j) is the lower edge of cell (i, j)
+    ca[1:, :] -= g.idy * r    # ... and the upper edge of cell (i, j-1)
+    cb[:, :-1] -= g.idx * r   # link b(i, j) is the left edge of cell (i, j)
+    cb[:, 1:] += g.idx * r    # ... and the right edge of cell (i-1, j)
+    ref = free_energy_jacobian_A(g, kappa2, H, mt, psi, abei, ab)
+    mag_ref = free_energy_jacobian_A(g, kappa2, H, mt, np.zeros_like(psi), abei, ab)
+    s = 2.0 * g.dx * g.dy
+    return ref - mag_ref + s * kappa2 * np.concatenate([ca.reshape(-1), cb.reshape(-1)])
+
+
 def _link_phase_scaled(g, abei, ab, d, which):
     """ph = d*abei + d*ab as accumulated by the coefficient kernels (``cg.h:410-412``)."""
     ph = 0.0

@@ -36,7 +36,7 @@ class TDStats(C.Structure):
     _fields_ = [("steps", C.c_int32), ("max_sweeps_psi", C.c_int32), ("max_sweeps_A", C.c_int32),
                 ("last_sweeps_psi", C.c_int32), ("last_sweeps_A", C.c_int32), ("nan_seen", C.c_int32),
                 ("total_sweeps_psi", C.c_int64), ("total_sweeps_A", C.c_int64), ("rand_t", C.c_uint32),
-                ("used_graph", C.c_int32)]
+                ("used_graph", C.c_int32), ("sweep_launches", C.c_int64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -46,6 +46,7 @@ _H = C.c_void_p
 _P = C.c_void_p
 _SIGNATURES = {
     "glgpu_version": (C.c_int, []),
+    "glgpu_psi_sweeps_per_launch": (C.c_int, []),
     "glgpu_last_error": (C.c_char_p, [_H]),
     "glgpu_create": (C.c_int, [C.POINTER(Grid), C.c_int32, C.POINTER(_H)]),
     "glgpu_destroy": (C.c_int, [_H]),
@@ -80,8 +81,27 @@ _SIGNATURES = {
     "glgpu_batch_last_error": (C.c_char_p, [_H]),
     "glgpu_batch_td": (C.c_int, [_H, C.c_double, C.c_int32, C.c_int32, C.POINTER(TDStats), C.POINTER(C.c_double)]),
     "glgpu_batch_set_use_graphs": (C.c_int, [_H, C.c_int32]),
-    "glgpu_batch_cg": (C.c_int, [_H, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+    "glgpu_batch_cg": (C.c_int, [_H, C.c_int32, C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    # learned warm start (include/glgpu_nn.h)
+    "glnn_conv3x3_fwd": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32,
+                                   C.c_int32, C.c_int32, _P]),
+    "glnn_conv3x3_bwd_data": (C.c_int, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32,
+                                        C.c_int32, C.c_int32, _P]),
+    "glnn_conv3x3_bwd_weight_work": (C.c_int64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "glnn_conv3x3_bwd_weight": (C.c_int, [_P, _P, C.c_int32, _P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int64,
+                                          C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "glnn_prep_weights": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, _P]),
+    "glnn_pool2_fwd": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "glnn_pool2_bwd": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "glnn_up2_fwd": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "glnn_up2_bwd": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "glnn_add": (C.c_int, [_P, _P, _P, C.c_int64, _P]),
+    "glnn_mse": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, _P, C.c_int64, _P]),
+    "glnn_adam": (C.c_int, [_P, _P, _P, _P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                            C.c_int32, _P]),
+    "glnn_f32_to_bf16": (C.c_int, [_P, _P, C.c_int64, _P]),
+    "glnn_bf16_to_f32": (C.c_int, [_P, _P, C.c_int64, _P]),
 }
 
 _lib = None

@@ -87,7 +87,7 @@ class GLBatch:
     def free_energies(self):
         return np.array([s.observables.free_energy for s in self.solvers])
 
-    def cg(self, n_iter=1000, rtol=None, gtol=0.0, mode="device", timed=False):
+    def cg(self, n_iter=1000, rtol=None, gtol=0.0, mode="device", exact_boundary=False, timed=False):
         """Free-energy minimisation of every solver.
 
         ``mode="device"``: one graph launch runs the CG of all instances; beta,
@@ -97,6 +97,9 @@ class GLBatch:
         solver's ``convergence_rtol``) or when the gradient norm falls below
         ``gtol`` times its first value.  Returns a dict of per-instance arrays
         ``iters``, ``energy``, ``grad_rel``, ``status`` (and ``ms`` if ``timed``).
+        ``exact_boundary``: use the exact dF/dA on the boundary links (the
+        reference's formula doubles it there, so at finite kappa its gradient
+        norm stalls above zero at the energy minimum).
 
         ``mode="reference"``: ``solve.cg(n_iter)`` of each solver in turn, the
         reference's decisions taken on the host."""
@@ -114,8 +117,8 @@ class GLBatch:
         grad_rel = (C.c_double * n)()
         status = (C.c_int32 * n)()
         ms = C.c_double()
-        rc = self.lib.glgpu_batch_cg(self.b, int(n_iter), float(rtol), float(gtol), iters, energy, grad_rel, status,
-                                     C.byref(ms))
+        rc = self.lib.glgpu_batch_cg(self.b, int(n_iter), float(rtol), float(gtol), 1 if exact_boundary else 0, iters,
+                                     energy, grad_rel, status, C.byref(ms))
         for s in self.solvers:
             s.solve.vortices_detected = False
         self._check(rc, "batch_cg")

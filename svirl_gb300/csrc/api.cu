@@ -52,10 +52,8 @@ void upload_inst(glgpu_handle* h) {
         I.stop_psi = (double)(float)I.stop_psi;
         I.stop_A = (double)(float)I.stop_A;
     }
-    for (int q = 0; q < 3; ++q) {
-        I.psi[q] = h->psi[q];
-        I.ab[q] = h->ab[q];
-    }
+    for (int q = 0; q < kPsiBufs; ++q) I.psi[q] = h->psi[q];
+    for (int q = 0; q < 3; ++q) I.ab[q] = h->ab[q];
     I.abei = h->abei;
     I.mt = h->mt;
     I.eps_sp = h->eps_sp;
@@ -92,10 +90,10 @@ void upload_inst(glgpu_handle* h) {
 static int check_handle(const glgpu_handle* h) { return h ? GLGPU_OK : GLGPU_E_ARG; }
 
 static void free_all(glgpu_handle* h) {
-    for (int q = 0; q < 3; ++q) {
+    for (int q = 0; q < kPsiBufs; ++q)
         if (h->psi[q]) cudaFree(h->psi[q]);
+    for (int q = 0; q < 3; ++q)
         if (h->ab[q]) cudaFree(h->ab[q]);
-    }
     for (int q = 0; q < 6; ++q)
         if (h->td_exec[q]) cudaGraphExecDestroy(h->td_exec[q]);
     if (h->st_gather) cudaFree(h->st_gather);
@@ -117,6 +115,8 @@ static void free_all(glgpu_handle* h) {
 extern "C" {
 
 int glgpu_version(void) { return 10000; }
+
+int glgpu_psi_sweeps_per_launch(void) { return kFuse; }
 
 const char* glgpu_last_error(const glgpu_handle* h) { return h ? h->last_error.c_str() : g_create_error.c_str(); }
 
@@ -145,7 +145,8 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     h->ntiles = blocks_for(h->g.N);
     const int nblk = blocks_for(h->g.N);
     bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
-    for (int q = 0; q < 3 && ok; ++q) ok = cudaMalloc(&h->psi[q], npsi) == cudaSuccess && cudaMalloc(&h->ab[q], nab) == cudaSuccess;
+    for (int q = 0; q < kPsiBufs && ok; ++q) ok = cudaMalloc(&h->psi[q], npsi) == cudaSuccess;
+    for (int q = 0; q < 3 && ok; ++q) ok = cudaMalloc(&h->ab[q], nab) == cudaSuccess;
     ok = ok && cudaMalloc(&h->U, (size_t)h->g.Nab * 2 * rs) == cudaSuccess;
     ok = ok && cudaMalloc(&h->code, (size_t)h->g.N) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st, sizeof(InstState)) == cudaSuccess;
@@ -185,10 +186,8 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(h->counter, 0, sizeof(unsigned) * 4, h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->dscal, 0, sizeof(double) * 32, h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->loop, 0, sizeof(LoopState), h->stream);
-    for (int q = 0; q < 3 && e == cudaSuccess; ++q) {
-        e = cudaMemsetAsync(h->psi[q], 0, npsi, h->stream);
-        if (e == cudaSuccess) e = cudaMemsetAsync(h->ab[q], 0, nab, h->stream);
-    }
+    for (int q = 0; q < kPsiBufs && e == cudaSuccess; ++q) e = cudaMemsetAsync(h->psi[q], 0, npsi, h->stream);
+    for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = cudaMemsetAsync(h->ab[q], 0, nab, h->stream);
     if (e == cudaSuccess) {
         upload_inst(h);
         e = cudaStreamSynchronize(h->stream);
@@ -449,11 +448,11 @@ int glgpu_batch_td(glgpu_batch* b, double dt, int32_t Nt, int32_t eqn, glgpu_td_
     return batch_td(b, dt, Nt, eqn, stats, elapsed_ms);
 }
 
-int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t* iters, double* energies,
-                   double* grad_rel, int32_t* status, double* elapsed_ms) {
+int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t flags, int32_t* iters,
+                   double* energies, double* grad_rel, int32_t* status, double* elapsed_ms) {
     if (!b) return GLGPU_E_ARG;
     cudaSetDevice(b->device);
-    return batch_cg(b, n_iter, rtol, gtol, iters, energies, grad_rel, status, elapsed_ms);
+    return batch_cg(b, n_iter, rtol, gtol, flags, iters, energies, grad_rel, status, elapsed_ms);
 }
 
 int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable) {

@@ -72,7 +72,7 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
                 const bool has = dir == 0 ? (i < g.Nx - 1) : (j < g.Ny - 1);
                 if (!has) continue;
                 const int l = dir == 0 ? i + (g.Nx - 1) * j : g.Na + i + g.Nx * j;
-                const T ga = grad_A_link<T>(g, k2, H, psi, abei, ab, n, i, j, cb, dir == 0);
+                const T ga = grad_A_link<T>(g, k2, H, psi, abei, ab, n, i, j, cb, dir == 0, I.cg_exact != 0);
                 GA[l] = ga;
                 const T gap = GAp[l];
                 v[2] += (double)(ga * (ga - gap));
@@ -574,7 +574,7 @@ fail:
 }
 #undef GCHK
 
-int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int32_t* iters, double* energies, double* grad_rel,
+int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, int32_t* iters, double* energies, double* grad_rel,
              int32_t* status, double* elapsed_ms) {
     if (n_iter < 0 || !(rtol >= 0.0) || !(gtol >= 0.0)) return batch_error(b, GLGPU_E_ARG, "batch_cg: bad n_iter, rtol or gtol");
     std::vector<Inst> insts(b->ninst);
@@ -586,6 +586,7 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int32_t* iter
         cudaStreamSynchronize(h->stream);
         insts[q] = h->inst_h;
         insts[q].tile0 = tile0;  // the batch's tile table lists the instances' tiles in order
+        insts[q].cg_exact = (flags & GLGPU_CG_EXACT_BOUNDARY) ? 1 : 0;
         tile0 += h->ntiles;
     }
     if (!b->cg_partials && cudaMalloc(&b->cg_partials, sizeof(double) * kPart * (size_t)b->ntiles) != cudaSuccess)

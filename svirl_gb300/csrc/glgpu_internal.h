@@ -14,15 +14,30 @@
 
 namespace glgpu {
 
+// Temporal blocking of the psi Jacobi loop: one launch of the psi sweep kernel
+// does kFuse consecutive sweeps and writes every one of them, so the loop can
+// stop after any of them exactly where the one-sweep-per-launch loop stops.
+#ifndef GLGPU_FUSE
+#define GLGPU_FUSE 2
+#endif
+#ifndef GLGPU_STRIP_ROWS
+#define GLGPU_STRIP_ROWS 16
+#endif
+constexpr int kFuse = GLGPU_FUSE;
+static_assert(kFuse >= 1 && kFuse <= 4, "1 <= GLGPU_FUSE <= 4");
+constexpr int kPsiBufs = kFuse + 2;  // right-hand side + input + kFuse outputs
+
 // Device-resident state of one instance's Jacobi loops (updated by the kernels
 // themselves so that a whole TD run needs no host round trip).
 struct InstState {
-    unsigned long long res;   // max residual of the current sweep, as IEEE bits
-    unsigned blocks_done;     // CTAs of this instance finished in the current sweep
+    unsigned long long res;   // A loop: max residual of the current sweep, as IEEE bits
+    unsigned long long resp[4];  // psi loop: max residual of each sweep of the current launch
+    int nanlv;                // psi loop: bit l set if sweep l of the current launch saw a NaN residual
+    unsigned blocks_done;     // CTAs (A) / strips (psi) of this instance finished in the current launch
     int sweep;                // sweeps done in the current Jacobi loop
     int done;                 // current Jacobi loop finished
-    int rhs;                  // buffer index (0..2) of psi^(0) = right-hand side of the psi loop
-    int rhsA;                 // same for the A loop
+    int rhs;                  // buffer index (0..kPsiBufs-1) of psi^(0) = right-hand side of the psi loop
+    int rhsA;                 // same for the A loop (0..2)
     uint32_t rand_t;          // Langevin time seed (svirl/solvers/td.py:35-37,204,313)
     int nan_seen;             // a NaN residual was seen (the reference counts it as converged)
     int last_sweeps_psi, last_sweeps_A, max_sweeps_psi, max_sweeps_A;
@@ -52,7 +67,7 @@ struct Inst {
     double stop_psi, stop_A;
     float fdt, fepsilon, fkappa2, frho, fH, flang_psi, flang_A, pad_f;  // the same, rounded to float
     int lang_psi_on, lang_A_on;  // Langevin coefficient (in the solver's precision) > 1e-32 (td.h:147,451)
-    void* psi[3];             // rotating TD buffers, psi[0] holds the state at rest
+    void* psi[kPsiBufs];      // rotating TD buffers, psi[0] holds the state at rest
     void* ab[3];              // rotating TD buffers, ab[0] holds the state at rest
     const void* abei;         // external+irregular vector potential or NULL
     const uint8_t* mt;        // material tiling (cells) or NULL
@@ -68,7 +83,7 @@ struct Inst {
     int tile0, ntiles;        // this instance's range in the tile table
     int nitems;               // number of warp-strip items of this instance
     int solveA;               // finite kappa
-    int pad_;
+    int cg_exact;             // batched device CG: exact dF/dA on boundary links
 };
 
 // Global state of one batched Jacobi/time loop.
@@ -80,6 +95,7 @@ struct LoopState {
     int step, Nt;             // time loop position / length
     int err;                  // error bits (kErr*)
     int ninst;
+    long long total_launches;  // sweep kernel launches (psi and A) in the current call
 };
 
 constexpr int kErrLoopGuard = 1;
@@ -90,9 +106,10 @@ struct Tile {
 };
 
 // Work item of the warp-strip psi sweep: kStripCols output columns (x0..) by
-// kStripRows rows (j0..) of one instance, processed by one warp.
-constexpr int kStripRows = 8;
-constexpr int kStripCols = 30;
+// kStripRows rows (j0..) of one instance, processed by one warp whose 32 lanes
+// also cover kFuse halo columns on each side.
+constexpr int kStripRows = GLGPU_STRIP_ROWS;
+constexpr int kStripCols = 32 - 2 * kFuse;
 struct Item {
     int inst, x0, j0, pad;
 };
@@ -107,7 +124,7 @@ struct glgpu_handle {
     cudaStream_t stream = nullptr;
     int device = 0;
     // device buffers
-    void* psi[3] = {nullptr, nullptr, nullptr};
+    void* psi[glgpu::kPsiBufs] = {};
     void* ab[3] = {nullptr, nullptr, nullptr};
     void* abei = nullptr;
     uint8_t* mt = nullptr;
@@ -205,7 +222,7 @@ int cg_update(glgpu_handle* h, double alpha_psi, double alpha_A, double* energy_
 int cg_read_gradient(glgpu_handle* h, void* gpsi_host, void* gA_host);
 int cg_coef_for(glgpu_handle* h, const void* dpsi_host, const void* dab_host, double* c_out);
 // cgb.cu
-int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int32_t* iters, double* energies, double* grad_rel,
+int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, int32_t* iters, double* energies, double* grad_rel,
              int32_t* status, double* elapsed_ms);
 // td.cu graph helpers
 cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps, void* fn, dim3 grid,

@@ -116,6 +116,32 @@ __device__ __forceinline__ T curlcurl_link(const Geo& g, const T* abei, const T*
     return c;
 }
 
+// The exact derivative of the magnetic energy kappa^2 sum_cells (curl A - H)^2
+// (before the 2 kappa^2 dx dy factor) on a link of the boundary rows/columns,
+// which belongs to one cell only.  The reference's formula above doubles the
+// H and ab terms there (the ghost-cell form of the TD equation), so its dF/dA
+// does not vanish at the energy minimum on those links; an interior link is the
+// same in both.
+template <typename T>
+__device__ __forceinline__ T curlcurl_link_exact(const Geo& g, const T* abei, const T* ab, T H, int i, int j, bool xdir) {
+    const int Nxa = g.Nx - 1, Na = g.Na, Nx = g.Nx;
+    const T idx = GT(g, idx), idy = GT(g, idy);
+    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
+    auto A = [&](int n) -> T { return link_phase(abei, ab, n); };
+    if (xdir) {
+        if (j == 0)  // cell (i, 0) above the link
+            return idy2 * (A(i) - A(i + Nxa)) + idxy * (A(Na + i + 1) - A(Na + i)) - H * idy;
+        if (j + 1 == g.Ny)  // cell (i, Ny-2) below the link
+            return idy2 * (A(i + Nxa * j) - A(i + Nxa * (j - 1))) - idxy * (A(Na + i + 1 + Nx * (j - 1)) - A(Na + i + Nx * (j - 1))) + H * idy;
+    } else {
+        if (i == 0)  // cell (0, j) to the right of the link
+            return idx2 * (A(Na + Nx * j) - A(Na + 1 + Nx * j)) + idxy * (A(Nxa * (j + 1)) - A(Nxa * j)) + H * idx;
+        if (i + 1 == g.Nx)  // cell (Nx-2, j) to the left of the link
+            return idx2 * (A(Na + i + Nx * j) - A(Na + i - 1 + Nx * j)) - idxy * (A((i - 1) + Nxa * (j + 1)) - A((i - 1) + Nxa * j)) - H * idx;
+    }
+    return curlcurl_link<T>(g, abei, ab, H, i, j, xdir);
+}
+
 // 2 (psi0 - psi1 U(ph)) (svirl/cuda/cg.h:4-12)
 template <typename T> __device__ __forceinline__ C2<T> gjac(C2<T> p0, T ph, C2<T> p1) {
     T s, c;
@@ -148,11 +174,12 @@ __device__ __forceinline__ C2<T> grad_psi_node(const Geo& g, T eps0, const T* ep
 }
 
 // dF/dA on the x link (xdir) or y link starting at node (i, j) (svirl/cuda/cg.h:124-301),
-// 2*dx*dy included.
+// 2*dx*dy included; exact: the boundary links use the exact derivative of the
+// magnetic energy instead of the reference's doubled form.
 template <typename T>
 __device__ __forceinline__ T grad_A_link(const Geo& g, T kappa2, T H, const C2<T>* psi, const T* abei, const T* ab,
-                                         int n, int i, int j, unsigned cb, bool xdir) {
-    T c = kappa2 * curlcurl_link<T>(g, abei, ab, H, i, j, xdir);
+                                         int n, int i, int j, unsigned cb, bool xdir, bool exact = false) {
+    T c = kappa2 * (exact ? curlcurl_link_exact<T>(g, abei, ab, H, i, j, xdir) : curlcurl_link<T>(g, abei, ab, H, i, j, xdir));
     if (xdir) {
         if (GL_PM(cb) || GL_PP(cb)) {
             const T r = T(0.5) * ((GL_PM(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));

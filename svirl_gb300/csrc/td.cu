@@ -7,10 +7,11 @@
 // svirl/solvers/td.py:157-218,252-325,342-377 (host loops, stop rule, swaps).
 //
 // Buffer rotation.  The reference copies psi into a separate right-hand-side
-// buffer each step and ping-pongs psi/psi_next.  Here three buffers rotate:
-// psi^(0) (the right-hand side) stays in buffer R, and sweep k reads psi^(k) and
-// writes psi^(k+1), with psi^(k) in buffer (R+1+((k-1)&1))%3 for k>=1.  No copy
-// is needed, and the values are those of the reference.  For A the same
+// buffer each step and ping-pongs psi/psi_next.  Here psi^(0) (the right-hand
+// side) stays in buffer R and the other kFuse+1 buffers rotate: a launch reads
+// psi^(k) and writes psi^(k+1) .. psi^(k+kFuse) (pbuf below), so no copy is
+// needed, the loop can end after any sweep, and the values are those of the
+// reference.  A uses three buffers, psi^(k) in (R+1+((k-1)&1))%3; this
 // rotation also reproduces the reference's aliasing of the supercurrent
 // argument (svirl/solvers/td.py:266,303): sweep k sees A^(2*floor(k/2)), which is
 // buffer R for k<2 and (R+2)%3 afterwards; in odd sweeps that buffer is also the
@@ -34,6 +35,7 @@ __device__ void finish_launch(LoopState* loop, cudaGraphConditionalHandle cond, 
     loop->blocks_done = 0u;
     int L = loop->launches + 1;
     loop->launches = L;
+    loop->total_launches += 1;
     int act = atomicAdd(&loop->active, 0);
     int cont = act > 0 ? 1 : 0;
     if (cont && L >= kLoopGuard) {
@@ -44,30 +46,62 @@ __device__ void finish_launch(LoopState* loop, cudaGraphConditionalHandle cond, 
     if (use_cond) cudaGraphSetConditional(cond, (unsigned)cont);
 }
 
+// Called by the CTA that finishes the last tile of an instance in an A sweep.
 template <typename T>
-__device__ void finish_instance(const Inst& I, LoopState* loop, int k, bool is_psi) {
+__device__ void finish_instance_A(const Inst& I, LoopState* loop, int k) {
     InstState* st = I.st;
     __threadfence();
     unsigned long long b = atomicExch(&st->res, 0ull);
     T r = res_from_bits<T>(b);
-    bool conv = jacobi_converged(r, is_psi ? I.stop_psi : I.stop_A);
+    bool conv = jacobi_converged(r, I.stop_A);
     int s = k + 1;
     st->sweep = s;
     st->blocks_done = 0u;
     if (conv || s >= kMaxSweeps) {
         st->done = 1;
-        if (is_psi) {
-            st->rhs = buf_of(st->rhs, s);
-            st->last_sweeps_psi = s;
-            st->total_sweeps_psi += s;
-            if (s > st->max_sweeps_psi) st->max_sweeps_psi = s;
-        } else {
-            st->rhsA = buf_of(st->rhsA, s);
-            st->last_sweeps_A = s;
-            st->total_sweeps_A += s;
-            if (s > st->max_sweeps_A) st->max_sweeps_A = s;
-        }
+        st->rhsA = buf_of(st->rhsA, s);
+        st->last_sweeps_A = s;
+        st->total_sweeps_A += s;
+        if (s > st->max_sweeps_A) st->max_sweeps_A = s;
         atomicSub(&loop->active, 1);
+    }
+}
+
+// Buffer of psi^(s) in a psi Jacobi loop whose right-hand side psi^(0) is in
+// buffer R: the kFuse + 1 other buffers rotate, so the input of a launch and its
+// kFuse outputs are always distinct.
+__device__ __forceinline__ int pbuf(int R, int s) { return s == 0 ? R : (R + 1 + (s - 1) % (kFuse + 1)) % kPsiBufs; }
+
+// Called by the warp that finishes the last strip of an instance in a psi
+// launch that did sweeps k+1 .. k+kFuse: the loop stops after the first of them
+// that meets the reference's stop rule (or reaches the sweep cap), exactly where
+// a loop of single sweeps stops; that sweep's output buffer becomes the state.
+template <typename T>
+__device__ void finish_instance_psi(const Inst& I, LoopState* loop, int k) {
+    InstState* st = I.st;
+    __threadfence();
+    T r[kFuse];
+#pragma unroll
+    for (int l = 0; l < kFuse; ++l) r[l] = res_from_bits<T>(atomicExch(&st->resp[l], 0ull));
+    const int nl = atomicExch(&st->nanlv, 0);
+    int stop = 0;
+#pragma unroll
+    for (int l = kFuse; l >= 1; --l)
+        if (jacobi_converged(r[l - 1], I.stop_psi) || k + l >= kMaxSweeps) stop = l;
+    const int upto = stop ? stop : kFuse;
+    if (nl & ((1 << upto) - 1)) st->nan_seen = 1;
+    st->blocks_done = 0u;
+    if (stop) {
+        const int s = k + stop;
+        st->sweep = s;
+        st->done = 1;
+        st->rhs = pbuf(st->rhs, s);
+        st->last_sweeps_psi = s;
+        st->total_sweeps_psi += s;
+        if (s > st->max_sweeps_psi) st->max_sweeps_psi = s;
+        atomicSub(&loop->active, 1);
+    } else {
+        st->sweep = k + kFuse;
     }
 }
 
@@ -89,23 +123,29 @@ __device__ __forceinline__ T block_max_res(T v, bool nan) {
     return v;
 }
 
-// Residual bookkeeping of one warp for the instance it is working on: the warp
-// max goes to the instance with one atomic, and the warp that completes the
-// instance's last item closes that instance's sweep.
+// Residual bookkeeping of one warp for the instance it is working on: per fused
+// sweep, the warp max goes to the instance with one atomic, and the warp that
+// completes the instance's last strip closes the launch for that instance.
 template <typename T>
-__device__ __forceinline__ void warp_flush(const Inst* insts, int inst, int k, T wmax, bool wnan, int count,
-                                           LoopState* loop) {
+__device__ __forceinline__ void warp_flush(const Inst* insts, int inst, int k, const T (&wmax)[kFuse],
+                                           const bool (&wnan)[kFuse], int count, LoopState* loop) {
     const unsigned full = 0xffffffffu;
-    T m = warp_max(wmax);
-    const bool anynan = __any_sync(full, wnan);
+    T m[kFuse];
+    int nanbits = 0;
+#pragma unroll
+    for (int l = 0; l < kFuse; ++l) {
+        m[l] = warp_max(wmax[l]);
+        if (__any_sync(full, wnan[l])) nanbits |= 1 << l;
+    }
     if ((threadIdx.x & 31) == 0 && count > 0) {
         const Inst& I = insts[inst];
         InstState* st = I.st;
-        if (anynan) atomicOr(&st->nan_seen, 1);
-        atomicMax(&st->res, res_bits(m));
+        if (nanbits) atomicOr(&st->nanlv, nanbits);
+#pragma unroll
+        for (int l = 0; l < kFuse; ++l) atomicMax(&st->resp[l], res_bits(m[l]));
         __threadfence();
         unsigned prev = atomicAdd(&st->blocks_done, (unsigned)count);
-        if (prev + (unsigned)count == (unsigned)I.nitems) finish_instance<T>(I, loop, k, true);
+        if (prev + (unsigned)count == (unsigned)I.nitems) finish_instance_psi<T>(I, loop, k);
     }
 }
 
@@ -116,29 +156,74 @@ template <typename T> __device__ __forceinline__ C2<T> shfl_down_c(C2<T> v, int 
     return cmk<T>(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
 }
 
-// One Jacobi sweep of the psi step (svirl/cuda/td.h:4-133, Winecki-Adams link
-// weights td.h:159-163) over every active instance, reading the per-step tables
-// of k_link_U (link factors U and link-weight codes), so the sweep itself does no
-// transcendental math and no mask logic.  A warp owns a strip of kStripCols = 30
-// output columns plus one halo column on each side (lanes 0 and 31) and
-// kStripRows rows: it walks down the rows keeping psi(j-1), psi(j), psi(j+1) and
-// the y link below in registers and takes the x neighbours and the x link on its
-// left from the adjacent lanes, so each node loads psi, rhs, its two link factors
-// and its code once.  The row walk is unrolled with every load issued ahead of
-// its use.  Persistent grid: warps stride over the item table.
+// The backward-Euler Jacobi update of one node (svirl/cuda/td.h:4-133 with the
+// Winecki-Adams link weights of td.h:159-163, coded as bits of cd: 0 left,
+// 1 right, 2 lower, 3 upper link).  rq is the right-hand side with the Langevin
+// term added.  A node with neither a left nor a right link gets 0.
+template <typename T>
+__device__ __forceinline__ C2<T> psi_node(C2<T> p_left, C2<T> p_right, C2<T> p_prev, C2<T> p_next, C2<T> ua_left,
+                                          C2<T> ua, C2<T> ub_down, C2<T> ub, C2<T> rq, T eps, unsigned cd, T dt,
+                                          T idx2, T idy2) {
+    const C2<T> z = cmk<T>(T(0), T(0));
+    C2<T> out = z;
+    if (cd & 3u) {
+        const bool rm0 = cd & 1u, rp0 = cd & 2u, r0m = cd & 4u, r0p = cd & 8u;
+        C2<T> sx = z, sy = z;
+        if (rm0) sx = cadd(sx, cmul(cconj(ua_left), p_left));
+        if (rp0) sx = cadd(sx, cmul(ua, p_right));
+        if (r0m) sy = cadd(sy, cmul(cconj(ub_down), p_prev));
+        if (r0p) sy = cadd(sy, cmul(ub, p_next));
+        const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
+        const T diag = T(1) + dt * (rq.x * rq.x + rq.y * rq.y - eps + (idx2 * wx + idy2 * wy));
+        const T inv = T(1) / diag;
+        out.x = (rq.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
+        out.y = (rq.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
+    }
+    return out;
+}
+
+// Per-row inputs of the psi update besides psi itself: the link factors of the
+// x link and the y link that start at the node, the right-hand side, the linear
+// coefficient and the link-weight code.
+template <typename T> struct PsiSide {
+    C2<T> ua, ub, rr;
+    T eps;
+    unsigned cd;
+};
+
+// kFuse Jacobi sweeps of the psi step (svirl/cuda/td.h:4-133) over every active
+// instance in one launch, reading the per-step tables of k_link_U (link factors
+// U and link-weight codes), so the sweep does no transcendental math and no mask
+// logic.  A warp owns a strip of kStripCols output columns and kStripRows rows;
+// its 32 lanes hold the columns x0-kFuse .. x0+31-kFuse, and sweep l (1..kFuse)
+// is valid on lanes l..31-l, so the halo columns are recomputed in registers
+// instead of being exchanged.  The warp walks down the rows: at step s it loads
+// row j0-kFuse+s of psi^(k) and the per-row inputs one row behind, and sweep l
+// produces row j0-kFuse+s-l from the three newest rows of sweep l-1 (each level
+// lags the previous one by a row).  x neighbours come from the adjacent lanes.
+// Every sweep's values on the strip are stored, and its residual kept, so the
+// loop can stop after any of the fused sweeps.  The row walk is unrolled with
+// every load issued one step ahead of its use.  Persistent grid: warps stride
+// over the item table.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
             cudaGraphConditionalHandle cond, int use_cond) {
+    constexpr int K = kFuse, RR = kStripRows, S = kStripRows + 2 * kFuse;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
     int cur_inst = -1, k = 0, count = 0, done = 1;
-    T wmax = T(0);
-    bool wnan = false;
+    T wmax[K];
+    bool wnan[K];
+#pragma unroll
+    for (int l = 0; l < K; ++l) {
+        wmax[l] = T(0);
+        wnan[l] = false;
+    }
     // per-instance values, refreshed when the warp moves to another instance
     const C2<T>* cur = nullptr;
     const C2<T>* rhs = nullptr;
-    C2<T>* nxt = nullptr;
+    C2<T>* outb[K];
     const C2<T>* U = nullptr;
     const uint8_t* code = nullptr;
     uint32_t rt = 0;
@@ -153,13 +238,16 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             const int R = *(volatile const int*)&st->rhs;
             rt = *(volatile const uint32_t*)&st->rand_t;
             const Inst& I = insts[cur_inst];
-            cur = (const C2<T>*)I.psi[buf_of(R, k)];
+            cur = (const C2<T>*)I.psi[pbuf(R, k)];
             rhs = (const C2<T>*)I.psi[R];
-            nxt = (C2<T>*)I.psi[(R + 1 + (k & 1)) % 3];
+#pragma unroll
+            for (int l = 0; l < K; ++l) {
+                outb[l] = (C2<T>*)I.psi[pbuf(R, k + 1 + l)];
+                wmax[l] = T(0);
+                wnan[l] = false;
+            }
             U = (const C2<T>*)I.U;
             code = I.code;
-            wmax = T(0);
-            wnan = false;
             count = 0;
         }
         if (done) continue;
@@ -171,81 +259,80 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
         const bool lang = I.lang_psi_on != 0;
         const T lc = gsel<T>(I.lang_psi, I.flang_psi);
         const int Nx = g.Nx, Ny = g.Ny, Nxa = g.Nx - 1, Na = g.Na;
-        // lane L holds column x0 - 1 + L: lanes 0 and 31 only supply the neighbours
-        // (halo lanes), lanes 1..30 produce the strip's 30 output columns
-        const int i = w.x0 - 1 + lane;
+        const int i = w.x0 - K + lane;
         const bool in_x = i >= 0 && i < Nx;
-        const bool out_lane = lane >= 1 && lane <= 30 && in_x;
+        const bool calc_lane = in_x && lane >= 1 && lane <= 30;        // lanes any sweep computes
+        const bool own_lane = in_x && lane >= K && lane <= 31 - K;     // the strip's own columns
         const int j0 = w.j0;
         const C2<T> z = cmk<T>(T(0), T(0));
-        C2<T> p_prev = (in_x && j0 > 0) ? __ldg(&cur[i + Nx * (j0 - 1)]) : z;
-        C2<T> p_c = in_x ? __ldg(&cur[i + Nx * j0]) : z;
-        C2<T> ub_down = (out_lane && j0 > 0) ? __ldg(&U[Na + i + Nx * (j0 - 1)]) : z;
-        // software pipeline: the loads of row r+1 are issued before row r is computed
-        struct Row {
-            C2<T> p_next, ua, ub, rr;
-            T eps;
-            unsigned cd;
-        };
-        auto load_row = [&](int r) -> Row {
-            Row q;
-            const int j = j0 + r;
-            const int n = i + Nx * j;
-            const bool ld = in_x && j < Ny, ldo = out_lane && j < Ny;
-            q.p_next = (ld && j + 1 < Ny) ? __ldg(&cur[n + Nx]) : z;
-            q.ua = (ld && i < Nx - 1) ? __ldg(&U[i + Nxa * j]) : z;
-            q.ub = (ldo && j < Ny - 1) ? __ldg(&U[Na + n]) : z;
-            q.cd = ldo ? (unsigned)__ldg(&code[n]) : 0u;
-            q.rr = ldo ? __ldg(&rhs[n]) : z;
-            q.eps = (ldo && eps_sp) ? __ldg(&eps_sp[n]) : eps0;
+        auto load_psi = [&](int y) -> C2<T> { return (in_x && y >= 0 && y < Ny) ? __ldg(&cur[i + Nx * y]) : z; };
+        auto load_side = [&](int y) -> PsiSide<T> {
+            PsiSide<T> q;
+            const bool row = y >= 0 && y < Ny;
+            const int n = i + Nx * y;
+            const bool ld = in_x && row, ldc = calc_lane && row;
+            q.ua = (ld && i < Nx - 1) ? __ldg(&U[i + Nxa * y]) : z;
+            q.ub = (ldc && y < Ny - 1) ? __ldg(&U[Na + n]) : z;
+            q.cd = ldc ? (unsigned)__ldg(&code[n]) : 0u;
+            q.rr = ldc ? __ldg(&rhs[n]) : z;
+            q.eps = (ldc && eps_sp) ? __ldg(&eps_sp[n]) : eps0;
             return q;
         };
-        Row nx = load_row(0);
+        // window of sweep l-1 (l = 1..K) as seen by sweep l: rows y-1 and y
+        C2<T> wp[K], wc[K];
+        PsiSide<T> D[K + 1];  // D[m]: per-row inputs of row (j0 - K + s - 1) - m
 #pragma unroll
-        for (int r = 0; r < kStripRows; ++r) {
-            const Row cu = nx;
-            if (r + 1 < kStripRows) nx = load_row(r + 1);
-            const int j = j0 + r;
-            const int n = i + Nx * j;
-            const bool ldo = out_lane && j < Ny;
-            const C2<T> p_next = cu.p_next, ua = cu.ua, ub = cu.ub, rr = cu.rr;
-            const unsigned cd = cu.cd;
-            const T eps = cu.eps;
-            // x neighbours and the x link on the left from the adjacent lanes
-            const C2<T> p_left = shfl_up_c<T>(p_c, 1), p_right = shfl_down_c<T>(p_c, 1);
-            const C2<T> ua_left = shfl_up_c<T>(ua, 1);
-            if (ldo) {
-                C2<T> out = z;
-                if (cd & 3u) {  // a node with a material cell has a left or a right link
-                    C2<T> rq = rr;
-                    if (lang) {
-                        rq.x += lc * (rand_1<T>((uint32_t)n, rt) - T(0.5));
-                        rq.y += lc * (rand_2<T>((uint32_t)n, rt) - T(0.5));
-                    }
-                    const bool rm0 = cd & 1u, rp0 = cd & 2u, r0m = cd & 4u, r0p = cd & 8u;
-                    C2<T> sx = z, sy = z;
-                    if (rm0) sx = cadd(sx, cmul(cconj(ua_left), p_left));
-                    if (rp0) sx = cadd(sx, cmul(ua, p_right));
-                    if (r0m) sy = cadd(sy, cmul(cconj(ub_down), p_prev));
-                    if (r0p) sy = cadd(sy, cmul(ub, p_next));
-                    const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
-                    const T diag = T(1) + dt * (rq.x * rq.x + rq.y * rq.y - eps + (idx2 * wx + idy2 * wy));
-                    const T inv = T(1) / diag;
-                    out.x = (rq.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
-                    out.y = (rq.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
-                }
-                nxt[n] = out;
-                const T dr = fabs(out.x - p_c.x), di = fabs(out.y - p_c.y);
-                T res = dr > di ? dr : di;
-                if (!(dr == dr) || !(di == di)) {  // NaN counts as 0, like the reference's int conversion
-                    wnan = true;
-                    res = (dr == dr) ? dr : ((di == di) ? di : T(0));
-                }
-                wmax = res > wmax ? res : wmax;
+        for (int l = 0; l < K; ++l) wp[l] = wc[l] = z;
+#pragma unroll
+        for (int m = 0; m <= K; ++m) D[m] = PsiSide<T>{z, z, z, eps0, 0u};
+        C2<T> nx_p = load_psi(j0 - K);
+        PsiSide<T> nx_s = load_side(j0 - K - 1);
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            C2<T> newrow = nx_p;  // psi^(k) on row j0 - K + s
+#pragma unroll
+            for (int m = K; m >= 1; --m) D[m] = D[m - 1];
+            D[0] = nx_s;
+            if (s + 1 < S) {
+                nx_p = load_psi(j0 - K + s + 1);
+                nx_s = load_side(j0 - K + s);
             }
-            p_prev = p_c;
-            p_c = p_next;
-            ub_down = ub;
+#pragma unroll
+            for (int l = 1; l <= K; ++l) {
+                C2<T> out = z;
+                if (s >= 2 * l) {  // earlier rows of sweep l are above the strip's halo
+                    const int y = j0 - K + s - l;
+                    const C2<T> pc = wc[l - 1];
+                    const C2<T> pl = shfl_up_c<T>(pc, 1), pr = shfl_down_c<T>(pc, 1);
+                    const PsiSide<T>& d = D[l - 1];
+                    const C2<T> ual = shfl_up_c<T>(d.ua, 1);
+                    const bool node = calc_lane && y >= 0 && y < Ny;
+                    if (node) {
+                        C2<T> rq = d.rr;
+                        if (lang) {
+                            const uint32_t n = (uint32_t)(i + Nx * y);
+                            rq.x += lc * (rand_1<T>(n, rt) - T(0.5));
+                            rq.y += lc * (rand_2<T>(n, rt) - T(0.5));
+                        }
+                        out = psi_node<T>(pl, pr, wp[l - 1], newrow, ual, d.ua, D[l].ub, d.ub, rq, d.eps, d.cd, dt,
+                                          idx2, idy2);
+                        if (own_lane && y >= j0 && y < j0 + RR) {
+                            outb[l - 1][i + Nx * y] = out;
+                            const T dr = fabs(out.x - pc.x), di = fabs(out.y - pc.y);
+                            T res = dr > di ? dr : di;
+                            if (!(dr == dr) || !(di == di)) {  // NaN counts as 0, like the reference's int conversion
+                                wnan[l - 1] = true;
+                                res = (dr == dr) ? dr : ((di == di) ? di : T(0));
+                            }
+                            wmax[l - 1] = res > wmax[l - 1] ? res : wmax[l - 1];
+                        }
+                    }
+                }
+                // sweep l has used the window of sweep l-1: advance it by one row
+                wp[l - 1] = wc[l - 1];
+                wc[l - 1] = newrow;
+                newrow = out;
+            }
         }
         ++count;
     }
@@ -356,7 +443,7 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
             atomicMax(&st->res, res_bits(bmax));
             __threadfence();
             unsigned prev = atomicAdd(&st->blocks_done, 1u);
-            if (prev == (unsigned)I.ntiles - 1u) finish_instance<T>(I, loop, k, false);
+            if (prev == (unsigned)I.ntiles - 1u) finish_instance_A<T>(I, loop, k);
         }
     }
     if (tid == 0) {
@@ -409,6 +496,8 @@ __global__ void k_loop_begin(const Inst* __restrict__ insts, int ninst, LoopStat
         st->done = part ? 0 : 1;
         st->blocks_done = 0u;
         st->res = 0ull;
+        for (int l = 0; l < 4; ++l) st->resp[l] = 0ull;
+        st->nanlv = 0;
         active += part ? 1 : 0;
     }
     for (int o = 16; o > 0; o >>= 1) active += __shfl_down_sync(0xffffffffu, active, o);
@@ -659,6 +748,8 @@ __global__ void k_bench_prep(const Inst* __restrict__ insts, int ninst, LoopStat
         st->done = 0;
         st->blocks_done = 0u;
         st->res = 0ull;
+        for (int l = 0; l < 4; ++l) st->resp[l] = 0ull;
+        st->nanlv = 0;
     }
     if (threadIdx.x == 0) {
         loop->active = ninst;
@@ -745,6 +836,7 @@ struct TDOutcome {
     cudaError_t err;
     int used_graph, loop_err, steps;
     float ms;
+    long long launches;
 };
 
 // One TD call over the instances of L: per-call counters reset, the graph (built
@@ -752,7 +844,7 @@ struct TDOutcome {
 // loop states gathered to the host.
 static TDOutcome td_core(cudaStream_t s, const TDLaunch& L, int Nt, int eqn, cudaGraphExec_t* execs, bool* graph_failed,
                          bool use_graphs, bool timed, InstState* gather_dev, InstState* gather_host) {
-    TDOutcome o = {cudaSuccess, 0, 0, 0, 0.f};
+    TDOutcome o = {cudaSuccess, 0, 0, 0, 0.f, 0};
     k_reset_counters<<<(L.ninst + 127) / 128, 128, 0, s>>>(L.insts, L.ninst);
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (timed) {
@@ -801,6 +893,7 @@ static TDOutcome td_core(cudaStream_t s, const TDLaunch& L, int Nt, int eqn, cud
     }
     o.loop_err = Nt > 0 ? hl.err : 0;
     o.steps = Nt > 0 ? hl.step : 0;
+    o.launches = Nt > 0 ? hl.total_launches : 0;
     return o;
 }
 
@@ -809,6 +902,7 @@ static void fill_stats(glgpu_td_stats* stats, const InstState* hs, int n, const 
     memset(stats, 0, sizeof(*stats));
     stats->steps = o.steps;
     stats->used_graph = o.used_graph;
+    stats->sweep_launches = o.launches;
     for (int q = 0; q < n; ++q) {
         const InstState& s = hs[q];
         if (s.max_sweeps_psi > stats->max_sweeps_psi) stats->max_sweeps_psi = s.max_sweeps_psi;

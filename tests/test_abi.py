@@ -1,5 +1,6 @@
 """The C-ABI library builds, loads without a GPU, and exports every entry point
-declared in include/glgpu.h; the Python binding declares them all."""
+declared in include/glgpu.h and include/glgpu_nn.h; the Python binding
+declares them all."""
 import ctypes
 import os
 import re
@@ -7,19 +8,23 @@ import re
 from svirl_gb300 import _lib
 from svirl_gb300 import build as B
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "glgpu.h")
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+HEADERS = [os.path.join(INCLUDE, f) for f in ("glgpu.h", "glgpu_nn.h")]
 
 
 def declared_symbols():
-    text = open(HEADER).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(glgpu_[a-z0-9_]+)\s*\(", text)))
+    syms = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        syms |= set(re.findall(r"\b((?:glgpu|glnn)_[a-z0-9_]+)\s*\(", text))
+    return sorted(syms)
 
 
 def test_header_declares_entry_points():
     syms = declared_symbols()
     assert "glgpu_create" in syms and "glgpu_td" in syms and "glgpu_cg_update" in syms
-    assert len(syms) >= 25
+    assert "glnn_conv3x3_fwd" in syms and "glnn_adam" in syms
+    assert len(syms) >= 40
 
 
 def test_library_loads_and_exports_every_declared_symbol():

@@ -108,6 +108,13 @@ def test_batch_cg_gradient_stop_and_zero_iterations():
     out = b.cg(n_iter=0)
     assert np.all(out["iters"] == 0)
     assert np.allclose(out["energy"], E0, rtol=1e-13, atol=0)
-    out = b.cg(n_iter=5000, rtol=0.0, gtol=1e-4)
-    assert np.all(out["status"] == 1) and np.all(out["grad_rel"] <= 1e-4)
+    # the reference's dF/dA doubles the magnetic terms on boundary links, so at
+    # finite kappa its gradient norm stalls (energy-ratio stop only); with the
+    # exact boundary derivative the gradient-norm stop is met
+    ref, _ = _solvers(configs=CONFIGS[1:2])
+    o_ref = GLBatch(ref).cg(n_iter=3000, rtol=0.0, gtol=1e-6)
+    assert o_ref["status"][0] == 3 and o_ref["grad_rel"][0] > 1e-5
+    out = b.cg(n_iter=5000, rtol=0.0, gtol=1e-6, exact_boundary=True)
+    assert np.all(out["status"] == 1) and np.all(out["grad_rel"] <= 1e-6)
     assert np.all(out["iters"] < 5000)
+    assert out["energy"][1] <= o_ref["energy"][0] + 1e-9 * abs(o_ref["energy"][0])

@@ -77,6 +77,35 @@ def test_jacobians_match_finite_differences(seed):
     assert np.allclose(jA, fdA, atol=1e-5, rtol=1e-3)
 
 
+@pytest.mark.parametrize("seed", range(4))
+def test_exact_A_jacobian_matches_finite_differences(seed):
+    """``free_energy_jacobian_A_exact`` (used by the device CG's exact-boundary
+    mode) is the derivative of the free energy on every link, and equals the
+    reference's dF/dA on the interior links, also where curl A != H."""
+    orc, rng = make_case(seed)
+    orc.ab = orc.ab + 0.05 * rng.standard_normal(orc.g.Nab)
+    g = orc.g
+    args = (g, orc.kappa2, orc.H, orc.mt, orc.psi, orc.abei, orc.ab)
+    jx = K.free_energy_jacobian_A_exact(*args)
+    jr = K.free_energy_jacobian_A(*args)
+    E0 = orc.free_energy()
+    h = 1e-7
+    ab0 = orc.ab.copy()
+    fd = np.empty_like(jx)
+    for n in range(g.Nab):
+        orc.ab = ab0.copy(); orc.ab[n] += h
+        Ep = orc.free_energy()
+        orc.ab = ab0.copy(); orc.ab[n] -= h
+        fd[n] = (Ep - orc.free_energy()) / (2 * h)
+    orc.ab = ab0
+    assert np.allclose(jx, fd, atol=1e-7, rtol=1e-6)
+    a_int = np.zeros((g.Ny, g.Nx - 1), bool); a_int[1:-1, :] = True
+    b_int = np.zeros((g.Ny - 1, g.Nx), bool); b_int[:, 1:-1] = True
+    interior = np.concatenate([a_int.reshape(-1), b_int.reshape(-1)])
+    assert np.allclose(jx[interior], jr[interior], atol=1e-12, rtol=1e-10)
+    assert not np.allclose(jx[~interior], jr[~interior], atol=1e-7)
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_coef_psi_polynomial_reproduces_energy(seed):
     orc, rng = make_case(100 + seed, kappa=np.inf)
