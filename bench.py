@@ -227,6 +227,112 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# states/s: relaxed GL states per second, batched device CG vs the plain solver
+# ---------------------------------------------------------------------------
+
+STATES_METRIC = "GL states/s to dF/F<=1e-6 (batched device CG vs plain single-instance CG)"
+STATE_SIZES = (129, 193, 257, 385, 513)  # Lx = Ly in {64, 96, 128, 192, 256}, dx = 0.5
+
+
+def states_instances(count, first_seed=1000):
+    """Instance k: its own generator default_rng(first_seed + k): size, H ~ U[0.02, 0.5], kappa = 4,
+    hole fraction U[0, 0.05] with radii U[2, 6], random psi (seeded)."""
+    from svirl_gb300 import learned as L
+    out = []
+    for k in range(count):
+        rng = np.random.default_rng(first_seed + k)
+        n = STATE_SIZES[int(rng.integers(len(STATE_SIZES)))]
+        out.append(L.Instance.sample(n, rng, H_range=(0.02, 0.5), kappa_range=(4.0, 4.0), hole_frac=(0.0, 0.05),
+                                     radius=(2.0, 6.0)))
+    return out
+
+
+def run_states(args):
+    """The batched pipeline (FP32 stencils, FP64 reductions, exact-boundary gradient,
+    device-decided steps) on `args.instances` instances, against F* from a tight FP64
+    relaxation of the same instances from the same start; the plain single-instance
+    CG (the reference's algorithm, step length on the host, FP64) timed on a sample."""
+    from svirl_gb300 import relax as RX
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    insts = states_instances(args.instances)
+    cache = RX.HandleCache()
+    nodes = sum(it.n * it.n for it in insts)
+    # warm-up: a few small instances through the same path
+    RX.relax(states_instances(4, first_seed=1), cache, np.float32, n_iter=50, gtol=1e-3)
+    t0 = time.perf_counter()
+    out, states, _ = RX.relax(insts, cache, np.float32, n_iter=args.cg_iters, gtol=args.gtol)
+    wall = time.perf_counter() - t0
+    # validation (untimed): tight FP64 relaxation from the same start, energies in FP64
+    ref, _, _ = RX.relax(insts, cache, np.float64, n_iter=4 * args.cg_iters, gtol=1e-9, fetch=False)
+    E = RX.energies_fp64(insts, states, cache)
+    Estar = ref["energy"]
+    rel = (E - Estar) / np.abs(Estar)
+    ok = rel <= 1e-6
+    value = float(ok.sum()) / wall
+    # plain single-instance CG on a sample: GLSolver-equivalent handle, reference decisions
+    from svirl_gb300 import GLSolver
+    sample = insts[:args.plain_sample]
+    t_plain, ok_plain = 0.0, 0
+    for q, it in enumerate(sample):
+        gl = GLSolver(Nx=it.n, Ny=it.n, dx=it.dx, dy=it.dx, gl_parameter=it.kappa, homogeneous_external_field=it.H,
+                      material_tiling=it.mt, dtype=np.float64)
+        gl.vars.order_parameter = it.psi0.reshape(it.n, it.n).T
+        a = it.ab0[:(it.n - 1) * it.n].reshape(it.n, it.n - 1).T
+        gl.vars.vector_potential = (a, np.zeros((it.n, it.n - 1)))
+        t1 = time.perf_counter()
+        gl.solve.cg(n_iter=1000)
+        t_plain += time.perf_counter() - t1
+        Ep = gl.observables.free_energy
+        ok_plain += int((Ep - Estar[q]) / abs(Estar[q]) <= 1e-6)
+        gl._h.close()
+    plain_rate = len(sample) / t_plain
+    line = {"metric": STATES_METRIC, "value": value, "unit": "states/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 stencils, f64 reductions", "data": "synthetic (seeded)",
+            "config": {"workload": "batched_field_sweep", "instances": len(insts), "sizes": list(STATE_SIZES),
+                       "kappa": 4.0, "H": "U[0.02,0.5]", "holes": "fraction U[0,0.05], radius U[2,6]",
+                       "nodes_total": nodes, "cg_iters_cap": args.cg_iters, "gtol_abs": args.gtol,
+                       "criterion": "(F - F*)/|F*| <= 1e-6, F* = FP64 relaxation to |grad F| <= 1e-9 from the same start"},
+            "states_ok": int(ok.sum()), "rel_err_quantiles": np.quantile(rel, [0, 0.5, 0.9, 1]).tolist(),
+            "cg_device_ms": out["ms"], "cg_iters": {"mean": float(out["iters"].mean()), "max": int(out["iters"].max())},
+            "plain": {"states_per_s": plain_rate, "sample": len(sample), "met_criterion": ok_plain,
+                      "how": "GLSolver.solve.cg(n_iter=1000), FP64, one instance at a time (the reference's algorithm)"},
+            "speedup_vs_plain": value / plain_rate if plain_rate > 0 else None,
+            "e2e": {"value": value, "unit": "states/s", "h2d_bytes_per_step": int(sum(it.n * it.n * 4 * 4 for it in insts)),
+                    "d2h_bytes_per_step": int(sum(it.n * it.n * 4 * 4 for it in insts)),
+                    "how": "wall time of load (H2D) + batched CG + fetch (D2H) of every instance"}}
+    print(json.dumps(line), flush=True)
+    cache.close()
+
+
+def run_serve(args):
+    """Poisson-arriving requests (mean 200/s), n ~ U{64..512}, kappa finite or inf,
+    fp32 or fp64, TDGL 500 steps then CG; throughput and latency percentiles."""
+    from svirl_gb300 import serve as S
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    reqs = S.poisson_requests(args.requests, 200.0, seed=7)
+    warm = S.Engine(td_steps=10, td_chunk=10, cg_chunk=50, cg_cap=100)
+    warm.run(S.poisson_requests(4, 1000.0, seed=1, sizes=(64, 96)), max_wall_s=60)
+    warm.close()
+    eng = S.Engine(td_steps=500)
+    done, wall = eng.run(reqs, max_wall_s=args.serve_seconds)
+    summ = S.summarize(done, wall)
+    eng.close()
+    line = {"metric": "GL solve requests/s (serving loop)", "value": summ["throughput_per_s"], "unit": "requests/s",
+            "n_gpus": 1, "steps": len(done), "warmup": 1, "ms_per_step": 1e3 * wall / max(len(done), 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 mix",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "serving", "arrivals": "Poisson, mean 200/s", "requests_offered": len(reqs),
+                       "sizes": "U{64..512}^2", "kappa": "U[2,10] or inf (50/50)", "dtype": "fp32/fp64 (50/50)",
+                       "td_steps": 500, "cg": "energy ratio < 1e-6, cap 4000", "wall_limit_s": args.serve_seconds},
+            "latency_s": summ["latency_s"], "completed": summ["completed"], "mean_cg_iters": summ["mean_cg_iters"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -238,10 +344,25 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graphs", action="store_true",
                     help="host-driven Jacobi loop (same kernels); ncu cannot profile kernels inside conditional graphs")
+    ap.add_argument("--workload", choices=["tdgl", "states", "serve"], default="tdgl",
+                    help="tdgl: node-steps/s on the 2049^2 domain; states: relaxed states/s of a batched sweep; "
+                         "serve: the serving loop")
+    ap.add_argument("--requests", type=int, default=2000)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--cg-iters", type=int, default=4000)
+    ap.add_argument("--gtol", type=float, default=1e-4)
+    ap.add_argument("--plain-sample", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "states":
+        run_states(args)
+        return
+    if args.workload == "serve":
+        run_serve(args)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

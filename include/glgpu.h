@@ -17,8 +17,9 @@
  *  - Every call is synchronous with respect to the host unless stated otherwise,
  *    runs on the handle's own CUDA stream, and returns GLGPU_OK (0) or a
  *    negative GLGPU_E_* code; glgpu_last_error() gives the message.
- *  - Device state is owned by the handle; host buffers are copied.  One handle
- *    per host thread (thread-compatible, not thread-safe).
+ *  - Device state is owned by the handle; caller buffers are copied.  The state
+ *    get/set calls accept host or device pointers (unified addressing).  One
+ *    handle per host thread (thread-compatible, not thread-safe).
  */
 #ifndef GLGPU_H
 #define GLGPU_H
@@ -173,7 +174,8 @@ int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable);
  * damped Newton descent of the (alpha_psi, alpha_A) polynomial from (0, 0)
  * (finite kappa) instead of numpy roots / scipy BFGS on the host.  Stops per
  * instance after n_iter updates, when |E_k/E_{k-1} - 1| < rtol (cg.py:315-318),
- * or when |grad F| <= gtol |grad F of the first iteration| (gtol = 0: off).
+ * or when |grad F| <= gtol |grad F of the first iteration| (gtol = 0: off;
+ * with GLGPU_CG_GTOL_ABS: |grad F| <= gtol, tested before the first update too).
  * Per-instance outputs (each may be NULL): iterations done, final energy,
  * final |grad F| relative to the first, status (1 gradient stop, 2 energy stop,
  * 3 n_iter reached, -1 no descent step; then GLGPU_E_NOROOT is returned).
@@ -182,6 +184,7 @@ int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable);
  * doubles the H and A terms there, so its gradient does not vanish at the
  * energy minimum and the gradient-norm stop cannot be met at finite kappa. */
 #define GLGPU_CG_EXACT_BOUNDARY 1
+#define GLGPU_CG_GTOL_ABS 2
 int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t flags, int32_t* iters,
                    double* energies, double* grad_rel, int32_t* status, double* elapsed_ms);
 

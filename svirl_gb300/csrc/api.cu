@@ -233,14 +233,14 @@ int glgpu_get_params(const glgpu_handle* h, glgpu_params* p) {
 
 static int h2d(glgpu_handle* h, void* dst, const void* src, size_t bytes, const char* what) {
     if (!src) return set_error(h, GLGPU_E_ARG, std::string(what) + ": NULL buffer");
-    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream);
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, h->stream);  // host or device source
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     return cuda_check(h, e, what);
 }
 
 static int d2h(glgpu_handle* h, void* dst, const void* src, size_t bytes, const char* what) {
     if (!dst) return set_error(h, GLGPU_E_ARG, std::string(what) + ": NULL buffer");
-    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, h->stream);  // host or device target
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     return cuda_check(h, e, what);
 }

@@ -29,8 +29,10 @@ struct CGLoop {
     int active;
     int iters;     // loop iterations done in this call
     int n_iter;
-    int pad_;
+    int pad_;      // last decision of the WHILE loop (read by the host-driven loop)
     double rtol, gtol;
+    int flags;     // GLGPU_CG_* bits
+    int pad2_;
 };
 
 template <typename T>
@@ -116,7 +118,9 @@ kb_inst_beta(const Inst* __restrict__ insts, int ninst, const double* __restrict
     }
     cs->g2 = v[4];
     cs->gi = 1 - cs->gi;
-    if (cs->iter > 0 && !(v[4] > loop->gtol * loop->gtol * cs->g2_0)) {
+    const bool abs_tol = (loop->flags & GLGPU_CG_GTOL_ABS) != 0;
+    const double thr = abs_tol ? loop->gtol * loop->gtol : loop->gtol * loop->gtol * cs->g2_0;
+    if ((cs->iter > 0 || abs_tol) && !(v[4] > thr)) {
         cs->done = 1;
         cs->status = 1;
         atomicSub(&loop->active, 1);
@@ -217,61 +221,73 @@ __device__ double smallest_nonneg_root_cubic(double d0, double d1, double d2, do
     return best;
 }
 
-// F(a, b) = sum c[i][j] a^i b^j for the 17-coefficient layout, with its
-// gradient and Hessian.
-__device__ void poly2(const double* c17, double a, double b, double* F, double* Fa, double* Fb, double* Faa,
-                      double* Fab, double* Fbb) {
-    double cc[5][5];
-    for (int i = 0; i < 5; ++i)
-        for (int j = 0; j < 5; ++j) cc[i][j] = 0.0;
-    for (int j = 0; j < 5; ++j) {
-        cc[0][j] = c17[j];
-        cc[1][j] = c17[5 + j];
-        cc[2][j] = c17[10 + j];
-    }
-    cc[3][0] = c17[15];
-    cc[4][0] = c17[16];
-    double ap[5] = {1, a, a * a, a * a * a, a * a * a * a}, bp[5] = {1, b, b * b, b * b * b, b * b * b * b};
-    double f = 0, fa = 0, fb = 0, faa = 0, fab = 0, fbb = 0;
-    for (int i = 0; i < 5; ++i)
-        for (int j = 0; j < 5; ++j) {
-            const double w = cc[i][j];
-            if (w == 0.0) continue;
-            f += w * ap[i] * bp[j];
-            if (i >= 1) fa += w * i * ap[i - 1] * bp[j];
-            if (j >= 1) fb += w * j * ap[i] * bp[j - 1];
-            if (i >= 2) faa += w * i * (i - 1) * ap[i - 2] * bp[j];
-            if (i >= 1 && j >= 1) fab += w * i * j * ap[i - 1] * bp[j - 1];
-            if (j >= 2) fbb += w * j * (j - 1) * ap[i] * bp[j - 2];
-        }
-    *F = f; *Fa = fa; *Fb = fb; *Faa = faa; *Fab = fab; *Fbb = fbb;
+// F(a, b) = sum c[i][j] a^i b^j (17-coefficient layout: c00..c04, c10..c14,
+// c20..c24, c30, c40) with its gradient and Hessian, evaluated by a whole warp:
+// lane l < 17 holds one term, the sums are reduced in a fixed tree and
+// broadcast from lane 0, so every lane sees the same values and takes the same
+// branches.
+struct P2 {
+    double f, fa, fb, faa, fab, fbb;
+};
+
+__device__ __forceinline__ double ipow(double x, int k) {
+    double r = 1.0;
+    for (int q = 0; q < k; ++q) r *= x;
+    return r;
 }
 
-// local minimum of the 2-D polynomial reached by descent from (0, 0)
-__device__ bool minimise_poly2(const double* c17, double* a_out, double* b_out) {
+__device__ __forceinline__ double warp_sum_bcast(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+__device__ P2 poly2_warp(double cl, int il, int jl, double a, double b) {
+    const double A0 = ipow(a, il), A1 = il >= 1 ? ipow(a, il - 1) : 0.0, A2 = il >= 2 ? ipow(a, il - 2) : 0.0;
+    const double B0 = ipow(b, jl), B1 = jl >= 1 ? ipow(b, jl - 1) : 0.0, B2 = jl >= 2 ? ipow(b, jl - 2) : 0.0;
+    P2 p;
+    p.f = warp_sum_bcast(cl * A0 * B0);
+    p.fa = warp_sum_bcast(cl * il * A1 * B0);
+    p.fb = warp_sum_bcast(cl * jl * A0 * B1);
+    p.faa = warp_sum_bcast(cl * il * (il - 1) * A2 * B0);
+    p.fab = warp_sum_bcast(cl * il * jl * A1 * B1);
+    p.fbb = warp_sum_bcast(cl * jl * (jl - 1) * A0 * B2);
+    return p;
+}
+
+// Local minimum of the 2-D polynomial reached by a damped Newton descent from
+// (0, 0) (Armijo backtracking; gradient steps where the Hessian is not positive
+// definite); called by all lanes of a warp with the same coefficients.
+__device__ bool minimise_poly2_warp(const double (&c17)[17], double* a_out, double* b_out) {
+    const int lane = threadIdx.x & 31;
+    double cl = 0.0;
+#pragma unroll
+    for (int k = 0; k < 17; ++k)
+        if (k == lane) cl = c17[k];
+    const int il = lane < 15 ? lane / 5 : (lane == 15 ? 3 : (lane == 16 ? 4 : 0));
+    const int jl = lane < 15 ? lane % 5 : 0;
     double a = 0.0, b = 0.0;
-    double F, Fa, Fb, Faa, Fab, Fbb;
-    poly2(c17, a, b, &F, &Fa, &Fb, &Faa, &Fab, &Fbb);
-    const double g0 = sqrt(Fa * Fa + Fb * Fb);
+    P2 P = poly2_warp(cl, il, jl, a, b);
+    const double g0 = sqrt(P.fa * P.fa + P.fb * P.fb);
     for (int it = 0; it < 60; ++it) {
-        const double gn = sqrt(Fa * Fa + Fb * Fb);
+        const double gn = sqrt(P.fa * P.fa + P.fb * P.fb);
         if (!(gn > 1e-14 * (g0 + 1e-300))) break;
         double sa, sb;
-        const double det = Faa * Fbb - Fab * Fab;
-        if (Faa > 0.0 && det > 0.0) {
-            sa = -(Fbb * Fa - Fab * Fb) / det;
-            sb = -(-Fab * Fa + Faa * Fb) / det;
+        const double det = P.faa * P.fbb - P.fab * P.fab;
+        if (P.faa > 0.0 && det > 0.0) {
+            sa = -(P.fbb * P.fa - P.fab * P.fb) / det;
+            sb = -(-P.fab * P.fa + P.faa * P.fb) / det;
         } else {
-            const double h = fabs(Faa) + fabs(Fbb) + 1e-300;
-            sa = -Fa / h;
-            sb = -Fb / h;
+            const double h = fabs(P.faa) + fabs(P.fbb) + 1e-300;
+            sa = -P.fa / h;
+            sb = -P.fb / h;
         }
-        double t = 1.0, Fn, Fna, Fnb, Fnaa, Fnab, Fnbb;
-        const double slope = Fa * sa + Fb * sb;
+        double t = 1.0;
+        const double slope = P.fa * sa + P.fb * sb;
         bool moved = false;
+        P2 Pn;
         for (int ls = 0; ls < 60; ++ls) {
-            poly2(c17, a + t * sa, b + t * sb, &Fn, &Fna, &Fnb, &Fnaa, &Fnab, &Fnbb);
-            if (Fn <= F + 1e-4 * t * slope) {
+            Pn = poly2_warp(cl, il, jl, a + t * sa, b + t * sb);
+            if (Pn.f <= P.f + 1e-4 * t * slope) {
                 moved = true;
                 break;
             }
@@ -280,7 +296,7 @@ __device__ bool minimise_poly2(const double* c17, double* a_out, double* b_out) 
         if (!moved) break;
         a += t * sa;
         b += t * sb;
-        F = Fn; Fa = Fna; Fb = Fnb; Faa = Fnaa; Fab = Fnab; Fbb = Fnbb;
+        P = Pn;
         if (fabs(t * sa) + fabs(t * sb) <= 1e-15 * (1.0 + fabs(a) + fabs(b))) break;
     }
     *a_out = a;
@@ -298,18 +314,20 @@ kb_inst_alpha(const Inst* __restrict__ insts, int ninst, const double* __restric
     CGState* cs = I.cg;
     if (cs->done) return;
     double c[17];
+#pragma unroll
     for (int k = 0; k < 17; ++k) c[k] = warp_tile_sum(partials, I.tile0, I.ntiles, k) * I.g.dxdy;
+    bool ok;
+    double ap = 0.0, aA = 0.0;
+    if (I.solveA) {
+        ok = minimise_poly2_warp(c, &ap, &aA);
+    } else {
+        ap = smallest_nonneg_root_cubic(c[5], 2.0 * c[10], 3.0 * c[15], 4.0 * c[16]);
+        ok = ap >= 0.0;
+    }
     if ((threadIdx.x & 31) != 0) return;
     for (int k = 0; k < 17; ++k) cs->c[k] = c[k];
-    bool ok;
-    if (I.solveA) {
-        ok = minimise_poly2(c, &cs->alpha_psi, &cs->alpha_A);
-    } else {
-        const double a = smallest_nonneg_root_cubic(c[5], 2.0 * c[10], 3.0 * c[15], 4.0 * c[16]);
-        ok = a >= 0.0;
-        cs->alpha_psi = a;
-        cs->alpha_A = 0.0;
-    }
+    cs->alpha_psi = ap;
+    cs->alpha_A = aA;
     cs->di = 1 - cs->di;  // the new direction is now current
     if (!ok) {
         cs->done = 1;
@@ -599,6 +617,7 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
     lp.n_iter = n_iter;
     lp.rtol = rtol;
     lp.gtol = gtol;
+    lp.flags = flags;
     cudaError_t e = cudaMemcpyAsync(b->insts, insts.data(), sizeof(Inst) * insts.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->cg_loop, &lp, sizeof(lp), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -158,36 +158,50 @@ template <typename T> __device__ __forceinline__ C2<T> shfl_down_c(C2<T> v, int 
 
 // The backward-Euler Jacobi update of one node (svirl/cuda/td.h:4-133 with the
 // Winecki-Adams link weights of td.h:159-163, coded as bits of cd: 0 left,
-// 1 right, 2 lower, 3 upper link).  rq is the right-hand side with the Langevin
-// term added.  A node with neither a left nor a right link gets 0.
+// 1 right, 2 lower, 3 upper link), in two parts.  The diagonal depends only on
+// the right-hand side (with the Langevin term, rq), the linear coefficient and
+// the link weights, which are fixed during a Jacobi loop, so its reciprocal is
+// formed once per node and launch (psi_diag_inv) and each sweep only forms the
+// neighbour sums (psi_node).  A node with neither a left nor a right link gets 0.
+template <typename T>
+__device__ __forceinline__ T psi_diag_inv(C2<T> rq, T eps, unsigned cd, T dt, T idx2, T idy2) {
+    const bool rm0 = cd & 1u, rp0 = cd & 2u, r0m = cd & 4u, r0p = cd & 8u;
+    const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
+    const T diag = T(1) + dt * (rq.x * rq.x + rq.y * rq.y - eps + (idx2 * wx + idy2 * wy));
+    return T(1) / diag;
+}
+
 template <typename T>
 __device__ __forceinline__ C2<T> psi_node(C2<T> p_left, C2<T> p_right, C2<T> p_prev, C2<T> p_next, C2<T> ua_left,
-                                          C2<T> ua, C2<T> ub_down, C2<T> ub, C2<T> rq, T eps, unsigned cd, T dt,
+                                          C2<T> ua, C2<T> ub_down, C2<T> ub, C2<T> rq, T inv, unsigned cd, T dt,
                                           T idx2, T idy2) {
     const C2<T> z = cmk<T>(T(0), T(0));
     C2<T> out = z;
     if (cd & 3u) {
-        const bool rm0 = cd & 1u, rp0 = cd & 2u, r0m = cd & 4u, r0p = cd & 8u;
         C2<T> sx = z, sy = z;
-        if (rm0) sx = cadd(sx, cmul(cconj(ua_left), p_left));
-        if (rp0) sx = cadd(sx, cmul(ua, p_right));
-        if (r0m) sy = cadd(sy, cmul(cconj(ub_down), p_prev));
-        if (r0p) sy = cadd(sy, cmul(ub, p_next));
-        const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
-        const T diag = T(1) + dt * (rq.x * rq.x + rq.y * rq.y - eps + (idx2 * wx + idy2 * wy));
-        const T inv = T(1) / diag;
+        if (cd & 1u) sx = cadd(sx, cmul(cconj(ua_left), p_left));
+        if (cd & 2u) sx = cadd(sx, cmul(ua, p_right));
+        if (cd & 4u) sy = cadd(sy, cmul(cconj(ub_down), p_prev));
+        if (cd & 8u) sy = cadd(sy, cmul(ub, p_next));
         out.x = (rq.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
         out.y = (rq.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
     }
     return out;
 }
 
-// Per-row inputs of the psi update besides psi itself: the link factors of the
-// x link and the y link that start at the node, the right-hand side, the linear
-// coefficient and the link-weight code.
+// Per-row inputs of the psi update besides psi itself, as loaded: the link
+// factors of the x link and the y link that start at the node, the right-hand
+// side, the linear coefficient and the link-weight code ...
 template <typename T> struct PsiSide {
     C2<T> ua, ub, rr;
     T eps;
+    unsigned cd;
+};
+// ... and as used by the sweeps: rq = right-hand side with the Langevin term,
+// inv = reciprocal of the diagonal.
+template <typename T> struct PsiRow {
+    C2<T> ua, ub, rq;
+    T inv;
     unsigned cd;
 };
 
@@ -205,13 +219,22 @@ template <typename T> struct PsiSide {
 // loop can stop after any of the fused sweeps.  The row walk is unrolled with
 // every load issued one step ahead of its use.  Persistent grid: warps stride
 // over the item table.
+// CTAs of the psi sweep are small: its warps are independent, and registers are
+// allocated per CTA, so small CTAs fill an SM with more warps.
+#ifndef GLGPU_PSI_THREADS
+#define GLGPU_PSI_THREADS 64
+#endif
+#ifndef GLGPU_PSI_MIN_CTAS
+#define GLGPU_PSI_MIN_CTAS 1
+#endif
+constexpr int kPsiThreads = GLGPU_PSI_THREADS, kPsiWarps = kPsiThreads / 32;
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kPsiThreads, GLGPU_PSI_MIN_CTAS)
 k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
             cudaGraphConditionalHandle cond, int use_cond) {
     constexpr int K = kFuse, RR = kStripRows, S = kStripRows + 2 * kFuse;
     const int lane = threadIdx.x & 31;
-    const int gw = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
+    const int gw = blockIdx.x * kPsiWarps + (threadIdx.x >> 5), nw = gridDim.x * kPsiWarps;
     int cur_inst = -1, k = 0, count = 0, done = 1;
     T wmax[K];
     bool wnan[K];
@@ -280,11 +303,26 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
         };
         // window of sweep l-1 (l = 1..K) as seen by sweep l: rows y-1 and y
         C2<T> wp[K], wc[K];
-        PsiSide<T> D[K + 1];  // D[m]: per-row inputs of row (j0 - K + s - 1) - m
+        PsiRow<T> D[K + 1];  // D[m]: per-row inputs of row (j0 - K + s - 1) - m
 #pragma unroll
         for (int l = 0; l < K; ++l) wp[l] = wc[l] = z;
 #pragma unroll
-        for (int m = 0; m <= K; ++m) D[m] = PsiSide<T>{z, z, z, eps0, 0u};
+        for (int m = 0; m <= K; ++m) D[m] = PsiRow<T>{z, z, z, T(0), 0u};
+        // loaded inputs of row y -> sweep inputs (done one step after the loads were issued)
+        auto finish_side = [&](const PsiSide<T>& q, int y) -> PsiRow<T> {
+            PsiRow<T> r;
+            r.ua = q.ua;
+            r.ub = q.ub;
+            r.cd = q.cd;
+            r.rq = q.rr;
+            if (lang && calc_lane && y >= 0 && y < Ny) {
+                const uint32_t n = (uint32_t)(i + Nx * y);
+                r.rq.x += lc * (rand_1<T>(n, rt) - T(0.5));
+                r.rq.y += lc * (rand_2<T>(n, rt) - T(0.5));
+            }
+            r.inv = (q.cd & 3u) ? psi_diag_inv<T>(r.rq, q.eps, q.cd, dt, idx2, idy2) : T(0);
+            return r;
+        };
         C2<T> nx_p = load_psi(j0 - K);
         PsiSide<T> nx_s = load_side(j0 - K - 1);
 #pragma unroll
@@ -292,7 +330,7 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             C2<T> newrow = nx_p;  // psi^(k) on row j0 - K + s
 #pragma unroll
             for (int m = K; m >= 1; --m) D[m] = D[m - 1];
-            D[0] = nx_s;
+            D[0] = finish_side(nx_s, j0 - K + s - 1);
             if (s + 1 < S) {
                 nx_p = load_psi(j0 - K + s + 1);
                 nx_s = load_side(j0 - K + s);
@@ -304,27 +342,19 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
                     const int y = j0 - K + s - l;
                     const C2<T> pc = wc[l - 1];
                     const C2<T> pl = shfl_up_c<T>(pc, 1), pr = shfl_down_c<T>(pc, 1);
-                    const PsiSide<T>& d = D[l - 1];
+                    const PsiRow<T>& d = D[l - 1];
                     const C2<T> ual = shfl_up_c<T>(d.ua, 1);
                     const bool node = calc_lane && y >= 0 && y < Ny;
                     if (node) {
-                        C2<T> rq = d.rr;
-                        if (lang) {
-                            const uint32_t n = (uint32_t)(i + Nx * y);
-                            rq.x += lc * (rand_1<T>(n, rt) - T(0.5));
-                            rq.y += lc * (rand_2<T>(n, rt) - T(0.5));
-                        }
-                        out = psi_node<T>(pl, pr, wp[l - 1], newrow, ual, d.ua, D[l].ub, d.ub, rq, d.eps, d.cd, dt,
+                        out = psi_node<T>(pl, pr, wp[l - 1], newrow, ual, d.ua, D[l].ub, d.ub, d.rq, d.inv, d.cd, dt,
                                           idx2, idy2);
                         if (own_lane && y >= j0 && y < j0 + RR) {
                             outb[l - 1][i + Nx * y] = out;
+                            // max(|d re|, |d im|); a NaN component counts as 0 (the reference's
+                            // int conversion), fmax drops NaN operands
                             const T dr = fabs(out.x - pc.x), di = fabs(out.y - pc.y);
-                            T res = dr > di ? dr : di;
-                            if (!(dr == dr) || !(di == di)) {  // NaN counts as 0, like the reference's int conversion
-                                wnan[l - 1] = true;
-                                res = (dr == dr) ? dr : ((di == di) ? di : T(0));
-                            }
-                            wmax[l - 1] = res > wmax[l - 1] ? res : wmax[l - 1];
+                            if (!(dr + di == dr + di)) wnan[l - 1] = true;
+                            wmax[l - 1] = fmax(wmax[l - 1], fmax(dr, di));
                         }
                     }
                 }
@@ -646,7 +676,7 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         {
             cudaGraphNode_t sw;
             void* a[] = {&insts, &items, &nitems, &loop, &hpsi, &one};
-            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype), dim3(L.psi_grid), bt, a));
+            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype), dim3(L.psi_grid), dim3(kPsiThreads), a));
         }
         {
             void* a[] = {&insts, &ninst, &zero};
@@ -716,8 +746,8 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
             for (;;) {
                 for (int c = 0; c < chunk; ++c) {
                     if (part == 0) {
-                        if (L.dtype == 8) k_psi_sweep<double><<<L.psi_grid, kThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
-                        else k_psi_sweep<float><<<L.psi_grid, kThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
+                        if (L.dtype == 8) k_psi_sweep<double><<<L.psi_grid, kPsiThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
+                        else k_psi_sweep<float><<<L.psi_grid, kPsiThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
                     } else {
                         if (L.dtype == 8) k_A_sweep<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
                         else k_A_sweep<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
@@ -797,8 +827,8 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
         k_bench_prep<<<1, 32, 0, h->stream>>>(h->inst, 1, h->loop, 1);
         cudaEventRecord(e0, h->stream);
         if (which == 0) {
-            if (h->dtype == 8) k_psi_sweep<double><<<h->psi_grid, kThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
-            else k_psi_sweep<float><<<h->psi_grid, kThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
+            if (h->dtype == 8) k_psi_sweep<double><<<h->psi_grid, kPsiThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
+            else k_psi_sweep<float><<<h->psi_grid, kPsiThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
         } else {
             if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
             else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
@@ -826,8 +856,8 @@ int psi_sweep_grid(int dtype, int nitems) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     void* fn = psi_sweep_fn(dtype);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
-    const int need = (nitems + kWarps - 1) / kWarps;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPsiThreads, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    const int need = (nitems + kPsiWarps - 1) / kPsiWarps;
     const int full = sms * per_sm;
     return need < full ? (need > 0 ? need : 1) : full;
 }
