@@ -24,15 +24,15 @@ k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const ui
           C2<T>* __restrict__ gpsi, T* __restrict__ gA, const C2<T>* __restrict__ gpsi_prev, const T* __restrict__ gA_prev,
           int solveA, double* partials, unsigned* counter, double* dscal) {
     const int n = blockIdx.x * kThreads + threadIdx.x;
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    T v[4] = {T(0), T(0), T(0), T(0)};
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, mt, i, j);
         const C2<T> G = grad_psi_node<T>(g, (T)eps0, eps_sp, psi, abei, ab, n, i, j, cb);
         gpsi[n] = G;
         const C2<T> Gp = gpsi_prev[n];
-        v[0] = (double)(G.x * (G.x - Gp.x) + G.y * (G.y - Gp.y));
-        v[1] = (double)(Gp.x * Gp.x + Gp.y * Gp.y);
+        v[0] = G.x * (G.x - Gp.x) + G.y * (G.y - Gp.y);
+        v[1] = Gp.x * Gp.x + Gp.y * Gp.y;
         if (solveA) {
             const T k2 = (T)kappa2, Hh = (T)H;
             if (i < g.Nx - 1) {
@@ -40,20 +40,20 @@ k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const ui
                 const T Ga = grad_A_link<T>(g, k2, Hh, psi, abei, ab, n, i, j, cb, true);
                 gA[na] = Ga;
                 const T Gpa = gA_prev[na];
-                v[2] += (double)(Ga * (Ga - Gpa));
-                v[3] += (double)(Gpa * Gpa);
+                v[2] += Ga * (Ga - Gpa);
+                v[3] += Gpa * Gpa;
             }
             if (j < g.Ny - 1) {
                 const int nb = g.Na + i + g.Nx * j;
                 const T Gb = grad_A_link<T>(g, k2, Hh, psi, abei, ab, n, i, j, cb, false);
                 gA[nb] = Gb;
                 const T Gpb = gA_prev[nb];
-                v[2] += (double)(Gb * (Gb - Gpb));
-                v[3] += (double)(Gpb * Gpb);
+                v[2] += Gb * (Gb - Gpb);
+                v[3] += Gpb * Gpb;
             }
         }
     }
-    grid_sum_finish<4>(v, partials, counter, dscal + 24, 1.0);
+    grid_sum_finish(v, partials, counter, dscal + 24, 1.0);
 }
 
 // beta = max(num/den, 0) with the reference's float semantics (divide_scalars_positive).
@@ -80,9 +80,9 @@ k_cg_dir_coef(Geo g, double kappa2, double eps0, const T* eps_sp, double H, cons
               C2<T>* __restrict__ dN, T* __restrict__ dAN, int dir_mode,
               double* partials, unsigned* counter, double* dscal) {
     const int n = blockIdx.x * kThreads + threadIdx.x;
-    double c[NV];
+    T c[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) c[k] = 0.0;
+    for (int k = 0; k < NV; ++k) c[k] = T(0);
     const T bp = (T)dscal[28], bA = (T)dscal[29];
     auto dpsi = [&](int m) -> C2<T> {
         const C2<T> o = dO[m];
@@ -107,7 +107,7 @@ k_cg_dir_coef(Geo g, double kappa2, double eps0, const T* eps_sp, double H, cons
         }
         coef_node<T, NV>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, psi, abei, ab, n, i, j, cb, dpsi, dA, c);
     }
-    grid_sum_finish<NV>(c, partials, counter, dscal, g.dxdy);
+    grid_sum_finish(c, partials, counter, dscal, g.dxdy);
 }
 
 template <typename T>

@@ -57,7 +57,7 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
     const C2<T>* Gp = (const C2<T>*)I.gpsi[gi];
     T* GA = (T*)I.gA[1 - gi];
     const T* GAp = (const T*)I.gA[gi];
-    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    T v[5] = {T(0), T(0), T(0), T(0), T(0)};
     const int n = t.n0 + threadIdx.x;
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
@@ -65,9 +65,9 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
         const C2<T> gv = grad_psi_node<T>(g, gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp, psi, abei, ab, n, i, j, cb);
         G[n] = gv;
         const C2<T> gp = Gp[n];
-        v[0] = (double)(gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y));
-        v[1] = (double)(gp.x * gp.x + gp.y * gp.y);
-        v[4] = (double)(gv.x * gv.x + gv.y * gv.y);
+        v[0] = gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y);
+        v[1] = gp.x * gp.x + gp.y * gp.y;
+        v[4] = gv.x * gv.x + gv.y * gv.y;
         if (I.solveA) {
             const T k2 = gsel<T>(I.kappa2, I.fkappa2), H = gsel<T>(I.H, I.fH);
             for (int dir = 0; dir < 2; ++dir) {
@@ -77,14 +77,15 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
                 const T ga = grad_A_link<T>(g, k2, H, psi, abei, ab, n, i, j, cb, dir == 0, I.cg_exact != 0);
                 GA[l] = ga;
                 const T gap = GAp[l];
-                v[2] += (double)(ga * (ga - gap));
-                v[3] += (double)(gap * gap);
-                v[4] += (double)(ga * ga);
+                v[2] += ga * (ga - gap);
+                v[3] += gap * gap;
+                v[4] += ga * ga;
             }
         }
     }
-    block_sum<5>(v);
-    if (threadIdx.x == 0) store_partials<T>(v, 5, partials + (size_t)blockIdx.x * kPart);
+    double vs[5];
+    block_sum<5>(v, vs);
+    if (threadIdx.x == 0) store_partials<T>(vs, 5, partials + (size_t)blockIdx.x * kPart);
 }
 
 // Sum of component k of the partials of instance I's tiles, in tile order, by one warp.
@@ -152,9 +153,9 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
         return cmk<T>(bp * o.x - gg.x, bp * o.y - gg.y);
     };
     auto dA = [&](int m) -> T { return bA * dAO[m] - GA[m]; };
-    double c[17];
+    T c[17];
 #pragma unroll
-    for (int k = 0; k < 17; ++k) c[k] = 0.0;
+    for (int k = 0; k < 17; ++k) c[k] = T(0);
     const int n = t.n0 + threadIdx.x;
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
@@ -167,13 +168,14 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
             coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, n, i, j, cb,
                              dpsi, dA, c);
         } else {
-            double c5[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+            T c5[5] = {T(0), T(0), T(0), T(0), T(0)};
             coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, n, i, j, cb, dpsi, dA, c5);
             c[0] = c5[0]; c[5] = c5[1]; c[10] = c5[2]; c[15] = c5[3]; c[16] = c5[4];
         }
     }
-    block_sum<17>(c);
-    if (threadIdx.x == 0) store_partials<T>(c, 17, partials + (size_t)blockIdx.x * kPart);
+    double cs17[17];
+    block_sum<17>(c, cs17);
+    if (threadIdx.x == 0) store_partials<T>(cs17, 17, partials + (size_t)blockIdx.x * kPart);
 }
 
 // Real roots of d0 + d1 a + d2 a^2 + d3 a^3; returns the smallest root >= 0 or -1.
@@ -369,14 +371,15 @@ kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double
     const Inst& I = insts[t.inst];
     if (!all && *(volatile const int*)&I.cg->done) return;
     const Geo g = I.g;
-    double v[1] = {0.0};
+    T v[1] = {T(0)};
     const int n = t.n0 + threadIdx.x;
     if (n < g.N)
-        v[0] = (double)energy_density<T>(g, gsel<T>(I.kappa2, I.fkappa2), gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp,
+        v[0] = energy_density<T>(g, gsel<T>(I.kappa2, I.fkappa2), gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp,
                                          gsel<T>(I.H, I.fH), I.mt, (const C2<T>*)I.psi[0], (const T*)I.abei,
                                          (const T*)I.ab[0], n);
-    block_sum<1>(v);
-    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kPart] = v[0];
+    double vs[1];
+    block_sum<1>(v, vs);
+    if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kPart] = vs[0];
 }
 
 // energies, the energy-ratio stop, the iteration cap, and the WHILE condition

@@ -201,15 +201,63 @@ template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV]) {
     }
 }
 
+// Error-free sum (Knuth's two-sum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Sum NV per-thread float values over the CTA into doubles (thread 0): the
+// warp stage is compensated (each partial carried as a float pair hi + lo, the
+// rounding error of every addition kept by two_sum), the warp results are
+// added in double.  FP32 arithmetic with close to double accuracy, without the
+// FP64 pipe in the 5-level warp tree.  Fixed order: deterministic.
+template <int NV> __device__ __forceinline__ void block_sum(const float (&v)[NV], double (&out)[NV]) {
+    __shared__ double sm[kWarps][NV];
+    const int tid = flat_tid(), lane = tid & 31, w = tid >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        float hi = v[k], lo = 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
+            float sum, err;
+            two_sum(hi, oh, sum, err);
+            hi = sum;
+            lo = lo + (ol + err);
+        }
+        out[k] = (double)hi + (double)lo;
+    }
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sm[w][k] = out[k];
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+            for (int q = 0; q < kWarps; ++q) s += sm[q][k];
+            out[k] = s;
+        }
+    }
+}
+template <int NV> __device__ __forceinline__ void block_sum(const double (&v)[NV], double (&out)[NV]) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = v[k];
+    block_sum<NV>(out);
+}
+
 // Grid-wide FP64 vector sum in one launch: every CTA stores its partials, the
 // last CTA to finish (ticket counter) adds the partials in block order and
 // writes NV results to out[] (scaled by `scale`).  `counter` must be 0 on entry
-// and is left 0.
-template <int NV>
-__device__ void grid_sum_finish(double (&v)[NV], double* __restrict__ partials, unsigned* counter,
+// and is left 0.  Per-thread inputs in the kernel's precision T.
+template <typename T, int NV>
+__device__ void grid_sum_finish(const T (&vin)[NV], double* __restrict__ partials, unsigned* counter,
                                 double* __restrict__ out, double scale) {
     __shared__ bool last;
-    block_sum<NV>(v);
+    double v[NV];
+    block_sum<NV>(vin, v);
     const int tid = flat_tid();
     const int nblk = gridDim.x * gridDim.y;
     const int bid = blockIdx.x + gridDim.x * blockIdx.y;

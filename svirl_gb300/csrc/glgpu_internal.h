@@ -18,7 +18,7 @@ namespace glgpu {
 // does kFuse consecutive sweeps and writes every one of them, so the loop can
 // stop after any of them exactly where the one-sweep-per-launch loop stops.
 #ifndef GLGPU_FUSE
-#define GLGPU_FUSE 2
+#define GLGPU_FUSE 3
 #endif
 #ifndef GLGPU_STRIP_ROWS
 #define GLGPU_STRIP_ROWS 16

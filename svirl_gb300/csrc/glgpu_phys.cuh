@@ -201,7 +201,7 @@ __device__ __forceinline__ T grad_A_link(const Geo& g, T kappa2, T H, const C2<T
 template <typename T, int NV, typename FD, typename FA>
 __device__ __forceinline__ void coef_node(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H, const C2<T>* psi,
                                           const T* abei, const T* ab, int n, int i, int j, unsigned cb,
-                                          const FD& dpsi, const FA& dA, double (&c)[NV]) {
+                                          const FD& dpsi, const FA& dA, T (&c)[NV]) {
     const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
     const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
     if (cb) {

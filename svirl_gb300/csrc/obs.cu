@@ -17,9 +17,9 @@ __global__ void __launch_bounds__(kThreads)
 k_energy(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const uint8_t* mt,
          const C2<T>* __restrict__ psi, const T* abei, const T* ab, double* partials, unsigned* counter, double* out) {
     const int n = blockIdx.x * kThreads + threadIdx.x;
-    double v[1] = {0.0};
-    if (n < g.N) v[0] = (double)energy_density<T>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, mt, psi, abei, ab, n);
-    grid_sum_finish<1>(v, partials, counter, out, g.dxdy);
+    T v[1] = {T(0)};
+    if (n < g.N) v[0] = energy_density<T>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, mt, psi, abei, ab, n);
+    grid_sum_finish(v, partials, counter, out, g.dxdy);
 }
 
 template <typename T>
@@ -118,7 +118,7 @@ k_vsum(const double* __restrict__ x, long long n, double* partials, unsigned* co
     for (long long m = (long long)blockIdx.x * kThreads + threadIdx.x; m < n; m += (long long)gridDim.x * kThreads)
 #pragma unroll
         for (int k = 0; k < NV; ++k) v[k] += x[m * NV + k];
-    grid_sum_finish<NV>(v, partials, counter, out, 1.0);
+    grid_sum_finish(v, partials, counter, out, 1.0);
 }
 
 // ---------------------------------------------------------------------------

@@ -49,8 +49,9 @@ class Engine:
     """Continuous batching of TDGL + CG requests."""
 
     def __init__(self, td_steps=500, td_chunk=50, cg_chunk=200, cg_cap=4000, rtol=1e-6, dt=0.1, reserve_bytes=8 << 30,
-                 device=0):
+                 max_active_nodes=6_000_000, device=0):
         self.td_steps, self.td_chunk, self.cg_chunk, self.cg_cap = td_steps, td_chunk, cg_chunk, cg_cap
+        self.max_active_nodes = max_active_nodes  # bounds a step's duration, hence latency
         self.rtol, self.dt, self.reserve = rtol, dt, reserve_bytes
         self.cache = HandleCache(device=device)
         self.active = []   # dicts: req, h, phase ('td' | 'cg'), td_left, cg_done, admitted
@@ -66,7 +67,12 @@ class Engine:
             return 1 << 40
 
     def admit(self, req, now):
+        """Admit a waiting request if device memory (with a reserve) and the
+        active-node budget allow it; first come, first served."""
         need = instance_bytes(req.n, req.dtype)
+        active_nodes = sum(a["req"].n ** 2 for a in self.active)
+        if self.active and active_nodes + req.n ** 2 > self.max_active_nodes:
+            return False
         if self._free_bytes() - need < self.reserve:
             return False
         h = self.cache.get(req.n, req.dtype)

@@ -1,0 +1,153 @@
+"""Generate the golden fixtures of tests/golden/ (run in a checkout where the
+reference sources are available; the fixtures are committed, the GPU tests only
+read them).
+
+For each case the unmodified reference (microsoft/svirl's host code) runs on the
+NumPy pycuda shim (oracle/fake_pycuda) from its own seeded initial state: the
+fixture keeps the inputs (psi0, A0, mask, external vector potential, parameters)
+and the reference's outputs (free energy, B, j, js, dF/dpsi, dF/dA and the 5/17
+line-search coefficients for a seeded direction at the initial state; psi, A and
+the Jacobi sweep counts after TDGL; the CG energies and state after a few
+iterations; the vortex list of the final state).  The oracle recomputes every
+output from the inputs and must agree before a fixture is written.
+
+    python tests/golden/make_golden.py [reference_dir]
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import gl_oracle as O  # noqa: E402
+
+CASES = {
+    # name: (Nx, Ny, dx, dy, kappa, sigma, H, external_field, mask_kind, seed, td_steps, cg_iters)
+    "k5_full": (12, 11, 0.5, 0.45, 5.0, 200.0, 0.1, 0.0, "none", 1, 6, 6),
+    "k2_random_ext": (10, 9, 0.5, 0.5, 2.0, 10.0, 0.3, 0.05, "random30", 2, 5, 5),
+    "kinf_holes": (13, 12, 0.5, 0.5, np.inf, 1.0, 0.2, 0.0, "holes", 3, 6, 8),
+}
+
+
+def mask_of(kind, nxc, nyc, rng):
+    if kind == "none":
+        return None
+    mt = np.ones((nxc, nyc), dtype=bool)
+    if kind == "random30":
+        k = int(0.3 * nxc * nyc)
+        mt[rng.integers(0, nxc, k), rng.integers(0, nyc, k)] = False
+    elif kind == "holes":
+        mt[2:5, 3:6] = False
+        mt[nxc - 4:nxc - 2, 1:3] = False
+    return mt
+
+
+def flat(x):
+    return O.flatten_ij(np.asarray(x))
+
+
+def close(x, y, tol):
+    x, y = np.asarray(x), np.asarray(y)
+    return np.max(np.abs(x - y)) <= tol * max(np.max(np.abs(y)), 1e-300)
+
+
+def make_case(svirl, name, spec):
+    Nx, Ny, dx, dy, kappa, sigma, H, ext, kind, seed, nt, ncg = spec
+    rng = np.random.default_rng(100 + seed)
+    mt = mask_of(kind, Nx - 1, Ny - 1, rng)
+    kw = dict(Nx=Nx, Ny=Ny, dx=dx, dy=dy, order_parameter="random", random_seed=seed, gl_parameter=kappa,
+              normal_conductivity=sigma, homogeneous_external_field=H)
+    if mt is not None:
+        kw["material_tiling"] = mt
+    if ext:
+        kw["external_field"] = ext
+    gl = svirl.GLSolver(**kw)
+    psi0 = flat(gl.vars.order_parameter)
+    a, b = gl.vars.vector_potential
+    ab0 = np.concatenate([flat(a), flat(b)])
+    ei = gl.params.external_irregular_vector_potential
+    abei = None if ei is None else np.concatenate([flat(ei[0]), flat(ei[1])])
+    orc = O.GLOracle(Nx, Ny, dx, dy, psi0, ab0, mt=None if mt is None else flat(mt), abei=abei, kappa=kappa,
+                     sigma=sigma, H=H, rand_t=seed)
+    out = {"Nx": Nx, "Ny": Ny, "dx": dx, "dy": dy, "kappa": kappa, "sigma": sigma, "H": H, "ext": ext, "seed": seed,
+           "td_steps": nt, "cg_iters": ncg, "psi0": psi0, "ab0": ab0,
+           "mt": np.zeros(0, bool) if mt is None else flat(mt), "abei": np.zeros(0) if abei is None else abei}
+    # observables, gradients and coefficients at the initial state
+    out["F0"] = gl.observables.free_energy
+    out["B0"] = flat(gl.observables.magnetic_field)
+    jx, jy = gl.observables.current_density
+    out["j0"] = np.concatenate([flat(jx), flat(jy)])
+    sx, sy = gl.observables.supercurrent_density
+    out["js0"] = np.concatenate([flat(sx), flat(sy)])
+    gl.solve._init_cg()
+    out["gpsi0"] = np.asarray(gl.solve._cg._free_energy_jacobian_psi.get()).reshape(-1)
+    drng = np.random.default_rng(7 + seed)
+    dpsi = drng.standard_normal(Nx * Ny) + 1j * drng.standard_normal(Nx * Ny)
+    out["dpsi"] = dpsi
+    if np.isfinite(kappa):
+        out["gA0"] = np.asarray(gl.solve._cg._free_energy_jacobian_A.get()).reshape(-1)
+        dab = 0.1 * drng.standard_normal(orc.g.Nab)
+        out["dab"] = dab
+        out["coef"] = np.asarray(orc.coef(dpsi, dab))
+        ref_c = np.asarray(gl.solve._cg._free_energy_conjgrad_coef(svirl_gpu(dpsi), svirl_gpu(dab)))
+        ref_c = np.concatenate([ref_c[0, :], ref_c[1, :], ref_c[2, :], [ref_c[3, 0], ref_c[4, 0]]])
+        assert close(out["coef"], ref_c, 1e-12), name
+    else:
+        out["coef"] = np.asarray(orc.coef_psi(dpsi))
+        ref_c = np.asarray(gl.solve._cg._free_energy_conjgrad_coef_psi(svirl_gpu(dpsi)))
+        assert close(out["coef"], ref_c, 1e-12), name
+    assert abs(orc.free_energy() - out["F0"]) <= 1e-13 * abs(out["F0"]), name
+    assert close(orc.magnetic_field(), out["B0"], 1e-12) and close(orc.current_density(), out["j0"], 1e-12)
+    assert close(orc.supercurrent_density(), out["js0"], 1e-12) and close(orc.jacobian_psi(), out["gpsi0"], 1e-12)
+    if np.isfinite(kappa):
+        assert close(orc.jacobian_A(), out["gA0"], 1e-12), name
+    # TDGL
+    gl.solve.td(dt=0.1, Nt=nt)
+    orc.td(dt=0.1, Nt=nt)
+    out["psi_td"] = flat(gl.vars.order_parameter)
+    a, b = gl.vars.vector_potential
+    out["ab_td"] = np.concatenate([flat(a), flat(b)])
+    out["sweeps_psi"] = np.array(orc.sweeps_psi)
+    out["sweeps_A"] = np.array(getattr(orc, "sweeps_A", []))
+    assert close(orc.psi, out["psi_td"], 1e-13) and close(orc.ab, out["ab_td"], 1e-13), name
+    # CG
+    gl.solve.cg(n_iter=ncg)
+    orc.cg(n_iter=ncg)
+    out["cg_energies"] = np.array(gl.solve._cg.cg_energies)
+    out["psi_cg"] = flat(gl.vars.order_parameter)
+    a, b = gl.vars.vector_potential
+    out["ab_cg"] = np.concatenate([flat(a), flat(b)])
+    tol = 1e-13 if np.isinf(kappa) else 1e-8
+    assert close(orc.cg_energies, out["cg_energies"], tol), name
+    # vortex detector on the final state
+    vx, vy, vv = gl.vortex_detector.vortices
+    out["vx"], out["vy"], out["vv"] = np.asarray(vx), np.asarray(vy), np.asarray(vv)
+    ox, oy, ov = O.detect_vortices(orc.g, out["psi_cg"], out["ab_cg"], H)
+    assert np.array_equal(ox, out["vx"]) and np.array_equal(ov, out["vv"]), name
+    np.savez_compressed(os.path.join(HERE, "case_%s.npz" % name), **out)
+    return out
+
+
+def svirl_gpu(x):
+    from pycuda import gpuarray  # the shim's
+    return gpuarray.to_gpu(np.ascontiguousarray(x))
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SVIRL_REFERENCE", "/root/reference")
+    for p in (os.path.join(ROOT, "oracle", "fake_pycuda"), ref):
+        sys.path.insert(0, p)
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        import svirl
+        for name, spec in CASES.items():
+            make_case(svirl, name, spec)
+            print("wrote case_%s.npz" % name)
+
+
+if __name__ == "__main__":
+    main()

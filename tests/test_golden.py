@@ -1,0 +1,59 @@
+"""The oracle against the committed golden fixtures (tests/golden/, made by
+tests/golden/make_golden.py from the reference's own host code on the NumPy
+pycuda shim): observables, gradients and line-search coefficients at the
+initial state, the TDGL state and Jacobi sweep counts, the CG energies and the
+vortex list.  Needs neither the reference sources nor a GPU."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import gl_oracle as O
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "case_*.npz")))
+
+
+def load(path):
+    z = np.load(path)
+    return {k: z[k] for k in z.files}
+
+
+def oracle_of(f):
+    mt = f["mt"] if f["mt"].size else None
+    abei = f["abei"] if f["abei"].size else None
+    return O.GLOracle(int(f["Nx"]), int(f["Ny"]), float(f["dx"]), float(f["dy"]), f["psi0"].copy(), f["ab0"].copy(),
+                      mt=mt, abei=abei, kappa=float(f["kappa"]), sigma=float(f["sigma"]), H=float(f["H"]),
+                      rand_t=int(f["seed"]))
+
+
+def rel(x, y):
+    return np.max(np.abs(np.asarray(x) - np.asarray(y))) / max(np.max(np.abs(np.asarray(y))), 1e-300)
+
+
+def test_fixtures_present():
+    assert len(GOLDEN) >= 3
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p))
+def test_oracle_reproduces_golden(path):
+    f = load(path)
+    orc = oracle_of(f)
+    assert abs(orc.free_energy() - f["F0"]) <= 1e-13 * abs(f["F0"])
+    assert rel(orc.magnetic_field(), f["B0"]) < 1e-12
+    assert rel(orc.current_density(), f["j0"]) < 1e-12
+    assert rel(orc.supercurrent_density(), f["js0"]) < 1e-12
+    assert rel(orc.jacobian_psi(), f["gpsi0"]) < 1e-12
+    if np.isfinite(f["kappa"]):
+        assert rel(orc.jacobian_A(), f["gA0"]) < 1e-12
+        assert rel(orc.coef(f["dpsi"], f["dab"]), f["coef"]) < 1e-12
+    else:
+        assert rel(orc.coef_psi(f["dpsi"]), f["coef"]) < 1e-12
+    orc.td(dt=0.1, Nt=int(f["td_steps"]))
+    assert rel(orc.psi, f["psi_td"]) < 1e-13 and rel(orc.ab, f["ab_td"]) < 1e-13
+    assert list(orc.sweeps_psi) == list(f["sweeps_psi"])
+    orc.cg(n_iter=int(f["cg_iters"]))
+    tol = 1e-13 if np.isinf(f["kappa"]) else 1e-8
+    assert rel(orc.cg_energies, f["cg_energies"]) < tol
+    vx, vy, vv = O.detect_vortices(orc.g, f["psi_cg"], f["ab_cg"], float(f["H"]))
+    assert np.array_equal(vx, f["vx"]) and np.array_equal(vy, f["vy"]) and np.array_equal(vv, f["vv"])
