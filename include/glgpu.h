@@ -178,11 +178,17 @@ int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable);
  * with GLGPU_CG_GTOL_ABS: |grad F| <= gtol, tested before the first update too).
  * Per-instance outputs (each may be NULL): iterations done, final energy,
  * final |grad F| relative to the first, status (1 gradient stop, 2 energy stop,
- * 3 n_iter reached, -1 no descent step; then GLGPU_E_NOROOT is returned).
+ * 3 n_iter reached, 4 energy target reached, -1 no descent step; then
+ * GLGPU_E_NOROOT is returned).
  * flags: GLGPU_CG_EXACT_BOUNDARY makes dF/dA the exact derivative of the free
  * energy on the boundary links too; the reference's formula (cg.h:174-300)
  * doubles the H and A terms there, so its gradient does not vanish at the
  * energy minimum and the gradient-norm stop cannot be met at finite kappa. */
+/* Energy targets for the next glgpu_batch_cg calls: instance q also stops (status
+ * 4) once its energy E <= targets[q] + rel_tol |targets[q]| (a NaN target: no
+ * such stop; targets = NULL clears them).  Measures the iterations a start needs
+ * to reach a known minimum energy. */
+int glgpu_batch_set_energy_targets(glgpu_batch* b, const double* targets, double rel_tol);
 #define GLGPU_CG_EXACT_BOUNDARY 1
 #define GLGPU_CG_GTOL_ABS 2
 int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t flags, int32_t* iters,

@@ -33,6 +33,14 @@ extern "C" {
 int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
                      void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, void* stream);
 
+/* The same forward convolution on the 5th-generation tensor cores (tcgen05.mma,
+ * FP32 accumulator in tensor memory, 128 x 64 output tile per CTA).  *err
+ * (device int) is set to 1 if a CTA's wait for its MMAs timed out (its outputs
+ * are then not written). */
+int glnn_conv3x3_fwd_tc(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
+                        void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, int32_t* err,
+                        void* stream);
+
 /* [dx1|dx2] = conv3x3^T(dy * relu'(y), Wt).  y may be NULL when relu = 0. */
 int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const void* wt, void* dx1, int32_t c1,
                           void* dx2, int32_t c2, int32_t n, int32_t h, int32_t w, int32_t cout, void* stream);

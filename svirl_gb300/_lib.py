@@ -81,11 +81,14 @@ _SIGNATURES = {
     "glgpu_batch_last_error": (C.c_char_p, [_H]),
     "glgpu_batch_td": (C.c_int, [_H, C.c_double, C.c_int32, C.c_int32, C.POINTER(TDStats), C.POINTER(C.c_double)]),
     "glgpu_batch_set_use_graphs": (C.c_int, [_H, C.c_int32]),
+    "glgpu_batch_set_energy_targets": (C.c_int, [_H, _P, C.c_double]),
     "glgpu_batch_cg": (C.c_int, [_H, C.c_int32, C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     # learned warm start (include/glgpu_nn.h)
     "glnn_conv3x3_fwd": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32,
                                    C.c_int32, C.c_int32, _P]),
+    "glnn_conv3x3_fwd_tc": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32,
+                                      C.c_int32, C.c_int32, _P, _P]),
     "glnn_conv3x3_bwd_data": (C.c_int, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32,
                                         C.c_int32, C.c_int32, _P]),
     "glnn_conv3x3_bwd_weight_work": (C.c_int64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),

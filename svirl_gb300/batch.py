@@ -80,6 +80,17 @@ class HandleBatch:
         self.last_stats = st
         return (st, ms.value) if timed else st
 
+    def set_energy_targets(self, targets, rel_tol=1e-6):
+        """Per-instance energy targets for the next device CG calls (None clears):
+        an instance also stops, with status 4, once E <= target + rel_tol |target|."""
+        if targets is None:
+            self._check(self.lib.glgpu_batch_set_energy_targets(self.b, None, 0.0), "set_energy_targets")
+            return
+        t = np.ascontiguousarray(targets, dtype=np.float64)
+        assert t.size == len(self.handles)
+        self._check(self.lib.glgpu_batch_set_energy_targets(self.b, t.ctypes.data_as(C.c_void_p), float(rel_tol)),
+                    "set_energy_targets")
+
     def cg_device(self, n_iter=1000, rtol=1e-6, gtol=0.0, exact_boundary=False, gtol_abs=False, timed=False):
         """``glgpu_batch_cg``; returns per-instance arrays (see ``GLBatch.cg``)."""
         n = len(self.handles)

@@ -1,6 +1,6 @@
 """Build libglgpu.so (sm_103a) in-tree: svirl_gb300/_build/libglgpu.so.
 
-Six translation units compiled in parallel by nvcc, then linked with the
+Seven translation units compiled in parallel by nvcc, then linked with the
 shared CUDA runtime.  ``python -m svirl_gb300.build`` or ``build()``.
 """
 import concurrent.futures as cf
@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libglgpu.so")
-SOURCES = ["api.cu", "td.cu", "obs.cu", "cg.cu", "cgb.cu", "nn.cu"]
+SOURCES = ["api.cu", "td.cu", "obs.cu", "cg.cu", "cgb.cu", "nn.cu", "nn_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
                      "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]

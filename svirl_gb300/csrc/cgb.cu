@@ -402,6 +402,10 @@ kb_inst_stop(const Inst* __restrict__ insts, int ninst, const double* __restrict
             cs->done = 1;
             cs->status = 2;
             atomicSub(&loop->active, 1);
+        } else if (I.cg_target == I.cg_target && E <= I.cg_target + I.cg_target_tol * fabs(I.cg_target)) {
+            cs->done = 1;
+            cs->status = 4;
+            atomicSub(&loop->active, 1);
         } else if (cs->iter >= loop->n_iter) {
             cs->done = 1;
             cs->status = 3;
@@ -595,6 +599,17 @@ fail:
 }
 #undef GCHK
 
+int batch_set_energy_targets(glgpu_batch* b, const double* targets, double rel_tol) {
+    if (!targets) {
+        b->cg_targets.clear();
+        return GLGPU_OK;
+    }
+    if (!(rel_tol >= 0.0)) return batch_error(b, GLGPU_E_ARG, "batch_set_energy_targets: rel_tol < 0");
+    b->cg_targets.assign(targets, targets + b->ninst);
+    b->cg_target_tol = rel_tol;
+    return GLGPU_OK;
+}
+
 int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, int32_t* iters, double* energies, double* grad_rel,
              int32_t* status, double* elapsed_ms) {
     if (n_iter < 0 || !(rtol >= 0.0) || !(gtol >= 0.0)) return batch_error(b, GLGPU_E_ARG, "batch_cg: bad n_iter, rtol or gtol");
@@ -608,6 +623,8 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
         insts[q] = h->inst_h;
         insts[q].tile0 = tile0;  // the batch's tile table lists the instances' tiles in order
         insts[q].cg_exact = (flags & GLGPU_CG_EXACT_BOUNDARY) ? 1 : 0;
+        insts[q].cg_target = b->cg_targets.empty() ? NAN : b->cg_targets[q];
+        insts[q].cg_target_tol = b->cg_target_tol;
         tile0 += h->ntiles;
     }
     if (!b->cg_partials && cudaMalloc(&b->cg_partials, sizeof(double) * kPart * (size_t)b->ntiles) != cudaSuccess)

@@ -84,6 +84,8 @@ struct Inst {
     int nitems;               // number of warp-strip items of this instance
     int solveA;               // finite kappa
     int cg_exact;             // batched device CG: exact dF/dA on boundary links
+    double cg_target;         // batched device CG: stop once E <= cg_target + cg_target_tol |cg_target| (NaN: off)
+    double cg_target_tol;
 };
 
 // Global state of one batched Jacobi/time loop.
@@ -188,6 +190,8 @@ struct glgpu_batch {
     void* cg_loop = nullptr;             // CGLoop
     cudaGraphExec_t cg_exec = nullptr;
     bool cg_graph_failed = false;
+    std::vector<double> cg_targets;      // per-instance energy targets (empty: none)
+    double cg_target_tol = 0.0;
     std::string last_error;
 };
 
@@ -222,6 +226,7 @@ int cg_update(glgpu_handle* h, double alpha_psi, double alpha_A, double* energy_
 int cg_read_gradient(glgpu_handle* h, void* gpsi_host, void* gA_host);
 int cg_coef_for(glgpu_handle* h, const void* dpsi_host, const void* dab_host, double* c_out);
 // cgb.cu
+int batch_set_energy_targets(glgpu_batch* b, const double* targets, double rel_tol);
 int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, int32_t* iters, double* energies, double* grad_rel,
              int32_t* status, double* elapsed_ms);
 // td.cu graph helpers

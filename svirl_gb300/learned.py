@@ -446,3 +446,35 @@ def train(net, x, y, epochs=5, batch=32, lr=1e-3, seed=0, log=None):
         if log:
             log("epoch %d loss %.5f" % (ep, hist[-1]))
     return hist
+
+
+def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=1e-7, tol=1e-6, cache=None):
+    """CG iterations and device time to reach F* within `tol` from the random start
+    and from the network's prediction; F* = the energy of a tight relaxation from
+    the random start (gradient norm `gtol`).  A prediction counts only where its
+    CG reaches that energy (status 4)."""
+    import time as _time
+    from .relax import HandleCache, relax
+    own = cache is None
+    cache = HandleCache() if own else cache
+    try:
+        ref, _, _ = relax(insts, cache, dtype, n_iter=n_iter, gtol=gtol, fetch=False)
+        Estar = ref["energy"]
+        r, _, _ = relax(insts, cache, dtype, n_iter=n_iter, gtol=0.0, fetch=False, targets=Estar, target_tol=tol)
+        torch.cuda.synchronize()
+        t0 = _time.perf_counter()
+        pred = net.predict(features(insts))
+        torch.cuda.synchronize()
+        t_net = _time.perf_counter() - t0
+        starts = decode(insts, pred, mode=mode)
+        w, _, _ = relax(insts, cache, dtype, starts=starts, n_iter=n_iter, gtol=0.0, fetch=False, targets=Estar,
+                        target_tol=tol)
+    finally:
+        if own:
+            cache.close()
+    ok_r, ok_w = r["status"] == 4, w["status"] == 4
+    return {"n": len(insts), "size": insts[0].n, "reached_random": int(ok_r.sum()), "reached_warm": int(ok_w.sum()),
+            "iters_random_median": float(np.median(r["iters"])), "iters_warm_median": float(np.median(w["iters"])),
+            "iters_random_mean": float(r["iters"].mean()), "iters_warm_mean": float(w["iters"].mean()),
+            "cg_ms_random": r["ms"], "cg_ms_warm": w["ms"], "net_ms": 1e3 * t_net,
+            "warm_lower_energy": int((w["energy"] < Estar - tol * np.abs(Estar)).sum())}

@@ -14,6 +14,13 @@ from tests._pairs import flat, gpu_state, rel_err
 
 pytestmark = pytest.mark.gpu
 
+
+def near(x, y, tol, floor):
+    """max|x - y| <= tol * max(max|y|, floor): fields that vanish in a case (the
+    current of the symmetric-gauge start) are rounding noise in both codes."""
+    x, y = np.asarray(x), np.asarray(y)
+    return np.max(np.abs(x - y)) <= tol * max(np.max(np.abs(y)), floor)
+
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "case_*.npz")))
 
 
@@ -44,11 +51,11 @@ def test_gpu_reproduces_golden(path):
     f = {k: z[k] for k in z.files}
     gl = solver_of(f)
     assert abs(gl.observables.free_energy - f["F0"]) <= 1e-12 * abs(f["F0"])
-    assert rel_err(flat(gl.observables.magnetic_field), f["B0"]) < 1e-12
+    assert near(flat(gl.observables.magnetic_field), f["B0"], 1e-12, float(f["H"]))
     jx, jy = gl.observables.current_density
-    assert rel_err(np.concatenate([flat(jx), flat(jy)]), f["j0"]) < 1e-12
+    assert near(np.concatenate([flat(jx), flat(jy)]), f["j0"], 1e-12, 1.0)
     sx, sy = gl.observables.supercurrent_density
-    assert rel_err(np.concatenate([flat(sx), flat(sy)]), f["js0"]) < 1e-12
+    assert near(np.concatenate([flat(sx), flat(sy)]), f["js0"], 1e-12, 1.0)
     gl.solve._init_cg()
     assert rel_err(gl.solve._cg._free_energy_jacobian_psi.get(), f["gpsi0"]) < 1e-12
     if np.isfinite(f["kappa"]):
