@@ -328,6 +328,89 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c1(args):
+    """The plain small configuration: 129x129 (Lx = Ly = 64, dx = dy = 0.5), FP64,
+    kappa = 5, sigma = 200, H = 0.1, A in the Landau gauge, full domain, seeded
+    random psi; td(dt=0.1, Nt=1000) then cg(n_iter=1000) through GLSolver (the
+    reference's API and decisions); the oracle times the same TD on one core."""
+    from svirl_gb300 import GLSolver
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    gl = GLSolver(dx=0.5, dy=0.5, Lx=64, Ly=64, order_parameter="random", random_seed=0, gl_parameter=5.0,
+                  normal_conductivity=200.0, homogeneous_external_field=0.1, dtype=np.float64)
+    ya = gl.mesh.xy_a_grid[1]
+    gl.vars.vector_potential = (-0.1 * ya, np.zeros((129, 128)))
+    gl.solve.td(dt=0.1, Nt=5)  # warm-up: graph build
+    st, ms = gl._h.td_timed(0.1, args.steps, 0)
+    t0 = time.perf_counter()
+    gl.solve.cg(n_iter=1000)
+    t_cg = time.perf_counter() - t0
+    n_cg = len(gl.solve._cg.cg_energies)
+    N = 129 * 129
+    value = N * args.steps / (ms * 1e-3)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import gl_oracle as O
+        psi, ab = gl._h.get_psi().astype(np.complex128), gl._h.get_ab().astype(np.float64)
+        orc = O.GLOracle(129, 129, 0.5, 0.5, psi, ab, kappa=5.0, sigma=200.0, H=0.1)
+        t1 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t1 < 20.0:
+            orc.td(dt=0.1, Nt=1)
+            k += 1
+        tc = time.perf_counter() - t1
+        cpu = {"value": N * k / tc, "unit": "node-steps/s", "cores": 1, "kind": "port",
+               "sample": "oracle (NumPy FP64, 1 thread), %d TD steps of the same 129x129 state" % k}
+    line = {"metric": "TDGL node-steps/s (129x129, kappa=5, FP64) and CG wall time", "value": value,
+            "unit": "node-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": 5, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "plain_small_129", "kappa": 5.0, "sigma": 200.0, "H": 0.1, "gauge": "Landau",
+                       "mean_sweeps_psi": st.total_sweeps_psi / args.steps,
+                       "mean_sweeps_A": st.total_sweeps_A / args.steps},
+            "cg": {"iterations": n_cg, "wall_s": t_cg, "ms_per_iteration": 1e3 * t_cg / max(n_cg, 1),
+                   "how": "GLSolver.solve.cg(n_iter=1000): GPU phases, step length on the host (reference decisions)"},
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
+def run_learned(args):
+    """Learned CG warm start: relaxed 128^2 states generated by the batched device CG
+    (kappa ~ U[2, 10], H ~ U[0.02, 0.5], hole masks), the network trained on them by
+    the library's BF16 kernels, then CG iterations and time to F* within 1e-6 from the
+    random start and from the prediction, on held-out instances at 128^2 and 256^2."""
+    import torch
+    from svirl_gb300 import learned as L
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    t0 = time.perf_counter()
+    x, y, _ = L.generate(args.train_states, n=128, seed=0, pool_size=256, n_iter=3000, gtol=1e-4)
+    t_gen = time.perf_counter() - t0
+    net = L.WarmStartNet(seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = L.train(net, x, y, epochs=args.epochs, batch=32, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    steps = args.epochs * (x.shape[0] // 32)
+    del x, y
+    evals = {}
+    for n, count in ((128, 64), (256, 24)):
+        rng = np.random.default_rng(777 + n)
+        evals["%d" % n] = L.evaluate(net, [L.Instance.sample(n, rng) for _ in range(count)])
+    e = evals["128"]
+    value = e["iters_random_median"] / max(e["iters_warm_median"], 1.0)
+    line = {"metric": "CG iterations to dF/F<=1e-6: random start / learned warm start (median, 128^2)",
+            "value": value, "unit": "x", "n_gpus": 1, "steps": steps, "warmup": 0,
+            "ms_per_step": 1e3 * t_train / max(steps, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 net (f32 accumulate), f64 CG", "data": "synthetic (solver-generated)",
+            "config": {"workload": "learned_warm_start", "train_states": args.train_states, "epochs": args.epochs,
+                       "params": net.n_params(), "levels": list(L.LEVELS), "target_mode": "amplitude",
+                       "train_loss_first_last": [hist[0], hist[-1]], "gen_s": t_gen, "train_s": t_train},
+            "eval": evals}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -339,9 +422,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graphs", action="store_true",
                     help="host-driven Jacobi loop (same kernels); ncu cannot profile kernels inside conditional graphs")
-    ap.add_argument("--workload", choices=["tdgl", "states", "serve"], default="tdgl",
+    ap.add_argument("--workload", choices=["tdgl", "states", "serve", "learned", "c1"], default="tdgl",
                     help="tdgl: node-steps/s on the 2049^2 domain; states: relaxed states/s of a batched sweep; "
-                         "serve: the serving loop")
+                         "serve: the serving loop; learned: the learned CG warm start")
+    ap.add_argument("--train-states", type=int, default=2048)
+    ap.add_argument("--epochs", type=int, default=10)
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--instances", type=int, default=64)
@@ -358,6 +443,12 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "learned":
+        run_learned(args)
+        return
+    if args.workload == "c1":
+        run_c1(args)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

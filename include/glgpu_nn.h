@@ -10,7 +10,8 @@
  *    W[cout][3][3][cin]; the kernels read bfloat16 copies made by
  *    glnn_prep_weights (Wb: same layout, Wt: [3][3][cin][cout]).  Weight and
  *    bias gradients, optimiser state: float32.  Products are accumulated in
- *    float32 (tensor cores, mma bf16 -> f32).
+ *    float32 on the tensor cores (tcgen05 for the forward pass and the data
+ *    gradient, mma for the weight gradient).
  *  - "Same" padding (zeros), stride 1.  A convolution may read the channel
  *    concatenation [x1 | x2] of two tensors (x2 may be NULL with c2 = 0), so the
  *    decoder's skip connections need no copy; the data gradient is written split
@@ -29,21 +30,18 @@
 extern "C" {
 #endif
 
-/* y = conv3x3([x1|x2], Wb) + b (+ ReLU).  y: n*h*w*cout. */
+/* y = conv3x3([x1|x2], Wb) + b (+ ReLU).  y: n*h*w*cout.  Runs on the
+ * 5th-generation tensor cores (tcgen05.mma, FP32 accumulator in tensor memory,
+ * 128 x 64 output tile per CTA).  *err (a device int) is set to 1 if a CTA's
+ * bounded wait for its MMAs ran out (that CTA's outputs are then not written). */
 int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
-                     void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, void* stream);
+                     void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, int32_t* err, void* stream);
 
-/* The same forward convolution on the 5th-generation tensor cores (tcgen05.mma,
- * FP32 accumulator in tensor memory, 128 x 64 output tile per CTA).  *err
- * (device int) is set to 1 if a CTA's wait for its MMAs timed out (its outputs
- * are then not written). */
-int glnn_conv3x3_fwd_tc(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
-                        void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, int32_t* err,
-                        void* stream);
-
-/* [dx1|dx2] = conv3x3^T(dy * relu'(y), Wt).  y may be NULL when relu = 0. */
+/* [dx1|dx2] = conv3x3^T(dy * relu'(y), Wt), on tcgen05 like the forward.  y may be
+ * NULL when relu = 0. */
 int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const void* wt, void* dx1, int32_t c1,
-                          void* dx2, int32_t c2, int32_t n, int32_t h, int32_t w, int32_t cout, void* stream);
+                          void* dx2, int32_t c2, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t* err,
+                          void* stream);
 
 /* dW[cout][9*cin] and db[cout] (float32, overwritten) from dy * relu'(y) and
  * the input [x1|x2].  work: float32 scratch of glnn_conv3x3_bwd_weight_work()

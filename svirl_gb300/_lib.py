@@ -86,11 +86,9 @@ _SIGNATURES = {
                                  C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     # learned warm start (include/glgpu_nn.h)
     "glnn_conv3x3_fwd": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32,
-                                   C.c_int32, C.c_int32, _P]),
-    "glnn_conv3x3_fwd_tc": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_int32, _P, _P]),
     "glnn_conv3x3_bwd_data": (C.c_int, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32,
-                                        C.c_int32, C.c_int32, _P]),
+                                        C.c_int32, C.c_int32, _P, _P]),
     "glnn_conv3x3_bwd_weight_work": (C.c_int64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "glnn_conv3x3_bwd_weight": (C.c_int, [_P, _P, C.c_int32, _P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int64,
                                           C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),

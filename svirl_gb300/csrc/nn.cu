@@ -1,17 +1,15 @@
-// Kernels of the learned CG warm start: 3x3 convolutions (forward, data and
-// weight gradients) as implicit GEMMs on the tensor cores (mma bf16 -> f32),
-// pooling/upsampling, a weighted squared-error loss and Adam.  No counterpart in
+// Kernels of the learned CG warm start: the weight gradient of the 3x3
+// convolution as an implicit GEMM on the tensor cores (mma bf16 -> f32),
+// pooling/upsampling, a weighted squared-error loss and Adam.  The forward
+// convolution and its data gradient run on tcgen05 (nn_tc.cu).  No counterpart in
 // the reference (its only minimiser is the CG of svirl/solvers/cg.py).
 //
-// GEMM tiling: a CTA of 4 warps computes a 64 x 64 tile of the output, each
-// warp 32 x 32 (2 x 4 mma.m16n8k16), over K chunks of 32 staged in shared memory
-// (register prefetch of the next chunk while the current one is multiplied).
-// Operands are gathered on the fly (im2col-free):
-//   forward     M = pixels, N = cout, K = 9 cin   A = x shifted by the tap, B = Wb
-//   data grad   M = pixels, N = cin,  K = 9 cout  A = dy shifted back,       B = Wt
-//   weight grad M = cout,   N = 9 cin, K = pixels A = dy^T, B = x shifted (split-K,
-//               partial sums reduced in a fixed order)
-// The ReLU derivative of the layer is applied to dy while it is gathered.
+// Weight gradient: M = cout, N = 9 cin, K = pixels; A = dy^T (with the layer's
+// ReLU derivative applied while gathering), B = the input shifted by the tap.
+// A CTA of 4 warps computes a 64 x 64 tile, each warp 32 x 32 (2 x 4
+// mma.m16n8k16), over K chunks of 32 staged in shared memory with register
+// prefetch of the next chunk; the pixel range is split over CTAs (split-K) and
+// the partial sums are reduced in a fixed order (deterministic).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -119,158 +117,6 @@ __device__ __forceinline__ uint4 load_cat8(const bf16* x1, int C1, const bf16* x
                                            int H, int W, int ci) {
     const size_t q = ((size_t)n * H + sy) * W + sx;
     return ci < C1 ? *(const uint4*)(x1 + q * C1 + ci) : *(const uint4*)(x2 + q * C2 + (ci - C1));
-}
-
-// ---------------------------------------------------------------------------
-// forward
-// ---------------------------------------------------------------------------
-template <int RELU>
-__global__ void __launch_bounds__(NT)
-k_conv_fwd(const bf16* __restrict__ x1, int C1, const bf16* __restrict__ x2, int C2, const bf16* __restrict__ Wb,
-           const float* __restrict__ bias, bf16* __restrict__ y, int NB, int H, int W, int Cout) {
-    __shared__ __align__(16) bf16 As[BM * SP];
-    __shared__ __align__(16) bf16 Bs[BN * SP];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, wm = warp >> 1, wn = warp & 1;
-    const int Cin = C1 + C2, K = 9 * Cin, P = NB * H * W;
-    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-    Pix px[2];
-#pragma unroll
-    for (int i = 0; i < 2; ++i) px[i] = pix_of(m0 + ((tid + i * NT) >> 2), P, H, W);
-    uint4 ra[2], rb[2];
-    const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
-    auto load = [&](int kc) {
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            const int v = tid + i * NT, r = v >> 2, k = kc + (v & 3) * 8;
-            uint4 a = z4;
-            if (px[i].ok && k < K) {
-                const int tap = k / Cin, ci = k - tap * Cin;
-                const int sy = px[i].y + tap / 3 - 1, sx = px[i].x + tap % 3 - 1;
-                if (sy >= 0 && sy < H && sx >= 0 && sx < W) a = load_cat8(x1, C1, x2, C2, px[i].n, sy, sx, H, W, ci);
-            }
-            ra[i] = a;
-            const int co = n0 + r;
-            rb[i] = (co < Cout && k < K) ? *(const uint4*)(Wb + (size_t)co * K + k) : z4;
-        }
-    };
-    float acc[2][4][4];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
-    const int nk = (K + BK - 1) / BK;
-    load(0);
-    for (int kt = 0; kt < nk; ++kt) {
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            const int v = tid + i * NT;
-            *(uint4*)(As + (v >> 2) * SP + (v & 3) * 8) = ra[i];
-            *(uint4*)(Bs + (v >> 2) * SP + (v & 3) * 8) = rb[i];
-        }
-        __syncthreads();
-        if (kt + 1 < nk) load((kt + 1) * BK);
-        mma_chunk<false, false>(As, Bs, acc, wm, wn, lane);
-        __syncthreads();
-    }
-    const int g = lane >> 2, c4 = lane & 3;
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-            for (int h2 = 0; h2 < 2; ++h2) {
-                const int p = m0 + wm * 32 + mt * 16 + g + 8 * h2;
-                const int col = n0 + wn * 32 + nt * 8 + 2 * c4;
-                if (p < P && col < Cout) {
-                    float v0 = acc[mt][nt][2 * h2] + bias[col], v1 = acc[mt][nt][2 * h2 + 1] + bias[col + 1];
-                    if (RELU) {
-                        v0 = fmaxf(v0, 0.f);
-                        v1 = fmaxf(v1, 0.f);
-                    }
-                    *(__nv_bfloat162*)(y + (size_t)p * Cout + col) = __floats2bfloat162_rn(v0, v1);
-                }
-            }
-}
-
-// ---------------------------------------------------------------------------
-// data gradient: dx[q][ci] = sum_{tap, co} dy'[q - off(tap)][co] W[co][tap][ci]
-// ---------------------------------------------------------------------------
-template <int RELU>
-__global__ void __launch_bounds__(NT)
-k_conv_bwd_data(const bf16* __restrict__ dy, const bf16* __restrict__ yv, const bf16* __restrict__ Wt,
-                bf16* __restrict__ dx1, int C1, bf16* __restrict__ dx2, int C2, int NB, int H, int W, int Cout) {
-    __shared__ __align__(16) bf16 As[BM * SP];
-    __shared__ __align__(16) bf16 Bs[BN * SP];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, wm = warp >> 1, wn = warp & 1;
-    const int Cin = C1 + C2, K = 9 * Cout, P = NB * H * W;
-    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-    Pix px[2];
-#pragma unroll
-    for (int i = 0; i < 2; ++i) px[i] = pix_of(m0 + ((tid + i * NT) >> 2), P, H, W);
-    uint4 ra[2], rb[2];
-    const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
-    auto load = [&](int kc) {
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            const int v = tid + i * NT, r = v >> 2, k = kc + (v & 3) * 8;
-            uint4 a = z4;
-            if (px[i].ok && k < K) {
-                const int tap = k / Cout, co = k - tap * Cout;
-                const int sy = px[i].y - (tap / 3 - 1), sx = px[i].x - (tap % 3 - 1);
-                if (sy >= 0 && sy < H && sx >= 0 && sx < W) {
-                    const size_t q = (((size_t)px[i].n * H + sy) * W + sx) * Cout + co;
-                    a = *(const uint4*)(dy + q);
-                    if (RELU) a = relu_mask8(a, *(const uint4*)(yv + q));
-                }
-            }
-            ra[i] = a;
-            const int ci = n0 + r;
-            uint4 b = z4;
-            if (ci < Cin && k < K) {
-                const int tap = k / Cout, co = k - tap * Cout;
-                b = *(const uint4*)(Wt + ((size_t)tap * Cin + ci) * Cout + co);
-            }
-            rb[i] = b;
-        }
-    };
-    float acc[2][4][4];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
-    const int nk = (K + BK - 1) / BK;
-    load(0);
-    for (int kt = 0; kt < nk; ++kt) {
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            const int v = tid + i * NT;
-            *(uint4*)(As + (v >> 2) * SP + (v & 3) * 8) = ra[i];
-            *(uint4*)(Bs + (v >> 2) * SP + (v & 3) * 8) = rb[i];
-        }
-        __syncthreads();
-        if (kt + 1 < nk) load((kt + 1) * BK);
-        mma_chunk<false, false>(As, Bs, acc, wm, wn, lane);
-        __syncthreads();
-    }
-    const int g = lane >> 2, c4 = lane & 3;
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-            for (int h2 = 0; h2 < 2; ++h2) {
-                const int p = m0 + wm * 32 + mt * 16 + g + 8 * h2;
-                const int ci = n0 + wn * 32 + nt * 8 + 2 * c4;
-                if (p < P && ci < Cin) {
-                    const __nv_bfloat162 v = __floats2bfloat162_rn(acc[mt][nt][2 * h2], acc[mt][nt][2 * h2 + 1]);
-                    if (ci < C1) *(__nv_bfloat162*)(dx1 + (size_t)p * C1 + ci) = v;
-                    else *(__nv_bfloat162*)(dx2 + (size_t)p * C2 + (ci - C1)) = v;
-                }
-            }
 }
 
 // ---------------------------------------------------------------------------
@@ -614,35 +460,6 @@ static WPlan wplan(int n, int h, int w, int cin, int cout) {
 using namespace glnn;
 
 extern "C" {
-
-int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
-                     void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, void* stream) {
-    if (!x1 || !wb || !bias || !y || (c2 > 0 && !x2) || !conv_shape_ok(c1, c2, n, h, w, cout)) return GLGPU_E_ARG;
-    if (!aligned16(x1) || (x2 && !aligned16(x2)) || !aligned16(wb) || !aligned16(y)) return GLGPU_E_ARG;
-    const long long P = (long long)n * h * w;
-    dim3 grid((unsigned)((P + BM - 1) / BM), (unsigned)((cout + BN - 1) / BN));
-    cudaStream_t s = (cudaStream_t)stream;
-    if (relu)
-        k_conv_fwd<1><<<grid, NT, 0, s>>>((const bf16*)x1, c1, (const bf16*)x2, c2, (const bf16*)wb, bias, (bf16*)y, n, h, w, cout);
-    else
-        k_conv_fwd<0><<<grid, NT, 0, s>>>((const bf16*)x1, c1, (const bf16*)x2, c2, (const bf16*)wb, bias, (bf16*)y, n, h, w, cout);
-    return ret(cudaGetLastError());
-}
-
-int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const void* wt, void* dx1, int32_t c1,
-                          void* dx2, int32_t c2, int32_t n, int32_t h, int32_t w, int32_t cout, void* stream) {
-    if (!dy || !wt || !dx1 || (relu && !y) || (c2 > 0 && !dx2) || !conv_shape_ok(c1, c2, n, h, w, cout)) return GLGPU_E_ARG;
-    if (!aligned16(dy) || (y && !aligned16(y)) || !aligned16(wt) || !aligned16(dx1) || (dx2 && !aligned16(dx2)))
-        return GLGPU_E_ARG;
-    const long long P = (long long)n * h * w;
-    dim3 grid((unsigned)((P + BM - 1) / BM), (unsigned)((c1 + c2 + BN - 1) / BN));
-    cudaStream_t s = (cudaStream_t)stream;
-    if (relu)
-        k_conv_bwd_data<1><<<grid, NT, 0, s>>>((const bf16*)dy, (const bf16*)y, (const bf16*)wt, (bf16*)dx1, c1, (bf16*)dx2, c2, n, h, w, cout);
-    else
-        k_conv_bwd_data<0><<<grid, NT, 0, s>>>((const bf16*)dy, (const bf16*)y, (const bf16*)wt, (bf16*)dx1, c1, (bf16*)dx2, c2, n, h, w, cout);
-    return ret(cudaGetLastError());
-}
 
 int64_t glnn_conv3x3_bwd_weight_work(int32_t n, int32_t h, int32_t w, int32_t cin, int32_t cout) {
     if (n <= 0 || h <= 0 || w <= 0 || cin <= 0 || cout <= 0) return 0;

@@ -1,15 +1,17 @@
-// Forward 3x3 convolution of the learned warm start on the 5th-generation tensor
-// cores: tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in tensor
-// memory), one 128 x 64 output tile per CTA.  Per K chunk of 64 the four warps
-// gather the implicit-GEMM operands (pixels x [tap, cin] of the input, cout x
-// [tap, cin] of the weights) into shared memory in the K-major core-matrix
+// 3x3 convolutions of the learned warm start on the 5th-generation tensor cores:
+// tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in tensor memory), one
+// 128 x 64 output tile per CTA, for the forward pass (M = pixels, N = cout,
+// K = [tap, cin] of the input shifted by the tap) and the data gradient
+// (M = pixels, N = cin, K = [tap, cout] of dy shifted back, with the layer's
+// ReLU derivative applied while gathering).  Per K chunk of 64 the four warps
+// gather the implicit-GEMM operands into shared memory in the K-major core-matrix
 // layout (8 rows x 16 bytes per core matrix, no swizzle), one thread issues four
 // 128x64x16 MMAs and commits them to an mbarrier, and the CTA waits on it before
 // the next chunk overwrites the operands.  The epilogue reads the accumulator
 // with tcgen05.ld (each warp its 32 TMEM lanes = 32 output pixels), adds the
 // bias, applies the ReLU and stores bfloat16.  Every wait is bounded; on a
 // timeout the kernel records an error, skips its stores and still frees its
-// tensor memory.
+// tensor memory.  The weight gradient (K = pixels) is in nn.cu.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -78,17 +80,28 @@ __device__ __forceinline__ uint4 load_cat8(const bf16* x1, int C1, const bf16* x
     return ci < C1 ? *(const uint4*)(x1 + q * C1 + ci) : *(const uint4*)(x2 + q * C2 + (ci - C1));
 }
 
-template <int RELU>
+// dy * (y > 0) on packed bf16 values (y > 0: sign clear and not zero)
+__device__ __forceinline__ uint32_t relu_mask2(uint32_t d, uint32_t y) {
+    const uint32_t lo = ((y & 0xffffu) - 1u) < 0x7fffu ? 0x0000ffffu : 0u;
+    const uint32_t hi = ((y >> 16) - 1u) < 0x7fffu ? 0xffff0000u : 0u;
+    return d & (lo | hi);
+}
+
+// MODE 0 (forward): A = [x1 | x2] shifted by +tap, B = Wb[n][k], out = y (+ bias, ReLU).
+// MODE 1 (data gradient): A = dy * relu'(mask) shifted by -tap (a1 = dy, Ca1 = cout),
+// B = Wt[tap][n][c], out = [o1 | o2] (the input's two channel groups).
+template <int MODE, int RELU>
 __global__ void __launch_bounds__(NTH)
-k_conv_fwd_tc(const bf16* __restrict__ x1, int C1, const bf16* __restrict__ x2, int C2, const bf16* __restrict__ Wb,
-              const float* __restrict__ bias, bf16* __restrict__ y, int NB, int H, int W, int Cout, int* err) {
+k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int Ca2, const bf16* __restrict__ mask,
+          const bf16* __restrict__ Bsrc, const float* __restrict__ bias, bf16* __restrict__ o1, int Co1,
+          bf16* __restrict__ o2, int Co2, int NB, int H, int W, int* err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* As = smem;
     unsigned char* Bs = smem + A_BYTES;
     uint64_t* bar = (uint64_t*)(smem + A_BYTES + B_BYTES);
     uint32_t* tslot = (uint32_t*)(smem + A_BYTES + B_BYTES + 8);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int Cin = C1 + C2, K = 9 * Cin, P = NB * H * W;
+    const int Ca = Ca1 + Ca2, K = 9 * Ca, Nout = Co1 + Co2, P = NB * H * W;
     const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
 
     if (warp == 0) {
@@ -129,17 +142,33 @@ k_conv_fwd_tc(const bf16* __restrict__ x1, int C1, const bf16* __restrict__ x2, 
             const int v = tid + i * NTH, row = v >> 3, kv = v & 7, k = kc + kv * 8;
             uint4 a = z4;
             if (pok[i] && k < K) {
-                const int tap = k / Cin, ci = k - tap * Cin;
-                const int sy = py[i] + tap / 3 - 1, sx = px[i] + tap % 3 - 1;
-                if (sy >= 0 && sy < H && sx >= 0 && sx < W) a = load_cat8(x1, C1, x2, C2, pn[i], sy, sx, H, W, ci);
+                const int tap = k / Ca, c = k - tap * Ca;
+                const int dy = MODE == 0 ? tap / 3 - 1 : 1 - tap / 3, dx = MODE == 0 ? tap % 3 - 1 : 1 - tap % 3;
+                const int sy = py[i] + dy, sx = px[i] + dx;
+                if (sy >= 0 && sy < H && sx >= 0 && sx < W) {
+                    a = load_cat8(a1, Ca1, a2, Ca2, pn[i], sy, sx, H, W, c);
+                    if (MODE == 1 && RELU) {
+                        const uint4 m = *(const uint4*)(mask + (((size_t)pn[i] * H + sy) * W + sx) * Ca1 + c);
+                        a = make_uint4(relu_mask2(a.x, m.x), relu_mask2(a.y, m.y), relu_mask2(a.z, m.z),
+                                       relu_mask2(a.w, m.w));
+                    }
+                }
             }
             *(uint4*)(As + core_off(row, kv * 8, TK / 8)) = a;
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int v = tid + i * NTH, row = v >> 3, kv = v & 7, k = kc + kv * 8;
-            const int co = n0 + row;
-            const uint4 b = (co < Cout && k < K) ? *(const uint4*)(Wb + (size_t)co * K + k) : z4;
+            const int nn = n0 + row;
+            uint4 b = z4;
+            if (nn < Nout && k < K) {
+                if (MODE == 0) {
+                    b = *(const uint4*)(Bsrc + (size_t)nn * K + k);
+                } else {
+                    const int tap = k / Ca, c = k - tap * Ca;
+                    b = *(const uint4*)(Bsrc + ((size_t)tap * Nout + nn) * Ca + c);
+                }
+            }
             *(uint4*)(Bs + core_off(row, kv * 8, TK / 8)) = b;
         }
         // generic-proxy stores -> visible to the tensor core's (async-proxy) reads
@@ -182,13 +211,19 @@ k_conv_fwd_tc(const bf16* __restrict__ x1, int C1, const bf16* __restrict__ x2, 
 #pragma unroll
                 for (int q = 0; q < 16; q += 2) {
                     const int col = n0 + c + q;
-                    if (col < Cout) {
-                        float v0 = __uint_as_float(r[q]) + bias[col], v1 = __uint_as_float(r[q + 1]) + bias[col + 1];
-                        if (RELU) {
-                            v0 = fmaxf(v0, 0.f);
-                            v1 = fmaxf(v1, 0.f);
+                    if (col < Nout) {
+                        float v0 = __uint_as_float(r[q]), v1 = __uint_as_float(r[q + 1]);
+                        if (MODE == 0) {
+                            v0 += bias[col];
+                            v1 += bias[col + 1];
+                            if (RELU) {
+                                v0 = fmaxf(v0, 0.f);
+                                v1 = fmaxf(v1, 0.f);
+                            }
                         }
-                        *(__nv_bfloat162*)(y + (size_t)p * Cout + col) = __floats2bfloat162_rn(v0, v1);
+                        const __nv_bfloat162 v = __floats2bfloat162_rn(v0, v1);
+                        if (col < Co1) *(__nv_bfloat162*)(o1 + (size_t)p * Co1 + col) = v;
+                        else *(__nv_bfloat162*)(o2 + (size_t)p * Co2 + (col - Co1)) = v;
                     }
                 }
             }
@@ -208,24 +243,45 @@ k_conv_fwd_tc(const bf16* __restrict__ x1, int C1, const bf16* __restrict__ x2, 
 
 using namespace glnn_tc;
 
+static int conv_tc_args_ok(int c1, int c2, int n, int h, int w, int cout) {
+    return n > 0 && h > 0 && w > 0 && c1 > 0 && c1 % 8 == 0 && c2 >= 0 && c2 % 8 == 0 && cout > 0 && cout % 8 == 0 &&
+           (long long)n * h * w < (1LL << 31);
+}
+
 extern "C" {
 
-int glnn_conv3x3_fwd_tc(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
+int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
                         void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, int32_t* err,
                         void* stream) {
-    if (!x1 || !wb || !bias || !y || !err || (c2 > 0 && !x2)) return GLGPU_E_ARG;
-    if (n <= 0 || h <= 0 || w <= 0 || c1 <= 0 || c1 % 8 || c2 < 0 || c2 % 8 || cout <= 0 || cout % 8) return GLGPU_E_ARG;
-    if ((long long)n * h * w >= (1LL << 31)) return GLGPU_E_ARG;
+    if (!x1 || !wb || !bias || !y || !err || (c2 > 0 && !x2) || !conv_tc_args_ok(c1, c2, n, h, w, cout)) return GLGPU_E_ARG;
     if (((uintptr_t)x1 | (uintptr_t)x2 | (uintptr_t)wb | (uintptr_t)y) & 15u) return GLGPU_E_ARG;
     const long long P = (long long)n * h * w;
     dim3 grid((unsigned)((P + TM - 1) / TM), (unsigned)((cout + TN - 1) / TN));
     cudaStream_t s = (cudaStream_t)stream;
     if (relu)
-        k_conv_fwd_tc<1><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)x1, c1, (const bf16*)x2, c2, (const bf16*)wb, bias,
-                                                      (bf16*)y, n, h, w, cout, err);
+        k_conv_tc<0, 1><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)x1, c1, (const bf16*)x2, c2, nullptr, (const bf16*)wb,
+                                                     bias, (bf16*)y, cout, nullptr, 0, n, h, w, err);
     else
-        k_conv_fwd_tc<0><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)x1, c1, (const bf16*)x2, c2, (const bf16*)wb, bias,
-                                                      (bf16*)y, n, h, w, cout, err);
+        k_conv_tc<0, 0><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)x1, c1, (const bf16*)x2, c2, nullptr, (const bf16*)wb,
+                                                     bias, (bf16*)y, cout, nullptr, 0, n, h, w, err);
+    return cudaGetLastError() == cudaSuccess ? GLGPU_OK : GLGPU_E_CUDA;
+}
+
+int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const void* wt, void* dx1, int32_t c1,
+                             void* dx2, int32_t c2, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t* err,
+                             void* stream) {
+    if (!dy || !wt || !dx1 || !err || (relu && !y) || (c2 > 0 && !dx2) || !conv_tc_args_ok(c1, c2, n, h, w, cout))
+        return GLGPU_E_ARG;
+    if (((uintptr_t)dy | (uintptr_t)y | (uintptr_t)wt | (uintptr_t)dx1 | (uintptr_t)dx2) & 15u) return GLGPU_E_ARG;
+    const long long P = (long long)n * h * w;
+    dim3 grid((unsigned)((P + TM - 1) / TM), (unsigned)((c1 + c2 + TN - 1) / TN));
+    cudaStream_t s = (cudaStream_t)stream;
+    if (relu)
+        k_conv_tc<1, 1><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)dy, cout, nullptr, 0, (const bf16*)y, (const bf16*)wt,
+                                                     nullptr, (bf16*)dx1, c1, (bf16*)dx2, c2, n, h, w, err);
+    else
+        k_conv_tc<1, 0><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)dy, cout, nullptr, 0, nullptr, (const bf16*)wt,
+                                                     nullptr, (bf16*)dx1, c1, (bf16*)dx2, c2, n, h, w, err);
     return cudaGetLastError() == cudaSuccess ? GLGPU_OK : GLGPU_E_CUDA;
 }
 

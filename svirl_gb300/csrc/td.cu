@@ -189,20 +189,6 @@ __device__ __forceinline__ C2<T> psi_node(C2<T> p_left, C2<T> p_right, C2<T> p_p
     return out;
 }
 
-// Asynchronous global->shared copies (cp.async) of one element per lane; a copy
-// with valid = false writes zeros and reads nothing.
-template <int BYTES> __device__ __forceinline__ void cp_async(void* smem, const void* gmem, bool valid);
-template <> __device__ __forceinline__ void cp_async<8>(void* smem, const void* gmem, bool valid) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 8 : 0) : "memory");
-}
-template <> __device__ __forceinline__ void cp_async<16>(void* smem, const void* gmem, bool valid) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 16 : 0) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
 // Per-row inputs of the psi update besides psi itself, as loaded: the link
 // factors of the x link and the y link that start at the node, the right-hand
 // side, the linear coefficient and the link-weight code ...
@@ -241,10 +227,7 @@ template <typename T> struct PsiRow {
 #ifndef GLGPU_PSI_MIN_CTAS
 #define GLGPU_PSI_MIN_CTAS 1
 #endif
-// 0: register prefetch one row ahead; n > 1: cp.async ring of n rows per warp
-#ifndef GLGPU_PSI_ASYNC
-#define GLGPU_PSI_ASYNC 4
-#endif
+
 constexpr int kPsiThreads = GLGPU_PSI_THREADS, kPsiWarps = kPsiThreads / 32;
 template <typename T>
 __global__ void __launch_bounds__(kPsiThreads, GLGPU_PSI_MIN_CTAS)
@@ -252,13 +235,6 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             cudaGraphConditionalHandle cond, int use_cond) {
     constexpr int K = kFuse, RR = kStripRows, S = kStripRows + 2 * kFuse;
     const int lane = threadIdx.x & 31;
-#if GLGPU_PSI_ASYNC
-    // per-warp ring of kRing rows of (psi^(k), rhs, x link, y link), filled by
-    // cp.async kRing-1 steps ahead of use, so loads stay in flight without registers
-    constexpr int kRing = GLGPU_PSI_ASYNC;
-    __shared__ __align__(16) C2<T> ring[kPsiWarps][kRing][4][32];
-    C2<T>(*my)[4][32] = ring[threadIdx.x >> 5];
-#endif
     const int gw = blockIdx.x * kPsiWarps + (threadIdx.x >> 5), nw = gridDim.x * kPsiWarps;
     int cur_inst = -1, k = 0, count = 0, done = 1;
     T wmax[K];
@@ -348,56 +324,10 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             r.inv = (q.cd & 3u) ? psi_diag_inv<T>(r.rq, q.eps, q.cd, dt, idx2, idy2) : T(0);
             return r;
         };
-#if GLGPU_PSI_ASYNC
-        // step t uses psi^(k) of row j0-K+t and rhs/links of row j0-K+t-1
-        auto issue = [&](int t) {
-            C2<T>(*sl)[32] = my[t % kRing];
-            const int yp = j0 - K + t, ys = yp - 1;
-            const bool vp = in_x && yp >= 0 && yp < Ny;
-            const bool rs = ys >= 0 && ys < Ny;
-            const int ns = i + Nx * ys;
-            const bool va = in_x && rs && i < Nx - 1, vb = calc_lane && rs && ys < Ny - 1, vr = calc_lane && rs;
-            constexpr int B = (int)sizeof(C2<T>);
-            cp_async<B>(&sl[0][lane], vp ? (const void*)&cur[i + Nx * yp] : (const void*)cur, vp);
-            cp_async<B>(&sl[1][lane], vr ? (const void*)&rhs[ns] : (const void*)rhs, vr);
-            cp_async<B>(&sl[2][lane], va ? (const void*)&U[i + Nxa * ys] : (const void*)U, va);
-            cp_async<B>(&sl[3][lane], vb ? (const void*)&U[Na + ns] : (const void*)U, vb);
-        };
-        auto load_small = [&](int y, PsiSide<T>& q) {
-            const bool ldc = calc_lane && y >= 0 && y < Ny;
-            const int n = i + Nx * y;
-            q.cd = ldc ? (unsigned)__ldg(&code[n]) : 0u;
-            q.eps = (ldc && eps_sp) ? __ldg(&eps_sp[n]) : eps0;
-        };
-        __syncwarp();  // the ring's previous reads are done before it is refilled
-#pragma unroll
-        for (int t = 0; t < kRing - 1; ++t) {
-            if (t < S) issue(t);
-            cp_async_commit();
-        }
-        PsiSide<T> nx_s;
-        load_small(j0 - K - 1, nx_s);
-#else
         C2<T> nx_p = load_psi(j0 - K);
         PsiSide<T> nx_s = load_side(j0 - K - 1);
-#endif
 #pragma unroll
         for (int s = 0; s < S; ++s) {
-#if GLGPU_PSI_ASYNC
-            cp_async_wait<kRing - 2>();
-            const C2<T>(*sl)[32] = my[s % kRing];
-            C2<T> newrow = sl[0][lane];  // psi^(k) on row j0 - K + s
-            nx_s.rr = sl[1][lane];
-            nx_s.ua = sl[2][lane];
-            nx_s.ub = sl[3][lane];
-#pragma unroll
-            for (int m = K; m >= 1; --m) D[m] = D[m - 1];
-            D[0] = finish_side(nx_s, j0 - K + s - 1);
-            __syncwarp();
-            if (s + kRing - 1 < S) issue(s + kRing - 1);
-            cp_async_commit();
-            if (s + 1 < S) load_small(j0 - K + s, nx_s);
-#else
             C2<T> newrow = nx_p;  // psi^(k) on row j0 - K + s
 #pragma unroll
             for (int m = K; m >= 1; --m) D[m] = D[m - 1];
@@ -406,7 +336,6 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
                 nx_p = load_psi(j0 - K + s + 1);
                 nx_s = load_side(j0 - K + s);
             }
-#endif
 #pragma unroll
             for (int l = 1; l <= K; ++l) {
                 C2<T> out = z;

@@ -6,9 +6,11 @@ tolerances.  No counterpart in the reference (its only minimiser is the CG of
 svirl/solvers/cg.py).
 
 Compute: every convolution, pooling/upsampling, the loss and the optimiser step
-run in the hand-written kernels of ``include/glgpu_nn.h`` (BF16 tensor-core
-implicit GEMMs, FP32 accumulation); PyTorch supplies device tensors, the
-stream and the autograd bookkeeping (``torch.autograd.Function`` wrappers).
+run in the hand-written kernels of ``include/glgpu_nn.h`` (BF16 implicit GEMMs
+on the tensor cores with FP32 accumulation: tcgen05 with tensor memory for the
+forward pass and the data gradient, mma for the weight gradient); PyTorch
+supplies device tensors, the stream and the autograd bookkeeping
+(``torch.autograd.Function`` wrappers).
 
 Network: 4 resolution levels (32, 64, 128, 128 channels), two 3x3 convolutions
 with ReLU per level and per decoder stage, 2x2 average pooling, nearest 2x
@@ -53,6 +55,25 @@ def _ok(rc, what):
         raise _lib.GLGPUError("glnn error %d in %s" % (rc, what))
 
 
+_err = {}
+
+
+def _err_flag(device):
+    """Device int the tcgen05 convolutions set when a bounded wait runs out."""
+    key = str(device)
+    if key not in _err:
+        _err[key] = torch.zeros(1, dtype=torch.int32, device=device)
+    return _err[key]
+
+
+def check_kernel_errors():
+    """Raise if a tensor-core convolution reported a timed-out wait (one sync)."""
+    for t in _err.values():
+        if int(t.item()) != 0:
+            t.zero_()
+            raise _lib.GLGPUError("glnn: a tensor-core convolution timed out waiting for its MMAs")
+
+
 # ---------------------------------------------------------------------------
 # autograd wrappers of the kernels
 # ---------------------------------------------------------------------------
@@ -72,7 +93,7 @@ class Conv3x3(torch.autograd.Function):
         _ok(lib.glnn_prep_weights(_ptr(w), _ptr(wb), _ptr(wt), cout, c1 + c2, s), "prep_weights")
         y = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
         _ok(lib.glnn_conv3x3_fwd(_ptr(x1), c1, _ptr(x2), c2, _ptr(wb), _ptr(b), _ptr(y), n, h, wd, cout,
-                                 1 if relu else 0, s), "conv3x3_fwd")
+                                 1 if relu else 0, _ptr(_err_flag(x1.device)), s), "conv3x3_fwd")
         ctx.save_for_backward(x1, x2, wt, y)
         ctx.relu = bool(relu)
         return y
@@ -92,7 +113,7 @@ class Conv3x3(torch.autograd.Function):
             dx1 = torch.empty_like(x1)
             dx2 = None if x2 is None else torch.empty_like(x2)
             _ok(lib.glnn_conv3x3_bwd_data(_ptr(dy), _ptr(y), relu, _ptr(wt), _ptr(dx1), c1, _ptr(dx2), c2, n, h, wd,
-                                          cout, s), "conv3x3_bwd_data")
+                                          cout, _ptr(_err_flag(dy.device)), s), "conv3x3_bwd_data")
         dw = torch.empty((cout, 3, 3, c1 + c2), dtype=torch.float32, device=dy.device)
         db = torch.empty((cout,), dtype=torch.float32, device=dy.device)
         nwork = int(lib.glnn_conv3x3_bwd_weight_work(n, h, wd, c1 + c2, cout))
@@ -216,11 +237,14 @@ class WarmStartNet:
         self.step += 1
         adam_step(self.params, [g.contiguous() for g in grads], self.m, self.v, self.step, lr=lr,
                   weight_decay=weight_decay)
+        check_kernel_errors()
         return loss.detach()
 
     @torch.no_grad()
     def predict(self, x):
-        return self.forward(x)
+        y = self.forward(x)
+        check_kernel_errors()
+        return y
 
     def state_dict(self):
         return {name: (self.w[name].detach().cpu().numpy(), self.b[name].detach().cpu().numpy())

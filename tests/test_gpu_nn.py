@@ -125,35 +125,30 @@ def test_network_overfits_one_batch():
     assert 1.0e6 < L.WarmStartNet(seed=0).n_params() < 1.5e6
 
 
-@pytest.mark.parametrize("shape", [(2, 10, 12, 16, 8, 24), (1, 9, 7, 8, 0, 8), (3, 16, 16, 32, 32, 64),
-                                   (2, 32, 24, 64, 64, 128), (1, 8, 8, 256, 0, 72)])
+@pytest.mark.parametrize("shape", [(2, 32, 24, 64, 64, 128), (1, 8, 8, 256, 0, 72), (1, 7, 9, 16, 0, 136)])
 @pytest.mark.parametrize("relu", [0, 1])
-def test_conv3x3_forward_tcgen05(relu, shape):
-    """The tensor-memory (tcgen05) forward convolution against the NumPy reference
-    and the mma.sync kernel; no wait may time out."""
+def test_conv3x3_tcgen05_larger_tiles(relu, shape):
+    """The tcgen05 forward and data-gradient kernels on shapes with several K
+    chunks and N tiles, and a channel count that is not a multiple of the tile;
+    no bounded wait may run out."""
     from svirl_gb300 import learned as L
     n, h, w, c1, c2, cout = shape
     rng = np.random.default_rng(5)
     x1 = R.bf16_round(rng.standard_normal((n, h, w, c1)).astype(np.float32))
     x2 = R.bf16_round(rng.standard_normal((n, h, w, c2)).astype(np.float32)) if c2 else None
-    W = (rng.standard_normal((cout, 3, 3, c1 + c2)) * 0.2).astype(np.float32)
+    W = (rng.standard_normal((cout, 3, 3, c1 + c2)) * 0.1).astype(np.float32)
     b = (rng.standard_normal(cout) * 0.1).astype(np.float32)
     xc = x1 if x2 is None else np.concatenate([x1, x2], axis=3)
     y_ref = R.conv3x3(xc, R.bf16_round(W), b, relu)
-    lib = L._lib_nn()
-    tx1, tx2 = _bf(x1), (_bf(x2) if c2 else None)
-    tW = torch.from_numpy(W).cuda()
-    tb = torch.from_numpy(b).cuda()
-    wb = torch.empty(tW.shape, dtype=torch.bfloat16, device="cuda")
-    assert lib.glnn_prep_weights(L._ptr(tW), L._ptr(wb), None, cout, c1 + c2, L._stream()) == 0
-    y_tc = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
-    y_mma = torch.empty_like(y_tc)
-    err = torch.zeros(1, dtype=torch.int32, device="cuda")
-    assert lib.glnn_conv3x3_fwd_tc(L._ptr(tx1), c1, L._ptr(tx2), c2, L._ptr(wb), L._ptr(tb), L._ptr(y_tc), n, h, w, cout,
-                                   relu, L._ptr(err), L._stream()) == 0
-    assert lib.glnn_conv3x3_fwd(L._ptr(tx1), c1, L._ptr(tx2), c2, L._ptr(wb), L._ptr(tb), L._ptr(y_mma), n, h, w, cout,
-                                relu, L._stream()) == 0
-    torch.cuda.synchronize()
-    assert int(err.item()) == 0
-    _close(_np(y_tc), y_ref)
-    _close(_np(y_tc), _np(y_mma), 1e-2)
+    tx1 = _bf(x1).requires_grad_()
+    tx2 = _bf(x2).requires_grad_() if c2 else None
+    tW = torch.from_numpy(W).cuda().requires_grad_()
+    tb = torch.from_numpy(b).cuda().requires_grad_()
+    y = L.Conv3x3.apply(tx1, tx2, tW, tb, relu)
+    _close(_np(y), y_ref)
+    dy = R.bf16_round(rng.standard_normal(y.shape).astype(np.float32))
+    dx_ref, _, _ = R.conv3x3_bwd(xc, R.bf16_round(W), _np(y), dy, relu)
+    grads = torch.autograd.grad(y, [tx1] + ([tx2] if c2 else []), grad_outputs=_bf(dy))
+    dx = _np(grads[0]) if not c2 else np.concatenate([_np(grads[0]), _np(grads[1])], axis=3)
+    _close(dx, dx_ref)
+    L.check_kernel_errors()
