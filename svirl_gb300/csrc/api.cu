@@ -432,7 +432,7 @@ int glgpu_batch_destroy(glgpu_batch* b) {
     for (int q = 0; q < 6; ++q)
         if (b->td_exec[q]) cudaGraphExecDestroy(b->td_exec[q]);
     if (b->cg_exec) cudaGraphExecDestroy(b->cg_exec);
-    void* ptrs[] = {b->insts, b->gather, b->tiles, b->items, b->loop, b->cg_partials, b->cg_loop};
+    void* ptrs[] = {b->insts, b->gather, b->tiles, b->items, b->loop, b->cg_partials, b->cg_loop, b->cg_tiles};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);

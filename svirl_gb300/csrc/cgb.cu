@@ -24,6 +24,11 @@
 namespace glgpu {
 
 constexpr int kPart = 17;  // doubles of per-tile partials
+// The CG kernels walk tiles of kCGRep x 256 nodes of one instance: each thread
+// accumulates kCGRep nodes in registers before the block reduction, so the
+// reduction's cost is shared by kCGRep nodes.
+constexpr int kCGRep = 4;
+constexpr int kCGTile = kCGRep * kThreads;
 
 struct CGLoop {
     int active;
@@ -58,16 +63,18 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
     T* GA = (T*)I.gA[1 - gi];
     const T* GAp = (const T*)I.gA[gi];
     T v[5] = {T(0), T(0), T(0), T(0), T(0)};
-    const int n = t.n0 + threadIdx.x;
+#pragma unroll
+    for (int r = 0; r < kCGRep; ++r) {
+    const int n = t.n0 + threadIdx.x + r * kThreads;
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, I.mt, i, j);
         const C2<T> gv = grad_psi_node<T>(g, gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp, psi, abei, ab, n, i, j, cb);
         G[n] = gv;
         const C2<T> gp = Gp[n];
-        v[0] = gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y);
-        v[1] = gp.x * gp.x + gp.y * gp.y;
-        v[4] = gv.x * gv.x + gv.y * gv.y;
+        v[0] += gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y);
+        v[1] += gp.x * gp.x + gp.y * gp.y;
+        v[4] += gv.x * gv.x + gv.y * gv.y;
         if (I.solveA) {
             const T k2 = gsel<T>(I.kappa2, I.fkappa2), H = gsel<T>(I.H, I.fH);
             for (int dir = 0; dir < 2; ++dir) {
@@ -82,6 +89,7 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
                 v[4] += ga * ga;
             }
         }
+    }
     }
     double vs[5];
     block_sum<5>(v, vs);
@@ -156,7 +164,9 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
     T c[17];
 #pragma unroll
     for (int k = 0; k < 17; ++k) c[k] = T(0);
-    const int n = t.n0 + threadIdx.x;
+#pragma unroll 1
+    for (int r = 0; r < kCGRep; ++r) {
+    const int n = t.n0 + threadIdx.x + r * kThreads;
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, I.mt, i, j);
@@ -170,8 +180,9 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
         } else {
             T c5[5] = {T(0), T(0), T(0), T(0), T(0)};
             coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, n, i, j, cb, dpsi, dA, c5);
-            c[0] = c5[0]; c[5] = c5[1]; c[10] = c5[2]; c[15] = c5[3]; c[16] = c5[4];
+            c[0] += c5[0]; c[5] += c5[1]; c[10] += c5[2]; c[15] += c5[3]; c[16] += c5[4];
         }
+    }
     }
     double cs17[17];
     block_sum<17>(c, cs17);
@@ -224,51 +235,43 @@ __device__ double smallest_nonneg_root_cubic(double d0, double d1, double d2, do
 }
 
 // F(a, b) = sum c[i][j] a^i b^j (17-coefficient layout: c00..c04, c10..c14,
-// c20..c24, c30, c40) with its gradient and Hessian, evaluated by a whole warp:
-// lane l < 17 holds one term, the sums are reduced in a fixed tree and
-// broadcast from lane 0, so every lane sees the same values and takes the same
-// branches.
+// c20..c24, c30, c40) with its gradient and Hessian, by Horner's scheme:
+// F = p0(b) + a p1(b) + a^2 p2(b) + c30 a^3 + c40 a^4 with quartics p_i, about
+// 60 FP64 operations (GB300 runs FP64 at a small fraction of its FP32 rate, so
+// the step-length search is kept to one thread and few operations).
 struct P2 {
     double f, fa, fb, faa, fab, fbb;
 };
 
-__device__ __forceinline__ double ipow(double x, int k) {
-    double r = 1.0;
-    for (int q = 0; q < k; ++q) r *= x;
+__device__ __forceinline__ void quartic3(const double* q, double b, double& p, double& dp, double& ddp) {
+    // p = q0 + q1 b + q2 b^2 + q3 b^3 + q4 b^4 and its first two derivatives
+    p = fma(fma(fma(fma(q[4], b, q[3]), b, q[2]), b, q[1]), b, q[0]);
+    dp = fma(fma(fma(4.0 * q[4], b, 3.0 * q[3]), b, 2.0 * q[2]), b, q[1]);
+    ddp = fma(fma(12.0 * q[4], b, 6.0 * q[3]), b, 2.0 * q[2]);
+}
+
+__device__ __forceinline__ P2 poly2(const double (&c)[17], double a, double b) {
+    double p0, p0b, p0bb, p1, p1b, p1bb, p2, p2b, p2bb;
+    quartic3(c + 0, b, p0, p0b, p0bb);
+    quartic3(c + 5, b, p1, p1b, p1bb);
+    quartic3(c + 10, b, p2, p2b, p2bb);
+    const double c3 = c[15], c4 = c[16];
+    P2 r;
+    r.f = fma(fma(fma(fma(c4, a, c3), a, p2), a, p1), a, p0);
+    r.fa = fma(fma(fma(4.0 * c4, a, 3.0 * c3), a, 2.0 * p2), a, p1);
+    r.faa = fma(fma(12.0 * c4, a, 6.0 * c3), a, 2.0 * p2);
+    r.fb = fma(fma(p2b, a, p1b), a, p0b);
+    r.fab = fma(2.0 * p2b, a, p1b);
+    r.fbb = fma(fma(p2bb, a, p1bb), a, p0bb);
     return r;
-}
-
-__device__ __forceinline__ double warp_sum_bcast(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return __shfl_sync(0xffffffffu, v, 0);
-}
-
-__device__ P2 poly2_warp(double cl, int il, int jl, double a, double b) {
-    const double A0 = ipow(a, il), A1 = il >= 1 ? ipow(a, il - 1) : 0.0, A2 = il >= 2 ? ipow(a, il - 2) : 0.0;
-    const double B0 = ipow(b, jl), B1 = jl >= 1 ? ipow(b, jl - 1) : 0.0, B2 = jl >= 2 ? ipow(b, jl - 2) : 0.0;
-    P2 p;
-    p.f = warp_sum_bcast(cl * A0 * B0);
-    p.fa = warp_sum_bcast(cl * il * A1 * B0);
-    p.fb = warp_sum_bcast(cl * jl * A0 * B1);
-    p.faa = warp_sum_bcast(cl * il * (il - 1) * A2 * B0);
-    p.fab = warp_sum_bcast(cl * il * jl * A1 * B1);
-    p.fbb = warp_sum_bcast(cl * jl * (jl - 1) * A0 * B2);
-    return p;
 }
 
 // Local minimum of the 2-D polynomial reached by a damped Newton descent from
 // (0, 0) (Armijo backtracking; gradient steps where the Hessian is not positive
-// definite); called by all lanes of a warp with the same coefficients.
-__device__ bool minimise_poly2_warp(const double (&c17)[17], double* a_out, double* b_out) {
-    const int lane = threadIdx.x & 31;
-    double cl = 0.0;
-#pragma unroll
-    for (int k = 0; k < 17; ++k)
-        if (k == lane) cl = c17[k];
-    const int il = lane < 15 ? lane / 5 : (lane == 15 ? 3 : (lane == 16 ? 4 : 0));
-    const int jl = lane < 15 ? lane % 5 : 0;
+// definite).
+__device__ bool minimise_poly2(const double (&c17)[17], double* a_out, double* b_out) {
     double a = 0.0, b = 0.0;
-    P2 P = poly2_warp(cl, il, jl, a, b);
+    P2 P = poly2(c17, a, b);
     const double g0 = sqrt(P.fa * P.fa + P.fb * P.fb);
     for (int it = 0; it < 60; ++it) {
         const double gn = sqrt(P.fa * P.fa + P.fb * P.fb);
@@ -288,7 +291,7 @@ __device__ bool minimise_poly2_warp(const double (&c17)[17], double* a_out, doub
         bool moved = false;
         P2 Pn;
         for (int ls = 0; ls < 60; ++ls) {
-            Pn = poly2_warp(cl, il, jl, a + t * sa, b + t * sb);
+            Pn = poly2(c17, a + t * sa, b + t * sb);
             if (Pn.f <= P.f + 1e-4 * t * slope) {
                 moved = true;
                 break;
@@ -318,15 +321,15 @@ kb_inst_alpha(const Inst* __restrict__ insts, int ninst, const double* __restric
     double c[17];
 #pragma unroll
     for (int k = 0; k < 17; ++k) c[k] = warp_tile_sum(partials, I.tile0, I.ntiles, k) * I.g.dxdy;
+    if ((threadIdx.x & 31) != 0) return;
     bool ok;
     double ap = 0.0, aA = 0.0;
     if (I.solveA) {
-        ok = minimise_poly2_warp(c, &ap, &aA);
+        ok = minimise_poly2(c, &ap, &aA);
     } else {
         ap = smallest_nonneg_root_cubic(c[5], 2.0 * c[10], 3.0 * c[15], 4.0 * c[16]);
         ok = ap >= 0.0;
     }
-    if ((threadIdx.x & 31) != 0) return;
     for (int k = 0; k < 17; ++k) cs->c[k] = c[k];
     cs->alpha_psi = ap;
     cs->alpha_A = aA;
@@ -346,21 +349,25 @@ kb_update(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
     const CGState* cs = I.cg;
     if (*(volatile const int*)&cs->done) return;
     const Geo g = I.g;
-    const int n = t.n0 + threadIdx.x;
-    if (n >= g.N) return;
     const T ap = (T)cs->alpha_psi, aA = (T)cs->alpha_A;
     C2<T>* psi = (C2<T>*)I.psi[0];
-    const C2<T> d = ((const C2<T>*)I.dpsi[cs->di])[n];
-    C2<T> p = psi[n];
-    p.x = ap * d.x + p.x;
-    p.y = ap * d.y + p.y;
-    psi[n] = p;
-    if (I.solveA) {
-        T* ab = (T*)I.ab[0];
-        const T* dA = (const T*)I.dA[cs->di];
-        const int i = n % g.Nx, j = n / g.Nx;
-        if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; ab[na] = aA * dA[na] + ab[na]; }
-        if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; ab[nb] = aA * dA[nb] + ab[nb]; }
+    const C2<T>* dpsi = (const C2<T>*)I.dpsi[cs->di];
+    T* ab = (T*)I.ab[0];
+    const T* dA = (const T*)I.dA[cs->di];
+#pragma unroll
+    for (int r = 0; r < kCGRep; ++r) {
+        const int n = t.n0 + threadIdx.x + r * kThreads;
+        if (n >= g.N) break;
+        const C2<T> d = dpsi[n];
+        C2<T> p = psi[n];
+        p.x = ap * d.x + p.x;
+        p.y = ap * d.y + p.y;
+        psi[n] = p;
+        if (I.solveA) {
+            const int i = n % g.Nx, j = n / g.Nx;
+            if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; ab[na] = aA * dA[na] + ab[na]; }
+            if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; ab[nb] = aA * dA[nb] + ab[nb]; }
+        }
     }
 }
 
@@ -372,11 +379,14 @@ kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double
     if (!all && *(volatile const int*)&I.cg->done) return;
     const Geo g = I.g;
     T v[1] = {T(0)};
-    const int n = t.n0 + threadIdx.x;
-    if (n < g.N)
-        v[0] = energy_density<T>(g, gsel<T>(I.kappa2, I.fkappa2), gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp,
-                                         gsel<T>(I.H, I.fH), I.mt, (const C2<T>*)I.psi[0], (const T*)I.abei,
-                                         (const T*)I.ab[0], n);
+#pragma unroll
+    for (int r = 0; r < kCGRep; ++r) {
+        const int n = t.n0 + threadIdx.x + r * kThreads;
+        if (n < g.N)
+            v[0] += energy_density<T>(g, gsel<T>(I.kappa2, I.fkappa2), gsel<T>(I.epsilon, I.fepsilon),
+                                      (const T*)I.eps_sp, gsel<T>(I.H, I.fH), I.mt, (const C2<T>*)I.psi[0],
+                                      (const T*)I.abei, (const T*)I.ab[0], n);
+    }
     double vs[1];
     block_sum<1>(v, vs);
     if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kPart] = vs[0];
@@ -431,13 +441,16 @@ kb_zero_dir(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
     const Tile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
     const Geo g = I.g;
-    const int n = t.n0 + threadIdx.x;
-    if (n >= g.N) return;
-    ((C2<T>*)I.dpsi[0])[n] = cmk<T>(T(0), T(0));
-    ((C2<T>*)I.gpsi[0])[n] = cmk<T>(T(0), T(0));
-    const int i = n % g.Nx, j = n / g.Nx;
-    if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; ((T*)I.dA[0])[na] = T(0); ((T*)I.gA[0])[na] = T(0); }
-    if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; ((T*)I.dA[0])[nb] = T(0); ((T*)I.gA[0])[nb] = T(0); }
+#pragma unroll
+    for (int r = 0; r < kCGRep; ++r) {
+        const int n = t.n0 + threadIdx.x + r * kThreads;
+        if (n >= g.N) break;
+        ((C2<T>*)I.dpsi[0])[n] = cmk<T>(T(0), T(0));
+        ((C2<T>*)I.gpsi[0])[n] = cmk<T>(T(0), T(0));
+        const int i = n % g.Nx, j = n / g.Nx;
+        if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; ((T*)I.dA[0])[na] = T(0); ((T*)I.gA[0])[na] = T(0); }
+        if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; ((T*)I.dA[0])[nb] = T(0); ((T*)I.gA[0])[nb] = T(0); }
+    }
 }
 
 __global__ void __launch_bounds__(1024)
@@ -614,20 +627,28 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
              int32_t* status, double* elapsed_ms) {
     if (n_iter < 0 || !(rtol >= 0.0) || !(gtol >= 0.0)) return batch_error(b, GLGPU_E_ARG, "batch_cg: bad n_iter, rtol or gtol");
     std::vector<Inst> insts(b->ninst);
-    int tile0 = 0;
+    std::vector<Tile> cgtiles;
     for (int q = 0; q < b->ninst; ++q) {
         glgpu_handle* h = b->hs[q];
         const int rc = cg_ensure(h);
         if (rc) return batch_error(b, rc, "batch_cg: " + h->last_error);
         cudaStreamSynchronize(h->stream);
         insts[q] = h->inst_h;
-        insts[q].tile0 = tile0;  // the batch's tile table lists the instances' tiles in order
+        // this copy of the descriptors indexes the CG tile table (kCGTile nodes per tile)
+        insts[q].tile0 = (int)cgtiles.size();
+        for (int n0 = 0; n0 < h->g.N; n0 += kCGTile) cgtiles.push_back(Tile{q, n0});
+        insts[q].ntiles = (int)cgtiles.size() - insts[q].tile0;
         insts[q].cg_exact = (flags & GLGPU_CG_EXACT_BOUNDARY) ? 1 : 0;
         insts[q].cg_target = b->cg_targets.empty() ? NAN : b->cg_targets[q];
         insts[q].cg_target_tol = b->cg_target_tol;
-        tile0 += h->ntiles;
     }
-    if (!b->cg_partials && cudaMalloc(&b->cg_partials, sizeof(double) * kPart * (size_t)b->ntiles) != cudaSuccess)
+    if (!b->cg_tiles) {
+        b->cg_ntiles = (int)cgtiles.size();
+        if (cudaMalloc(&b->cg_tiles, sizeof(Tile) * cgtiles.size()) != cudaSuccess ||
+            cudaMemcpy(b->cg_tiles, cgtiles.data(), sizeof(Tile) * cgtiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return batch_error(b, GLGPU_E_OOM, "batch_cg: cannot place the tile table");
+    }
+    if (!b->cg_partials && cudaMalloc(&b->cg_partials, sizeof(double) * kPart * (size_t)b->cg_ntiles) != cudaSuccess)
         return batch_error(b, GLGPU_E_OOM, "batch_cg: out of device memory");
     if (!b->cg_loop && cudaMalloc(&b->cg_loop, sizeof(CGLoop)) != cudaSuccess)
         return batch_error(b, GLGPU_E_OOM, "batch_cg: out of device memory");
@@ -644,11 +665,11 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
     if (e != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_cg: ") + cudaGetErrorString(e));
     CGLaunch L;
     L.insts = b->insts;
-    L.tiles = b->tiles;
+    L.tiles = (const Tile*)b->cg_tiles;
     L.partials = b->cg_partials;
     L.loop = (CGLoop*)b->cg_loop;
     L.ninst = b->ninst;
-    L.ntiles = b->ntiles;
+    L.ntiles = b->cg_ntiles;
     L.dtype = b->dtype;
     if (b->use_graphs && !b->cg_graph_failed && !b->cg_exec && build_cg_graph(L, &b->cg_exec) != cudaSuccess) {
         b->cg_graph_failed = true;

@@ -186,7 +186,9 @@ struct glgpu_batch {
     cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool td_graph_failed = false, use_graphs = true;
     // batched device CG (allocated on first use)
-    double* cg_partials = nullptr;       // ntiles * 17 doubles
+    void* cg_tiles = nullptr;            // CG tile table (larger tiles than the TD one)
+    int cg_ntiles = 0;
+    double* cg_partials = nullptr;       // cg_ntiles * 17 doubles
     void* cg_loop = nullptr;             // CGLoop
     cudaGraphExec_t cg_exec = nullptr;
     bool cg_graph_failed = false;
