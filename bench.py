@@ -374,6 +374,70 @@ def run_c1(args):
     print(json.dumps(line), flush=True)
 
 
+def run_conv(args):
+    """The learned warm start's hottest kernels: the tcgen05 3x3 convolution (forward
+    and data gradient) and the mma weight gradient on a 32 x 128 x 128 x 64 -> 64
+    layer, timed with CUDA events; FLOP rate against the measured bf16 peak."""
+    import ctypes as C
+    import torch
+    from svirl_gb300 import learned as L
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    lib = L._lib_nn()
+    n, h, w, cin, cout = 32, 128, 128, 64, 64
+    g = torch.Generator(device="cpu").manual_seed(0)
+    x = torch.randn((n, h, w, cin), generator=g).to("cuda", torch.bfloat16)
+    W = (0.05 * torch.randn((cout, 3, 3, cin), generator=g)).cuda()
+    b = torch.zeros(cout, device="cuda")
+    wb = torch.empty(W.shape, dtype=torch.bfloat16, device="cuda")
+    wt = torch.empty((3, 3, cin, cout), dtype=torch.bfloat16, device="cuda")
+    y = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
+    dy = torch.randn((n, h, w, cout), generator=g).to("cuda", torch.bfloat16)
+    dx = torch.empty_like(x)
+    dw = torch.empty_like(W)
+    db = torch.empty_like(b)
+    nwork = int(lib.glnn_conv3x3_bwd_weight_work(n, h, w, cin, cout))
+    work = torch.empty(nwork, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = L._stream()
+    P = L._ptr
+    assert lib.glnn_prep_weights(P(W), P(wb), P(wt), cout, cin, s) == 0
+    flop = 2.0 * n * h * w * 9 * cin * cout
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    f = lambda: lib.glnn_conv3x3_fwd(P(x), cin, None, 0, P(wb), P(b), P(y), n, h, w, cout, 1, P(err), s)
+    bd = lambda: lib.glnn_conv3x3_bwd_data(P(dy), P(y), 1, P(wt), P(dx), cin, None, 0, n, h, w, cout, P(err), s)
+    bw = lambda: lib.glnn_conv3x3_bwd_weight(P(dy), P(y), 1, P(x), cin, None, 0, P(dw), P(db), P(work), nwork, n, h, w,
+                                            cout, s)
+    ms_f, ms_d, ms_w = timed(f, args.steps), timed(bd, args.steps), timed(bw, args.steps)
+    assert int(err.item()) == 0
+    peak = 1922.0
+    pth = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pth):
+        peak = float(json.load(open(pth))["bf16_tflops"])
+    tf = flop / (ms_f * 1e-3) / 1e12
+    line = {"metric": "3x3 conv TFLOP/s (tcgen05 forward, 32x128x128x64->64, bf16 in, fp32 accumulate)", "value": tf,
+            "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": 3, "ms_per_step": ms_f,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "conv3x3_layer", "n": n, "h": h, "w": w, "cin": cin, "cout": cout},
+            "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
+                         "peak_kind": "measured bf16 burst"},
+            "data_grad": {"ms": ms_d, "tflops": flop / (ms_d * 1e-3) / 1e12, "kernel": "tcgen05"},
+            "weight_grad": {"ms": ms_w, "tflops": flop / (ms_w * 1e-3) / 1e12, "kernel": "mma.sync"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_learned(args):
     """Learned CG warm start: relaxed 128^2 states generated by the batched device CG
     (kappa ~ U[2, 10], H ~ U[0.02, 0.5], hole masks), the network trained on them by
@@ -422,7 +486,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graphs", action="store_true",
                     help="host-driven Jacobi loop (same kernels); ncu cannot profile kernels inside conditional graphs")
-    ap.add_argument("--workload", choices=["tdgl", "states", "serve", "learned", "c1"], default="tdgl",
+    ap.add_argument("--workload", choices=["tdgl", "states", "serve", "learned", "c1", "conv"], default="tdgl",
                     help="tdgl: node-steps/s on the 2049^2 domain; states: relaxed states/s of a batched sweep; "
                          "serve: the serving loop; learned: the learned CG warm start")
     ap.add_argument("--train-states", type=int, default=2048)
@@ -449,6 +513,9 @@ def main():
         return
     if args.workload == "c1":
         run_c1(args)
+        return
+    if args.workload == "conv":
+        run_conv(args)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -189,44 +189,50 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
     if (threadIdx.x == 0) store_partials<T>(cs17, 17, partials + (size_t)blockIdx.x * kPart);
 }
 
-// Real roots of d0 + d1 a + d2 a^2 + d3 a^3; returns the smallest root >= 0 or -1.
+// GB300 runs FP64 at a small fraction of its FP32 rate, and a single thread's
+// chain of dependent FP64 operations is slow: the step lengths are found in FP32
+// and then polished by FP64 Newton steps, which restore full FP64 accuracy.
+
+// Real roots of d0 + d1 a + d2 a^2 + d3 a^3 (FP32 closed form, each root polished
+// by two FP64 Newton steps on the cubic); returns the smallest root >= 0 or -1.
 __device__ double smallest_nonneg_root_cubic(double d0, double d1, double d2, double d3) {
-    double roots[3];
+    float roots[3];
     int nr = 0;
     const double scale = fabs(d0) + fabs(d1) + fabs(d2) + fabs(d3);
     if (!(scale > 0.0)) return -1.0;
-    if (fabs(d3) <= 1e-14 * scale) {
-        if (fabs(d2) <= 1e-14 * scale) {
-            if (d1 != 0.0) roots[nr++] = -d0 / d1;
+    const float f0 = (float)(d0 / scale), f1 = (float)(d1 / scale), f2 = (float)(d2 / scale), f3 = (float)(d3 / scale);
+    if (fabsf(f3) <= 1e-7f) {
+        if (fabsf(f2) <= 1e-7f) {
+            if (f1 != 0.f) roots[nr++] = -f0 / f1;
         } else {
-            const double disc = d1 * d1 - 4.0 * d2 * d0;
-            if (disc >= 0.0) {
-                const double s = sqrt(disc);
-                const double qq = -0.5 * (d1 + (d1 >= 0.0 ? s : -s));
-                if (qq != 0.0) roots[nr++] = d0 / qq;
-                roots[nr++] = qq / d2;
+            const float disc = f1 * f1 - 4.f * f2 * f0;
+            if (disc >= 0.f) {
+                const float sq = sqrtf(disc);
+                const float qq = -0.5f * (f1 + (f1 >= 0.f ? sq : -sq));
+                if (qq != 0.f) roots[nr++] = f0 / qq;
+                roots[nr++] = qq / f2;
             }
         }
     } else {
-        const double a = d2 / d3, b = d1 / d3, c = d0 / d3;
-        const double p = b - a * a / 3.0, qv = 2.0 * a * a * a / 27.0 - a * b / 3.0 + c;
-        const double disc = 0.25 * qv * qv + p * p * p / 27.0;
-        if (disc > 0.0) {
-            const double s = sqrt(disc);
-            roots[nr++] = cbrt(-0.5 * qv + s) + cbrt(-0.5 * qv - s) - a / 3.0;
+        const float a = f2 / f3, b = f1 / f3, c = f0 / f3;
+        const float p = b - a * a / 3.f, qv = 2.f * a * a * a / 27.f - a * b / 3.f + c;
+        const float disc = 0.25f * qv * qv + p * p * p / 27.f;
+        if (disc > 0.f) {
+            const float sq = sqrtf(disc);
+            roots[nr++] = cbrtf(-0.5f * qv + sq) + cbrtf(-0.5f * qv - sq) - a / 3.f;
         } else {
-            const double r = 2.0 * sqrt(-p / 3.0);
-            double arg = r != 0.0 ? 3.0 * qv / (p * r) : 0.0;
-            arg = fmax(-1.0, fmin(1.0, arg));
-            const double phi = acos(arg);
-            for (int k = 0; k < 3; ++k) roots[nr++] = r * cos((phi - 2.0 * 3.141592653589793 * k) / 3.0) - a / 3.0;
+            const float r = 2.f * sqrtf(-p / 3.f);
+            float arg = r != 0.f ? 3.f * qv / (p * r) : 0.f;
+            arg = fmaxf(-1.f, fminf(1.f, arg));
+            const float phi = acosf(arg);
+            for (int k = 0; k < 3; ++k) roots[nr++] = r * cosf((phi - 2.f * 3.14159265f * k) / 3.f) - a / 3.f;
         }
     }
     double best = -1.0;
     for (int k = 0; k < nr; ++k) {
-        double x = roots[k];
-        for (int it = 0; it < 3; ++it) {  // Newton polish on the cubic
-            const double f = ((d3 * x + d2) * x + d1) * x + d0, df = (3.0 * d3 * x + 2.0 * d2) * x + d1;
+        double x = (double)roots[k];
+        for (int it = 0; it < 2; ++it) {  // Newton polish on the cubic, FP64
+            const double f = fma(fma(fma(d3, x, d2), x, d1), x, d0), df = fma(fma(3.0 * d3, x, 2.0 * d2), x, d1);
             if (df != 0.0) x -= f / df;
         }
         if (x >= 0.0 && (best < 0.0 || x < best)) best = x;
@@ -234,79 +240,109 @@ __device__ double smallest_nonneg_root_cubic(double d0, double d1, double d2, do
     return best;
 }
 
-// F(a, b) = sum c[i][j] a^i b^j (17-coefficient layout: c00..c04, c10..c14,
-// c20..c24, c30, c40) with its gradient and Hessian, by Horner's scheme:
-// F = p0(b) + a p1(b) + a^2 p2(b) + c30 a^3 + c40 a^4 with quartics p_i, about
-// 60 FP64 operations (GB300 runs FP64 at a small fraction of its FP32 rate, so
-// the step-length search is kept to one thread and few operations).
-struct P2 {
-    double f, fa, fb, faa, fab, fbb;
+// F(a, b) - c00 = sum c[i][j] a^i b^j over (i, j) != (0, 0) (17-coefficient
+// layout: c00..c04, c10..c14, c20..c24, c30, c40) with its gradient and Hessian,
+// by Horner's scheme: F = p0(b) + a p1(b) + a^2 p2(b) + c30 a^3 + c40 a^4 with
+// quartics p_i.  The constant c00 is left out: the descent compares values of F
+// that differ by far less than F itself.
+template <typename T> struct P2 {
+    T f, fa, fb, faa, fab, fbb;
 };
 
-__device__ __forceinline__ void quartic3(const double* q, double b, double& p, double& dp, double& ddp) {
-    // p = q0 + q1 b + q2 b^2 + q3 b^3 + q4 b^4 and its first two derivatives
-    p = fma(fma(fma(fma(q[4], b, q[3]), b, q[2]), b, q[1]), b, q[0]);
-    dp = fma(fma(fma(4.0 * q[4], b, 3.0 * q[3]), b, 2.0 * q[2]), b, q[1]);
-    ddp = fma(fma(12.0 * q[4], b, 6.0 * q[3]), b, 2.0 * q[2]);
+template <typename T>
+__device__ __forceinline__ void quartic3(const T* q, T b, T& p, T& dp, T& ddp) {
+    p = fma(fma(fma(q[4], b, q[3]), b, q[2]), b, q[1]) * b + q[0];
+    dp = fma(fma(fma(T(4) * q[4], b, T(3) * q[3]), b, T(2) * q[2]), b, q[1]);
+    ddp = fma(fma(T(12) * q[4], b, T(6) * q[3]), b, T(2) * q[2]);
 }
 
-__device__ __forceinline__ P2 poly2(const double (&c)[17], double a, double b) {
-    double p0, p0b, p0bb, p1, p1b, p1bb, p2, p2b, p2bb;
-    quartic3(c + 0, b, p0, p0b, p0bb);
-    quartic3(c + 5, b, p1, p1b, p1bb);
-    quartic3(c + 10, b, p2, p2b, p2bb);
-    const double c3 = c[15], c4 = c[16];
-    P2 r;
+template <typename T>
+__device__ __forceinline__ P2<T> poly2(const T (&c)[17], T a, T b) {
+    T p0, p0b, p0bb, p1, p1b, p1bb, p2, p2b, p2bb;
+    quartic3<T>(c + 0, b, p0, p0b, p0bb);
+    quartic3<T>(c + 5, b, p1, p1b, p1bb);
+    quartic3<T>(c + 10, b, p2, p2b, p2bb);
+    const T c3 = c[15], c4 = c[16];
+    P2<T> r;
     r.f = fma(fma(fma(fma(c4, a, c3), a, p2), a, p1), a, p0);
-    r.fa = fma(fma(fma(4.0 * c4, a, 3.0 * c3), a, 2.0 * p2), a, p1);
-    r.faa = fma(fma(12.0 * c4, a, 6.0 * c3), a, 2.0 * p2);
+    r.fa = fma(fma(fma(T(4) * c4, a, T(3) * c3), a, T(2) * p2), a, p1);
+    r.faa = fma(fma(T(12) * c4, a, T(6) * c3), a, T(2) * p2);
     r.fb = fma(fma(p2b, a, p1b), a, p0b);
-    r.fab = fma(2.0 * p2b, a, p1b);
+    r.fab = fma(T(2) * p2b, a, p1b);
     r.fbb = fma(fma(p2bb, a, p1bb), a, p0bb);
     return r;
 }
 
+// Newton step of the 2-D polynomial at P (gradient steps where the Hessian is
+// not positive definite).
+template <typename T>
+__device__ __forceinline__ void newton_dir(const P2<T>& P, T& sa, T& sb) {
+    const T det = P.faa * P.fbb - P.fab * P.fab;
+    if (P.faa > T(0) && det > T(0)) {
+        sa = -(P.fbb * P.fa - P.fab * P.fb) / det;
+        sb = -(-P.fab * P.fa + P.faa * P.fb) / det;
+    } else {
+        const T h = fabs(P.faa) + fabs(P.fbb) + T(1e-30);
+        sa = -P.fa / h;
+        sb = -P.fb / h;
+    }
+}
+
 // Local minimum of the 2-D polynomial reached by a damped Newton descent from
-// (0, 0) (Armijo backtracking; gradient steps where the Hessian is not positive
-// definite).
+// (0, 0) (Armijo backtracking) in FP32, then two FP64 Newton steps.  The
+// polynomial is scaled to O(1) coefficients first.
 __device__ bool minimise_poly2(const double (&c17)[17], double* a_out, double* b_out) {
-    double a = 0.0, b = 0.0;
-    P2 P = poly2(c17, a, b);
-    const double g0 = sqrt(P.fa * P.fa + P.fb * P.fb);
-    for (int it = 0; it < 60; ++it) {
-        const double gn = sqrt(P.fa * P.fa + P.fb * P.fb);
-        if (!(gn > 1e-14 * (g0 + 1e-300))) break;
-        double sa, sb;
-        const double det = P.faa * P.fbb - P.fab * P.fab;
-        if (P.faa > 0.0 && det > 0.0) {
-            sa = -(P.fbb * P.fa - P.fab * P.fb) / det;
-            sb = -(-P.fab * P.fa + P.faa * P.fb) / det;
-        } else {
-            const double h = fabs(P.faa) + fabs(P.fbb) + 1e-300;
-            sa = -P.fa / h;
-            sb = -P.fb / h;
-        }
-        double t = 1.0;
-        const double slope = P.fa * sa + P.fb * sb;
+    double scale = 0.0;
+    for (int k = 1; k < 17; ++k) scale = fmax(scale, fabs(c17[k]));
+    if (!(scale > 0.0)) {
+        *a_out = *b_out = 0.0;
+        return true;
+    }
+    float cf[17];
+    double cd[17];
+    cf[0] = 0.f;
+    cd[0] = 0.0;
+    for (int k = 1; k < 17; ++k) {
+        cd[k] = c17[k] / scale;
+        cf[k] = (float)cd[k];
+    }
+    float a = 0.f, b = 0.f;
+    P2<float> P = poly2<float>(cf, a, b);
+    const float g0 = sqrtf(P.fa * P.fa + P.fb * P.fb);
+    for (int it = 0; it < 100; ++it) {
+        const float gn = sqrtf(P.fa * P.fa + P.fb * P.fb);
+        if (!(gn > 1e-6f * g0)) break;
+        float sa, sb;
+        newton_dir<float>(P, sa, sb);
+        float t = 1.f;
+        const float slope = P.fa * sa + P.fb * sb;
         bool moved = false;
-        P2 Pn;
-        for (int ls = 0; ls < 60; ++ls) {
-            Pn = poly2(c17, a + t * sa, b + t * sb);
-            if (Pn.f <= P.f + 1e-4 * t * slope) {
+        P2<float> Pn;
+        for (int ls = 0; ls < 40; ++ls) {
+            Pn = poly2<float>(cf, a + t * sa, b + t * sb);
+            if (Pn.f <= P.f + 1e-4f * t * slope) {
                 moved = true;
                 break;
             }
-            t *= 0.5;
+            t *= 0.5f;
         }
         if (!moved) break;
         a += t * sa;
         b += t * sb;
         P = Pn;
-        if (fabs(t * sa) + fabs(t * sb) <= 1e-15 * (1.0 + fabs(a) + fabs(b))) break;
+        if (fabsf(t * sa) + fabsf(t * sb) <= 1e-7f * (1.f + fabsf(a) + fabsf(b))) break;
     }
-    *a_out = a;
-    *b_out = b;
-    return isfinite(a) && isfinite(b);
+    double ad = a, bd = b;
+    for (int it = 0; it < 2; ++it) {  // FP64 polish
+        const P2<double> Q = poly2<double>(cd, ad, bd);
+        const double det = Q.faa * Q.fbb - Q.fab * Q.fab;
+        if (!(Q.faa > 0.0 && det > 0.0)) break;
+        ad += -(Q.fbb * Q.fa - Q.fab * Q.fb) / det;
+        bd += -(-Q.fab * Q.fa + Q.faa * Q.fb) / det;
+    }
+    *a_out = ad;
+    *b_out = bd;
+    return isfinite(ad) && isfinite(bd);
 }
 
 // coefficients of each instance and its step lengths, one warp per instance
