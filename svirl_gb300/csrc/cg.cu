@@ -28,7 +28,7 @@ k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const ui
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, mt, i, j);
-        const C2<T> G = grad_psi_node<T>(g, (T)eps0, eps_sp, psi, abei, ab, n, i, j, cb);
+        const C2<T> G = grad_psi_node<T>(g, (T)eps0, eps_sp, psi, PhaseLinks<T>{abei, ab}, n, i, j, cb);
         gpsi[n] = G;
         const C2<T> Gp = gpsi_prev[n];
         v[0] = G.x * (G.x - Gp.x) + G.y * (G.y - Gp.y);
@@ -37,7 +37,7 @@ k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const ui
             const T k2 = (T)kappa2, Hh = (T)H;
             if (i < g.Nx - 1) {
                 const int na = i + (g.Nx - 1) * j;
-                const T Ga = grad_A_link<T>(g, k2, Hh, psi, abei, ab, n, i, j, cb, true);
+                const T Ga = grad_A_link<T>(g, k2, Hh, psi, abei, ab, PhaseLinks<T>{abei, ab}, n, i, j, cb, true);
                 gA[na] = Ga;
                 const T Gpa = gA_prev[na];
                 v[2] += Ga * (Ga - Gpa);
@@ -45,7 +45,7 @@ k_cg_grad(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const ui
             }
             if (j < g.Ny - 1) {
                 const int nb = g.Na + i + g.Nx * j;
-                const T Gb = grad_A_link<T>(g, k2, Hh, psi, abei, ab, n, i, j, cb, false);
+                const T Gb = grad_A_link<T>(g, k2, Hh, psi, abei, ab, PhaseLinks<T>{abei, ab}, n, i, j, cb, false);
                 gA[nb] = Gb;
                 const T Gpb = gA_prev[nb];
                 v[2] += Gb * (Gb - Gpb);
@@ -105,7 +105,8 @@ k_cg_dir_coef(Geo g, double kappa2, double eps0, const T* eps_sp, double H, cons
                 if (j < g.Ny - 1) { int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
             }
         }
-        coef_node<T, NV>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, psi, abei, ab, n, i, j, cb, dpsi, dA, c);
+        coef_node<T, NV>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, psi, abei, ab, PhaseLinks<T>{abei, ab}, n, i, j, cb, dpsi, dA,
+                         c);
     }
     grid_sum_finish(c, partials, counter, dscal, g.dxdy);
 }

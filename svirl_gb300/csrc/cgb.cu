@@ -62,6 +62,7 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
     const C2<T>* Gp = (const C2<T>*)I.gpsi[gi];
     T* GA = (T*)I.gA[1 - gi];
     const T* GAp = (const T*)I.gA[gi];
+    const TableLinks<T> lk{(const C2<T>*)I.U};
     T v[5] = {T(0), T(0), T(0), T(0), T(0)};
 #pragma unroll
     for (int r = 0; r < kCGRep; ++r) {
@@ -69,7 +70,7 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
     if (n < g.N) {
         const int i = n % g.Nx, j = n / g.Nx;
         const unsigned cb = cell_bits(g, I.mt, i, j);
-        const C2<T> gv = grad_psi_node<T>(g, gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp, psi, abei, ab, n, i, j, cb);
+        const C2<T> gv = grad_psi_node<T>(g, gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp, psi, lk, n, i, j, cb);
         G[n] = gv;
         const C2<T> gp = Gp[n];
         v[0] += gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y);
@@ -81,7 +82,7 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
                 const bool has = dir == 0 ? (i < g.Nx - 1) : (j < g.Ny - 1);
                 if (!has) continue;
                 const int l = dir == 0 ? i + (g.Nx - 1) * j : g.Na + i + g.Nx * j;
-                const T ga = grad_A_link<T>(g, k2, H, psi, abei, ab, n, i, j, cb, dir == 0, I.cg_exact != 0);
+                const T ga = grad_A_link<T>(g, k2, H, psi, abei, ab, lk, n, i, j, cb, dir == 0, I.cg_exact != 0);
                 GA[l] = ga;
                 const T gap = GAp[l];
                 v[2] += ga * (ga - gap);
@@ -156,6 +157,7 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
     const T* dAO = (const T*)I.dA[di];
     C2<T>* dN = (C2<T>*)I.dpsi[1 - di];
     T* dAN = (T*)I.dA[1 - di];
+    const TableLinks<T> lk{(const C2<T>*)I.U};
     auto dpsi = [&](int m) -> C2<T> {
         const C2<T> o = dO[m], gg = G[m];
         return cmk<T>(bp * o.x - gg.x, bp * o.y - gg.y);
@@ -175,11 +177,11 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
         if (I.solveA) {
             if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
             if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
-            coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, n, i, j, cb,
+            coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb,
                              dpsi, dA, c);
         } else {
             T c5[5] = {T(0), T(0), T(0), T(0), T(0)};
-            coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, n, i, j, cb, dpsi, dA, c5);
+            coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb, dpsi, dA, c5);
             c[0] += c5[0]; c[5] += c5[1]; c[10] += c5[2]; c[15] += c5[3]; c[16] += c5[4];
         }
     }
@@ -400,9 +402,22 @@ kb_update(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
         p.y = ap * d.y + p.y;
         psi[n] = p;
         if (I.solveA) {
+            // new A and its link factors for the next iteration's kernels
             const int i = n % g.Nx, j = n / g.Nx;
-            if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; ab[na] = aA * dA[na] + ab[na]; }
-            if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; ab[nb] = aA * dA[nb] + ab[nb]; }
+            const T* abei = (const T*)I.abei;
+            C2<T>* U = (C2<T>*)I.U;
+            if (i < g.Nx - 1) {
+                const int na = i + (g.Nx - 1) * j;
+                const T v = aA * dA[na] + ab[na];
+                ab[na] = v;
+                U[na] = link_U<T>(GT(g, dx) * (abei ? abei[na] + v : v));
+            }
+            if (j < g.Ny - 1) {
+                const int nb = g.Na + i + g.Nx * j;
+                const T v = aA * dA[nb] + ab[nb];
+                ab[nb] = v;
+                U[nb] = link_U<T>(GT(g, dy) * (abei ? abei[nb] + v : v));
+            }
         }
     }
 }
@@ -414,6 +429,7 @@ kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double
     const Inst& I = insts[t.inst];
     if (!all && *(volatile const int*)&I.cg->done) return;
     const Geo g = I.g;
+    const TableLinks<T> lk{(const C2<T>*)I.U};
     T v[1] = {T(0)};
 #pragma unroll
     for (int r = 0; r < kCGRep; ++r) {
@@ -421,7 +437,7 @@ kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double
         if (n < g.N)
             v[0] += energy_density<T>(g, gsel<T>(I.kappa2, I.fkappa2), gsel<T>(I.epsilon, I.fepsilon),
                                       (const T*)I.eps_sp, gsel<T>(I.H, I.fH), I.mt, (const C2<T>*)I.psi[0],
-                                      (const T*)I.abei, (const T*)I.ab[0], n);
+                                      (const T*)I.abei, (const T*)I.ab[0], lk, n);
     }
     double vs[1];
     block_sum<1>(v, vs);
@@ -470,7 +486,8 @@ kb_inst_stop(const Inst* __restrict__ insts, int ninst, const double* __restrict
     }
 }
 
-// start of a CG call: zero direction, beta = 0, counters; energy of the start state
+// start of a CG call: zero direction and gradient, the link-factor table of the
+// start state (TableLinks), then the energy of the start state
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 kb_zero_dir(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
@@ -484,8 +501,21 @@ kb_zero_dir(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
         ((C2<T>*)I.dpsi[0])[n] = cmk<T>(T(0), T(0));
         ((C2<T>*)I.gpsi[0])[n] = cmk<T>(T(0), T(0));
         const int i = n % g.Nx, j = n / g.Nx;
-        if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; ((T*)I.dA[0])[na] = T(0); ((T*)I.gA[0])[na] = T(0); }
-        if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; ((T*)I.dA[0])[nb] = T(0); ((T*)I.gA[0])[nb] = T(0); }
+        const T* abei = (const T*)I.abei;
+        const T* ab = (const T*)I.ab[0];
+        C2<T>* U = (C2<T>*)I.U;
+        if (i < g.Nx - 1) {
+            const int na = i + (g.Nx - 1) * j;
+            ((T*)I.dA[0])[na] = T(0);
+            ((T*)I.gA[0])[na] = T(0);
+            U[na] = link_U<T>(GT(g, dx) * link_phase(abei, ab, na));
+        }
+        if (j < g.Ny - 1) {
+            const int nb = g.Na + i + g.Nx * j;
+            ((T*)I.dA[0])[nb] = T(0);
+            ((T*)I.gA[0])[nb] = T(0);
+            U[nb] = link_U<T>(GT(g, dy) * link_phase(abei, ab, nb));
+        }
     }
 }
 

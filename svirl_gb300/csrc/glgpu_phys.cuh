@@ -34,6 +34,34 @@ template <typename T> __device__ __forceinline__ T link_phase(const T* abei, con
     return p;
 }
 
+// (sin, cos) of the phase d * A of link l, two ways.  PhaseLinks evaluates them
+// on the spot from abei + ab, in the two forms the reference's kernels use:
+// sc_sum: d * (abei + ab) (observables.h, cg.h:15-301), sc_split: d*abei + d*ab
+// (the coefficient kernels, cg.h:410-412).  TableLinks reads a table
+// U[l] = exp(-i d A_l) = (cos, -sin) made once per CG iteration by the kernel
+// that updates A, so the gradient, coefficient and energy kernels of the batched
+// CG do no transcendental math.
+template <typename T> struct PhaseLinks {
+    const T* abei;
+    const T* ab;
+    __device__ __forceinline__ void sc_sum(int l, T d, T& s, T& c) const { sincos_t(d * link_phase(abei, ab, l), &s, &c); }
+    __device__ __forceinline__ void sc_split(int l, T d, T& s, T& c) const {
+        T ph = T(0);
+        if (abei) ph += d * abei[l];
+        if (ab) ph += d * ab[l];
+        sincos_t(ph, &s, &c);
+    }
+};
+template <typename T> struct TableLinks {
+    const C2<T>* U;
+    __device__ __forceinline__ void sc_sum(int l, T, T& s, T& c) const {
+        const C2<T> u = U[l];
+        c = u.x;
+        s = -u.y;
+    }
+    __device__ __forceinline__ void sc_split(int l, T d, T& s, T& c) const { sc_sum(l, d, s, c); }
+};
+
 // curl of one link field on cell (i, j): idx*(b[i+1,j]-b[i,j]) - idy*(a[i,j+1]-a[i,j]).
 template <typename T> __device__ __forceinline__ T cell_curl(const Geo& g, const T* A, int i, int j, T idx, T idy) {
     const int Nxa = g.Nx - 1;
@@ -42,9 +70,10 @@ template <typename T> __device__ __forceinline__ T cell_curl(const Geo& g, const
 
 // Free-energy pseudo-density at node n before the dx*dy factor
 // (svirl/cuda/observables.h:276-356).
-template <typename T>
+template <typename T, typename LK>
 __device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H,
-                                            const uint8_t* mt, const C2<T>* psi, const T* abei, const T* ab, int n) {
+                                            const uint8_t* mt, const C2<T>* psi, const T* abei, const T* ab,
+                                            const LK& lk, int n) {
     const int i = n % g.Nx, j = n / g.Nx;
     const unsigned cb = cell_bits(g, mt, i, j);
     const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
@@ -57,12 +86,16 @@ __device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, cons
         const T eps = eps_sp ? eps_sp[n] : eps0;
         e += w.g * (T(0.5) * p2 - eps) * p2;
         if (GL_PM(cb) || GL_PP(cb)) {
-            T ph = link_phase(abei, ab, i + (g.Nx - 1) * j);
-            e += w.r_p0 * idx2 * g_grad<T>(p00, dx * ph, psi[n + 1]);
+            T sn, cs;
+            lk.sc_sum(i + (g.Nx - 1) * j, dx, sn, cs);
+            const C2<T> gr = grad_c_sc<T>(p00, sn, cs, psi[n + 1]);
+            e += w.r_p0 * idx2 * (gr.x * gr.x + gr.y * gr.y);
         }
         if (GL_MP(cb) || GL_PP(cb)) {
-            T ph = link_phase(abei, ab, g.Na + i + g.Nx * j);
-            e += w.r_0p * idy2 * g_grad<T>(p00, dy * ph, psi[n + g.Nx]);
+            T sn, cs;
+            lk.sc_sum(g.Na + i + g.Nx * j, dy, sn, cs);
+            const C2<T> gr = grad_c_sc<T>(p00, sn, cs, psi[n + g.Nx]);
+            e += w.r_0p * idy2 * (gr.x * gr.x + gr.y * gr.y);
         }
     }
     if (kappa2 > T(0) && i < g.Nxc && j < g.Nyc) {
@@ -142,17 +175,15 @@ __device__ __forceinline__ T curlcurl_link_exact(const Geo& g, const T* abei, co
     return curlcurl_link<T>(g, abei, ab, H, i, j, xdir);
 }
 
-// 2 (psi0 - psi1 U(ph)) (svirl/cuda/cg.h:4-12)
-template <typename T> __device__ __forceinline__ C2<T> gjac(C2<T> p0, T ph, C2<T> p1) {
-    T s, c;
-    sincos_t(ph, &s, &c);
+// 2 (psi0 - psi1 U(ph)) with (s, c) = sincos(ph) (svirl/cuda/cg.h:4-12)
+template <typename T> __device__ __forceinline__ C2<T> gjac_sc(C2<T> p0, T s, T c, C2<T> p1) {
     return cmk<T>(T(2) * (p0.x - (p1.x * c + p1.y * s)), T(2) * (p0.y - (p1.y * c - p1.x * s)));
 }
 
 // dF/d(Re psi) + i dF/d(Im psi) at node n (svirl/cuda/cg.h:15-121), dx*dy included.
-template <typename T>
-__device__ __forceinline__ C2<T> grad_psi_node(const Geo& g, T eps0, const T* eps_sp, const C2<T>* psi, const T* abei,
-                                               const T* ab, int n, int i, int j, unsigned cb) {
+template <typename T, typename LK>
+__device__ __forceinline__ C2<T> grad_psi_node(const Geo& g, T eps0, const T* eps_sp, const C2<T>* psi, const LK& lk,
+                                               int n, int i, int j, unsigned cb) {
     const T dx = GT(g, dx), dy = GT(g, dy), idx2 = GT(g, idx2), idy2 = GT(g, idy2);
     C2<T> gj = cmk<T>(T(0), T(0));
     if (cb) {
@@ -161,14 +192,23 @@ __device__ __forceinline__ C2<T> grad_psi_node(const Geo& g, T eps0, const T* ep
         const T eps = eps_sp ? eps_sp[n] : eps0;
         const T p = p0.x * p0.x + p0.y * p0.y - eps;
         gj = cadd(gj, cscale(T(2) * w.g * p, p0));
-        if (GL_MM(cb) || GL_MP(cb))
-            gj = cadd(gj, cscale(w.r_m0 * idx2, gjac<T>(p0, -dx * link_phase(abei, ab, (i - 1) + (g.Nx - 1) * j), psi[n - 1])));
-        if (GL_PM(cb) || GL_PP(cb))
-            gj = cadd(gj, cscale(w.r_p0 * idx2, gjac<T>(p0, dx * link_phase(abei, ab, i + (g.Nx - 1) * j), psi[n + 1])));
-        if (GL_MM(cb) || GL_PM(cb))
-            gj = cadd(gj, cscale(w.r_0m * idy2, gjac<T>(p0, -dy * link_phase(abei, ab, g.Na + i + g.Nx * (j - 1)), psi[n - g.Nx])));
-        if (GL_MP(cb) || GL_PP(cb))
-            gj = cadd(gj, cscale(w.r_0p * idy2, gjac<T>(p0, dy * link_phase(abei, ab, g.Na + i + g.Nx * j), psi[n + g.Nx])));
+        T sn, cs;  // the links below and left of the node enter with the opposite phase: sin(-x) = -sin(x)
+        if (GL_MM(cb) || GL_MP(cb)) {
+            lk.sc_sum((i - 1) + (g.Nx - 1) * j, dx, sn, cs);
+            gj = cadd(gj, cscale(w.r_m0 * idx2, gjac_sc<T>(p0, -sn, cs, psi[n - 1])));
+        }
+        if (GL_PM(cb) || GL_PP(cb)) {
+            lk.sc_sum(i + (g.Nx - 1) * j, dx, sn, cs);
+            gj = cadd(gj, cscale(w.r_p0 * idx2, gjac_sc<T>(p0, sn, cs, psi[n + 1])));
+        }
+        if (GL_MM(cb) || GL_PM(cb)) {
+            lk.sc_sum(g.Na + i + g.Nx * (j - 1), dy, sn, cs);
+            gj = cadd(gj, cscale(w.r_0m * idy2, gjac_sc<T>(p0, -sn, cs, psi[n - g.Nx])));
+        }
+        if (GL_MP(cb) || GL_PP(cb)) {
+            lk.sc_sum(g.Na + i + g.Nx * j, dy, sn, cs);
+            gj = cadd(gj, cscale(w.r_0p * idy2, gjac_sc<T>(p0, sn, cs, psi[n + g.Nx])));
+        }
     }
     return cscale(GT(g, dxdy), gj);
 }
@@ -176,19 +216,25 @@ __device__ __forceinline__ C2<T> grad_psi_node(const Geo& g, T eps0, const T* ep
 // dF/dA on the x link (xdir) or y link starting at node (i, j) (svirl/cuda/cg.h:124-301),
 // 2*dx*dy included; exact: the boundary links use the exact derivative of the
 // magnetic energy instead of the reference's doubled form.
-template <typename T>
+template <typename T, typename LK>
 __device__ __forceinline__ T grad_A_link(const Geo& g, T kappa2, T H, const C2<T>* psi, const T* abei, const T* ab,
-                                         int n, int i, int j, unsigned cb, bool xdir, bool exact = false) {
+                                         const LK& lk, int n, int i, int j, unsigned cb, bool xdir, bool exact = false) {
     T c = kappa2 * (exact ? curlcurl_link_exact<T>(g, abei, ab, H, i, j, xdir) : curlcurl_link<T>(g, abei, ab, H, i, j, xdir));
     if (xdir) {
         if (GL_PM(cb) || GL_PP(cb)) {
             const T r = T(0.5) * ((GL_PM(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));
-            c += -r * GT(g, idx) * js_of<T>(psi[n], GT(g, dx) * link_phase(abei, ab, i + (g.Nx - 1) * j), psi[n + 1]);
+            T sn, cs;
+            lk.sc_sum(i + (g.Nx - 1) * j, GT(g, dx), sn, cs);
+            const C2<T> p0 = psi[n], p1 = psi[n + 1];
+            c += -r * GT(g, idx) * ((p0.x * p1.y - p0.y * p1.x) * cs - (p0.x * p1.x + p0.y * p1.y) * sn);
         }
     } else {
         if (GL_MP(cb) || GL_PP(cb)) {
             const T r = T(0.5) * ((GL_MP(cb) ? T(1) : T(0)) + (GL_PP(cb) ? T(1) : T(0)));
-            c += -r * GT(g, idy) * js_of<T>(psi[n], GT(g, dy) * link_phase(abei, ab, g.Na + i + g.Nx * j), psi[n + g.Nx]);
+            T sn, cs;
+            lk.sc_sum(g.Na + i + g.Nx * j, GT(g, dy), sn, cs);
+            const C2<T> p0 = psi[n], p1 = psi[n + g.Nx];
+            c += -r * GT(g, idy) * ((p0.x * p1.y - p0.y * p1.x) * cs - (p0.x * p1.x + p0.y * p1.y) * sn);
         }
     }
     return T(2) * GT(g, dxdy) * c;
@@ -198,9 +244,9 @@ __device__ __forceinline__ T grad_A_link(const Geo& g, T kappa2, T H, const C2<T
 // NV = 5: c0..c4 of F(psi + a dpsi) (svirl/cuda/cg.h:314-474); NV = 17: c00..c04,
 // c10..c14, c20..c24, c30, c40 of F(psi + a_psi dpsi, A + a_A dA)
 // (svirl/cuda/cg.h:477-731).  dpsi(m) and dA(l) give the search direction.
-template <typename T, int NV, typename FD, typename FA>
+template <typename T, int NV, typename FD, typename FA, typename LK>
 __device__ __forceinline__ void coef_node(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H, const C2<T>* psi,
-                                          const T* abei, const T* ab, int n, int i, int j, unsigned cb,
+                                          const T* abei, const T* ab, const LK& lk, int n, int i, int j, unsigned cb,
                                           const FD& dpsi, const FA& dA, T (&c)[NV]) {
     const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
     const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
@@ -229,12 +275,9 @@ __device__ __forceinline__ void coef_node(const Geo& g, T kappa2, T eps0, const 
             const int m1 = dir == 0 ? n + 1 : n + g.Nx;
             const T d = dir == 0 ? dx : dy;
             const T wr = (dir == 0 ? w.r_p0 : w.r_0p) * (dir == 0 ? idx2 : idy2);
-            T ph = T(0);
-            if (abei) ph += d * abei[nl];
-            if (ab) ph += d * ab[nl];
             const C2<T> p1 = psi[m1], d1 = dpsi(m1);
             T s, cs;
-            sincos_t(ph, &s, &cs);
+            lk.sc_split(nl, d, s, cs);
             const C2<T> gp = grad_c_sc<T>(p0, s, cs, p1), gd = grad_c_sc<T>(d0, s, cs, d1);
             const T gg_p = gp.x * gp.x + gp.y * gp.y;
             const T gg_d = gd.x * gd.x + gd.y * gd.y;

@@ -18,7 +18,7 @@ k_energy(Geo g, double kappa2, double eps0, const T* eps_sp, double H, const uin
          const C2<T>* __restrict__ psi, const T* abei, const T* ab, double* partials, unsigned* counter, double* out) {
     const int n = blockIdx.x * kThreads + threadIdx.x;
     T v[1] = {T(0)};
-    if (n < g.N) v[0] = energy_density<T>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, mt, psi, abei, ab, n);
+    if (n < g.N) v[0] = energy_density<T>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, mt, psi, abei, ab, PhaseLinks<T>{abei, ab}, n);
     grid_sum_finish(v, partials, counter, out, g.dxdy);
 }
 
