@@ -6,8 +6,9 @@
 // ReLU derivative applied while gathering).  Per K chunk of 64 the four warps
 // gather the implicit-GEMM operands into shared memory in the K-major core-matrix
 // layout (8 rows x 16 bytes per core matrix, no swizzle), one thread issues four
-// 128x64x16 MMAs and commits them to an mbarrier, and the CTA waits on it before
-// the next chunk overwrites the operands.  The epilogue reads the accumulator
+// 128x64x16 MMAs and commits them to that stage's mbarrier, and the loads of the
+// next chunk go out while they run; there are two operand stages, and a stage is
+// refilled only after the MMAs that read it have signalled completion.  The epilogue reads the accumulator
 // with tcgen05.ld (each warp its 32 TMEM lanes = 32 output pixels), adds the
 // bias, applies the ReLU and stores bfloat16.  Every wait is bounded; on a
 // timeout the kernel records an error, skips its stores and still frees its
@@ -26,7 +27,8 @@ typedef __nv_bfloat16 bf16;
 constexpr int TM = 128, TN = 64, TK = 64, NTH = 128;
 constexpr int A_BYTES = TM * TK * 2;        // 16 KB
 constexpr int B_BYTES = TN * TK * 2;        // 8 KB
-constexpr int SMEM_BYTES = A_BYTES + B_BYTES + 16;
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int SMEM_BYTES = 2 * STAGE_BYTES + 32;  // two operand stages, two barriers, the TMEM address
 constexpr uint32_t kTmemCols = 64;          // FP32 accumulator: TN columns
 constexpr uint32_t kSpinLimit = 1u << 20;   // mbarrier polls before giving up
 // instruction descriptor (kind::f16): D f32 (bits 4-5 = 1), A bf16 (7-9 = 1),
@@ -96,10 +98,8 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
           const bf16* __restrict__ Bsrc, const float* __restrict__ bias, bf16* __restrict__ o1, int Co1,
           bf16* __restrict__ o2, int Co2, int NB, int H, int W, int* err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* As = smem;
-    unsigned char* Bs = smem + A_BYTES;
-    uint64_t* bar = (uint64_t*)(smem + A_BYTES + B_BYTES);
-    uint32_t* tslot = (uint32_t*)(smem + A_BYTES + B_BYTES + 8);
+    uint64_t* bar = (uint64_t*)(smem + 2 * STAGE_BYTES);  // bar[s]: MMAs of stage s done
+    uint32_t* tslot = (uint32_t*)(smem + 2 * STAGE_BYTES + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Ca = Ca1 + Ca2, K = 9 * Ca, Nout = Co1 + Co2, P = NB * H * W;
     const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
@@ -112,6 +112,7 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar + 1)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -133,13 +134,14 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
     }
     const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
     const int nk = (K + TK - 1) / TK;
-    uint32_t phase = 0;
-    bool ok = true;
-    for (int kt = 0; kt < nk; ++kt) {
-        const int kc = kt * TK;
+    // operands of the next chunk are loaded into registers while the tensor core
+    // works on the current one; two shared-memory stages, each reused only after
+    // the MMAs that read it (two chunks earlier) have completed
+    uint4 ra[8], rb[4];
+    auto gather = [&](int kc) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const int v = tid + i * NTH, row = v >> 3, kv = v & 7, k = kc + kv * 8;
+            const int kv = (tid + i * NTH) & 7, k = kc + kv * 8;
             uint4 a = z4;
             if (pok[i] && k < K) {
                 const int tap = k / Ca, c = k - tap * Ca;
@@ -154,7 +156,7 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
                     }
                 }
             }
-            *(uint4*)(As + core_off(row, kv * 8, TK / 8)) = a;
+            ra[i] = a;
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -169,7 +171,33 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
                     b = *(const uint4*)(Bsrc + ((size_t)tap * Nout + nn) * Ca + c);
                 }
             }
-            *(uint4*)(Bs + core_off(row, kv * 8, TK / 8)) = b;
+            rb[i] = b;
+        }
+    };
+    uint32_t phase[2] = {0u, 0u};
+    bool ok = true;
+    gather(0);
+    for (int kt = 0; kt < nk; ++kt) {
+        const int st = kt & 1;
+        unsigned char* As = smem + st * STAGE_BYTES;
+        unsigned char* Bs = As + A_BYTES;
+        if (kt >= 2) {  // the MMAs of chunk kt-2 read this stage
+            const bool got = wait_parity(saddr(bar + st), phase[st]);
+            phase[st] ^= 1u;
+            if (__syncthreads_or(got ? 0 : 1)) {
+                ok = false;
+                break;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int v = tid + i * NTH;
+            *(uint4*)(As + core_off(v >> 3, (v & 7) * 8, TK / 8)) = ra[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int v = tid + i * NTH;
+            *(uint4*)(Bs + core_off(v >> 3, (v & 7) * 8, TK / 8)) = rb[i];
         }
         // generic-proxy stores -> visible to the tensor core's (async-proxy) reads
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -183,18 +211,20 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
                 mma_f16(tmem, ad, bd, kIdesc, (kt > 0 || j > 0) ? 1u : 0u);
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                             saddr(bar))
+                             saddr(bar + st))
                          : "memory");
         }
-        // the MMAs read As/Bs: wait for them before the next chunk overwrites
-        const bool got = wait_parity(saddr(bar), phase);
-        phase ^= 1u;
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        if (__syncthreads_or(got ? 0 : 1)) {
-            ok = false;
-            break;
-        }
+        if (kt + 1 < nk) gather((kt + 1) * TK);
     }
+    // the last one or two chunks' MMAs (each stage's most recent commit)
+    for (int q = nk >= 2 ? nk - 2 : 0; q < nk; ++q) {
+        const int st = q & 1;
+        const bool got = wait_parity(saddr(bar + st), phase[st]);
+        phase[st] ^= 1u;
+        if (!got) ok = false;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (__syncthreads_or(ok ? 0 : 1)) ok = false;
     if (ok) {
         const int p = m0 + warp * 32 + lane;  // TMEM lane = output row
 #pragma unroll
@@ -228,10 +258,8 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
                 }
             }
         }
-    } else {
-        // a commit that never arrived: wait once more (bounded) before the memory goes
-        wait_parity(saddr(bar), phase ^ 1u);
-        if (tid == 0) atomicExch(err, 1);
+    } else if (tid == 0) {
+        atomicExch(err, 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
@@ -242,6 +270,13 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
 }  // namespace glnn_tc
 
 using namespace glnn_tc;
+
+// The kernels use more than the default 48 KB of dynamic shared memory.
+template <int MODE, int RELU> static cudaError_t conv_tc_smem_attr() {
+    static cudaError_t e = cudaFuncSetAttribute(k_conv_tc<MODE, RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                SMEM_BYTES);
+    return e;
+}
 
 static int conv_tc_args_ok(int c1, int c2, int n, int h, int w, int cout) {
     return n > 0 && h > 0 && w > 0 && c1 > 0 && c1 % 8 == 0 && c2 >= 0 && c2 % 8 == 0 && cout > 0 && cout % 8 == 0 &&
@@ -258,6 +293,7 @@ int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, con
     const long long P = (long long)n * h * w;
     dim3 grid((unsigned)((P + TM - 1) / TM), (unsigned)((cout + TN - 1) / TN));
     cudaStream_t s = (cudaStream_t)stream;
+    if ((relu ? conv_tc_smem_attr<0, 1>() : conv_tc_smem_attr<0, 0>()) != cudaSuccess) return GLGPU_E_CUDA;
     if (relu)
         k_conv_tc<0, 1><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)x1, c1, (const bf16*)x2, c2, nullptr, (const bf16*)wb,
                                                      bias, (bf16*)y, cout, nullptr, 0, n, h, w, err);
@@ -276,6 +312,7 @@ int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const voi
     const long long P = (long long)n * h * w;
     dim3 grid((unsigned)((P + TM - 1) / TM), (unsigned)((c1 + c2 + TN - 1) / TN));
     cudaStream_t s = (cudaStream_t)stream;
+    if ((relu ? conv_tc_smem_attr<1, 1>() : conv_tc_smem_attr<1, 0>()) != cudaSuccess) return GLGPU_E_CUDA;
     if (relu)
         k_conv_tc<1, 1><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)dy, cout, nullptr, 0, (const bf16*)y, (const bf16*)wt,
                                                      nullptr, (bf16*)dx1, c1, (bf16*)dx2, c2, n, h, w, err);

@@ -227,22 +227,13 @@ template <typename T> struct PsiRow {
 #ifndef GLGPU_PSI_MIN_CTAS
 #define GLGPU_PSI_MIN_CTAS 1
 #endif
-// row lag between consecutive fused sweeps: 1 (a sweep uses the row its
-// predecessor made in the same step) or 2 (only rows of earlier steps)
-#ifndef GLGPU_PSI_LAG
-#define GLGPU_PSI_LAG 2
-#endif
 
 constexpr int kPsiThreads = GLGPU_PSI_THREADS, kPsiWarps = kPsiThreads / 32;
 template <typename T>
 __global__ void __launch_bounds__(kPsiThreads, GLGPU_PSI_MIN_CTAS)
 k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
             cudaGraphConditionalHandle cond, int use_cond) {
-#if GLGPU_PSI_LAG == 2
-    constexpr int K = kFuse, RR = kStripRows, S = kStripRows + 3 * kFuse - 1;
-#else
     constexpr int K = kFuse, RR = kStripRows, S = kStripRows + 2 * kFuse;
-#endif
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kPsiWarps + (threadIdx.x >> 5), nw = gridDim.x * kPsiWarps;
     int cur_inst = -1, k = 0, count = 0, done = 1;
@@ -311,81 +302,6 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             q.eps = (ldc && eps_sp) ? __ldg(&eps_sp[n]) : eps0;
             return q;
         };
-#if GLGPU_PSI_LAG == 2
-        // The fused sweeps lag two rows apart: sweep l produces row y_1(s) - 2(l-1) at
-        // step s from rows that sweep l-1 produced in the three previous steps, so the
-        // sweeps of one step are independent chains (instruction-level parallelism).
-        C2<T> w0m2 = z, w0m1 = z;  // psi^(k) on rows y_0(s)-2 and y_0(s)-1
-        C2<T> Wl[K][3];            // Wl[l]: rows of sweep l made in steps s-3, s-2, s-1 (l = 1..K-1)
-#pragma unroll
-        for (int l = 0; l < K; ++l) Wl[l][0] = Wl[l][1] = Wl[l][2] = z;
-        PsiRow<T> D[2 * K];        // D[m]: per-row inputs of row y_1(s) - m, y_1(s) = j0 - K + s - 1
-#pragma unroll
-        for (int m = 0; m < 2 * K; ++m) D[m] = PsiRow<T>{z, z, z, T(0), 0u};
-        // loaded inputs of row y -> sweep inputs (done one step after the loads were issued)
-        auto finish_side = [&](const PsiSide<T>& q, int y) -> PsiRow<T> {
-            PsiRow<T> r;
-            r.ua = q.ua;
-            r.ub = q.ub;
-            r.cd = q.cd;
-            r.rq = q.rr;
-            if (lang && calc_lane && y >= 0 && y < Ny) {
-                const uint32_t n = (uint32_t)(i + Nx * y);
-                r.rq.x += lc * (rand_1<T>(n, rt) - T(0.5));
-                r.rq.y += lc * (rand_2<T>(n, rt) - T(0.5));
-            }
-            r.inv = (q.cd & 3u) ? psi_diag_inv<T>(r.rq, q.eps, q.cd, dt, idx2, idy2) : T(0);
-            return r;
-        };
-        C2<T> nx_p = load_psi(j0 - K);
-        PsiSide<T> nx_s = load_side(j0 - K - 1);
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const C2<T> r0 = nx_p;  // psi^(k) on row y_0(s) = j0 - K + s
-#pragma unroll
-            for (int m = 2 * K - 1; m >= 1; --m) D[m] = D[m - 1];
-            D[0] = finish_side(nx_s, j0 - K + s - 1);
-            if (s + 1 < S && s + 1 - K <= RR - 1 + K) nx_p = load_psi(j0 - K + s + 1);  // rows any sweep needs
-            if (s + 1 < S && s - K <= RR - 2 + K) nx_s = load_side(j0 - K + s);
-            C2<T> outl[K + 1];
-#pragma unroll
-            for (int l = 1; l <= K; ++l) {
-                C2<T> out = z;
-                const int yr = s - K - (2 * l - 1);  // row of sweep l in this step, relative to j0
-                if (yr >= -(K - l) && yr <= RR - 1 + (K - l)) {  // rows the later sweeps need
-                    const int y = j0 + yr;
-                    const C2<T> pm = l == 1 ? w0m2 : Wl[l - 1][0];
-                    const C2<T> pc = l == 1 ? w0m1 : Wl[l - 1][1];
-                    const C2<T> pp = l == 1 ? r0 : Wl[l - 1][2];
-                    const C2<T> pl = shfl_up_c<T>(pc, 1), pr = shfl_down_c<T>(pc, 1);
-                    const PsiRow<T>& d = D[2 * (l - 1)];
-                    const C2<T> ual = shfl_up_c<T>(d.ua, 1);
-                    const bool node = calc_lane && y >= 0 && y < Ny;
-                    if (node) {
-                        out = psi_node<T>(pl, pr, pm, pp, ual, d.ua, D[2 * (l - 1) + 1].ub, d.ub, d.rq, d.inv, d.cd,
-                                          dt, idx2, idy2);
-                        if (own_lane && yr >= 0 && yr < RR) {
-                            outb[l - 1][i + Nx * y] = out;
-                            // max(|d re|, |d im|); a NaN component counts as 0 (the reference's
-                            // int conversion), fmax drops NaN operands
-                            const T dr = fabs(out.x - pc.x), di = fabs(out.y - pc.y);
-                            if (!(dr + di == dr + di)) wnan[l - 1] = true;
-                            wmax[l - 1] = fmax(wmax[l - 1], fmax(dr, di));
-                        }
-                    }
-                }
-                outl[l] = out;
-            }
-            w0m2 = w0m1;
-            w0m1 = r0;
-#pragma unroll
-            for (int l = 1; l < K; ++l) {
-                Wl[l][0] = Wl[l][1];
-                Wl[l][1] = Wl[l][2];
-                Wl[l][2] = outl[l];
-            }
-        }
-#else
         // window of sweep l-1 (l = 1..K) as seen by sweep l: rows y-1 and y
         C2<T> wp[K], wc[K];
         PsiRow<T> D[K + 1];  // D[m]: per-row inputs of row (j0 - K + s - 1) - m
@@ -449,7 +365,6 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
                 newrow = out;
             }
         }
-#endif
         ++count;
     }
     if (cur_inst >= 0 && !done) warp_flush<T>(insts, cur_inst, k, wmax, wnan, count, loop);
