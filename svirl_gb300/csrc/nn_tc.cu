@@ -6,9 +6,10 @@
 // ReLU derivative applied while gathering).  Per K chunk of 64 the four warps
 // gather the implicit-GEMM operands into shared memory in the K-major core-matrix
 // layout (8 rows x 16 bytes per core matrix, no swizzle), one thread issues four
-// 128x64x16 MMAs and commits them to that stage's mbarrier, and the loads of the
-// next chunk go out while they run; there are two operand stages, and a stage is
-// refilled only after the MMAs that read it have signalled completion.  The epilogue reads the accumulator
+// 128x64x16 MMAs and commits them to the stage's mbarrier, and the loads of the
+// next chunk go out while they run; a stage is refilled only after the MMAs that
+// read it have signalled completion.  One stage (24 KB) keeps about nine CTAs per
+// SM; two stages measured slower (fewer CTAs per SM).  The epilogue reads the accumulator
 // with tcgen05.ld (each warp its 32 TMEM lanes = 32 output pixels), adds the
 // bias, applies the ReLU and stores bfloat16.  Every wait is bounded; on a
 // timeout the kernel records an error, skips its stores and still frees its
@@ -27,8 +28,12 @@ typedef __nv_bfloat16 bf16;
 constexpr int TM = 128, TN = 64, TK = 64, NTH = 128;
 constexpr int A_BYTES = TM * TK * 2;        // 16 KB
 constexpr int B_BYTES = TN * TK * 2;        // 8 KB
+#ifndef GLNN_TC_STAGES
+#define GLNN_TC_STAGES 1
+#endif
+constexpr int kStages = GLNN_TC_STAGES;       // operand stages in shared memory (1 or 2)
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int SMEM_BYTES = 2 * STAGE_BYTES + 32;  // two operand stages, two barriers, the TMEM address
+constexpr int SMEM_BYTES = kStages * STAGE_BYTES + 32;  // stages, a barrier per stage, the TMEM address
 constexpr uint32_t kTmemCols = 64;          // FP32 accumulator: TN columns
 constexpr uint32_t kSpinLimit = 1u << 20;   // mbarrier polls before giving up
 // instruction descriptor (kind::f16): D f32 (bits 4-5 = 1), A bf16 (7-9 = 1),
@@ -98,8 +103,8 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
           const bf16* __restrict__ Bsrc, const float* __restrict__ bias, bf16* __restrict__ o1, int Co1,
           bf16* __restrict__ o2, int Co2, int NB, int H, int W, int* err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    uint64_t* bar = (uint64_t*)(smem + 2 * STAGE_BYTES);  // bar[s]: MMAs of stage s done
-    uint32_t* tslot = (uint32_t*)(smem + 2 * STAGE_BYTES + 16);
+    uint64_t* bar = (uint64_t*)(smem + kStages * STAGE_BYTES);  // bar[s]: MMAs of stage s done
+    uint32_t* tslot = (uint32_t*)(smem + kStages * STAGE_BYTES + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Ca = Ca1 + Ca2, K = 9 * Ca, Nout = Co1 + Co2, P = NB * H * W;
     const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
@@ -111,8 +116,8 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar + 1)) : "memory");
+        for (int q = 0; q < kStages; ++q)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar + q)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -178,10 +183,10 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
     bool ok = true;
     gather(0);
     for (int kt = 0; kt < nk; ++kt) {
-        const int st = kt & 1;
+        const int st = kt % kStages;
         unsigned char* As = smem + st * STAGE_BYTES;
         unsigned char* Bs = As + A_BYTES;
-        if (kt >= 2) {  // the MMAs of chunk kt-2 read this stage
+        if (kt >= kStages) {  // the MMAs of chunk kt - kStages read this stage
             const bool got = wait_parity(saddr(bar + st), phase[st]);
             phase[st] ^= 1u;
             if (__syncthreads_or(got ? 0 : 1)) {
@@ -216,9 +221,9 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
         }
         if (kt + 1 < nk) gather((kt + 1) * TK);
     }
-    // the last one or two chunks' MMAs (each stage's most recent commit)
-    for (int q = nk >= 2 ? nk - 2 : 0; q < nk; ++q) {
-        const int st = q & 1;
+    // each stage's most recent commit (the last kStages chunks)
+    for (int q = nk >= kStages ? nk - kStages : 0; q < nk; ++q) {
+        const int st = q % kStages;
         const bool got = wait_parity(saddr(bar + st), phase[st]);
         phase[st] ^= 1u;
         if (!got) ok = false;
