@@ -4,11 +4,16 @@
 // for (alpha_psi, alpha_A)), with the step length, beta and the stop test decided
 // on the device, so a whole CG run is one CUDA-graph launch for all instances.
 //
-// Per iteration: tile kernels (256 nodes of one instance per CTA) write per-tile
-// FP64 partial sums; one warp per instance then adds its tiles' partials in tile
-// order (deterministic) and takes the scalar decisions:
-//   kb_grad -> kb_inst_beta -> kb_dir_coef -> kb_inst_alpha -> kb_update ->
-//   kb_energy -> kb_inst_stop (sets the WHILE condition).
+// Per iteration three tile kernels (kCGTile nodes of one instance per CTA) write
+// per-tile FP64 partial sums; in each, the CTA that finishes an instance's last
+// tile adds that instance's partials in tile order (one warp, deterministic) and
+// takes the instance's scalar decisions:
+//   kb_grad (+ beta, gradient stop) -> kb_dir_coef (+ step lengths) ->
+//   kb_step (update, energy, + energy stop; the launch's last CTA sets the WHILE
+//   condition).
+// The state alternates between buffers 0 and 1 (psi[pi], ab[pi]) so that kb_step
+// reads the old state while it writes the new one; kb_finish copies it back to
+// buffer 0 at the end of a call.
 // alpha: kappa = inf, the smallest non-negative real root of dP/dalpha (the
 // reference uses numpy polyroots, svirl/solvers/cg.py:227-235); finite kappa, a
 // damped Newton descent of the 2-D polynomial from (0, 0) (the reference uses
@@ -29,6 +34,11 @@ constexpr int kPart = 17;  // doubles of per-tile partials
 // reduction's cost is shared by kCGRep nodes.
 constexpr int kCGRep = 4;
 constexpr int kCGTile = kCGRep * kThreads;
+// Resident CTAs per SM asked of the compiler for the two stencil-heavy FP32 CG
+// kernels (caps their registers at 65536 / (kThreads * GLGPU_CG_MINB)).
+#ifndef GLGPU_CG_MINB
+#define GLGPU_CG_MINB 4
+#endif
 
 struct CGLoop {
     int active;
@@ -37,7 +47,7 @@ struct CGLoop {
     int pad_;      // last decision of the WHILE loop (read by the host-driven loop)
     double rtol, gtol;
     int flags;     // GLGPU_CG_* bits
-    int pad2_;
+    int ticket;    // CTAs finished in the running launch of the step kernel
 };
 
 template <typename T>
@@ -45,18 +55,113 @@ __device__ __forceinline__ void store_partials(const double* v, int nv, double* 
     for (int k = 0; k < nv; ++k) out[k] = v[k];
 }
 
+// Components 0..NV-1 of the partials of one instance's tiles summed by one
+// warp (lane l adds tiles l, l+32, ... in order, then a fixed shuffle tree),
+// every lane receiving the sums.  All NV components are loaded per tile, so the
+// loads and the shuffle levels of the components overlap.
+template <int NV>
+__device__ __forceinline__ void warp_tile_sums(const double* partials, int tile0, int ntiles, double (&s)[NV]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) s[k] = 0.0;
+#pragma unroll 4
+    for (int q = lane; q < ntiles; q += 32) {
+        const double* p = partials + (size_t)(tile0 + q) * kPart;
+        double t[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) t[k] = __ldcg(p + k);  // written by other CTAs of this launch
+#pragma unroll
+        for (int k = 0; k < NV; ++k) s[k] += t[k];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) s[k] += __shfl_down_sync(0xffffffffu, s[k], o);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) s[k] = __shfl_sync(0xffffffffu, s[k], 0);
+}
+
+// The same sums by a whole CTA, times `scale`, into out[] (shared memory): warp w
+// adds components w, w + kWarps, ..., each exactly as warp_tile_sums does, so
+// the FP64 additions are spread over the CTA's warps.  Ends with a barrier.
+template <int NV>
+__device__ __forceinline__ void cta_tile_sums(const double* partials, int tile0, int ntiles, double scale,
+                                              double* out) {
+    constexpr int KPW = (NV + kWarps - 1) / kWarps;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double s[KPW];
+#pragma unroll
+    for (int c = 0; c < KPW; ++c) s[c] = 0.0;
+    for (int q = lane; q < ntiles; q += 32) {
+        const double* p = partials + (size_t)(tile0 + q) * kPart;
+#pragma unroll
+        for (int c = 0; c < KPW; ++c)
+            if (w + c * kWarps < NV) s[c] += __ldcg(p + w + c * kWarps);  // written by other CTAs of this launch
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < KPW; ++c) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < KPW; ++c)
+            if (w + c * kWarps < NV) out[w + c * kWarps] = s[c] * scale;
+    __syncthreads();
+}
+
+// beta (Polak-Ribiere+, cg.py:422-449) and the gradient-norm stop of one
+// instance, by the CTA that finished its last tile
+__device__ __noinline__ void inst_beta(const Inst& I, CGState* cs, const double* partials, CGLoop* loop) {
+    __shared__ double v[5];
+    cta_tile_sums<5>(partials, I.tile0, I.ntiles, 1.0, v);
+    if (threadIdx.x != 0) return;
+    if (cs->iter > 0) {
+        cs->beta_psi = fmax(v[0] / v[1], 0.0);
+        cs->beta_A = I.solveA ? fmax(v[2] / v[3], 0.0) : 0.0;
+    } else {
+        cs->beta_psi = 0.0;
+        cs->beta_A = 0.0;
+        cs->g2_0 = v[4];
+    }
+    cs->g2 = v[4];
+    cs->gi = 1 - cs->gi;
+    const bool abs_tol = (loop->flags & GLGPU_CG_GTOL_ABS) != 0;
+    const double thr = abs_tol ? loop->gtol * loop->gtol : loop->gtol * loop->gtol * cs->g2_0;
+    if ((cs->iter > 0 || abs_tol) && !(v[4] > thr)) {
+        cs->done = 1;
+        cs->status = 1;
+        atomicSub(&loop->active, 1);
+    }
+}
+
+// The CTA that finishes the last tile of an instance in a launch (a ticket per
+// instance) takes that instance's scalar decisions: the instance's partials are
+// then all stored.  The ticket is left at 0 for the next launch.
+__device__ __forceinline__ bool last_cta_of_instance(CGState* cs, int ntiles) {
+    __shared__ int s_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const int tk = atomicAdd(&cs->ticket, 1);
+        s_last = tk == ntiles - 1;
+        if (s_last) cs->ticket = 0;
+    }
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last;
+}
+
 // gradient (new buffer), Polak-Ribiere sums and |g|^2 per tile
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials) {
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB : 1)
+kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop) {
     const Tile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
-    const CGState* cs = I.cg;
+    CGState* cs = I.cg;
     if (*(volatile const int*)&cs->done) return;
     const Geo g = I.g;
-    const int gi = cs->gi;
-    const C2<T>* psi = (const C2<T>*)I.psi[0];
-    const T* ab = (const T*)I.ab[0];
+    const int gi = cs->gi, pi = cs->pi;
+    const C2<T>* psi = (const C2<T>*)I.psi[pi];
+    const T* ab = (const T*)I.ab[I.solveA ? pi : 0];
     const T* abei = (const T*)I.abei;
     C2<T>* G = (C2<T>*)I.gpsi[1 - gi];
     const C2<T>* Gp = (const C2<T>*)I.gpsi[gi];
@@ -95,114 +200,27 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
     double vs[5];
     block_sum<5>(v, vs);
     if (threadIdx.x == 0) store_partials<T>(vs, 5, partials + (size_t)blockIdx.x * kPart);
-}
-
-// Sum of component k of the partials of instance I's tiles, in tile order, by one warp.
-__device__ __forceinline__ double warp_tile_sum(const double* partials, int tile0, int ntiles, int k) {
-    const int lane = threadIdx.x & 31;
-    double s = 0.0;
-    for (int q = lane; q < ntiles; q += 32) s += partials[(size_t)(tile0 + q) * kPart + k];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    return __shfl_sync(0xffffffffu, s, 0);
-}
-
-// beta (Polak-Ribiere+, cg.py:422-449) and the gradient-norm stop, one warp per instance
-__global__ void __launch_bounds__(128)
-kb_inst_beta(const Inst* __restrict__ insts, int ninst, const double* __restrict__ partials,
-                             CGLoop* loop) {
-    const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (q >= ninst) return;
-    const Inst& I = insts[q];
-    CGState* cs = I.cg;
-    if (cs->done) return;
-    double v[5];
-    for (int k = 0; k < 5; ++k) v[k] = warp_tile_sum(partials, I.tile0, I.ntiles, k);
-    if ((threadIdx.x & 31) != 0) return;
-    if (cs->iter > 0) {
-        cs->beta_psi = fmax(v[0] / v[1], 0.0);
-        cs->beta_A = I.solveA ? fmax(v[2] / v[3], 0.0) : 0.0;
-    } else {
-        cs->beta_psi = 0.0;
-        cs->beta_A = 0.0;
-        cs->g2_0 = v[4];
-    }
-    cs->g2 = v[4];
-    cs->gi = 1 - cs->gi;
-    const bool abs_tol = (loop->flags & GLGPU_CG_GTOL_ABS) != 0;
-    const double thr = abs_tol ? loop->gtol * loop->gtol : loop->gtol * loop->gtol * cs->g2_0;
-    if ((cs->iter > 0 || abs_tol) && !(v[4] > thr)) {
-        cs->done = 1;
-        cs->status = 1;
-        atomicSub(&loop->active, 1);
-    }
-}
-
-// new direction (written) and the per-tile line-search coefficient partials
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials) {
-    const Tile t = tiles[blockIdx.x];
-    const Inst& I = insts[t.inst];
-    const CGState* cs = I.cg;
-    if (*(volatile const int*)&cs->done) return;
-    const Geo g = I.g;
-    const int gi = cs->gi, di = cs->di;
-    const T bp = (T)cs->beta_psi, bA = (T)cs->beta_A;
-    const C2<T>* psi = (const C2<T>*)I.psi[0];
-    const T* ab = (const T*)I.ab[0];
-    const T* abei = (const T*)I.abei;
-    const C2<T>* G = (const C2<T>*)I.gpsi[gi];
-    const T* GA = (const T*)I.gA[gi];
-    const C2<T>* dO = (const C2<T>*)I.dpsi[di];
-    const T* dAO = (const T*)I.dA[di];
-    C2<T>* dN = (C2<T>*)I.dpsi[1 - di];
-    T* dAN = (T*)I.dA[1 - di];
-    const TableLinks<T> lk{(const C2<T>*)I.U};
-    auto dpsi = [&](int m) -> C2<T> {
-        const C2<T> o = dO[m], gg = G[m];
-        return cmk<T>(bp * o.x - gg.x, bp * o.y - gg.y);
-    };
-    auto dA = [&](int m) -> T { return bA * dAO[m] - GA[m]; };
-    T c[17];
-#pragma unroll
-    for (int k = 0; k < 17; ++k) c[k] = T(0);
-#pragma unroll 1
-    for (int r = 0; r < kCGRep; ++r) {
-    const int n = t.n0 + threadIdx.x + r * kThreads;
-    if (n < g.N) {
-        const int i = n % g.Nx, j = n / g.Nx;
-        const unsigned cb = cell_bits(g, I.mt, i, j);
-        dN[n] = dpsi(n);
-        const T eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
-        if (I.solveA) {
-            if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
-            if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
-            coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb,
-                             dpsi, dA, c);
-        } else {
-            T c5[5] = {T(0), T(0), T(0), T(0), T(0)};
-            coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb, dpsi, dA, c5);
-            c[0] += c5[0]; c[5] += c5[1]; c[10] += c5[2]; c[15] += c5[3]; c[16] += c5[4];
-        }
-    }
-    }
-    double cs17[17];
-    block_sum<17>(c, cs17);
-    if (threadIdx.x == 0) store_partials<T>(cs17, 17, partials + (size_t)blockIdx.x * kPart);
+    if (last_cta_of_instance(cs, I.ntiles)) inst_beta(I, cs, partials, loop);
 }
 
 // GB300 runs FP64 at a small fraction of its FP32 rate, and a single thread's
 // chain of dependent FP64 operations is slow: the step lengths are found in FP32
-// and then polished by FP64 Newton steps, which restore full FP64 accuracy.
+// and, for FP64 instances, polished by FP64 Newton steps, which restore full FP64
+// accuracy (FP32 instances polish in FP32).
 
 // Real roots of d0 + d1 a + d2 a^2 + d3 a^3 (FP32 closed form, each root polished
-// by two FP64 Newton steps on the cubic); returns the smallest root >= 0 or -1.
+// by two Newton steps on the cubic, in FP64 when FP64); returns the smallest
+// root >= 0 or -1.
+template <bool FP64>
 __device__ double smallest_nonneg_root_cubic(double d0, double d1, double d2, double d3) {
     float roots[3];
     int nr = 0;
     const double scale = fabs(d0) + fabs(d1) + fabs(d2) + fabs(d3);
     if (!(scale > 0.0)) return -1.0;
-    const float f0 = (float)(d0 / scale), f1 = (float)(d1 / scale), f2 = (float)(d2 / scale), f3 = (float)(d3 / scale);
+    int e;
+    frexp(scale, &e);
+    const double inv = ldexp(1.0, -e);  // power of two: the scaling is exact
+    const float f0 = (float)(d0 * inv), f1 = (float)(d1 * inv), f2 = (float)(d2 * inv), f3 = (float)(d3 * inv);
     if (fabsf(f3) <= 1e-7f) {
         if (fabsf(f2) <= 1e-7f) {
             if (f1 != 0.f) roots[nr++] = -f0 / f1;
@@ -232,10 +250,21 @@ __device__ double smallest_nonneg_root_cubic(double d0, double d1, double d2, do
     }
     double best = -1.0;
     for (int k = 0; k < nr; ++k) {
-        double x = (double)roots[k];
-        for (int it = 0; it < 2; ++it) {  // Newton polish on the cubic, FP64
-            const double f = fma(fma(fma(d3, x, d2), x, d1), x, d0), df = fma(fma(3.0 * d3, x, 2.0 * d2), x, d1);
-            if (df != 0.0) x -= f / df;
+        double x;
+        if (FP64) {
+            x = (double)roots[k];
+            for (int it = 0; it < 2; ++it) {  // Newton polish on the cubic, FP64
+                const double f = fma(fma(fma(d3, x, d2), x, d1), x, d0), df = fma(fma(3.0 * d3, x, 2.0 * d2), x, d1);
+                if (df != 0.0) x -= f / df;
+            }
+        } else {
+            float xf = roots[k];
+            for (int it = 0; it < 2; ++it) {  // Newton polish on the scaled cubic, FP32
+                const float f = fmaf(fmaf(fmaf(f3, xf, f2), xf, f1), xf, f0);
+                const float df = fmaf(fmaf(3.f * f3, xf, 2.f * f2), xf, f1);
+                if (df != 0.f) xf -= f / df;
+            }
+            x = (double)xf;
         }
         if (x >= 0.0 && (best < 0.0 || x < best)) best = x;
     }
@@ -291,23 +320,13 @@ __device__ __forceinline__ void newton_dir(const P2<T>& P, T& sa, T& sb) {
 }
 
 // Local minimum of the 2-D polynomial reached by a damped Newton descent from
-// (0, 0) (Armijo backtracking) in FP32, then two FP64 Newton steps.  The
-// polynomial is scaled to O(1) coefficients first.
-__device__ bool minimise_poly2(const double (&c17)[17], double* a_out, double* b_out) {
-    double scale = 0.0;
-    for (int k = 1; k < 17; ++k) scale = fmax(scale, fabs(c17[k]));
-    if (!(scale > 0.0)) {
-        *a_out = *b_out = 0.0;
-        return true;
-    }
+// (0, 0) (Armijo backtracking) in FP32, then, when FP64, two FP64 Newton steps.
+// cf / cd: the coefficients scaled to O(1) (c00 = 0), in FP32 / FP64.
+template <bool FP64>
+__device__ bool minimise_poly2(const float* cfs, const double* cds, double* a_out, double* b_out) {
     float cf[17];
-    double cd[17];
-    cf[0] = 0.f;
-    cd[0] = 0.0;
-    for (int k = 1; k < 17; ++k) {
-        cd[k] = c17[k] / scale;
-        cf[k] = (float)cd[k];
-    }
+#pragma unroll
+    for (int k = 0; k < 17; ++k) cf[k] = cfs[k];
     float a = 0.f, b = 0.f;
     P2<float> P = poly2<float>(cf, a, b);
     const float g0 = sqrtf(P.fa * P.fa + P.fb * P.fb);
@@ -335,39 +354,61 @@ __device__ bool minimise_poly2(const double (&c17)[17], double* a_out, double* b
         if (fabsf(t * sa) + fabsf(t * sb) <= 1e-7f * (1.f + fabsf(a) + fabsf(b))) break;
     }
     double ad = a, bd = b;
+    if (!FP64) {
+        *a_out = ad;
+        *b_out = bd;
+        return isfinite(a) && isfinite(b);
+    }
+    double cd[17];
+#pragma unroll
+    for (int k = 0; k < 17; ++k) cd[k] = cds[k];
     for (int it = 0; it < 2; ++it) {  // FP64 polish
         const P2<double> Q = poly2<double>(cd, ad, bd);
         const double det = Q.faa * Q.fbb - Q.fab * Q.fab;
         if (!(Q.faa > 0.0 && det > 0.0)) break;
-        ad += -(Q.fbb * Q.fa - Q.fab * Q.fb) / det;
-        bd += -(-Q.fab * Q.fa + Q.faa * Q.fb) / det;
+        const double idet = 1.0 / det;
+        ad -= (Q.fbb * Q.fa - Q.fab * Q.fb) * idet;
+        bd -= (Q.faa * Q.fb - Q.fab * Q.fa) * idet;
     }
     *a_out = ad;
     *b_out = bd;
     return isfinite(ad) && isfinite(bd);
 }
 
-// coefficients of each instance and its step lengths, one warp per instance
-__global__ void __launch_bounds__(128)
-kb_inst_alpha(const Inst* __restrict__ insts, int ninst, const double* __restrict__ partials,
-                              CGLoop* loop) {
-    const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (q >= ninst) return;
-    const Inst& I = insts[q];
-    CGState* cs = I.cg;
-    if (cs->done) return;
-    double c[17];
-#pragma unroll
-    for (int k = 0; k < 17; ++k) c[k] = warp_tile_sum(partials, I.tile0, I.ntiles, k) * I.g.dxdy;
-    if ((threadIdx.x & 31) != 0) return;
-    bool ok;
+// line-search coefficients of one instance and its step lengths, by the CTA
+// that finished its last tile (the sums on all warps, the scaling on warp 0,
+// the search on thread 0)
+template <bool FP64>
+__device__ __noinline__ void inst_alpha(const Inst& I, CGState* cs, const double* partials, CGLoop* loop) {
+    __shared__ double c[17], cd[17];
+    __shared__ float cf[17];
+    cta_tile_sums<17>(partials, I.tile0, I.ntiles, I.g.dxdy, c);
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    bool ok = true;
     double ap = 0.0, aA = 0.0;
     if (I.solveA) {
-        ok = minimise_poly2(c, &ap, &aA);
-    } else {
-        ap = smallest_nonneg_root_cubic(c[5], 2.0 * c[10], 3.0 * c[15], 4.0 * c[16]);
+        // scale: the largest |c_k| (k >= 1) as a power of two, so the scaling is exact
+        double m = (lane >= 1 && lane < 17) ? fabs(c[lane]) : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (m > 0.0) {
+            int e;
+            frexp(m, &e);
+            const double inv = ldexp(1.0, -e);
+            if (lane < 17) {
+                const double d = lane == 0 ? 0.0 : c[lane] * inv;
+                cd[lane] = d;
+                cf[lane] = (float)d;
+            }
+            __syncwarp();
+            if (lane == 0) ok = minimise_poly2<FP64>(cf, cd, &ap, &aA);
+        }
+    } else if (lane == 0) {
+        ap = smallest_nonneg_root_cubic<FP64>(c[5], 2.0 * c[10], 3.0 * c[15], 4.0 * c[16]);
         ok = ap >= 0.0;
     }
+    if (lane != 0) return;
     for (int k = 0; k < 17; ++k) cs->c[k] = c[k];
     cs->alpha_psi = ap;
     cs->alpha_A = aA;
@@ -379,55 +420,182 @@ kb_inst_alpha(const Inst* __restrict__ insts, int ninst, const double* __restric
     }
 }
 
+// new direction (written) and the per-tile line-search coefficient partials
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-kb_update(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB : 1)
+kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials,
+            CGLoop* loop) {
     const Tile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
-    const CGState* cs = I.cg;
+    CGState* cs = I.cg;
     if (*(volatile const int*)&cs->done) return;
     const Geo g = I.g;
-    const T ap = (T)cs->alpha_psi, aA = (T)cs->alpha_A;
-    C2<T>* psi = (C2<T>*)I.psi[0];
-    const C2<T>* dpsi = (const C2<T>*)I.dpsi[cs->di];
-    T* ab = (T*)I.ab[0];
-    const T* dA = (const T*)I.dA[cs->di];
+    const int gi = cs->gi, di = cs->di, pi = cs->pi;
+    const T bp = (T)cs->beta_psi, bA = (T)cs->beta_A;
+    const C2<T>* psi = (const C2<T>*)I.psi[pi];
+    const T* ab = (const T*)I.ab[I.solveA ? pi : 0];
+    const T* abei = (const T*)I.abei;
+    const C2<T>* G = (const C2<T>*)I.gpsi[gi];
+    const T* GA = (const T*)I.gA[gi];
+    const C2<T>* dO = (const C2<T>*)I.dpsi[di];
+    const T* dAO = (const T*)I.dA[di];
+    C2<T>* dN = (C2<T>*)I.dpsi[1 - di];
+    T* dAN = (T*)I.dA[1 - di];
+    const TableLinks<T> lk{(const C2<T>*)I.U};
+    auto dpsi = [&](int m) -> C2<T> {
+        const C2<T> o = dO[m], gg = G[m];
+        return cmk<T>(bp * o.x - gg.x, bp * o.y - gg.y);
+    };
+    auto dA = [&](int m) -> T { return bA * dAO[m] - GA[m]; };
+    T c[17];
 #pragma unroll
+    for (int k = 0; k < 17; ++k) c[k] = T(0);
+#pragma unroll 1
     for (int r = 0; r < kCGRep; ++r) {
-        const int n = t.n0 + threadIdx.x + r * kThreads;
-        if (n >= g.N) break;
-        const C2<T> d = dpsi[n];
-        C2<T> p = psi[n];
-        p.x = ap * d.x + p.x;
-        p.y = ap * d.y + p.y;
-        psi[n] = p;
+    const int n = t.n0 + threadIdx.x + r * kThreads;
+    if (n < g.N) {
+        const int i = n % g.Nx, j = n / g.Nx;
+        const unsigned cb = cell_bits(g, I.mt, i, j);
+        dN[n] = dpsi(n);
+        const T eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
         if (I.solveA) {
-            // new A and its link factors for the next iteration's kernels
-            const int i = n % g.Nx, j = n / g.Nx;
-            const T* abei = (const T*)I.abei;
-            C2<T>* U = (C2<T>*)I.U;
-            if (i < g.Nx - 1) {
-                const int na = i + (g.Nx - 1) * j;
-                const T v = aA * dA[na] + ab[na];
-                ab[na] = v;
-                U[na] = link_U<T>(GT(g, dx) * (abei ? abei[na] + v : v));
+            if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
+            if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
+            coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb,
+                             dpsi, dA, c);
+        } else {
+            T c5[5] = {T(0), T(0), T(0), T(0), T(0)};
+            coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb, dpsi, dA, c5);
+            c[0] += c5[0]; c[5] += c5[1]; c[10] += c5[2]; c[15] += c5[3]; c[16] += c5[4];
+        }
+    }
+    }
+    double cs17[17];
+    block_sum<17>(c, cs17);
+    if (threadIdx.x == 0) store_partials<T>(cs17, 17, partials + (size_t)blockIdx.x * kPart);
+    if (last_cta_of_instance(cs, I.ntiles)) inst_alpha<sizeof(T) == 8>(I, cs, partials, loop);
+}
+
+// energy-ratio stop, target stop and iteration cap of one instance, by the CTA
+// that finished its last tile
+__device__ __noinline__ void inst_energy_stop(const Inst& I, CGState* cs, const double* partials, CGLoop* loop) {
+    __shared__ double e1[1];
+    cta_tile_sums<1>(partials, I.tile0, I.ntiles, I.g.dxdy, e1);
+    if (threadIdx.x != 0) return;
+    const double E = e1[0];
+    cs->E_prev = cs->E;
+    cs->E = E;
+    const int it = cs->iter;
+    cs->iter = it + 1;
+    if (it > 0 && fabs(E / cs->E_prev - 1.0) < loop->rtol) {
+        cs->done = 1;
+        cs->status = 2;
+        atomicSub(&loop->active, 1);
+    } else if (I.cg_target == I.cg_target && E <= I.cg_target + I.cg_target_tol * fabs(I.cg_target)) {
+        cs->done = 1;
+        cs->status = 4;
+        atomicSub(&loop->active, 1);
+    } else if (cs->iter >= loop->n_iter) {
+        cs->done = 1;
+        cs->status = 3;
+        atomicSub(&loop->active, 1);
+    }
+}
+
+// Step psi += alpha_psi dpsi, A += alpha_A dA into the other state buffer (with
+// the new link factors of the links a node owns), the energy of the new state
+// per tile, and the instance's stop test in its last CTA.  Neighbour values of
+// the new state are formed from the old buffer by the same arithmetic that their
+// owners store, so the energy equals that of the stored state bit for bit.  The
+// last CTA of the launch counts the active instances and sets the WHILE
+// condition.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+kb_step(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop,
+        cudaGraphConditionalHandle cond, int use_cond) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    CGState* cs = I.cg;
+    if (!*(volatile const int*)&cs->done) {
+        const Geo g = I.g;
+        const int pi = cs->pi, di = cs->di, ai = I.solveA ? pi : 0;
+        const T ap = (T)cs->alpha_psi, aA = (T)cs->alpha_A;
+        const C2<T>* psi = (const C2<T>*)I.psi[pi];
+        C2<T>* psiN = (C2<T>*)I.psi[1 - pi];
+        const C2<T>* dpsi = (const C2<T>*)I.dpsi[di];
+        const T* ab = (const T*)I.ab[ai];
+        const T* dA = (const T*)I.dA[di];
+        const T* abei = (const T*)I.abei;
+        C2<T>* U = (C2<T>*)I.U;
+        auto psi_new = [&](int m) -> C2<T> {
+            const C2<T> d = dpsi[m];
+            C2<T> p = psi[m];
+            p.x = ap * d.x + p.x;
+            p.y = ap * d.y + p.y;
+            return p;
+        };
+        auto ab_new = [&](int l) -> T { return aA * dA[l] + ab[l]; };
+        const TableLinks<T> lk{(const C2<T>*)U};
+        const T k2 = gsel<T>(I.kappa2, I.fkappa2), eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
+        T v[1] = {T(0)};
+#pragma unroll
+        for (int r = 0; r < kCGRep; ++r) {
+            const int n = t.n0 + threadIdx.x + r * kThreads;
+            if (n < g.N) {
+                psiN[n] = psi_new(n);
+                const int i = n % g.Nx, j = n / g.Nx;
+                if (I.solveA) {
+                    T* abN = (T*)I.ab[1 - pi];
+                    if (i < g.Nx - 1) {
+                        const int na = i + (g.Nx - 1) * j;
+                        const T a = ab_new(na);
+                        abN[na] = a;
+                        U[na] = link_U<T>(GT(g, dx) * (abei ? abei[na] + a : a));
+                    }
+                    if (j < g.Ny - 1) {
+                        const int nb = g.Na + i + g.Nx * j;
+                        const T a = ab_new(nb);
+                        abN[nb] = a;
+                        U[nb] = link_U<T>(GT(g, dy) * (abei ? abei[nb] + a : a));
+                    }
+                }
+                // the node's own links' factors were written above by this thread
+                v[0] += energy_density_f<T>(g, k2, eps0, (const T*)I.eps_sp, H, I.mt, psi_new, abei, I.solveA != 0,
+                                            ab_new, lk, n);
             }
-            if (j < g.Ny - 1) {
-                const int nb = g.Na + i + g.Nx * j;
-                const T v = aA * dA[nb] + ab[nb];
-                ab[nb] = v;
-                U[nb] = link_U<T>(GT(g, dy) * (abei ? abei[nb] + v : v));
-            }
+        }
+        double vs[1];
+        block_sum<1>(v, vs);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kPart] = vs[0];
+        if (last_cta_of_instance(cs, I.ntiles)) {
+            inst_energy_stop(I, cs, partials, loop);
+            if (threadIdx.x == 0) cs->pi = 1 - pi;
+        }
+    }
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&loop->ticket, 1) == (int)(gridDim.x - 1);
+        if (s_last) {
+            __threadfence();
+            loop->ticket = 0;
+            const int iters = loop->iters + 1;
+            loop->iters = iters;
+            const int act = atomicAdd(&loop->active, 0);
+            const unsigned go = (act > 0 && iters < loop->n_iter + 2) ? 1u : 0u;
+            if (use_cond) cudaGraphSetConditional(cond, go);
+            loop->pad_ = (int)go;
         }
     }
 }
 
+// energy of the start state per tile (buffer 0)
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials, int all) {
+kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials) {
     const Tile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
-    if (!all && *(volatile const int*)&I.cg->done) return;
     const Geo g = I.g;
     const TableLinks<T> lk{(const C2<T>*)I.U};
     T v[1] = {T(0)};
@@ -444,45 +612,26 @@ kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double
     if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kPart] = vs[0];
 }
 
-// energies, the energy-ratio stop, the iteration cap, and the WHILE condition
-// (one CTA for the whole batch).
-__global__ void __launch_bounds__(1024)
-kb_inst_stop(const Inst* __restrict__ insts, int ninst, const double* __restrict__ partials,
-                             CGLoop* loop, cudaGraphConditionalHandle cond, int use_cond) {
-    const int nw = blockDim.x >> 5;
-    for (int q = threadIdx.x >> 5; q < ninst; q += nw) {
-        const Inst& I = insts[q];
-        CGState* cs = I.cg;
-        if (cs->done) continue;
-        const double E = warp_tile_sum(partials, I.tile0, I.ntiles, 0) * I.g.dxdy;
-        if ((threadIdx.x & 31) != 0) continue;
-        cs->E_prev = cs->E;
-        cs->E = E;
-        const int it = cs->iter;
-        cs->iter = it + 1;
-        if (it > 0 && fabs(E / cs->E_prev - 1.0) < loop->rtol) {
-            cs->done = 1;
-            cs->status = 2;
-            atomicSub(&loop->active, 1);
-        } else if (I.cg_target == I.cg_target && E <= I.cg_target + I.cg_target_tol * fabs(I.cg_target)) {
-            cs->done = 1;
-            cs->status = 4;
-            atomicSub(&loop->active, 1);
-        } else if (cs->iter >= loop->n_iter) {
-            cs->done = 1;
-            cs->status = 3;
-            atomicSub(&loop->active, 1);
+// end of a CG call: the state is copied back to buffer 0 where it ended in buffer 1
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+kb_finish(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    if (I.cg->pi == 0) return;
+    const Geo g = I.g;
+#pragma unroll
+    for (int r = 0; r < kCGRep; ++r) {
+        const int n = t.n0 + threadIdx.x + r * kThreads;
+        if (n >= g.N) break;
+        ((C2<T>*)I.psi[0])[n] = ((const C2<T>*)I.psi[1])[n];
+        if (I.solveA) {
+            const int i = n % g.Nx, j = n / g.Nx;
+            const T* src = (const T*)I.ab[1];
+            T* dst = (T*)I.ab[0];
+            if (i < g.Nx - 1) dst[i + (g.Nx - 1) * j] = src[i + (g.Nx - 1) * j];
+            if (j < g.Ny - 1) dst[g.Na + i + g.Nx * j] = src[g.Na + i + g.Nx * j];
         }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const int iters = loop->iters + 1;
-        loop->iters = iters;
-        const int act = atomicAdd(&loop->active, 0);
-        const unsigned go = (act > 0 && iters < loop->n_iter + 2) ? 1u : 0u;
-        if (use_cond) cudaGraphSetConditional(cond, go);
-        loop->pad_ = (int)go;
     }
 }
 
@@ -525,7 +674,9 @@ kb_init(const Inst* __restrict__ insts, int ninst, const double* __restrict__ pa
     const int nw = blockDim.x >> 5;
     for (int q = threadIdx.x >> 5; q < ninst; q += nw) {
         const Inst& I = insts[q];
-        const double E = warp_tile_sum(partials, I.tile0, I.ntiles, 0) * I.g.dxdy;
+        double e1[1];
+        warp_tile_sums<1>(partials, I.tile0, I.ntiles, e1);
+        const double E = e1[0] * I.g.dxdy;
         if ((threadIdx.x & 31) != 0) continue;
         CGState* cs = I.cg;
         cs->beta_psi = cs->beta_A = 0.0;
@@ -538,11 +689,14 @@ kb_init(const Inst* __restrict__ insts, int ninst, const double* __restrict__ pa
         cs->gi = 0;
         cs->di = 0;
         cs->status = 0;
+        cs->pi = 0;
+        cs->ticket = 0;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         loop->active = ninst;
         loop->iters = 0;
+        loop->ticket = 0;
         const unsigned go = (ninst > 0 && loop->n_iter > 0) ? 1u : 0u;
         if (use_cond) cudaGraphSetConditional(cond, go);
         loop->pad_ = (int)go;
@@ -563,27 +717,20 @@ struct CGLaunch {
 
 static void* fn_grad(int dt) { return dt == 8 ? (void*)kb_grad<double> : (void*)kb_grad<float>; }
 static void* fn_dir_coef(int dt) { return dt == 8 ? (void*)kb_dir_coef<double> : (void*)kb_dir_coef<float>; }
-static void* fn_update(int dt) { return dt == 8 ? (void*)kb_update<double> : (void*)kb_update<float>; }
+static void* fn_step(int dt) { return dt == 8 ? (void*)kb_step<double> : (void*)kb_step<float>; }
 static void* fn_energy(int dt) { return dt == 8 ? (void*)kb_energy<double> : (void*)kb_energy<float>; }
 static void* fn_zero_dir(int dt) { return dt == 8 ? (void*)kb_zero_dir<double> : (void*)kb_zero_dir<float>; }
-
-static inline int warp_blocks(int ninst) { return (ninst + 3) / 4; }  // 4 warps of 32 per CTA
+static void* fn_finish(int dt) { return dt == 8 ? (void*)kb_finish<double> : (void*)kb_finish<float>; }
 
 // Host-driven loop body (the graph holds the same launches).
 static cudaError_t cg_launch_body(const CGLaunch& L, cudaStream_t s) {
     const cudaGraphConditionalHandle none = 0;
-    const int wb = warp_blocks(L.ninst);
-    if (L.dtype == 8) kb_grad<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
-    else kb_grad<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
-    kb_inst_beta<<<wb, 128, 0, s>>>(L.insts, L.ninst, L.partials, L.loop);
-    if (L.dtype == 8) kb_dir_coef<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
-    else kb_dir_coef<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
-    kb_inst_alpha<<<wb, 128, 0, s>>>(L.insts, L.ninst, L.partials, L.loop);
-    if (L.dtype == 8) kb_update<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
-    else kb_update<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
-    if (L.dtype == 8) kb_energy<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, 0);
-    else kb_energy<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, 0);
-    kb_inst_stop<<<1, 1024, 0, s>>>(L.insts, L.ninst, L.partials, L.loop, none, 0);
+    if (L.dtype == 8) kb_grad<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, L.loop);
+    else kb_grad<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, L.loop);
+    if (L.dtype == 8) kb_dir_coef<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, L.loop);
+    else kb_dir_coef<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, L.loop);
+    if (L.dtype == 8) kb_step<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, L.loop, none, 0);
+    else kb_step<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, L.loop, none, 0);
     return cudaGetLastError();
 }
 
@@ -591,24 +738,29 @@ static cudaError_t cg_launch_prologue(const CGLaunch& L, cudaStream_t s) {
     const cudaGraphConditionalHandle none = 0;
     if (L.dtype == 8) kb_zero_dir<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
     else kb_zero_dir<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
-    if (L.dtype == 8) kb_energy<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, 1);
-    else kb_energy<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials, 1);
+    if (L.dtype == 8) kb_energy<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
+    else kb_energy<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.partials);
     kb_init<<<1, 1024, 0, s>>>(L.insts, L.ninst, L.partials, L.loop, none, 0);
+    return cudaGetLastError();
+}
+
+static cudaError_t cg_launch_epilogue(const CGLaunch& L, cudaStream_t s) {
+    if (L.dtype == 8) kb_finish<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    else kb_finish<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
     return cudaGetLastError();
 }
 
 #define GCHK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { err = e_; goto fail; } } while (0)
 
 // The whole CG run of all instances as one graph:
-//   zero_dir -> energy -> init -> WHILE(active) {
-//       grad -> beta -> dir_coef -> alpha -> update -> energy -> stop }
+//   zero_dir -> energy -> init -> WHILE(active) { grad -> dir_coef -> step } -> finish
 static cudaError_t build_cg_graph(const CGLaunch& L, cudaGraphExec_t* exec) {
     cudaError_t err = cudaSuccess;
     cudaGraph_t top = nullptr, body = nullptr;
     cudaGraphConditionalHandle h;
-    cudaGraphNode_t prev = nullptr, nd;
-    int zero = 0, one = 1;
-    const dim3 gt(L.ntiles), bt(kThreads), gw(warp_blocks(L.ninst)), bw(128), g1(1), b1(1024);
+    cudaGraphNode_t prev = nullptr, nd, wh;
+    int one = 1;
+    const dim3 gt(L.ntiles), bt(kThreads), g1(1), b1(1024);
     const Inst* insts = L.insts;
     const Tile* tiles = L.tiles;
     double* partials = L.partials;
@@ -623,7 +775,7 @@ static cudaError_t build_cg_graph(const CGLaunch& L, cudaGraphExec_t* exec) {
         prev = nd;
     }
     {
-        void* a[] = {&insts, &tiles, &partials, &one};
+        void* a[] = {&insts, &tiles, &partials};
         GCHK(add_kernel(top, &nd, &prev, 1, fn_energy(L.dtype), gt, bt, a));
         prev = nd;
     }
@@ -632,41 +784,25 @@ static cudaError_t build_cg_graph(const CGLaunch& L, cudaGraphExec_t* exec) {
         GCHK(add_kernel(top, &nd, &prev, 1, (void*)kb_init, g1, b1, a));
         prev = nd;
     }
-    GCHK(add_while(top, &nd, &prev, 1, h, &body));
+    GCHK(add_while(top, &wh, &prev, 1, h, &body));
+    {
+        void* a[] = {&insts, &tiles};
+        GCHK(add_kernel(top, &nd, &wh, 1, fn_finish(L.dtype), gt, bt, a));
+    }
     prev = nullptr;
     {
-        void* a[] = {&insts, &tiles, &partials};
+        void* a[] = {&insts, &tiles, &partials, &loop};
         GCHK(add_kernel(body, &nd, nullptr, 0, fn_grad(L.dtype), gt, bt, a));
         prev = nd;
     }
     {
-        void* a[] = {&insts, &ninst, &partials, &loop};
-        GCHK(add_kernel(body, &nd, &prev, 1, (void*)kb_inst_beta, gw, bw, a));
-        prev = nd;
-    }
-    {
-        void* a[] = {&insts, &tiles, &partials};
+        void* a[] = {&insts, &tiles, &partials, &loop};
         GCHK(add_kernel(body, &nd, &prev, 1, fn_dir_coef(L.dtype), gt, bt, a));
         prev = nd;
     }
     {
-        void* a[] = {&insts, &ninst, &partials, &loop};
-        GCHK(add_kernel(body, &nd, &prev, 1, (void*)kb_inst_alpha, gw, bw, a));
-        prev = nd;
-    }
-    {
-        void* a[] = {&insts, &tiles};
-        GCHK(add_kernel(body, &nd, &prev, 1, fn_update(L.dtype), gt, bt, a));
-        prev = nd;
-    }
-    {
-        void* a[] = {&insts, &tiles, &partials, &zero};
-        GCHK(add_kernel(body, &nd, &prev, 1, fn_energy(L.dtype), gt, bt, a));
-        prev = nd;
-    }
-    {
-        void* a[] = {&insts, &ninst, &partials, &loop, &h, &one};
-        GCHK(add_kernel(body, &nd, &prev, 1, (void*)kb_inst_stop, g1, b1, a));
+        void* a[] = {&insts, &tiles, &partials, &loop, &h, &one};
+        GCHK(add_kernel(body, &nd, &prev, 1, fn_step(L.dtype), gt, bt, a));
     }
     GCHK(cudaGraphInstantiate(exec, top, 0));
     cudaGraphDestroy(top);
@@ -762,6 +898,7 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
             e = cg_launch_body(L, s);
         }
         if (go_h) cudaFreeHost(go_h);
+        if (e == cudaSuccess) e = cg_launch_epilogue(L, s);
     }
     if (elapsed_ms) cudaEventRecord(ev1, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -216,6 +216,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 template <int NV> __device__ __forceinline__ void block_sum(const float (&v)[NV], double (&out)[NV]) {
     __shared__ double sm[kWarps][NV];
     const int tid = flat_tid(), lane = tid & 31, w = tid >> 5;
+    __syncthreads();
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         float hi = v[k], lo = 0.f;
@@ -226,12 +227,10 @@ template <int NV> __device__ __forceinline__ void block_sum(const float (&v)[NV]
             hi = sum;
             lo = lo + (ol + err);
         }
-        out[k] = (double)hi + (double)lo;
+        // Only lane 0 widens to double: the FP64 pipe runs at a small fraction
+        // of the FP32 rate, and the other lanes' pairs are discarded.
+        if (lane == 0) sm[w][k] = (double)hi + (double)lo;
     }
-    __syncthreads();
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) sm[w][k] = out[k];
     __syncthreads();
     if (tid == 0) {
 #pragma unroll

@@ -21,7 +21,7 @@ namespace glgpu {
 #define GLGPU_FUSE 3
 #endif
 #ifndef GLGPU_STRIP_ROWS
-#define GLGPU_STRIP_ROWS 16
+#define GLGPU_STRIP_ROWS 12
 #endif
 constexpr int kFuse = GLGPU_FUSE;
 static_assert(kFuse >= 1 && kFuse <= 4, "1 <= GLGPU_FUSE <= 4");
@@ -55,7 +55,9 @@ struct CGState {
     double g2, g2_0;          // |gradient|^2 now and at the first iteration
     int iter, done, gi, di;   // iterations done, finished, current gradient / direction buffer
     int status;               // 0 ok, 1 gradient-norm stop, 2 energy stop, 3 n_iter, -1 no step found
-    int pad_[3];
+    int pi;                   // buffer (psi[pi], ab[pi]) holding the current state during a CG call
+    int ticket;               // CTAs of this instance finished in the running launch
+    int pad_;
 };
 
 // Everything a kernel needs to process one instance.  Lives in device memory,

@@ -62,18 +62,24 @@ template <typename T> struct TableLinks {
     __device__ __forceinline__ void sc_split(int l, T d, T& s, T& c) const { sc_sum(l, d, s, c); }
 };
 
-// curl of one link field on cell (i, j): idx*(b[i+1,j]-b[i,j]) - idy*(a[i,j+1]-a[i,j]).
-template <typename T> __device__ __forceinline__ T cell_curl(const Geo& g, const T* A, int i, int j, T idx, T idy) {
+// curl of one link field on cell (i, j): idx*(b[i+1,j]-b[i,j]) - idy*(a[i,j+1]-a[i,j]);
+// A(l) gives link l's value.
+template <typename T, typename AF>
+__device__ __forceinline__ T cell_curl_f(const Geo& g, const AF& A, int i, int j, T idx, T idy) {
     const int Nxa = g.Nx - 1;
-    return idx * (A[g.Na + (i + 1) + g.Nx * j] - A[g.Na + i + g.Nx * j]) - idy * (A[i + Nxa * (j + 1)] - A[i + Nxa * j]);
+    return idx * (A(g.Na + (i + 1) + g.Nx * j) - A(g.Na + i + g.Nx * j)) - idy * (A(i + Nxa * (j + 1)) - A(i + Nxa * j));
+}
+template <typename T> __device__ __forceinline__ T cell_curl(const Geo& g, const T* A, int i, int j, T idx, T idy) {
+    return cell_curl_f<T>(g, [A](int l) { return A[l]; }, i, j, idx, idy);
 }
 
 // Free-energy pseudo-density at node n before the dx*dy factor
-// (svirl/cuda/observables.h:276-356).
-template <typename T, typename LK>
-__device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H,
-                                            const uint8_t* mt, const C2<T>* psi, const T* abei, const T* ab,
-                                            const LK& lk, int n) {
+// (svirl/cuda/observables.h:276-356).  psi(m) gives the order parameter at node
+// m, ab(l) the vector potential of link l (used only when has_ab).
+template <typename T, typename LK, typename PF, typename AF>
+__device__ __forceinline__ T energy_density_f(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H,
+                                              const uint8_t* mt, const PF& psi, const T* abei, bool has_ab,
+                                              const AF& ab, const LK& lk, int n) {
     const int i = n % g.Nx, j = n / g.Nx;
     const unsigned cb = cell_bits(g, mt, i, j);
     const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
@@ -81,30 +87,37 @@ __device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, cons
     T e = T(0);
     if (cb) {
         const DuW<T> w = du_weights<T>(cb);
-        const C2<T> p00 = psi[n];
+        const C2<T> p00 = psi(n);
         const T p2 = cabs2(p00);
         const T eps = eps_sp ? eps_sp[n] : eps0;
         e += w.g * (T(0.5) * p2 - eps) * p2;
         if (GL_PM(cb) || GL_PP(cb)) {
             T sn, cs;
             lk.sc_sum(i + (g.Nx - 1) * j, dx, sn, cs);
-            const C2<T> gr = grad_c_sc<T>(p00, sn, cs, psi[n + 1]);
+            const C2<T> gr = grad_c_sc<T>(p00, sn, cs, psi(n + 1));
             e += w.r_p0 * idx2 * (gr.x * gr.x + gr.y * gr.y);
         }
         if (GL_MP(cb) || GL_PP(cb)) {
             T sn, cs;
             lk.sc_sum(g.Na + i + g.Nx * j, dy, sn, cs);
-            const C2<T> gr = grad_c_sc<T>(p00, sn, cs, psi[n + g.Nx]);
+            const C2<T> gr = grad_c_sc<T>(p00, sn, cs, psi(n + g.Nx));
             e += w.r_0p * idy2 * (gr.x * gr.x + gr.y * gr.y);
         }
     }
     if (kappa2 > T(0) && i < g.Nxc && j < g.Nyc) {
         T dB = -H;
         if (abei) dB += cell_curl(g, abei, i, j, idx, idy);
-        if (ab) dB += cell_curl(g, ab, i, j, idx, idy);
+        if (has_ab) dB += cell_curl_f<T>(g, ab, i, j, idx, idy);
         e += kappa2 * dB * dB;
     }
     return e;
+}
+template <typename T, typename LK>
+__device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H,
+                                            const uint8_t* mt, const C2<T>* psi, const T* abei, const T* ab,
+                                            const LK& lk, int n) {
+    return energy_density_f<T>(g, kappa2, eps0, eps_sp, H, mt, [psi](int m) { return psi[m]; }, abei, ab != nullptr,
+                               [ab](int l) { return ab[l]; }, lk, n);
 }
 
 // curl curl A (times 1/kappa^2) on the link starting at node (i, j) along x (xdir)
