@@ -150,7 +150,54 @@ __device__ __forceinline__ bool last_cta_of_instance(CGState* cs, int ntiles) {
     return s_last;
 }
 
-// gradient (new buffer), Polak-Ribiere sums and |g|^2 per tile
+// The tile bodies take every field as a __restrict__ pointer (the buffers are
+// distinct), so the compiler may keep loaded values across the stores, and they
+// store a node's results after its loads.
+
+// gradient (new buffer), Polak-Ribiere sums and |g|^2 of one tile
+template <typename T>
+__device__ __forceinline__ void grad_tile(const Inst& I, int n0, const C2<T>* __restrict__ psi,
+                                          const T* __restrict__ ab, const T* __restrict__ abei,
+                                          const C2<T>* __restrict__ U, C2<T>* __restrict__ G,
+                                          const C2<T>* __restrict__ Gp, T* __restrict__ GA,
+                                          const T* __restrict__ GAp, T (&v)[5]) {
+    const Geo g = I.g;
+    const TableLinks<T> lk{U};
+    const T eps0 = gsel<T>(I.epsilon, I.fepsilon), k2 = gsel<T>(I.kappa2, I.fkappa2), H = gsel<T>(I.H, I.fH);
+#pragma unroll
+    for (int r = 0; r < kCGRep; ++r) {
+        const int n = n0 + threadIdx.x + r * kThreads;
+        if (n < g.N) {
+            const int i = n % g.Nx, j = n / g.Nx;
+            const unsigned cb = cell_bits(g, I.mt, i, j);
+            const C2<T> gv = grad_psi_node<T>(g, eps0, (const T*)I.eps_sp, psi, lk, n, i, j, cb);
+            const C2<T> gp = Gp[n];
+            v[0] += gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y);
+            v[1] += gp.x * gp.x + gp.y * gp.y;
+            v[4] += gv.x * gv.x + gv.y * gv.y;
+            T ga[2] = {T(0), T(0)};
+            const bool has[2] = {i < g.Nx - 1, j < g.Ny - 1};
+            const int l[2] = {i + (g.Nx - 1) * j, g.Na + i + g.Nx * j};
+            if (I.solveA) {
+#pragma unroll
+                for (int dir = 0; dir < 2; ++dir) {
+                    if (!has[dir]) continue;
+                    ga[dir] = grad_A_link<T>(g, k2, H, psi, abei, ab, lk, n, i, j, cb, dir == 0, I.cg_exact != 0);
+                    const T gap = GAp[l[dir]];
+                    v[2] += ga[dir] * (ga[dir] - gap);
+                    v[3] += gap * gap;
+                    v[4] += ga[dir] * ga[dir];
+                }
+            }
+            G[n] = gv;
+            if (I.solveA)
+#pragma unroll
+                for (int dir = 0; dir < 2; ++dir)
+                    if (has[dir]) GA[l[dir]] = ga[dir];
+        }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB : 1)
 kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop) {
@@ -158,45 +205,11 @@ kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
     const Inst& I = insts[t.inst];
     CGState* cs = I.cg;
     if (*(volatile const int*)&cs->done) return;
-    const Geo g = I.g;
     const int gi = cs->gi, pi = cs->pi;
-    const C2<T>* psi = (const C2<T>*)I.psi[pi];
-    const T* ab = (const T*)I.ab[I.solveA ? pi : 0];
-    const T* abei = (const T*)I.abei;
-    C2<T>* G = (C2<T>*)I.gpsi[1 - gi];
-    const C2<T>* Gp = (const C2<T>*)I.gpsi[gi];
-    T* GA = (T*)I.gA[1 - gi];
-    const T* GAp = (const T*)I.gA[gi];
-    const TableLinks<T> lk{(const C2<T>*)I.U};
     T v[5] = {T(0), T(0), T(0), T(0), T(0)};
-#pragma unroll
-    for (int r = 0; r < kCGRep; ++r) {
-    const int n = t.n0 + threadIdx.x + r * kThreads;
-    if (n < g.N) {
-        const int i = n % g.Nx, j = n / g.Nx;
-        const unsigned cb = cell_bits(g, I.mt, i, j);
-        const C2<T> gv = grad_psi_node<T>(g, gsel<T>(I.epsilon, I.fepsilon), (const T*)I.eps_sp, psi, lk, n, i, j, cb);
-        G[n] = gv;
-        const C2<T> gp = Gp[n];
-        v[0] += gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y);
-        v[1] += gp.x * gp.x + gp.y * gp.y;
-        v[4] += gv.x * gv.x + gv.y * gv.y;
-        if (I.solveA) {
-            const T k2 = gsel<T>(I.kappa2, I.fkappa2), H = gsel<T>(I.H, I.fH);
-            for (int dir = 0; dir < 2; ++dir) {
-                const bool has = dir == 0 ? (i < g.Nx - 1) : (j < g.Ny - 1);
-                if (!has) continue;
-                const int l = dir == 0 ? i + (g.Nx - 1) * j : g.Na + i + g.Nx * j;
-                const T ga = grad_A_link<T>(g, k2, H, psi, abei, ab, lk, n, i, j, cb, dir == 0, I.cg_exact != 0);
-                GA[l] = ga;
-                const T gap = GAp[l];
-                v[2] += ga * (ga - gap);
-                v[3] += gap * gap;
-                v[4] += ga * ga;
-            }
-        }
-    }
-    }
+    grad_tile<T>(I, t.n0, (const C2<T>*)I.psi[pi], (const T*)I.ab[I.solveA ? pi : 0], (const T*)I.abei,
+                 (const C2<T>*)I.U, (C2<T>*)I.gpsi[1 - gi], (const C2<T>*)I.gpsi[gi], (T*)I.gA[1 - gi],
+                 (const T*)I.gA[gi], v);
     double vs[5];
     block_sum<5>(v, vs);
     if (threadIdx.x == 0) store_partials<T>(vs, 5, partials + (size_t)blockIdx.x * kPart);
@@ -354,21 +367,18 @@ __device__ bool minimise_poly2(const float* cfs, const double* cds, double* a_ou
         if (fabsf(t * sa) + fabsf(t * sb) <= 1e-7f * (1.f + fabsf(a) + fabsf(b))) break;
     }
     double ad = a, bd = b;
-    if (!FP64) {
-        *a_out = ad;
-        *b_out = bd;
-        return isfinite(a) && isfinite(b);
-    }
-    double cd[17];
+    if constexpr (FP64) {
+        double cd[17];
 #pragma unroll
-    for (int k = 0; k < 17; ++k) cd[k] = cds[k];
-    for (int it = 0; it < 2; ++it) {  // FP64 polish
-        const P2<double> Q = poly2<double>(cd, ad, bd);
-        const double det = Q.faa * Q.fbb - Q.fab * Q.fab;
-        if (!(Q.faa > 0.0 && det > 0.0)) break;
-        const double idet = 1.0 / det;
-        ad -= (Q.fbb * Q.fa - Q.fab * Q.fb) * idet;
-        bd -= (Q.faa * Q.fb - Q.fab * Q.fa) * idet;
+        for (int k = 0; k < 17; ++k) cd[k] = cds[k];
+        for (int it = 0; it < 2; ++it) {  // FP64 polish
+            const P2<double> Q = poly2<double>(cd, ad, bd);
+            const double det = Q.faa * Q.fbb - Q.fab * Q.fab;
+            if (!(Q.faa > 0.0 && det > 0.0)) break;
+            const double idet = 1.0 / det;
+            ad -= (Q.fbb * Q.fa - Q.fab * Q.fb) * idet;
+            bd -= (Q.faa * Q.fb - Q.fab * Q.fa) * idet;
+        }
     }
     *a_out = ad;
     *b_out = bd;
@@ -420,7 +430,45 @@ __device__ __noinline__ void inst_alpha(const Inst& I, CGState* cs, const double
     }
 }
 
-// new direction (written) and the per-tile line-search coefficient partials
+// new direction (written) and the line-search coefficients of one tile
+template <typename T>
+__device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, T bp, T bA, const C2<T>* __restrict__ psi,
+                                              const T* __restrict__ ab, const T* __restrict__ abei,
+                                              const C2<T>* __restrict__ U, const C2<T>* __restrict__ G,
+                                              const T* __restrict__ GA, const C2<T>* __restrict__ dO,
+                                              const T* __restrict__ dAO, C2<T>* __restrict__ dN,
+                                              T* __restrict__ dAN, T (&c)[17]) {
+    const Geo g = I.g;
+    const TableLinks<T> lk{U};
+    auto dpsi = [&](int m) -> C2<T> {
+        const C2<T> o = dO[m], gg = G[m];
+        return cmk<T>(bp * o.x - gg.x, bp * o.y - gg.y);
+    };
+    auto dA = [&](int m) -> T { return bA * dAO[m] - GA[m]; };
+    const T eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
+#pragma unroll 1
+    for (int r = 0; r < kCGRep; ++r) {
+        const int n = n0 + threadIdx.x + r * kThreads;
+        if (n < g.N) {
+            const int i = n % g.Nx, j = n / g.Nx;
+            const unsigned cb = cell_bits(g, I.mt, i, j);
+            if (I.solveA) {
+                coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i,
+                                 j, cb, dpsi, dA, c);
+            } else {
+                T c5[5] = {T(0), T(0), T(0), T(0), T(0)};
+                coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb, dpsi, dA, c5);
+                c[0] += c5[0]; c[5] += c5[1]; c[10] += c5[2]; c[15] += c5[3]; c[16] += c5[4];
+            }
+            dN[n] = dpsi(n);
+            if (I.solveA) {
+                if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
+                if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
+            }
+        }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB : 1)
 kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials,
@@ -429,47 +477,14 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
     const Inst& I = insts[t.inst];
     CGState* cs = I.cg;
     if (*(volatile const int*)&cs->done) return;
-    const Geo g = I.g;
     const int gi = cs->gi, di = cs->di, pi = cs->pi;
-    const T bp = (T)cs->beta_psi, bA = (T)cs->beta_A;
-    const C2<T>* psi = (const C2<T>*)I.psi[pi];
-    const T* ab = (const T*)I.ab[I.solveA ? pi : 0];
-    const T* abei = (const T*)I.abei;
-    const C2<T>* G = (const C2<T>*)I.gpsi[gi];
-    const T* GA = (const T*)I.gA[gi];
-    const C2<T>* dO = (const C2<T>*)I.dpsi[di];
-    const T* dAO = (const T*)I.dA[di];
-    C2<T>* dN = (C2<T>*)I.dpsi[1 - di];
-    T* dAN = (T*)I.dA[1 - di];
-    const TableLinks<T> lk{(const C2<T>*)I.U};
-    auto dpsi = [&](int m) -> C2<T> {
-        const C2<T> o = dO[m], gg = G[m];
-        return cmk<T>(bp * o.x - gg.x, bp * o.y - gg.y);
-    };
-    auto dA = [&](int m) -> T { return bA * dAO[m] - GA[m]; };
     T c[17];
 #pragma unroll
     for (int k = 0; k < 17; ++k) c[k] = T(0);
-#pragma unroll 1
-    for (int r = 0; r < kCGRep; ++r) {
-    const int n = t.n0 + threadIdx.x + r * kThreads;
-    if (n < g.N) {
-        const int i = n % g.Nx, j = n / g.Nx;
-        const unsigned cb = cell_bits(g, I.mt, i, j);
-        dN[n] = dpsi(n);
-        const T eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
-        if (I.solveA) {
-            if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
-            if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
-            coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb,
-                             dpsi, dA, c);
-        } else {
-            T c5[5] = {T(0), T(0), T(0), T(0), T(0)};
-            coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb, dpsi, dA, c5);
-            c[0] += c5[0]; c[5] += c5[1]; c[10] += c5[2]; c[15] += c5[3]; c[16] += c5[4];
-        }
-    }
-    }
+    dir_coef_tile<T>(I, t.n0, (T)cs->beta_psi, (T)cs->beta_A, (const C2<T>*)I.psi[pi],
+                     (const T*)I.ab[I.solveA ? pi : 0], (const T*)I.abei, (const C2<T>*)I.U,
+                     (const C2<T>*)I.gpsi[gi], (const T*)I.gA[gi], (const C2<T>*)I.dpsi[di], (const T*)I.dA[di],
+                     (C2<T>*)I.dpsi[1 - di], (T*)I.dA[1 - di], c);
     double cs17[17];
     block_sum<17>(c, cs17);
     if (threadIdx.x == 0) store_partials<T>(cs17, 17, partials + (size_t)blockIdx.x * kPart);
@@ -502,6 +517,50 @@ __device__ __noinline__ void inst_energy_stop(const Inst& I, CGState* cs, const 
     }
 }
 
+// step and energy of the new state of one tile
+template <typename T>
+__device__ __forceinline__ void step_tile(const Inst& I, int n0, T ap, T aA, const C2<T>* __restrict__ psi,
+                                          C2<T>* __restrict__ psiN, const C2<T>* __restrict__ dpsi,
+                                          const T* __restrict__ ab, T* __restrict__ abN, const T* __restrict__ dA,
+                                          const T* __restrict__ abei, C2<T>* __restrict__ U, T (&v)[1]) {
+    const Geo g = I.g;
+    auto psi_new = [&](int m) -> C2<T> {
+        const C2<T> d = dpsi[m];
+        C2<T> p = psi[m];
+        p.x = ap * d.x + p.x;
+        p.y = ap * d.y + p.y;
+        return p;
+    };
+    auto ab_new = [&](int l) -> T { return aA * dA[l] + ab[l]; };
+    const TableLinks<T> lk{U};
+    const T k2 = gsel<T>(I.kappa2, I.fkappa2), eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
+#pragma unroll
+    for (int r = 0; r < kCGRep; ++r) {
+        const int n = n0 + threadIdx.x + r * kThreads;
+        if (n < g.N) {
+            const int i = n % g.Nx, j = n / g.Nx;
+            if (I.solveA) {
+                if (i < g.Nx - 1) {
+                    const int na = i + (g.Nx - 1) * j;
+                    const T a = ab_new(na);
+                    abN[na] = a;
+                    U[na] = link_U<T>(GT(g, dx) * (abei ? abei[na] + a : a));
+                }
+                if (j < g.Ny - 1) {
+                    const int nb = g.Na + i + g.Nx * j;
+                    const T a = ab_new(nb);
+                    abN[nb] = a;
+                    U[nb] = link_U<T>(GT(g, dy) * (abei ? abei[nb] + a : a));
+                }
+            }
+            // the node's own links' factors were written above by this thread
+            v[0] += energy_density_f<T>(g, k2, eps0, (const T*)I.eps_sp, H, I.mt, psi_new, abei, I.solveA != 0,
+                                        ab_new, lk, n);
+            psiN[n] = psi_new(n);
+        }
+    }
+}
+
 // Step psi += alpha_psi dpsi, A += alpha_A dA into the other state buffer (with
 // the new link factors of the links a node owns), the energy of the new state
 // per tile, and the instance's stop test in its last CTA.  Neighbour values of
@@ -517,53 +576,11 @@ kb_step(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
     const Inst& I = insts[t.inst];
     CGState* cs = I.cg;
     if (!*(volatile const int*)&cs->done) {
-        const Geo g = I.g;
-        const int pi = cs->pi, di = cs->di, ai = I.solveA ? pi : 0;
-        const T ap = (T)cs->alpha_psi, aA = (T)cs->alpha_A;
-        const C2<T>* psi = (const C2<T>*)I.psi[pi];
-        C2<T>* psiN = (C2<T>*)I.psi[1 - pi];
-        const C2<T>* dpsi = (const C2<T>*)I.dpsi[di];
-        const T* ab = (const T*)I.ab[ai];
-        const T* dA = (const T*)I.dA[di];
-        const T* abei = (const T*)I.abei;
-        C2<T>* U = (C2<T>*)I.U;
-        auto psi_new = [&](int m) -> C2<T> {
-            const C2<T> d = dpsi[m];
-            C2<T> p = psi[m];
-            p.x = ap * d.x + p.x;
-            p.y = ap * d.y + p.y;
-            return p;
-        };
-        auto ab_new = [&](int l) -> T { return aA * dA[l] + ab[l]; };
-        const TableLinks<T> lk{(const C2<T>*)U};
-        const T k2 = gsel<T>(I.kappa2, I.fkappa2), eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
+        const int pi = cs->pi, di = cs->di;
         T v[1] = {T(0)};
-#pragma unroll
-        for (int r = 0; r < kCGRep; ++r) {
-            const int n = t.n0 + threadIdx.x + r * kThreads;
-            if (n < g.N) {
-                psiN[n] = psi_new(n);
-                const int i = n % g.Nx, j = n / g.Nx;
-                if (I.solveA) {
-                    T* abN = (T*)I.ab[1 - pi];
-                    if (i < g.Nx - 1) {
-                        const int na = i + (g.Nx - 1) * j;
-                        const T a = ab_new(na);
-                        abN[na] = a;
-                        U[na] = link_U<T>(GT(g, dx) * (abei ? abei[na] + a : a));
-                    }
-                    if (j < g.Ny - 1) {
-                        const int nb = g.Na + i + g.Nx * j;
-                        const T a = ab_new(nb);
-                        abN[nb] = a;
-                        U[nb] = link_U<T>(GT(g, dy) * (abei ? abei[nb] + a : a));
-                    }
-                }
-                // the node's own links' factors were written above by this thread
-                v[0] += energy_density_f<T>(g, k2, eps0, (const T*)I.eps_sp, H, I.mt, psi_new, abei, I.solveA != 0,
-                                            ab_new, lk, n);
-            }
-        }
+        step_tile<T>(I, t.n0, (T)cs->alpha_psi, (T)cs->alpha_A, (const C2<T>*)I.psi[pi], (C2<T>*)I.psi[1 - pi],
+                     (const C2<T>*)I.dpsi[di], (const T*)I.ab[I.solveA ? pi : 0], I.solveA ? (T*)I.ab[1 - pi] : nullptr,
+                     (const T*)I.dA[di], (const T*)I.abei, (C2<T>*)I.U, v);
         double vs[1];
         block_sum<1>(v, vs);
         if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kPart] = vs[0];
