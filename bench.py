@@ -152,21 +152,21 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(dtype_name, fuse):
+def ncu_traffic(dtype_name, fuse, rows):
     """DRAM bytes per psi-sweep launch from the committed ncu summary of the same
-    kernel build (same sweeps per launch), or None."""
+    kernel build (same sweeps per launch and strip height), or None."""
     p = os.path.join(ROOT, "profiles", "psi_sweep_%s_2049.md" % dtype_name)
     if not os.path.exists(p):
         return None
     vals = {}
     for line in open(p):
-        if ":" in line and line.split(":", 1)[0] in ("traffic_bytes_per_launch", "sweeps_per_launch"):
+        if ":" in line and line.split(":", 1)[0] in ("traffic_bytes_per_launch", "sweeps_per_launch", "strip_rows"):
             k, v = line.split(":", 1)
             try:
                 vals[k] = float(v.strip())
             except ValueError:
                 return None
-    if int(vals.get("sweeps_per_launch", 1)) != fuse:
+    if int(vals.get("sweeps_per_launch", 1)) != fuse or int(vals.get("strip_rows", 0)) != rows:
         return None
     return vals.get("traffic_bytes_per_launch")
 
@@ -441,10 +441,15 @@ def run_conv(args):
 def run_learned(args):
     """Learned CG warm start: relaxed 128^2 states generated by the batched device CG
     (kappa ~ U[2, 10], H ~ U[0.02, 0.5], hole masks), the network trained on them by
-    the library's BF16 kernels, then CG iterations and time to F* within 1e-6 from the
-    random start and from the prediction, on held-out instances at 128^2 and 256^2."""
+    the library's BF16 kernels; then, on held-out instances at 128^2 and 256^2,
+    (1) relaxed states/s of the learned + batched method (prediction, batched FP32
+    device CG) against the plain single-instance FP64 CG from the random start, one
+    stop rule and one criterion for both (`learned.states_throughput`), and
+    (2) CG iterations to F* within 1e-6 from the random start and from the
+    prediction (`learned.evaluate`)."""
     import torch
     from svirl_gb300 import learned as L
+    from svirl_gb300.relax import HandleCache
     if int(os.environ.get("RANK", "0")) != 0:
         return
     t0 = time.perf_counter()
@@ -458,20 +463,35 @@ def run_learned(args):
     t_train = time.perf_counter() - t0
     steps = args.epochs * (x.shape[0] // 32)
     del x, y
-    evals = {}
+    evals, thr = {}, {}
     for n, count in ((128, 64), (256, 24)):
         rng = np.random.default_rng(777 + n)
-        evals["%d" % n] = L.evaluate(net, [L.Instance.sample(n, rng) for _ in range(count)])
-    e = evals["128"]
-    value = e["iters_random_median"] / max(e["iters_warm_median"], 1.0)
-    line = {"metric": "CG iterations to dF/F<=1e-6: random start / learned warm start (median, 128^2)",
-            "value": value, "unit": "x", "n_gpus": 1, "steps": steps, "warmup": 0,
-            "ms_per_step": 1e3 * t_train / max(steps, 1), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16 net (f32 accumulate), f64 CG", "data": "synthetic (solver-generated)",
+        insts = [L.Instance.sample(n, rng) for _ in range(count)]
+        cache = HandleCache()
+        try:
+            Estar = L.reference_energies(insts, cache)  # untimed validation
+            thr["%d" % n] = L.states_throughput(net, insts, Estar, cache, cap=args.learned_cap, gtol=args.gtol,
+                                                plain_sample=args.plain_sample)
+            evals["%d" % n] = L.evaluate(net, insts, cache=cache, Estar=Estar)
+        finally:
+            cache.close()
+    t = thr["128"]
+    nodes = 128 * 128 * 64
+    line = {"metric": "GL states/s to dF/F<=1e-6, learned warm start + batched FP32 CG (128^2, 64 instances)",
+            "value": t["states_per_s"], "unit": "states/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1e3 * t["wall_s"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 net (f32 accumulate), f32 CG stencils, f64 reductions", "data": "synthetic (solver-generated)",
             "config": {"workload": "learned_warm_start", "train_states": args.train_states, "epochs": args.epochs,
                        "params": net.n_params(), "levels": list(L.LEVELS), "target_mode": "amplitude",
-                       "train_loss_first_last": [hist[0], hist[-1]], "gen_s": t_gen, "train_s": t_train},
-            "eval": evals}
+                       "train_loss_first_last": [hist[0], hist[-1]], "gen_s": t_gen, "train_s": t_train,
+                       "cg_cap": args.learned_cap, "gtol_abs": args.gtol,
+                       "criterion": "(F - F*)/|F*| <= 1e-6, F* = FP64 relaxation from the random start (gradient "
+                                    "norm 1e-7, 20000 iterations)"},
+            "speedup_vs_plain": t["speedup_vs_plain"], "throughput": thr, "eval": evals,
+            "e2e": {"value": t["states_per_s"], "unit": "states/s", "h2d_bytes_per_step": nodes * 8 * 2,
+                    "d2h_bytes_per_step": nodes * 4 * 4,
+                    "how": "wall time of features to the device, prediction, decoding to host, states into the "
+                           "handles, batched CG, states back"}}
     print(json.dumps(line), flush=True)
 
 
@@ -496,7 +516,9 @@ def main():
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--cg-iters", type=int, default=12000)
     ap.add_argument("--gtol", type=float, default=1e-4)
-    ap.add_argument("--plain-sample", type=int, default=4)
+    ap.add_argument("--plain-sample", type=int, default=8)
+    ap.add_argument("--learned-cap", type=int, default=4000,
+                    help="CG iteration cap of both arms of the learned + batched states/s comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -559,6 +581,7 @@ def main():
     # the right-hand side and two link values of A, write psi^(k+1) (32 B FP32,
     # 64 B FP64), +1 B for the material mask.
     fuse = int(h.lib.glgpu_psi_sweeps_per_launch())
+    rows = int(h.lib.glgpu_psi_strip_rows(h.h))
     sweep_ms = h.time_sweeps(0, 20)
     bytes_per_node_sweep = (32 if dtype == np.float32 else 64) + 1
     alg_bytes = N * bytes_per_node_sweep * fuse
@@ -601,8 +624,8 @@ def main():
                              % (N * (3 * (8 if dtype == np.float32 else 16) + (8 if dtype == np.float32 else 16)) / 1e6),
                        "mean_sweeps_per_step": sweeps / args.steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": ncu_traffic(args.dtype, fuse),
-                         "kernel": "k_psi_sweep", "sweeps_per_launch": fuse,
+                         "frac": achieved / peak, "traffic": ncu_traffic(args.dtype, fuse, rows),
+                         "kernel": "k_psi_sweep", "sweeps_per_launch": fuse, "strip_rows": rows,
                          "bytes_per_node_sweep": bytes_per_node_sweep, "bytes_per_launch": alg_bytes,
                          "launch_ms": sweep_ms, "peak_kind": peak_kind},
             "e2e": {"value": e2e_value, "unit": "node-steps/s",

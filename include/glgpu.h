@@ -84,6 +84,12 @@ int glgpu_version(void);
  * (temporal blocking; every sweep is still written, so the loop stops exactly
  * where the reference's one-sweep-per-launch loop stops). */
 int glgpu_psi_sweeps_per_launch(void);
+/* Rows per warp strip of the psi sweep chosen for this handle (from the compiled
+ * strip heights, by the item-count model of the persistent sweep); 0 if h is NULL. */
+int glgpu_psi_strip_rows(const glgpu_handle* h);
+/* Force the strip height (one of the compiled heights; 0 = the model's choice).
+ * Results do not depend on it: every node gets the same arithmetic. */
+int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows);
 
 /* --- state and parameters (svirl/vars/vars.py:53-127, svirl/vars/params.py,
  *     svirl/mesh/grid.py:102-127) */

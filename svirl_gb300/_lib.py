@@ -47,6 +47,8 @@ _P = C.c_void_p
 _SIGNATURES = {
     "glgpu_version": (C.c_int, []),
     "glgpu_psi_sweeps_per_launch": (C.c_int, []),
+    "glgpu_psi_strip_rows": (C.c_int, [_H]),
+    "glgpu_set_psi_strip_rows": (C.c_int, [_H, C.c_int32]),
     "glgpu_last_error": (C.c_char_p, [_H]),
     "glgpu_create": (C.c_int, [C.POINTER(Grid), C.c_int32, C.POINTER(_H)]),
     "glgpu_destroy": (C.c_int, [_H]),
@@ -234,6 +236,12 @@ class Handle:
     def set_eps_field(self, eps_flat):
         a = None if eps_flat is None else np.ascontiguousarray(eps_flat, dtype=self.dtype)
         check(self.lib.glgpu_set_linear_coefficient_field(self.h, ptr(a)), self.h, "set_linear_coefficient_field")
+
+    def psi_strip_rows(self):
+        return int(self.lib.glgpu_psi_strip_rows(self.h))
+
+    def set_psi_strip_rows(self, rows):
+        check(self.lib.glgpu_set_psi_strip_rows(self.h, int(rows)), self.h, "set_psi_strip_rows")
 
     def set_use_graphs(self, enable):
         check(self.lib.glgpu_set_use_graphs(self.h, 1 if enable else 0), self.h, "set_use_graphs")

@@ -118,6 +118,8 @@ int glgpu_version(void) { return 10000; }
 
 int glgpu_psi_sweeps_per_launch(void) { return kFuse; }
 
+int glgpu_psi_strip_rows(const glgpu_handle* h) { return h ? h->strip_rows : 0; }
+
 const char* glgpu_last_error(const glgpu_handle* h) { return h ? h->last_error.c_str() : g_create_error.c_str(); }
 
 int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
@@ -153,8 +155,11 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     ok = ok && cudaMalloc(&h->st_gather, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->inst, sizeof(Inst)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->tiles, sizeof(Tile) * (size_t)h->ntiles) == cudaSuccess;
-    const int nstrips = (h->g.Nx + kStripCols - 1) / kStripCols, nrows = (h->g.Ny + kStripRows - 1) / kStripRows;
-    h->nitems = nstrips * nrows;
+    {
+        const Geo* gp = &h->g;
+        h->strip_rows = choose_strip_rows(h->dtype, &gp, 1);
+    }
+    h->nitems = strip_items(h->g.Nx, h->g.Ny, h->strip_rows);
     ok = ok && cudaMalloc(&h->items, sizeof(Item) * (size_t)h->nitems) == cudaSuccess;
     ok = ok && cudaMalloc(&h->loop, sizeof(LoopState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->partials, sizeof(double) * 17 * (size_t)nblk) == cudaSuccess;
@@ -171,12 +176,8 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     }
     std::vector<Tile> tiles(h->ntiles);
     for (int k = 0; k < h->ntiles; ++k) tiles[k] = Tile{0, k * kThreads};
-    // items row-block major, so that concurrently running warps share halo rows in L2
-    std::vector<Item> items;
-    items.reserve(h->nitems);
-    for (int r = 0; r < nrows; ++r)
-        for (int s = 0; s < nstrips; ++s) items.push_back(Item{0, kStripCols * s, kStripRows * r, 0});
-    h->psi_grid = psi_sweep_grid(h->dtype, h->nitems);
+    const std::vector<Item> items = make_items(h->g, 0, h->strip_rows);
+    h->psi_grid = psi_sweep_grid(h->dtype, h->strip_rows, h->nitems);
     InstState st;
     memset(&st, 0, sizeof(st));
     st.rand_t = h->p.rand_t;
@@ -304,6 +305,40 @@ int glgpu_set_use_graphs(glgpu_handle* h, int32_t enable) {
     return GLGPU_OK;
 }
 
+int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    cudaSetDevice(h->device);
+    if (rows == 0) {
+        const Geo* gp = &h->g;
+        rows = choose_strip_rows(h->dtype, &gp, 1);
+    }
+    bool known = false;
+    for (int v = 0; v < kNumStripRows; ++v) known = known || kStripRowsSet[v] == rows;
+    if (!known) return set_error(h, GLGPU_E_ARG, "set_psi_strip_rows: strip height not compiled in");
+    if (rows == h->strip_rows) return GLGPU_OK;
+    const std::vector<Item> items = make_items(h->g, 0, rows);
+    Item* buf = nullptr;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&buf, sizeof(Item) * items.size());
+    if (e == cudaSuccess) e = cudaMemcpy(buf, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        if (buf) cudaFree(buf);
+        return cuda_check(h, e, "set_psi_strip_rows");
+    }
+    cudaFree(h->items);
+    h->items = buf;
+    h->strip_rows = rows;
+    h->nitems = (int)items.size();
+    h->psi_grid = psi_sweep_grid(h->dtype, rows, h->nitems);
+    for (int q = 0; q < 6; ++q)  // the TD graphs hold the old kernel, grid and table
+        if (h->td_exec[q]) {
+            cudaGraphExecDestroy(h->td_exec[q]);
+            h->td_exec[q] = nullptr;
+        }
+    upload_inst(h);
+    return cuda_check(h, cudaStreamSynchronize(h->stream), "set_psi_strip_rows");
+}
+
 int glgpu_td(glgpu_handle* h, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats) {
     if (check_handle(h)) return GLGPU_E_ARG;
     cudaSetDevice(h->device);
@@ -395,16 +430,19 @@ int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** ou
     cudaSetDevice(b->device);
     std::vector<Tile> tiles;
     std::vector<Item> items;
+    std::vector<const Geo*> geos(n);
+    for (int q = 0; q < n; ++q) geos[q] = &handles[q]->g;
+    b->strip_rows = choose_strip_rows(b->dtype, geos.data(), n);
+    b->inst_items.resize(n);
     for (int q = 0; q < n; ++q) {
-        const Geo& g = handles[q]->g;
         for (int k = 0; k < handles[q]->ntiles; ++k) tiles.push_back(Tile{q, k * kThreads});
-        const int nstrips = (g.Nx + kStripCols - 1) / kStripCols, nrows = (g.Ny + kStripRows - 1) / kStripRows;
-        for (int r = 0; r < nrows; ++r)
-            for (int s = 0; s < nstrips; ++s) items.push_back(Item{q, kStripCols * s, kStripRows * r, 0});
+        const std::vector<Item> it = make_items(handles[q]->g, q, b->strip_rows);
+        b->inst_items[q] = (int)it.size();
+        items.insert(items.end(), it.begin(), it.end());
     }
     b->ntiles = (int)tiles.size();
     b->nitems = (int)items.size();
-    b->psi_grid = psi_sweep_grid(b->dtype, b->nitems);
+    b->psi_grid = psi_sweep_grid(b->dtype, b->strip_rows, b->nitems);
     b->gather_h.resize(n);
     bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && cudaMalloc(&b->insts, sizeof(Inst) * (size_t)n) == cudaSuccess;

@@ -20,9 +20,6 @@ namespace glgpu {
 #ifndef GLGPU_FUSE
 #define GLGPU_FUSE 3
 #endif
-#ifndef GLGPU_STRIP_ROWS
-#define GLGPU_STRIP_ROWS 12
-#endif
 constexpr int kFuse = GLGPU_FUSE;
 static_assert(kFuse >= 1 && kFuse <= 4, "1 <= GLGPU_FUSE <= 4");
 constexpr int kPsiBufs = kFuse + 2;  // right-hand side + input + kFuse outputs
@@ -110,10 +107,20 @@ struct Tile {
 };
 
 // Work item of the warp-strip psi sweep: kStripCols output columns (x0..) by
-// kStripRows rows (j0..) of one instance, processed by one warp whose 32 lanes
-// also cover kFuse halo columns on each side.
-constexpr int kStripRows = GLGPU_STRIP_ROWS;
+// `rows` rows (j0..) of one instance, processed by one warp whose 32 lanes also
+// cover kFuse halo columns on each side.  The sweep kernel is compiled for the
+// strip heights of kStripRowsSet; a handle or batch uses the one that
+// choose_strip_rows (td.cu) picks for its item count.
+#ifdef GLGPU_STRIP_ROWS
+constexpr int kStripRowsSet[] = {GLGPU_STRIP_ROWS};
+#else
+constexpr int kStripRowsSet[] = {8, 12, 17};
+#endif
+constexpr int kNumStripRows = (int)(sizeof(kStripRowsSet) / sizeof(kStripRowsSet[0]));
 constexpr int kStripCols = 32 - 2 * kFuse;
+inline int strip_items(int Nx, int Ny, int rows) {
+    return ((Nx + kStripCols - 1) / kStripCols) * ((Ny + rows - 1) / rows);
+}
 struct Item {
     int inst, x0, j0, pad;
 };
@@ -141,6 +148,7 @@ struct glgpu_handle {
     glgpu::Tile* tiles = nullptr;
     glgpu::Item* items = nullptr;
     int nitems = 0;
+    int strip_rows = 0;                 // strip height of the psi sweep items
     int psi_grid = 0;                   // CTAs of the persistent psi sweep
     glgpu::LoopState* loop = nullptr;
     int ntiles = 0;
@@ -184,7 +192,8 @@ struct glgpu_batch {
     glgpu::LoopState* loop = nullptr;
     glgpu::InstState* gather = nullptr;
     std::vector<glgpu::InstState> gather_h;
-    int ntiles = 0, nitems = 0, psi_grid = 0;
+    int ntiles = 0, nitems = 0, psi_grid = 0, strip_rows = 0;
+    std::vector<int> inst_items;         // psi sweep items of each instance (at strip_rows)
     cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool td_graph_failed = false, use_graphs = true;
     // batched device CG (allocated on first use)
@@ -211,7 +220,9 @@ size_t real_size(const glgpu_handle* h);
 // td.cu
 int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms);
 int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms);
-int psi_sweep_grid(int dtype, int nitems);
+int choose_strip_rows(int dtype, const Geo* const* geos, int n);
+int psi_sweep_grid(int dtype, int rows, int nitems);
+std::vector<Item> make_items(const Geo& g, int inst, int rows);
 // obs.cu
 int obs_free_energy(glgpu_handle* h, double* out);
 int obs_magnetic_field(glgpu_handle* h, void* host_out);

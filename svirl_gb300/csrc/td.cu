@@ -208,7 +208,7 @@ template <typename T> struct PsiRow {
 // kFuse Jacobi sweeps of the psi step (svirl/cuda/td.h:4-133) over every active
 // instance in one launch, reading the per-step tables of k_link_U (link factors
 // U and link-weight codes), so the sweep does no transcendental math and no mask
-// logic.  A warp owns a strip of kStripCols output columns and kStripRows rows;
+// logic.  A warp owns a strip of kStripCols output columns and RR rows;
 // its 32 lanes hold the columns x0-kFuse .. x0+31-kFuse, and sweep l (1..kFuse)
 // is valid on lanes l..31-l, so the halo columns are recomputed in registers
 // instead of being exchanged.  The warp walks down the rows: at step s it loads
@@ -229,11 +229,11 @@ template <typename T> struct PsiRow {
 #endif
 
 constexpr int kPsiThreads = GLGPU_PSI_THREADS, kPsiWarps = kPsiThreads / 32;
-template <typename T>
+template <typename T, int RR>
 __global__ void __launch_bounds__(kPsiThreads, GLGPU_PSI_MIN_CTAS)
 k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
             cudaGraphConditionalHandle cond, int use_cond) {
-    constexpr int K = kFuse, RR = kStripRows, S = kStripRows + 2 * kFuse;
+    constexpr int K = kFuse, S = RR + 2 * kFuse;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kPsiWarps + (threadIdx.x >> 5), nw = gridDim.x * kPsiWarps;
     int cur_inst = -1, k = 0, count = 0, done = 1;
@@ -593,12 +593,29 @@ struct TDLaunch {
     const Tile* tiles;
     const Item* items;
     LoopState* loop;
-    int ninst, ntiles, nitems, psi_grid, dtype;
+    int ninst, ntiles, nitems, psi_grid, dtype, strip_rows;
     bool any_solveA;
 };
 
-static void* psi_sweep_fn(int dtype) {
-    return dtype == 8 ? (void*)k_psi_sweep<double> : (void*)k_psi_sweep<float>;
+template <int V>
+static void* psi_sweep_fn_v(int dtype, int rows) {
+    if constexpr (V < kNumStripRows) {
+        constexpr int R = kStripRowsSet[V];
+        if (rows == R) return dtype == 8 ? (void*)k_psi_sweep<double, R> : (void*)k_psi_sweep<float, R>;
+        return psi_sweep_fn_v<V + 1>(dtype, rows);
+    } else {
+        return nullptr;
+    }
+}
+// the sweep kernel compiled for strip height `rows` (one of kStripRowsSet)
+static void* psi_sweep_fn(int dtype, int rows) { return psi_sweep_fn_v<0>(dtype, rows); }
+
+static cudaError_t launch_psi_sweep(int dtype, int rows, int grid, cudaStream_t s, const Inst* insts, const Item* items,
+                                    int nitems, LoopState* loop) {
+    cudaGraphConditionalHandle none = 0;
+    int zero = 0;
+    void* a[] = {&insts, &items, &nitems, &loop, &none, &zero};
+    return cudaLaunchKernel(psi_sweep_fn(dtype, rows), dim3(grid), dim3(kPsiThreads), a, 0, s);
 }
 static void* A_sweep_fn(int dtype) {
     return dtype == 8 ? (void*)k_A_sweep<double> : (void*)k_A_sweep<float>;
@@ -677,7 +694,8 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         {
             cudaGraphNode_t sw;
             void* a[] = {&insts, &items, &nitems, &loop, &hpsi, &one};
-            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype), dim3(L.psi_grid), dim3(kPsiThreads), a));
+            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype, L.strip_rows), dim3(L.psi_grid),
+                            dim3(kPsiThreads), a));
         }
         {
             void* a[] = {&insts, &ninst, &zero};
@@ -747,8 +765,7 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
             for (;;) {
                 for (int c = 0; c < chunk; ++c) {
                     if (part == 0) {
-                        if (L.dtype == 8) k_psi_sweep<double><<<L.psi_grid, kPsiThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
-                        else k_psi_sweep<float><<<L.psi_grid, kPsiThreads, 0, s>>>(L.insts, L.items, L.nitems, L.loop, none, 0);
+                        launch_psi_sweep(L.dtype, L.strip_rows, L.psi_grid, s, L.insts, L.items, L.nitems, L.loop);
                     } else {
                         if (L.dtype == 8) k_A_sweep<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
                         else k_A_sweep<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
@@ -828,8 +845,7 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
         k_bench_prep<<<1, 32, 0, h->stream>>>(h->inst, 1, h->loop, 1);
         cudaEventRecord(e0, h->stream);
         if (which == 0) {
-            if (h->dtype == 8) k_psi_sweep<double><<<h->psi_grid, kPsiThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
-            else k_psi_sweep<float><<<h->psi_grid, kPsiThreads, 0, h->stream>>>(h->inst, h->items, h->nitems, h->loop, none, 0);
+            launch_psi_sweep(h->dtype, h->strip_rows, h->psi_grid, h->stream, h->inst, h->items, h->nitems, h->loop);
         } else {
             if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
             else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
@@ -852,15 +868,49 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
 
 // CTAs of the persistent psi sweep: all SMs at full occupancy, or fewer if
 // there are fewer items than warps.
-int psi_sweep_grid(int dtype, int nitems) {
+// CTAs of the persistent sweep: one warp per item up to a full device.
+int psi_sweep_grid(int dtype, int rows, int nitems) {
     int dev = 0, sms = 1, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void* fn = psi_sweep_fn(dtype);
+    void* fn = psi_sweep_fn(dtype, rows);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPsiThreads, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
     const int need = (nitems + kPsiWarps - 1) / kPsiWarps;
     const int full = sms * per_sm;
     return need < full ? (need > 0 ? need : 1) : full;
+}
+
+// Strip height for a set of instances (a handle or a batch), from a model of
+// the persistent sweep: warps take items round-robin, so a launch lasts as long
+// as the warp with the most items, ceil(items / warps), and an item of R rows
+// costs about 3R + 6 row-sweeps (sweep l of the kFuse = 3 fused sweeps covers
+// R + 2(3 - l) rows).  Measured on 2049^2 (FP32, us per node-sweep): R = 8: 38.1,
+// 12: 34.7, 14: 33.5, 17: 32.2, 18: 32.7; the model ranks them the same way.
+int choose_strip_rows(int dtype, const Geo* const* geos, int n) {
+    int best = kStripRowsSet[0];
+    long long best_cost = -1;
+    for (int v = 0; v < kNumStripRows; ++v) {
+        const int R = kStripRowsSet[v];
+        long long items = 0;
+        for (int q = 0; q < n; ++q) items += strip_items(geos[q]->Nx, geos[q]->Ny, R);
+        const long long warps = (long long)psi_sweep_grid(dtype, R, (int)items) * kPsiWarps;
+        const long long cost = (items + warps - 1) / warps * (3LL * R + 2LL * kFuse);
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = R;
+        }
+    }
+    return best;
+}
+
+// Items of one instance, row-block major (concurrently running warps share halo rows in L2).
+std::vector<Item> make_items(const Geo& g, int inst, int rows) {
+    std::vector<Item> items;
+    const int nstrips = (g.Nx + kStripCols - 1) / kStripCols, nrows = (g.Ny + rows - 1) / rows;
+    items.reserve((size_t)nstrips * nrows);
+    for (int r = 0; r < nrows; ++r)
+        for (int s = 0; s < nstrips; ++s) items.push_back(Item{inst, kStripCols * s, rows * r, 0});
+    return items;
 }
 
 struct TDOutcome {
@@ -957,6 +1007,7 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     TDLaunch L;
     L.insts = h->inst; L.tiles = h->tiles; L.items = h->items; L.loop = h->loop;
     L.ninst = 1; L.ntiles = h->ntiles; L.nitems = h->nitems; L.psi_grid = h->psi_grid; L.dtype = h->dtype;
+    L.strip_rows = h->strip_rows;
     L.any_solveA = h->inst_h.solveA != 0;
     InstState hs;
     TDOutcome o = td_core(h->stream, L, Nt, eqn, h->td_exec, &h->td_graph_failed, h->use_graphs, elapsed_ms != nullptr,
@@ -980,6 +1031,7 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
         h->inst_h.dt = dt;
         h->inst_h.fdt = (float)dt;
         insts[q] = h->inst_h;
+        insts[q].nitems = b->inst_items[q];  // at the batch's strip height
         any_solveA = any_solveA || h->inst_h.solveA != 0;
     }
     cudaError_t e = cudaMemcpyAsync(b->insts, insts.data(), sizeof(Inst) * insts.size(), cudaMemcpyHostToDevice, b->stream);
@@ -987,6 +1039,7 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
     TDLaunch L;
     L.insts = b->insts; L.tiles = b->tiles; L.items = b->items; L.loop = b->loop;
     L.ninst = b->ninst; L.ntiles = b->ntiles; L.nitems = b->nitems; L.psi_grid = b->psi_grid; L.dtype = b->dtype;
+    L.strip_rows = b->strip_rows;
     L.any_solveA = any_solveA;
     TDOutcome o = td_core(b->stream, L, Nt, eqn, b->td_exec, &b->td_graph_failed, b->use_graphs, elapsed_ms != nullptr,
                           b->gather, b->gather_h.data());

@@ -472,7 +472,15 @@ def train(net, x, y, epochs=5, batch=32, lr=1e-3, seed=0, log=None):
     return hist
 
 
-def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=1e-7, tol=1e-6, cache=None):
+def reference_energies(insts, cache, n_iter=20000, gtol=1e-7):
+    """F*: the FP64 energy of a tight relaxation of each instance from its random start."""
+    from .relax import relax
+    ref, _, _ = relax(insts, cache, np.float64, n_iter=n_iter, gtol=gtol, fetch=False)
+    return ref["energy"]
+
+
+def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=1e-7, tol=1e-6, cache=None,
+             Estar=None):
     """CG iterations and device time to reach F* within `tol` from the random start
     and from the network's prediction; F* = the energy of a tight relaxation from
     the random start (gradient norm `gtol`).  A prediction counts only where its
@@ -482,8 +490,8 @@ def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=
     own = cache is None
     cache = HandleCache() if own else cache
     try:
-        ref, _, _ = relax(insts, cache, dtype, n_iter=n_iter, gtol=gtol, fetch=False)
-        Estar = ref["energy"]
+        if Estar is None:
+            Estar = reference_energies(insts, cache, n_iter=n_iter, gtol=gtol)
         r, _, _ = relax(insts, cache, dtype, n_iter=n_iter, gtol=0.0, fetch=False, targets=Estar, target_tol=tol)
         torch.cuda.synchronize()
         t0 = _time.perf_counter()
@@ -502,3 +510,38 @@ def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=
             "iters_random_mean": float(r["iters"].mean()), "iters_warm_mean": float(w["iters"].mean()),
             "cg_ms_random": r["ms"], "cg_ms_warm": w["ms"], "net_ms": 1e3 * t_net,
             "warm_lower_energy": int((w["energy"] < Estar - tol * np.abs(Estar)).sum())}
+
+
+def states_throughput(net, insts, Estar, cache, cap=4000, gtol=1e-4, tol=1e-6, plain_sample=8, mode="amplitude"):
+    """Relaxed states per second, the learned + batched method against the plain
+    one, with one stop rule for both (absolute gradient norm `gtol` or `cap`
+    iterations) and one criterion: a state counts when (F - F*)/|F*| <= tol.
+    Learned + batched (timed end to end): features to the device, the network's
+    prediction, decoding, the predicted states into the handles, the batched FP32
+    device CG of all instances, the states back to the host.  Plain: the same
+    device CG on one instance at a time in FP64 from its random start, on the
+    first `plain_sample` instances."""
+    import time as _time
+    from .relax import energies_fp64, relax
+    torch.cuda.synchronize()
+    t0 = _time.perf_counter()
+    pred = net.predict(features(insts))
+    starts = decode(insts, pred, mode=mode)
+    out, states, _ = relax(insts, cache, np.float32, starts=starts, n_iter=cap, gtol=gtol)
+    wall = _time.perf_counter() - t0
+    rel = (energies_fp64(insts, states, cache) - Estar) / np.abs(Estar)
+    ok = int((rel <= tol).sum())
+    t_plain, ok_plain = 0.0, 0
+    for q, it in enumerate(insts[:plain_sample]):
+        t1 = _time.perf_counter()
+        _, st, _ = relax([it], cache, np.float64, n_iter=cap, gtol=gtol)
+        t_plain += _time.perf_counter() - t1
+        ok_plain += int((energies_fp64([it], st, cache)[0] - Estar[q]) / abs(Estar[q]) <= tol)
+    rate = ok / wall
+    plain_rate = ok_plain / t_plain if t_plain > 0 else 0.0
+    return {"states_per_s": rate, "ok": ok, "n": len(insts), "wall_s": wall, "cg_ms": out["ms"],
+            "rel_err_quantiles": np.quantile(rel, [0, 0.5, 0.9, 1]).tolist(),
+            "plain": {"states_per_s": plain_rate, "ok": ok_plain, "sample": min(plain_sample, len(insts)),
+                      "wall_s": t_plain},
+            "speedup_vs_plain": rate / plain_rate if plain_rate > 0 else None,
+            "cap": cap, "gtol_abs": gtol}
