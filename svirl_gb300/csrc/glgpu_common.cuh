@@ -208,13 +208,18 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
-// Sum NV per-thread float values over the CTA into doubles (thread 0): the
-// warp stage is compensated (each partial carried as a float pair hi + lo, the
-// rounding error of every addition kept by two_sum), the warp results are
-// added in double.  FP32 arithmetic with close to double accuracy, without the
-// FP64 pipe in the 5-level warp tree.  Fixed order: deterministic.
+// Sum NV per-thread float values over the CTA into doubles (thread 0).  Every
+// partial is carried as a float pair hi + lo, the rounding error of each
+// addition kept by two_sum (double-float arithmetic, close to FP64 accuracy):
+// a 5-level shuffle tree per warp, then thread k adds the warps' pairs of
+// component k in warp order and widens once to double.  GB300 issues an FP64
+// instruction at a small fraction of the FP32 rate whatever the number of
+// active lanes, so the reduction keeps FP64 to three instructions per CTA.
+// Fixed order: deterministic.
 template <int NV> __device__ __forceinline__ void block_sum(const float (&v)[NV], double (&out)[NV]) {
-    __shared__ double sm[kWarps][NV];
+    static_assert(NV <= kThreads, "one thread per component");
+    __shared__ float sh[kWarps][NV], sl[kWarps][NV];
+    __shared__ double so[NV];
     const int tid = flat_tid(), lane = tid & 31, w = tid >> 5;
     __syncthreads();
 #pragma unroll
@@ -227,19 +232,27 @@ template <int NV> __device__ __forceinline__ void block_sum(const float (&v)[NV]
             hi = sum;
             lo = lo + (ol + err);
         }
-        // Only lane 0 widens to double: the FP64 pipe runs at a small fraction
-        // of the FP32 rate, and the other lanes' pairs are discarded.
-        if (lane == 0) sm[w][k] = (double)hi + (double)lo;
-    }
-    __syncthreads();
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            double s = 0.0;
-            for (int q = 0; q < kWarps; ++q) s += sm[q][k];
-            out[k] = s;
+        if (lane == 0) {
+            sh[w][k] = hi;
+            sl[w][k] = lo;
         }
     }
+    __syncthreads();
+    if (tid < NV) {
+        float hi = sh[0][tid], lo = sl[0][tid];
+#pragma unroll
+        for (int q = 1; q < kWarps; ++q) {
+            float sum, err;
+            two_sum(hi, sh[q][tid], sum, err);
+            hi = sum;
+            lo = lo + (sl[q][tid] + err);
+        }
+        so[tid] = (double)hi + (double)lo;
+    }
+    __syncthreads();
+    if (tid == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[k] = so[k];
 }
 template <int NV> __device__ __forceinline__ void block_sum(const double (&v)[NV], double (&out)[NV]) {
 #pragma unroll

@@ -227,6 +227,10 @@ template <typename T> struct PsiRow {
 #ifndef GLGPU_PSI_MIN_CTAS
 #define GLGPU_PSI_MIN_CTAS 1
 #endif
+// Row steps of the strip walk unrolled together (0: the whole walk).
+#ifndef GLGPU_PSI_ROW_UNROLL
+#define GLGPU_PSI_ROW_UNROLL 0
+#endif
 
 constexpr int kPsiThreads = GLGPU_PSI_THREADS, kPsiWarps = kPsiThreads / 32;
 template <typename T, int RR>
@@ -234,6 +238,7 @@ __global__ void __launch_bounds__(kPsiThreads, GLGPU_PSI_MIN_CTAS)
 k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
             cudaGraphConditionalHandle cond, int use_cond) {
     constexpr int K = kFuse, S = RR + 2 * kFuse;
+    constexpr int kRowUnroll = GLGPU_PSI_ROW_UNROLL > 0 ? GLGPU_PSI_ROW_UNROLL : S;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kPsiWarps + (threadIdx.x >> 5), nw = gridDim.x * kPsiWarps;
     int cur_inst = -1, k = 0, count = 0, done = 1;
@@ -326,7 +331,7 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
         };
         C2<T> nx_p = load_psi(j0 - K);
         PsiSide<T> nx_s = load_side(j0 - K - 1);
-#pragma unroll
+#pragma unroll kRowUnroll
         for (int s = 0; s < S; ++s) {
             C2<T> newrow = nx_p;  // psi^(k) on row j0 - K + s
 #pragma unroll
