@@ -61,6 +61,7 @@ void upload_inst(glgpu_handle* h) {
     I.code = h->code;
     I.st = h->st;
     I.cg = h->cgst;
+    I.cbits = h->cbits;
     for (int q = 0; q < 2; ++q) {
         I.gpsi[q] = h->g_psi[q];
         I.gA[q] = h->g_A[q];
@@ -98,6 +99,7 @@ static void free_all(glgpu_handle* h) {
         if (h->td_exec[q]) cudaGraphExecDestroy(h->td_exec[q]);
     if (h->st_gather) cudaFree(h->st_gather);
     if (h->cgst) cudaFree(h->cgst);
+    if (h->cbits) cudaFree(h->cbits);
     for (int q = 0; q < 2; ++q) {
         if (h->g_psi[q]) cudaFree(h->g_psi[q]);
         if (h->g_A[q]) cudaFree(h->g_A[q]);

@@ -105,8 +105,9 @@ k_cg_dir_coef(Geo g, double kappa2, double eps0, const T* eps_sp, double H, cons
                 if (j < g.Ny - 1) { int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
             }
         }
-        coef_node<T, NV>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, psi, abei, ab, PhaseLinks<T>{abei, ab}, n, i, j, cb, dpsi, dA,
-                         c);
+        coef_node<T, NV>(g, (T)kappa2, (T)eps0, eps_sp, (T)H, [psi](int m) { return psi[m]; },
+                         [abei, ab](int l) { return link_phase(abei, ab, l); }, ab, PhaseLinks<T>{abei, ab}, n, i, j, cb,
+                         dpsi, dA, c);
     }
     grid_sum_finish(c, partials, counter, dscal, g.dxdy);
 }
@@ -151,7 +152,8 @@ int cg_ensure(glgpu_handle* h) {
         cudaMemsetAsync(h->dir_A[q], 0, ab, h->stream);
     }
     cudaMemsetAsync(h->dscal + 28, 0, 2 * sizeof(double), h->stream);  // beta = 0
-    if (cudaMalloc(&h->cgst, sizeof(CGState)) != cudaSuccess) return set_error(h, GLGPU_E_OOM, "cg: out of device memory");
+    if (cudaMalloc(&h->cgst, sizeof(CGState)) != cudaSuccess || cudaMalloc(&h->cbits, (size_t)h->g.N) != cudaSuccess)
+        return set_error(h, GLGPU_E_OOM, "cg: out of device memory");
     cudaMemsetAsync(h->cgst, 0, sizeof(CGState), h->stream);
     h->cg_g = 0;
     h->cg_dir = 0;

@@ -169,7 +169,7 @@ __device__ __forceinline__ void grad_tile(const Inst& I, int n0, const C2<T>* __
         const int n = n0 + threadIdx.x + r * kThreads;
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
-            const unsigned cb = cell_bits(g, I.mt, i, j);
+            const unsigned cb = I.cbits[n];
             const C2<T> gv = grad_psi_node<T>(g, eps0, (const T*)I.eps_sp, psi, lk, n, i, j, cb);
             const C2<T> gp = Gp[n];
             v[0] += gv.x * (gv.x - gp.x) + gv.y * (gv.y - gp.y);
@@ -445,19 +445,22 @@ __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, T bp, T bA,
         return cmk<T>(bp * o.x - gg.x, bp * o.y - gg.y);
     };
     auto dA = [&](int m) -> T { return bA * dAO[m] - GA[m]; };
+    auto psi_at = [&](int m) -> C2<T> { return psi[m]; };
+    auto phase = [&](int l) -> T { return link_phase(abei, ab, l); };
     const T eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
 #pragma unroll 1
     for (int r = 0; r < kCGRep; ++r) {
         const int n = n0 + threadIdx.x + r * kThreads;
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
-            const unsigned cb = cell_bits(g, I.mt, i, j);
+            const unsigned cb = I.cbits[n];
             if (I.solveA) {
-                coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i,
-                                 j, cb, dpsi, dA, c);
+                coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi_at, phase, ab, lk,
+                                 n, i, j, cb, dpsi, dA, c);
             } else {
                 T c5[5] = {T(0), T(0), T(0), T(0), T(0)};
-                coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi, abei, ab, lk, n, i, j, cb, dpsi, dA, c5);
+                coef_node<T, 5>(g, T(-1), eps0, (const T*)I.eps_sp, H, psi_at, phase, ab, lk, n, i, j, cb, dpsi, dA,
+                                c5);
                 c[0] += c5[0]; c[5] += c5[1]; c[10] += c5[2]; c[15] += c5[3]; c[16] += c5[4];
             }
             dN[n] = dpsi(n);
@@ -554,8 +557,8 @@ __device__ __forceinline__ void step_tile(const Inst& I, int n0, T ap, T aA, con
                 }
             }
             // the node's own links' factors were written above by this thread
-            v[0] += energy_density_f<T>(g, k2, eps0, (const T*)I.eps_sp, H, I.mt, psi_new, abei, I.solveA != 0,
-                                        ab_new, lk, n);
+            v[0] += energy_density_f<T>(g, k2, eps0, (const T*)I.eps_sp, H, (unsigned)I.cbits[n], psi_new, abei,
+                                        I.solveA != 0, ab_new, lk, n, i, j);
             psiN[n] = psi_new(n);
         }
     }
@@ -652,8 +655,10 @@ kb_finish(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
     }
 }
 
-// start of a CG call: zero direction and gradient, the link-factor table of the
-// start state (TableLinks), then the energy of the start state
+// start of a CG call: zero direction and gradient, the per-node cell bits (so
+// the iteration kernels read one byte instead of four mask cells), the
+// link-factor table of the start state (TableLinks), then the energy of the
+// start state
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 kb_zero_dir(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
@@ -667,6 +672,7 @@ kb_zero_dir(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
         ((C2<T>*)I.dpsi[0])[n] = cmk<T>(T(0), T(0));
         ((C2<T>*)I.gpsi[0])[n] = cmk<T>(T(0), T(0));
         const int i = n % g.Nx, j = n / g.Nx;
+        I.cbits[n] = (uint8_t)cell_bits(g, I.mt, i, j);
         const T* abei = (const T*)I.abei;
         const T* ab = (const T*)I.ab[0];
         C2<T>* U = (C2<T>*)I.U;

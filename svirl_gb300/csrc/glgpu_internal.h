@@ -73,6 +73,7 @@ struct Inst {
     const void* eps_sp;       // spatial linear coefficient (nodes) or NULL
     void* U;                  // link factors exp(-i d a) of the psi loop, Nab complex
     uint8_t* code;            // per-node link-weight bits of the psi loop, N bytes
+    uint8_t* cbits;           // per-node cell bits (cell_bits) for the batched CG, N bytes (NULL until CG)
     InstState* st;
     CGState* cg;              // batched device CG state (NULL until used)
     void* gpsi[2];            // CG gradient buffers (psi part, A part) and directions
@@ -167,6 +168,7 @@ struct glgpu_handle {
     void* dir_A[2] = {nullptr, nullptr};
     int cg_g = 0, cg_dir = 0;           // current index of g / dir
     glgpu::CGState* cgst = nullptr;     // batched device CG state
+    uint8_t* cbits = nullptr;           // batched CG: cell bits per node, written at the start of a call
     // TD graphs, one per (equation mode, kappa finite)
     cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     glgpu::InstState* st_gather = nullptr;  // device copy target of the loop state
@@ -246,7 +248,7 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
              int32_t* status, double* elapsed_ms);
 // td.cu graph helpers
 cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps, void* fn, dim3 grid,
-                       dim3 block, void** args);
+                       dim3 block, void** args, unsigned smem_bytes = 0);
 cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
                       cudaGraphConditionalHandle h, cudaGraph_t* body);
 

@@ -73,15 +73,13 @@ template <typename T> __device__ __forceinline__ T cell_curl(const Geo& g, const
     return cell_curl_f<T>(g, [A](int l) { return A[l]; }, i, j, idx, idy);
 }
 
-// Free-energy pseudo-density at node n before the dx*dy factor
-// (svirl/cuda/observables.h:276-356).  psi(m) gives the order parameter at node
-// m, ab(l) the vector potential of link l (used only when has_ab).
+// Free-energy pseudo-density at node n = (i, j) with cell bits cb before the
+// dx*dy factor (svirl/cuda/observables.h:276-356).  psi(m) gives the order
+// parameter at node m, ab(l) the vector potential of link l (used only when has_ab).
 template <typename T, typename LK, typename PF, typename AF>
-__device__ __forceinline__ T energy_density_f(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H,
-                                              const uint8_t* mt, const PF& psi, const T* abei, bool has_ab,
-                                              const AF& ab, const LK& lk, int n) {
-    const int i = n % g.Nx, j = n / g.Nx;
-    const unsigned cb = cell_bits(g, mt, i, j);
+__device__ __forceinline__ T energy_density_f(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H, unsigned cb,
+                                              const PF& psi, const T* abei, bool has_ab, const AF& ab, const LK& lk,
+                                              int n, int i, int j) {
     const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
     const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
     T e = T(0);
@@ -116,8 +114,9 @@ template <typename T, typename LK>
 __device__ __forceinline__ T energy_density(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H,
                                             const uint8_t* mt, const C2<T>* psi, const T* abei, const T* ab,
                                             const LK& lk, int n) {
-    return energy_density_f<T>(g, kappa2, eps0, eps_sp, H, mt, [psi](int m) { return psi[m]; }, abei, ab != nullptr,
-                               [ab](int l) { return ab[l]; }, lk, n);
+    const int i = n % g.Nx, j = n / g.Nx;
+    return energy_density_f<T>(g, kappa2, eps0, eps_sp, H, cell_bits(g, mt, i, j), [psi](int m) { return psi[m]; },
+                               abei, ab != nullptr, [ab](int l) { return ab[l]; }, lk, n, i, j);
 }
 
 // curl curl A (times 1/kappa^2) on the link starting at node (i, j) along x (xdir)
@@ -257,15 +256,19 @@ __device__ __forceinline__ T grad_A_link(const Geo& g, T kappa2, T H, const C2<T
 // NV = 5: c0..c4 of F(psi + a dpsi) (svirl/cuda/cg.h:314-474); NV = 17: c00..c04,
 // c10..c14, c20..c24, c30, c40 of F(psi + a_psi dpsi, A + a_A dA)
 // (svirl/cuda/cg.h:477-731).  dpsi(m) and dA(l) give the search direction.
-template <typename T, int NV, typename FD, typename FA, typename LK>
-__device__ __forceinline__ void coef_node(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H, const C2<T>* psi,
-                                          const T* abei, const T* ab, const LK& lk, int n, int i, int j, unsigned cb,
-                                          const FD& dpsi, const FA& dA, T (&c)[NV]) {
+// psi(m) gives the order parameter at node m, phase(l) the phase A_ei + A of link l
+// (link_phase), ab5 the vector potential alone (read by the NV = 5 magnetic term
+// only, which the kappa = inf callers never reach); lk the link factors of the
+// node's own links.
+template <typename T, int NV, typename PS, typename PH, typename FD, typename FA, typename LK>
+__device__ __forceinline__ void coef_node(const Geo& g, T kappa2, T eps0, const T* eps_sp, T H, const PS& psi,
+                                          const PH& phase, const T* ab5, const LK& lk, int n, int i, int j,
+                                          unsigned cb, const FD& dpsi, const FA& dA, T (&c)[NV]) {
     const T dx = GT(g, dx), dy = GT(g, dy), idx = GT(g, idx), idy = GT(g, idy);
     const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
     if (cb) {
         const DuW<T> w = du_weights<T>(cb);
-        const C2<T> p0 = psi[n];
+        const C2<T> p0 = psi(n);
         const C2<T> d0 = dpsi(n);
         const T eps = eps_sp ? eps_sp[n] : eps0;
         const T p2 = cabs2(p0), d2 = cabs2(d0);
@@ -288,7 +291,7 @@ __device__ __forceinline__ void coef_node(const Geo& g, T kappa2, T eps0, const 
             const int m1 = dir == 0 ? n + 1 : n + g.Nx;
             const T d = dir == 0 ? dx : dy;
             const T wr = (dir == 0 ? w.r_p0 : w.r_0p) * (dir == 0 ? idx2 : idy2);
-            const C2<T> p1 = psi[m1], d1 = dpsi(m1);
+            const C2<T> p1 = psi(m1), d1 = dpsi(m1);
             T s, cs;
             lk.sc_split(nl, d, s, cs);
             const C2<T> gp = grad_c_sc<T>(p0, s, cs, p1), gd = grad_c_sc<T>(d0, s, cs, d1);
@@ -325,11 +328,11 @@ __device__ __forceinline__ void coef_node(const Geo& g, T kappa2, T eps0, const 
         const int Nxa = g.Nx - 1;
         const int ia00 = i + Nxa * j, ia0p = i + Nxa * (j + 1), ib00 = g.Na + i + g.Nx * j, ibp0 = g.Na + i + 1 + g.Nx * j;
         if (NV == 5) {
-            const T dB = idx * (ab[ibp0] - ab[ib00]) - idy * (ab[ia0p] - ab[ia00]) - H;
+            const T dB = idx * (ab5[ibp0] - ab5[ib00]) - idy * (ab5[ia0p] - ab5[ia00]) - H;
             c[0] += kappa2 * dB * dB;
         } else {
-            const T a00 = link_phase(abei, ab, ia00), a0p = link_phase(abei, ab, ia0p);
-            const T b00 = link_phase(abei, ab, ib00), bp0 = link_phase(abei, ab, ibp0);
+            const T a00 = phase(ia00), a0p = phase(ia0p);
+            const T b00 = phase(ib00), bp0 = phase(ibp0);
             const T BH = idx * (bp0 - b00) - idy * (a0p - a00) - H;
             const T dB = idx * (dA(ibp0) - dA(ib00)) - idy * (dA(ia0p) - dA(ia00));
             c[0] += kappa2 * BH * BH;

@@ -630,13 +630,13 @@ static void* link_fn(int dtype) {
 }
 
 cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, int ndeps,
-                              void* fn, dim3 grid, dim3 block, void** args) {
+                              void* fn, dim3 grid, dim3 block, void** args, unsigned smem_bytes) {
     cudaKernelNodeParams p;
     memset(&p, 0, sizeof(p));
     p.func = fn;
     p.gridDim = grid;
     p.blockDim = block;
-    p.sharedMemBytes = 0;
+    p.sharedMemBytes = smem_bytes;
     p.kernelParams = args;
     p.extra = nullptr;
     return cudaGraphAddKernelNode(node, g, deps, ndeps, &p);
