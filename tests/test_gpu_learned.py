@@ -22,9 +22,15 @@ def test_trained_network_gain_is_measured():
     ev = [L.Instance.sample(64, rng) for _ in range(16)]
     cache = HandleCache()
     try:
-        res = L.evaluate(net, ev, n_iter=8000, cache=cache)
+        Estar = L.reference_energies(ev, cache, n_iter=8000)
+        res = L.evaluate(net, ev, n_iter=8000, cache=cache, Estar=Estar)
+        thr = L.states_throughput(net, ev, Estar, cache, cap=1500, plain_sample=4)
     finally:
         cache.close()
     assert res["reached_random"] >= 8
     assert 0 <= res["reached_warm"] <= res["n"]
+    # the throughput comparison counts states by the same criterion on both arms
+    assert 0 <= thr["ok"] <= thr["n"] and 0 <= thr["plain"]["ok"] <= thr["plain"]["sample"]
+    assert thr["wall_s"] > 0 and thr["plain"]["wall_s"] > 0
     print("learned warm start (64^2):", res)
+    print("learned + batched states/s (64^2):", thr)
