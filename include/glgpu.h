@@ -91,6 +91,18 @@ int glgpu_psi_strip_rows(const glgpu_handle* h);
  * Results do not depend on it: every node gets the same arithmetic. */
 int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows);
 
+/* --- fixed vortices (svirl/vars/fixed_vortices.py, svirl/solvers/td.py:120-154,
+ *     204-216, 252-325): the irregular vector potential A_irr (Nab values, flat
+ *     [a | b], or NULL to remove it) and the phase-lock node list (flat node
+ *     indices; count 0 removes it).  The TD step adds A_irr to the first N elements
+ *     of A around the psi loop and A to the first N elements of A_irr around the A
+ *     loop, as the reference does, so the device copy of A_irr changes during A
+ *     loops: the getter returns it.  With td_copy_only the setter only replaces
+ *     the values of an A_irr already set (resuming from a checkpoint). */
+int glgpu_set_irregular_vector_potential(glgpu_handle* h, const void* vpi, int32_t td_copy_only);
+int glgpu_get_irregular_vector_potential(glgpu_handle* h, void* out);
+int glgpu_set_phase_lock(glgpu_handle* h, const int32_t* nodes, int32_t count);
+
 /* --- state and parameters (svirl/vars/vars.py:53-127, svirl/vars/params.py,
  *     svirl/mesh/grid.py:102-127) */
 int glgpu_set_params(glgpu_handle* h, const glgpu_params* p);

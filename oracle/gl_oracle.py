@@ -94,19 +94,23 @@ class GLOracle:
     """One GL instance in flat reference layout, FP64 arithmetic.
 
     ``psi`` complex (N,), ``ab`` real (Nab,), ``mt`` bool cells (Nc,) or None,
-    ``abei`` real (Nab,) or None (external + irregular vector potential).
+    ``abei`` real (Nab,) or None (external + irregular vector potential),
+    ``vpi`` real (Nab,) or None (irregular vector potential of fixed vortices, as
+    the TD step uses it), ``lock_ns`` int node indices or None (phase lock).
     """
 
     def __init__(self, Nx, Ny, dx, dy, psi, ab, mt=None, abei=None, kappa=np.inf, sigma=1.0,
                  epsilon=1.0, epsilon_spatial=None, H=0.0, stop_psi=1e-6, stop_A=1e-6,
                  rand_t=1, langevin_psi=0.0, langevin_A=0.0, convergence_rtol=1e-6,
-                 dtype=np.float64):
+                 dtype=np.float64, vpi=None, lock_ns=None):
         self.g = K.Grid(Nx, Ny, dx, dy)
         self.dtype = dtype
         self.psi = np.array(psi, dtype=np.complex128).reshape(-1).copy()
         self.ab = np.array(ab, dtype=np.float64).reshape(-1).copy()
         self.mt = None if mt is None else np.asarray(mt, dtype=bool).reshape(-1).copy()
         self.abei = None if abei is None else np.asarray(abei, dtype=np.float64).reshape(-1).copy()
+        self.vpi = None if vpi is None else np.asarray(vpi, dtype=np.float64).reshape(-1).copy()
+        self.lock_ns = None if lock_ns is None or len(lock_ns) == 0 else np.asarray(lock_ns, dtype=np.int64).copy()
         self.kappa = float(kappa)
         self.sigma = float(sigma)
         self.rho = 1.0 / self.sigma
@@ -159,13 +163,33 @@ class GLOracle:
         self.psi = cur
         self.rand_t = (self.rand_t + 1) & 0xFFFFFFFF
         self.sweeps_psi.append(nsw)
+        if self.lock_ns is not None:  # td.py:206-216
+            K.order_parameter_phase_lock(self.psi, self.lock_ns)
+
+    # fixed vortices around the psi step (td.py:120-154): xpy_r / xmy_r over the
+    # first N elements of the link array
+    def _fv_pre(self):
+        if self.vpi is not None:
+            N = self.g.N
+            self.ab[:N] += self.vpi[:N]
+
+    def _fv_post(self):
+        if self.vpi is not None:
+            N = self.g.N
+            self.ab[:N] -= self.vpi[:N]
 
     def _A_step(self, dt, stop):
         g = self.g
-        X = self.ab                       # buffer bound to the supercurrent argument
-        Y = np.empty_like(X)
-        rhs = X.copy()
-        cur, nxt_buf = X, Y
+        if self.vpi is not None:
+            # td.py:256-270: A_irr += A on the first N elements, and A_irr is the
+            # supercurrent argument (no aliasing with the A iterates)
+            self.vpi[:g.N] += self.ab[:g.N]
+            X = self.vpi
+            cur, nxt_buf = self.ab, np.empty_like(self.ab)
+        else:
+            X = self.ab                       # buffer bound to the supercurrent argument
+            cur, nxt_buf = X, np.empty_like(X)
+        rhs = self.ab.copy()
         nsw = 0
         for j in range(1024):
             vals, code = K.iterate_vector_potential_jacobi_step(
@@ -179,15 +203,20 @@ class GLOracle:
         self.ab = cur
         self.rand_t = (self.rand_t + 1) & 0xFFFFFFFF
         self.sweeps_A.append(nsw)
+        if self.vpi is not None:  # td.py:314-322
+            self.vpi[:g.N] -= self.ab[:g.N]
 
     def td(self, dt=0.1, Nt=1000, eqn=None):
         """``TD._solve`` (``svirl/solvers/td.py:370-377``)."""
         dt = float(self.dtype(dt))
         sp, sa = self._clamped_stops()
         if eqn == "order_parameter":
+            # td.py:216-223: A += A_irr once before the time loop, A -= A_irr after every step
             self._dt = dt
+            self._fv_pre()
             for _ in range(Nt):
                 self._psi_step(dt, sp)
+                self._fv_post()
         elif eqn == "vector_potential":
             if self.solveA:
                 if self._dt is None:
@@ -197,7 +226,9 @@ class GLOracle:
         else:
             self._dt = dt
             for _ in range(Nt):
+                self._fv_pre()
                 self._psi_step(dt, sp)
+                self._fv_post()
                 if self.solveA:
                     self._A_step(dt, sa)
 

@@ -49,6 +49,9 @@ _SIGNATURES = {
     "glgpu_psi_sweeps_per_launch": (C.c_int, []),
     "glgpu_psi_strip_rows": (C.c_int, [_H]),
     "glgpu_set_psi_strip_rows": (C.c_int, [_H, C.c_int32]),
+    "glgpu_set_irregular_vector_potential": (C.c_int, [_H, _P, C.c_int32]),
+    "glgpu_get_irregular_vector_potential": (C.c_int, [_H, _P]),
+    "glgpu_set_phase_lock": (C.c_int, [_H, _P, C.c_int32]),
     "glgpu_last_error": (C.c_char_p, [_H]),
     "glgpu_create": (C.c_int, [C.POINTER(Grid), C.c_int32, C.POINTER(_H)]),
     "glgpu_destroy": (C.c_int, [_H]),
@@ -236,6 +239,22 @@ class Handle:
     def set_eps_field(self, eps_flat):
         a = None if eps_flat is None else np.ascontiguousarray(eps_flat, dtype=self.dtype)
         check(self.lib.glgpu_set_linear_coefficient_field(self.h, ptr(a)), self.h, "set_linear_coefficient_field")
+
+    def set_irregular_vector_potential(self, vpi_flat, td_copy_only=False):
+        a = None if vpi_flat is None else np.ascontiguousarray(vpi_flat, dtype=self.dtype)
+        if a is not None:
+            assert a.size == self.Nab
+        check(self.lib.glgpu_set_irregular_vector_potential(self.h, ptr(a), 1 if td_copy_only else 0), self.h,
+              "set_irregular_vector_potential")
+
+    def get_irregular_vector_potential(self):
+        a = np.empty(self.Nab, dtype=self.dtype)
+        check(self.lib.glgpu_get_irregular_vector_potential(self.h, ptr(a)), self.h, "get_irregular_vector_potential")
+        return a
+
+    def set_phase_lock(self, nodes):
+        a = np.ascontiguousarray([] if nodes is None else nodes, dtype=np.int32)
+        check(self.lib.glgpu_set_phase_lock(self.h, ptr(a) if a.size else None, int(a.size)), self.h, "set_phase_lock")
 
     def psi_strip_rows(self):
         return int(self.lib.glgpu_psi_strip_rows(self.h))

@@ -47,6 +47,14 @@ def _state(gl):
         a=np.asarray(a), b=np.asarray(b),
         ext_a=np.zeros((0, 0)) if ext is None else np.asarray(ext[0]),
         ext_b=np.zeros((0, 0)) if ext is None else np.asarray(ext[1]),
+        fv=np.stack(p.fixed_vortices.fixed_vortices) if p.fixed_vortices.fixed_vortices_x.size else np.zeros((3, 0)),
+        fv_lock_radius=np.float64(np.nan if p.fixed_vortices.phase_lock_radius is None
+                                  else p.fixed_vortices.phase_lock_radius),
+        fv_td=(gl._h.get_irregular_vector_potential() if p.fixed_vortices.fixed_vortices_x.size
+               else np.zeros(0)),
+        # the external + irregular potential in use (set when the external potential was)
+        vpei_a=np.zeros((0, 0)) if p._vpei is None else np.asarray(p._vpei[0]),
+        vpei_b=np.zeros((0, 0)) if p._vpei is None else np.asarray(p._vpei[1]),
     )
 
 
@@ -75,7 +83,19 @@ def _apply(gl, d):
     eps = d["linear_coefficient"]
     p.linear_coefficient = float(eps) if eps.ndim == 0 else eps
     p.homogeneous_external_field = float(d["homogeneous_external_field"])
+    fv = d["fv"]
+    r = float(d["fv_lock_radius"])
+    p.fixed_vortices.phase_lock_radius = None if np.isnan(r) else r
+    p.fixed_vortices.fixed_vortices = None if fv.shape[1] == 0 else (fv[0], fv[1], fv[2])
+    if fv.shape[1]:  # the TD step's copy of A_irr, changed by A loops since it was set
+        gl._h.set_irregular_vector_potential(d["fv_td"], td_copy_only=True)
     p.external_vector_potential = None if d["ext_a"].size == 0 else (d["ext_a"], d["ext_b"])
+    p._vpei = None if d["vpei_a"].size == 0 else (d["vpei_a"], d["vpei_b"])
+    if p._vpei is None:
+        gl._h.set_abei(None)
+    else:
+        flat = np.concatenate([d["vpei_a"].T.reshape(-1), d["vpei_b"].T.reshape(-1)]).astype(c.dtype)
+        gl._h.set_abei(None if not np.any(flat) else flat)
     p.order_parameter_Langevin_coefficient = float(d["langevin_psi"])
     p.vector_potential_Langevin_coefficient = float(d["langevin_A"])
     gl.vars.order_parameter = d["psi"]

@@ -62,6 +62,9 @@ void upload_inst(glgpu_handle* h) {
     I.st = h->st;
     I.cg = h->cgst;
     I.cbits = h->cbits;
+    I.vpi = h->vpi;
+    I.lock = h->lock;
+    I.lock_n = h->lock_n;
     for (int q = 0; q < 2; ++q) {
         I.gpsi[q] = h->g_psi[q];
         I.gA[q] = h->g_A[q];
@@ -95,11 +98,13 @@ static void free_all(glgpu_handle* h) {
         if (h->psi[q]) cudaFree(h->psi[q]);
     for (int q = 0; q < 3; ++q)
         if (h->ab[q]) cudaFree(h->ab[q]);
-    for (int q = 0; q < 6; ++q)
+    for (int q = 0; q < kTDGraphs; ++q)
         if (h->td_exec[q]) cudaGraphExecDestroy(h->td_exec[q]);
     if (h->st_gather) cudaFree(h->st_gather);
     if (h->cgst) cudaFree(h->cgst);
     if (h->cbits) cudaFree(h->cbits);
+    if (h->vpi) cudaFree(h->vpi);
+    if (h->lock) cudaFree(h->lock);
     for (int q = 0; q < 2; ++q) {
         if (h->g_psi[q]) cudaFree(h->g_psi[q]);
         if (h->g_A[q]) cudaFree(h->g_A[q]);
@@ -307,6 +312,14 @@ int glgpu_set_use_graphs(glgpu_handle* h, int32_t enable) {
     return GLGPU_OK;
 }
 
+static void drop_td_graphs(glgpu_handle* h) {
+    for (int q = 0; q < kTDGraphs; ++q)
+        if (h->td_exec[q]) {
+            cudaGraphExecDestroy(h->td_exec[q]);
+            h->td_exec[q] = nullptr;
+        }
+}
+
 int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows) {
     if (check_handle(h)) return GLGPU_E_ARG;
     cudaSetDevice(h->device);
@@ -332,13 +345,72 @@ int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows) {
     h->strip_rows = rows;
     h->nitems = (int)items.size();
     h->psi_grid = psi_sweep_grid(h->dtype, rows, h->nitems);
-    for (int q = 0; q < 6; ++q)  // the TD graphs hold the old kernel, grid and table
-        if (h->td_exec[q]) {
-            cudaGraphExecDestroy(h->td_exec[q]);
-            h->td_exec[q] = nullptr;
-        }
+    drop_td_graphs(h);  // the TD graphs hold the old kernel, grid and table
     upload_inst(h);
     return cuda_check(h, cudaStreamSynchronize(h->stream), "set_psi_strip_rows");
+}
+
+int glgpu_set_irregular_vector_potential(glgpu_handle* h, const void* vpi, int32_t td_copy_only) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "set_irregular_vector_potential");
+    const size_t bytes = (size_t)h->g.Nab * real_size(h);
+    if (!vpi) {
+        if (h->vpi) cudaFree(h->vpi);
+        h->vpi = nullptr;
+    } else if (td_copy_only) {
+        if (!h->vpi) return set_error(h, GLGPU_E_ARG, "set_irregular_vector_potential: no irregular potential set");
+        e = cudaMemcpy(h->vpi, vpi, bytes, cudaMemcpyDefault);
+        if (e != cudaSuccess) return cuda_check(h, e, "set_irregular_vector_potential");
+    } else {
+        if (!h->vpi && cudaMalloc(&h->vpi, bytes) != cudaSuccess)
+            return set_error(h, GLGPU_E_OOM, "set_irregular_vector_potential: out of device memory");
+        e = cudaMemcpy(h->vpi, vpi, bytes, cudaMemcpyDefault);
+        if (e != cudaSuccess) return cuda_check(h, e, "set_irregular_vector_potential");
+    }
+    drop_td_graphs(h);
+    upload_inst(h);
+    return cuda_check(h, cudaStreamSynchronize(h->stream), "set_irregular_vector_potential");
+}
+
+int glgpu_get_irregular_vector_potential(glgpu_handle* h, void* out) {
+    if (check_handle(h) || !out) return GLGPU_E_ARG;
+    cudaSetDevice(h->device);
+    const size_t bytes = (size_t)h->g.Nab * real_size(h);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) {
+        if (h->vpi) {
+            e = cudaMemcpy(out, h->vpi, bytes, cudaMemcpyDefault);
+        } else {
+            const std::vector<unsigned char> zeros(bytes, 0);
+            e = cudaMemcpy(out, zeros.data(), bytes, cudaMemcpyDefault);
+        }
+    }
+    return cuda_check(h, e, "get_irregular_vector_potential");
+}
+
+int glgpu_set_phase_lock(glgpu_handle* h, const int32_t* nodes, int32_t count) {
+    if (check_handle(h) || count < 0 || (count > 0 && !nodes)) return GLGPU_E_ARG;
+    for (int32_t k = 0; k < count; ++k)
+        if (nodes[k] < 0 || nodes[k] >= h->g.N) return set_error(h, GLGPU_E_ARG, "set_phase_lock: node index out of range");
+    if (count > h->g.N) return set_error(h, GLGPU_E_ARG, "set_phase_lock: more locked nodes than nodes");
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "set_phase_lock");
+    if (h->lock) cudaFree(h->lock);
+    h->lock = nullptr;
+    h->lock_n = 0;
+    if (count > 0) {
+        if (cudaMalloc(&h->lock, sizeof(int32_t) * (size_t)count) != cudaSuccess)
+            return set_error(h, GLGPU_E_OOM, "set_phase_lock: out of device memory");
+        e = cudaMemcpy(h->lock, nodes, sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_check(h, e, "set_phase_lock");
+        h->lock_n = count;
+    }
+    drop_td_graphs(h);
+    upload_inst(h);
+    return cuda_check(h, cudaStreamSynchronize(h->stream), "set_phase_lock");
 }
 
 int glgpu_td(glgpu_handle* h, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats) {
@@ -469,7 +541,7 @@ int glgpu_batch_destroy(glgpu_batch* b) {
     if (!b) return GLGPU_OK;
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
-    for (int q = 0; q < 6; ++q)
+    for (int q = 0; q < kTDGraphs; ++q)
         if (b->td_exec[q]) cudaGraphExecDestroy(b->td_exec[q]);
     if (b->cg_exec) cudaGraphExecDestroy(b->cg_exec);
     void* ptrs[] = {b->insts, b->gather, b->tiles, b->items, b->loop, b->cg_partials, b->cg_loop, b->cg_tiles};

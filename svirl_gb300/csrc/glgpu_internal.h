@@ -23,6 +23,9 @@ namespace glgpu {
 constexpr int kFuse = GLGPU_FUSE;
 static_assert(kFuse >= 1 && kFuse <= 4, "1 <= GLGPU_FUSE <= 4");
 constexpr int kPsiBufs = kFuse + 2;  // right-hand side + input + kFuse outputs
+// TD graphs cached per handle / batch: eqn mode (3) x any finite kappa (2) x any
+// fixed vortices (2)
+constexpr int kTDGraphs = 12;
 
 // Device-resident state of one instance's Jacobi loops (updated by the kernels
 // themselves so that a whole TD run needs no host round trip).
@@ -74,6 +77,9 @@ struct Inst {
     void* U;                  // link factors exp(-i d a) of the psi loop, Nab complex
     uint8_t* code;            // per-node link-weight bits of the psi loop, N bytes
     uint8_t* cbits;           // per-node cell bits (cell_bits) for the batched CG, N bytes (NULL until CG)
+    void* vpi;                // irregular vector potential of fixed vortices, Nab, or NULL
+    const int32_t* lock;      // phase-lock node list or NULL
+    int lock_n, pad_lock;
     InstState* st;
     CGState* cg;              // batched device CG state (NULL until used)
     void* gpsi[2];            // CG gradient buffers (psi part, A part) and directions
@@ -168,9 +174,12 @@ struct glgpu_handle {
     void* dir_A[2] = {nullptr, nullptr};
     int cg_g = 0, cg_dir = 0;           // current index of g / dir
     glgpu::CGState* cgst = nullptr;     // batched device CG state
+    void* vpi = nullptr;                // irregular vector potential (fixed vortices), Nab, or NULL (the TD step's copy)
+    int32_t* lock = nullptr;            // phase-lock node list (fixed vortices) or NULL
+    int lock_n = 0;
     uint8_t* cbits = nullptr;           // batched CG: cell bits per node, written at the start of a call
     // TD graphs, one per (equation mode, kappa finite)
-    cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t td_exec[glgpu::kTDGraphs] = {};
     glgpu::InstState* st_gather = nullptr;  // device copy target of the loop state
     bool td_graph_failed = false;
     bool use_graphs = true;
@@ -196,7 +205,7 @@ struct glgpu_batch {
     std::vector<glgpu::InstState> gather_h;
     int ntiles = 0, nitems = 0, psi_grid = 0, strip_rows = 0;
     std::vector<int> inst_items;         // psi sweep items of each instance (at strip_rows)
-    cudaGraphExec_t td_exec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t td_exec[glgpu::kTDGraphs] = {};
     bool td_graph_failed = false, use_graphs = true;
     // batched device CG (allocated on first use)
     void* cg_tiles = nullptr;            // CG tile table (larger tiles than the TD one)

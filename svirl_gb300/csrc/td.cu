@@ -405,7 +405,10 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
         const int k = s_k, R = s_R;
         const T* cur = (const T*)I.ab[buf_of(R, k)];
         const T* rhs = (const T*)I.ab[R];
-        const T* abi = (const T*)I.ab[k < 2 ? R : (R + 2) % 3];
+        // with fixed vortices the supercurrent phases come from the irregular
+        // potential buffer, which holds A_irr + A^(0) on its first N elements
+        // (td.py:256-270), so there is no aliasing
+        const T* abi = I.vpi ? (const T*)I.vpi : (const T*)I.ab[k < 2 ? R : (R + 2) % 3];
         T* nxt = (T*)I.ab[(R + 1 + (k & 1)) % 3];
         const C2<T>* __restrict__ psi = (const C2<T>*)I.psi[s_P];
         const Geo g = I.g;
@@ -498,7 +501,8 @@ __global__ void __launch_bounds__(kThreads)
 k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int only_solveA) {
     const Tile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
-    if (only_solveA && !I.solveA) return;  // A of a kappa=inf instance does not change
+    // A of a kappa=inf instance does not change, unless fixed vortices add to it
+    if (only_solveA && !I.solveA && !I.vpi) return;
     const Geo g = I.g;
     const int n = t.n0 + threadIdx.x;
     if (n >= g.N) return;
@@ -517,6 +521,55 @@ k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int onl
         int nb = g.Na + i + g.Nx * j;
         U[nb] = link_U<T>(GT(g, dy) * A[nb]);
     }
+}
+
+// Fixed vortices (svirl/solvers/td.py:120-154,204-216,252-325).  Around each psi
+// step the reference adds the irregular vector potential to A and subtracts it
+// again, and around each A loop it adds A to the irregular potential (used as
+// the supercurrent argument) and subtracts the final A; xpy_r / xmy_r run over
+// the first N elements of the Nab-long link arrays, and these kernels keep that
+// range: thread n handles element n < N.  After the psi loop, psi at the
+// phase-lock nodes becomes |psi| (td.h:295-307).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_fv_psi_pre(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const int n = t.n0 + threadIdx.x;
+    if (!I.vpi || n >= I.g.N) return;
+    T* A = (T*)I.ab[*(volatile const int*)&I.st->rhsA];
+    A[n] += ((const T*)I.vpi)[n];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_fv_psi_post(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const int n = t.n0 + threadIdx.x;
+    if (n < I.lock_n) {
+        C2<T>* psi = (C2<T>*)I.psi[*(volatile const int*)&I.st->rhs];
+        const int m = I.lock[n];
+        const C2<T> p = psi[m];
+        psi[m] = cmk<T>(hypot(p.x, p.y), T(0));
+    }
+    if (I.vpi && n < I.g.N) {
+        T* A = (T*)I.ab[*(volatile const int*)&I.st->rhsA];
+        A[n] -= ((const T*)I.vpi)[n];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_fv_A(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int post) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const int n = t.n0 + threadIdx.x;
+    if (!I.vpi || !I.solveA || n >= I.g.N) return;
+    const T a = ((const T*)I.ab[*(volatile const int*)&I.st->rhsA])[n];
+    T* vpi = (T*)I.vpi;
+    if (post) vpi[n] -= a;
+    else vpi[n] += a;
 }
 
 // Start of a Jacobi loop: reset the per-instance loop state and the while
@@ -600,7 +653,12 @@ struct TDLaunch {
     LoopState* loop;
     int ninst, ntiles, nitems, psi_grid, dtype, strip_rows;
     bool any_solveA;
+    bool any_fv;  // an instance has fixed vortices (irregular potential or phase lock)
 };
+
+static void* fv_psi_pre_fn(int dt) { return dt == 8 ? (void*)k_fv_psi_pre<double> : (void*)k_fv_psi_pre<float>; }
+static void* fv_psi_post_fn(int dt) { return dt == 8 ? (void*)k_fv_psi_post<double> : (void*)k_fv_psi_post<float>; }
+static void* fv_A_fn(int dt) { return dt == 8 ? (void*)k_fv_A<double> : (void*)k_fv_A<float>; }
 
 template <int V>
 static void* psi_sweep_fn_v(int dtype, int rows) {
@@ -657,15 +715,20 @@ cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_
 #define GCHK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { err = e_; goto fail; } } while (0)
 
 // Build the whole TD run of all instances as one graph:
-//   [tables, all instances] -> WHILE(step < Nt) {
-//       [tables, finite-kappa instances] -> loop_begin(psi) -> WHILE(active) { psi sweep } -> loop_end(psi)
-//       -> loop_begin(A) -> WHILE(active) { A sweep } -> loop_end(A) -> step_end }
+//   [fixed vortices: A += A_irr, psi-only mode] -> [tables, all instances] -> WHILE(step < Nt) {
+//       [A += A_irr] -> [tables, finite-kappa / fixed-vortex instances]
+//       -> loop_begin(psi) -> WHILE(active) { psi sweep } -> loop_end(psi) -> [phase lock, A -= A_irr]
+//       -> [A_irr += A] -> loop_begin(A) -> WHILE(active) { A sweep } -> loop_end(A) -> [A_irr -= A]
+//       -> step_end }
 //   -> canonical copy -> canonical reset
+// (bracketed fixed-vortex kernels only when an instance has fixed vortices; in
+// psi-only mode A += A_irr runs once before the time loop, as in the reference,
+// td.py:216-223).
 static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* exec) {
     cudaError_t err = cudaSuccess;
     cudaGraph_t top = nullptr, obody = nullptr, pbody = nullptr, abody = nullptr;
     cudaGraphConditionalHandle hout, hpsi = 0, hA = 0;
-    cudaGraphNode_t n_pre = nullptr, n_out = nullptr, n_cc = nullptr, n_cr = nullptr, prev = nullptr, nd;
+    cudaGraphNode_t n_out = nullptr, n_cc = nullptr, n_cr = nullptr, prev = nullptr, nd;
     const bool do_psi = eqn != 2, do_A = (eqn != 1) && L.any_solveA;
     int zero = 0, one = 1;
     const dim3 gt(L.ntiles), bt(kThreads), g1(1), b1(32);
@@ -674,25 +737,38 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
     Item const* items = L.items;
     LoopState* loop = L.loop;
     int ninst = L.ninst, nitems = L.nitems;
+    // appends a kernel node after `prev` in graph `g`
+    auto chain = [&](cudaGraph_t g, void* fn, dim3 grid, dim3 block, void** a) -> cudaError_t {
+        cudaError_t e = add_kernel(g, &nd, prev ? &prev : nullptr, prev ? 1 : 0, fn, grid, block, a);
+        if (e == cudaSuccess) prev = nd;
+        return e;
+    };
 
     GCHK(cudaGraphCreate(&top, 0));
     GCHK(cudaGraphConditionalHandleCreate(&hout, top, 1, cudaGraphCondAssignDefault));
+    if (do_psi && eqn == 1 && L.any_fv) {
+        void* a[] = {&insts, &tiles};
+        GCHK(chain(top, fv_psi_pre_fn(L.dtype), gt, bt, a));
+    }
     if (do_psi) {
         void* a[] = {&insts, &tiles, &zero};
-        GCHK(add_kernel(top, &n_pre, nullptr, 0, link_fn(L.dtype), gt, bt, a));
+        GCHK(chain(top, link_fn(L.dtype), gt, bt, a));
     }
-    GCHK(add_while(top, &n_out, n_pre ? &n_pre : nullptr, n_pre ? 1 : 0, hout, &obody));
+    GCHK(add_while(top, &n_out, prev ? &prev : nullptr, prev ? 1 : 0, hout, &obody));
+    prev = nullptr;
     if (do_psi) {
         GCHK(cudaGraphConditionalHandleCreate(&hpsi, obody, 1, cudaGraphCondAssignDefault));
-        if (L.any_solveA) {
+        if (eqn == 0 && L.any_fv) {
+            void* a[] = {&insts, &tiles};
+            GCHK(chain(obody, fv_psi_pre_fn(L.dtype), gt, bt, a));
+        }
+        if (L.any_solveA || L.any_fv) {
             void* a[] = {&insts, &tiles, &one};
-            GCHK(add_kernel(obody, &nd, nullptr, 0, link_fn(L.dtype), gt, bt, a));
-            prev = nd;
+            GCHK(chain(obody, link_fn(L.dtype), gt, bt, a));
         }
         {
             void* a[] = {&insts, &ninst, &loop, &hpsi, &one, &zero};
-            GCHK(add_kernel(obody, &nd, prev ? &prev : nullptr, prev ? 1 : 0, (void*)k_loop_begin, g1, b1, a));
-            prev = nd;
+            GCHK(chain(obody, (void*)k_loop_begin, g1, b1, a));
         }
         GCHK(add_while(obody, &nd, &prev, 1, hpsi, &pbody));
         prev = nd;
@@ -704,16 +780,22 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         }
         {
             void* a[] = {&insts, &ninst, &zero};
-            GCHK(add_kernel(obody, &nd, &prev, 1, (void*)k_loop_end, g1, b1, a));
-            prev = nd;
+            GCHK(chain(obody, (void*)k_loop_end, g1, b1, a));
+        }
+        if (L.any_fv) {
+            void* a[] = {&insts, &tiles};
+            GCHK(chain(obody, fv_psi_post_fn(L.dtype), gt, bt, a));
         }
     }
     if (do_A) {
         GCHK(cudaGraphConditionalHandleCreate(&hA, obody, 1, cudaGraphCondAssignDefault));
+        if (L.any_fv) {
+            void* a[] = {&insts, &tiles, &zero};
+            GCHK(chain(obody, fv_A_fn(L.dtype), gt, bt, a));
+        }
         {
             void* a[] = {&insts, &ninst, &loop, &hA, &one, &one};
-            GCHK(add_kernel(obody, &nd, prev ? &prev : nullptr, prev ? 1 : 0, (void*)k_loop_begin, g1, b1, a));
-            prev = nd;
+            GCHK(chain(obody, (void*)k_loop_begin, g1, b1, a));
         }
         GCHK(add_while(obody, &nd, &prev, 1, hA, &abody));
         prev = nd;
@@ -724,13 +806,16 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         }
         {
             void* a[] = {&insts, &ninst, &one};
-            GCHK(add_kernel(obody, &nd, &prev, 1, (void*)k_loop_end, g1, b1, a));
-            prev = nd;
+            GCHK(chain(obody, (void*)k_loop_end, g1, b1, a));
+        }
+        if (L.any_fv) {
+            void* a[] = {&insts, &tiles, &one};
+            GCHK(chain(obody, fv_A_fn(L.dtype), gt, bt, a));
         }
     }
     {
         void* a[] = {&insts, &ninst, &loop, &hout, &one};
-        GCHK(add_kernel(obody, &nd, prev ? &prev : nullptr, prev ? 1 : 0, (void*)k_step_end, g1, b1, a));
+        GCHK(chain(obody, (void*)k_step_end, g1, b1, a));
     }
     {
         void* a[] = {&insts, &tiles};
@@ -760,12 +845,28 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
     const int chunk = 4;
     cudaGraphConditionalHandle none = 0;
     int cont = 1;
+    auto fv_psi = [&](bool post) {
+        if (L.dtype == 8) {
+            if (post) k_fv_psi_post<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+            else k_fv_psi_pre<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+        } else {
+            if (post) k_fv_psi_post<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+            else k_fv_psi_pre<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+        }
+    };
+    auto fv_A = [&](int post) {
+        if (L.dtype == 8) k_fv_A<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, post);
+        else k_fv_A<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, post);
+    };
+    if (do_psi && eqn == 1 && L.any_fv) fv_psi(false);
     if (do_psi) launch_link_U(L, 0, s);
     for (int step = 0; step < Nt; ++step) {
         for (int part = 0; part < 2; ++part) {
             if (part == 0 && !do_psi) continue;
             if (part == 1 && !do_A) continue;
-            if (part == 0 && L.any_solveA) launch_link_U(L, 1, s);
+            if (part == 0 && eqn == 0 && L.any_fv) fv_psi(false);
+            if (part == 0 && (L.any_solveA || L.any_fv)) launch_link_U(L, 1, s);
+            if (part == 1 && L.any_fv) fv_A(0);
             k_loop_begin<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0, part);
             for (;;) {
                 for (int c = 0; c < chunk; ++c) {
@@ -783,6 +884,8 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
                 if (!cont) break;
             }
             k_loop_end<<<1, 32, 0, s>>>(L.insts, L.ninst, part);
+            if (part == 0 && L.any_fv) fv_psi(true);
+            if (part == 1 && L.any_fv) fv_A(1);
         }
         k_step_end<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0);
     }
@@ -946,7 +1049,7 @@ static TDOutcome td_core(cudaStream_t s, const TDLaunch& L, int Nt, int eqn, cud
         ls.ninst = L.ninst;
         o.err = cudaMemcpyAsync(L.loop, &ls, sizeof(ls), cudaMemcpyHostToDevice, s);
         if (o.err != cudaSuccess) return o;
-        const int slot = eqn * 2 + (L.any_solveA ? 1 : 0);
+        const int slot = eqn * 4 + (L.any_solveA ? 2 : 0) + (L.any_fv ? 1 : 0);
         if (use_graphs && !*graph_failed) {
             if (execs[slot] == nullptr) {
                 if (build_td_graph(L, eqn, &execs[slot]) != cudaSuccess) {
@@ -1014,6 +1117,7 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     L.ninst = 1; L.ntiles = h->ntiles; L.nitems = h->nitems; L.psi_grid = h->psi_grid; L.dtype = h->dtype;
     L.strip_rows = h->strip_rows;
     L.any_solveA = h->inst_h.solveA != 0;
+    L.any_fv = h->vpi != nullptr || h->lock_n > 0;
     InstState hs;
     TDOutcome o = td_core(h->stream, L, Nt, eqn, h->td_exec, &h->td_graph_failed, h->use_graphs, elapsed_ms != nullptr,
                           h->st_gather, &hs);
@@ -1029,7 +1133,7 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
 int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms) {
     if (eqn < 0 || eqn > 2 || Nt < 0) return batch_error(b, GLGPU_E_ARG, "batch_td: bad eqn or Nt");
     std::vector<Inst> insts(b->ninst);
-    bool any_solveA = false;
+    bool any_solveA = false, any_fv = false;
     for (int q = 0; q < b->ninst; ++q) {
         glgpu_handle* h = b->hs[q];
         cudaStreamSynchronize(h->stream);
@@ -1038,6 +1142,7 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
         insts[q] = h->inst_h;
         insts[q].nitems = b->inst_items[q];  // at the batch's strip height
         any_solveA = any_solveA || h->inst_h.solveA != 0;
+        any_fv = any_fv || h->vpi != nullptr || h->lock_n > 0;
     }
     cudaError_t e = cudaMemcpyAsync(b->insts, insts.data(), sizeof(Inst) * insts.size(), cudaMemcpyHostToDevice, b->stream);
     if (e != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_td: ") + cudaGetErrorString(e));
@@ -1046,6 +1151,7 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
     L.ninst = b->ninst; L.ntiles = b->ntiles; L.nitems = b->nitems; L.psi_grid = b->psi_grid; L.dtype = b->dtype;
     L.strip_rows = b->strip_rows;
     L.any_solveA = any_solveA;
+    L.any_fv = any_fv;
     TDOutcome o = td_core(b->stream, L, Nt, eqn, b->td_exec, &b->td_graph_failed, b->use_graphs, elapsed_ms != nullptr,
                           b->gather, b->gather_h.data());
     if (o.err != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_td: ") + cudaGetErrorString(o.err));

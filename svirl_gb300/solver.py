@@ -186,17 +186,27 @@ class Vars:
 
 
 class FixedVortices:
-    """Fixed-vortex helpers (``svirl/vars/fixed_vortices.py``).  Pinned vortices
-    (irregular vector potential, phase lock) are not part of this GPU path;
-    ``order_parameter_add_vortices`` (host-side phase winding) and the
-    ``vortices`` alias documented in the reference's README are provided."""
+    """Fixed (pinned) vortices (``svirl/vars/fixed_vortices.py``): the irregular
+    vector potential A_irr of phase windings around the given points, which the
+    TDGL step adds to A (``svirl/solvers/td.py:120-154``) and the A step adds to
+    the supercurrent argument (``td.py:252-325``), with the reference's element
+    ranges; the phase lock (|psi| at the lock nodes after each psi step); the
+    host-side phase winding of psi and the release of fixed vortices.  A_irr as
+    set is kept here (``irregular_vector_potential``); the device copy the TD step
+    works on changes during A loops, as the reference's does."""
 
     def __init__(self, gl):
         self._gl = gl
-        self._vpi = None
-        self.fixed_vortices_x = np.zeros(0)
-        self.fixed_vortices_y = np.zeros(0)
-        self.fixed_vortices_vorticity = np.zeros(0)
+        c = gl.cfg
+        self._ai = None  # A_irr as set: (a, b) or None
+        corr = c.fixed_vortices_correction if c.fixed_vortices_correction is not None else "none"
+        assert corr in ("none", "cell centers", "vertices")
+        self.fixed_vortices_correction = corr
+        self._phase_lock_radius = c.phase_lock_radius
+        self.fixed_vortices_x = np.zeros(0, dtype=c.dtype)
+        self.fixed_vortices_y = np.zeros(0, dtype=c.dtype)
+        self.fixed_vortices_vorticity = np.zeros(0, dtype=c.dtype)
+        self.fixed_vortices = c.fixed_vortices
 
     @staticmethod
     def _psi_abs(x, y):
@@ -217,6 +227,7 @@ class FixedVortices:
         vN = max(vx.size, vy.size, vv.size)
         if vx.size > 0 and vv.size == 0:
             vv = np.array([1])
+        assert vx.size in (1, vN) and vy.size in (1, vN) and vv.size in (1, vN)
         fvx, fvy, fvv = [], [], []
         x = y = v = np.nan
         for i in range(vN):
@@ -227,6 +238,18 @@ class FixedVortices:
                 continue
             fvx.append(x); fvy.append(y); fvv.append(v)
         return (np.array(fvx).astype(c.dtype), np.array(fvy).astype(c.dtype), np.array(fvv).astype(c.dtype))
+
+    def _correct(self):
+        """Integer vorticity; positions moved to cell centres or vertices
+        (``fixed_vortices.py:113-126``)."""
+        c = self._gl.cfg
+        self.fixed_vortices_vorticity = np.round(self.fixed_vortices_vorticity)
+        if self.fixed_vortices_correction == "cell centers":
+            self.fixed_vortices_x = c.dx * (np.round(self.fixed_vortices_x / c.dx + 0.5) - 0.5)
+            self.fixed_vortices_y = c.dy * (np.round(self.fixed_vortices_y / c.dy + 0.5) - 0.5)
+        elif self.fixed_vortices_correction == "vertices":
+            self.fixed_vortices_x = c.dx * np.round(self.fixed_vortices_x / c.dx)
+            self.fixed_vortices_y = c.dy * np.round(self.fixed_vortices_y / c.dy)
 
     def order_parameter_add_vortices(self, vortices, phase=True, deep=False):
         """Adds phase windings (and optionally |psi| dips) around the given points."""
@@ -243,7 +266,29 @@ class FixedVortices:
     @property
     def irregular_vector_potential(self):
         c = self._gl.cfg
-        return np.zeros((c.Nxa, c.Nya), dtype=c.dtype), np.zeros((c.Nxb, c.Nyb), dtype=c.dtype)
+        if self._ai is None:
+            return np.zeros((c.Nxa, c.Nya), dtype=c.dtype), np.zeros((c.Nxb, c.Nyb), dtype=c.dtype)
+        return self._ai[0].copy(), self._ai[1].copy()
+
+    def _ab_phase(self, a, b):
+        """Phase whose link differences are (a, b), zero at node (0, 0)."""
+        c = self._gl.cfg
+        a = c.dx * np.r_[np.zeros((1, c.Nya), dtype=c.dtype), a].cumsum(axis=0)
+        b = c.dy * np.c_[np.zeros((c.Nxb, 1), dtype=c.dtype), b].cumsum(axis=1)
+        return np.repeat(b[0:1, :], c.Nx, axis=0) + a
+
+    @property
+    def fixed_vortices_phase(self):
+        return self._ab_phase(*self.irregular_vector_potential)
+
+    def fixed_vortices_release(self):
+        """Turns the fixed vortices into free ones: their phase goes into psi, then
+        A_irr and the phase lock are removed (``fixed_vortices.py:60-73``)."""
+        psi = self._gl.vars.order_parameter
+        psi *= np.exp(-1.0j * self.fixed_vortices_phase)
+        self._gl._h.set_psi(_flat(psi.astype(self._gl.cfg.dtype_complex)))
+        self.fixed_vortices = None
+        self.phase_lock_radius = None
 
     @property
     def fixed_vortices(self):
@@ -251,13 +296,50 @@ class FixedVortices:
 
     @fixed_vortices.setter
     def fixed_vortices(self, fixed_vortices):
-        vx, vy, vv = self._vortices_format(fixed_vortices)
-        if vx.size > 0:
-            raise NotImplementedError("pinned (fixed) vortices are not supported by the GB300 path")
+        c = self._gl.cfg
+        self.fixed_vortices_x, self.fixed_vortices_y, self.fixed_vortices_vorticity = self._vortices_format(fixed_vortices)
+        self._correct()
+        if self.fixed_vortices_x.size > 0:
+            ai = np.zeros((c.Nxa, c.Nya), dtype=c.dtype)
+            bi = np.zeros((c.Nxb, c.Nyb), dtype=c.dtype)
+            xg, yg = self._gl.mesh.xy_grid
+            for k in range(self.fixed_vortices_x.size):
+                # winding angle around the vortex, zero at node (0, 0); its link differences
+                ang = np.arctan2(yg - self.fixed_vortices_y[k], xg - self.fixed_vortices_x[k])
+                ang -= ang[0, 0]
+                ai += self.fixed_vortices_vorticity[k] * c.idx * np.diff(ang, axis=0)
+                bi += self.fixed_vortices_vorticity[k] * c.idy * np.diff(ang, axis=1)
+            self._ai = (ai, bi)
+            self._gl._h.set_irregular_vector_potential(np.concatenate([_flat(ai), _flat(bi)]))
+        else:
+            self._ai = None
+            self._gl._h.set_irregular_vector_potential(None)
+        self._update_phase_lock()
 
     @property
     def phase_lock_radius(self):
-        return None
+        return self._phase_lock_radius
+
+    @phase_lock_radius.setter
+    def phase_lock_radius(self, radius):
+        assert radius is None or (isinstance(radius, (np.floating, float, np.integer, int)) and radius > 0.0)
+        self._phase_lock_radius = radius
+        self._update_phase_lock()
+
+    def _update_phase_lock(self):
+        """Nodes within the lock radius of a fixed vortex.  The reference takes
+        ``np.where(lock_grid)[0]`` of the (Nx, Ny) grid, the x index of each locked
+        node, as the flat node index (``fixed_vortices.py:218-236``); kept."""
+        c = self._gl.cfg
+        ns = None
+        if self._phase_lock_radius is not None:
+            xg, yg = self._gl.mesh.xy_grid
+            lock = np.zeros((c.Nx, c.Ny), dtype=bool)
+            for k in range(self.fixed_vortices_x.size):
+                lock |= (np.square(xg - self.fixed_vortices_x[k]) + np.square(yg - self.fixed_vortices_y[k])
+                         <= np.square(self._phase_lock_radius))
+            ns = np.where(lock)[0].astype(np.int32)
+        self._gl._h.set_phase_lock(ns if ns is not None and ns.size > 0 else None)
 
     @property
     def vortices(self):
@@ -278,6 +360,7 @@ class Params:
         self._H = cfg.dtype(0.0)
         self.homogeneous_external_field_reset = cfg.homogeneous_external_field
         self.ae, self.be = None, None
+        self._vpei = None
         self.external_field = cfg.external_field
         self.order_parameter_Langevin_coefficient = cfg.order_parameter_Langevin_coefficient
         self.vector_potential_Langevin_coefficient = cfg.vector_potential_Langevin_coefficient
@@ -386,12 +469,21 @@ class Params:
 
     # external vector potential ------------------------------------------------------
     def _update_gvpei(self):
-        if self.ae is None:
+        """The external + irregular vector potential the energy, currents and CG
+        use: A_ext + A_irr of the fixed vortices at this moment (``params.py:193-222``;
+        like the reference, setting fixed vortices later does not update it)."""
+        ai = self.fixed_vortices._ai
+        if self.ae is None and ai is None:
             self._vpei = None
             self._gl._h.set_abei(None)
             return
-        self._vpei = (self.ae, self.be)
-        flat = np.concatenate([_flat(self.ae), _flat(self.be)]).astype(self._cfg.dtype)
+        if self.ae is None:
+            self._vpei = ai
+        elif ai is None:
+            self._vpei = (self.ae, self.be)
+        else:
+            self._vpei = (self.ae + ai[0], self.be + ai[1])
+        flat = np.concatenate([_flat(self._vpei[0]), _flat(self._vpei[1])]).astype(self._cfg.dtype)
         # an all-zero external potential adds exact zeros: leave it out of the kernels
         self._gl._h.set_abei(None if not np.any(flat) else flat)
 
@@ -414,7 +506,7 @@ class Params:
 
     @property
     def external_irregular_vector_potential(self):
-        return None if self.ae is None else (self.ae, self.be)
+        return self._vpei
 
     @property
     def external_field(self):
@@ -543,6 +635,15 @@ class VortexDetector:
                 - 4.0 * np.pi
                 + c.dx * c.dy * H)
             sel = (np.abs(v) > 0.5) & (np.abs(v - np.round(v)) < 0.1)
+            ai = gl.params.fixed_vortices._ai
+            if ai is not None:
+                # the triangulation reads A + A_irr (host copy, as set), the winding A alone
+                # (vortex_detector.py:43-50,55-72)
+                ci, cj = cells % c.Nxc, cells // c.Nxc
+                a00 = a00 + ai[0][ci, cj]
+                a0p = a0p + ai[0][ci, cj + 1]
+                b00 = b00 + ai[1][ci, cj]
+                bp0 = bp0 + ai[1][ci + 1, cj]
             found = []
             for k in np.nonzero(sel)[0]:
                 r = _triangulate(c, int(cells[k]), v[k], psi[k], a00[k], a0p[k], b00[k], bp0[k])
@@ -922,8 +1023,6 @@ class GLSolver:
         else:
             self.vars.order_parameter = order_parameter
         self.params = Params(self, cfg)
-        if fixed_vortices is not None:
-            self.params.fixed_vortices.fixed_vortices = fixed_vortices
         self.observables = Observables(self)
         self.solve = Solvers(self)
         self.vortex_detector = VortexDetector(self)

@@ -131,6 +131,81 @@ def make_case(svirl, name, spec):
     return out
 
 
+FV_CASES = {
+    # name: (Nx, Ny, dx, dy, kappa, sigma, H, mask_kind, seed, vortices (x, y, v), lock_radius, steps (td, psi, A))
+    "fv_k3": (14, 12, 0.5, 0.5, 3.0, 200.0, 0.1, "none", 4, ([2.1, 4.3], [2.4, 3.1], [1, -1]), 0.8, (4, 3, 2)),
+    "fv_kinf_holes": (13, 12, 0.5, 0.5, np.inf, 1.0, 0.2, "holes", 5, ([3.0], [2.0], [2]), 1.0, (4, 3, 0)),
+}
+
+
+def make_fv_case(svirl, name, spec):
+    """Fixed vortices: the irregular vector potential and phase lock as the
+    reference sets them, then TDGL in the combined, psi-only and A-only modes
+    (td.py:120-154,204-223,252-325) and the vortex list."""
+    Nx, Ny, dx, dy, kappa, sigma, H, kind, seed, vort, radius, (n0, n1, n2) = spec
+    rng = np.random.default_rng(200 + seed)
+    mt = mask_of(kind, Nx - 1, Ny - 1, rng)
+    kw = dict(Nx=Nx, Ny=Ny, dx=dx, dy=dy, order_parameter="random", random_seed=seed, gl_parameter=kappa,
+              normal_conductivity=sigma, homogeneous_external_field=H, fixed_vortices=vort,
+              fixed_vortices_correction="cell centers", phase_lock_radius=radius)
+    if mt is not None:
+        kw["material_tiling"] = mt
+    gl = svirl.GLSolver(**kw)
+    fvs = gl.params.fixed_vortices
+    psi0 = flat(gl.vars.order_parameter)
+    a, b = gl.vars.vector_potential
+    ab0 = np.concatenate([flat(a), flat(b)])
+    ai, bi = fvs.irregular_vector_potential
+    ai0 = np.concatenate([flat(ai), flat(bi)])
+    ei = gl.params.external_irregular_vector_potential
+    abei = None if ei is None else np.concatenate([flat(ei[0]), flat(ei[1])])
+    lock = fvs._phase_lock_ns.get_d_obj().get().astype(np.int64) if fvs._phase_lock_ns is not None else np.zeros(0, int)
+    orc = O.GLOracle(Nx, Ny, dx, dy, psi0, ab0, mt=None if mt is None else flat(mt), abei=abei, kappa=kappa,
+                     sigma=sigma, H=H, rand_t=seed, vpi=ai0, lock_ns=lock)
+    fx, fy, fv = fvs.fixed_vortices
+    out = {"Nx": Nx, "Ny": Ny, "dx": dx, "dy": dy, "kappa": kappa, "sigma": sigma, "H": H, "seed": seed,
+           "vort_in": np.array(vort, dtype=float), "lock_radius": radius, "steps": np.array([n0, n1, n2]),
+           "fv": np.stack([fx, fy, fv]), "psi0": psi0, "ab0": ab0, "ai0": ai0, "lock": lock,
+           "mt": np.zeros(0, bool) if mt is None else flat(mt), "abei": np.zeros(0) if abei is None else abei}
+
+    def device_vpi():
+        return np.asarray(fvs._vpi.get_d_obj().get()).reshape(-1)
+
+    def snap(tag):
+        out["psi_" + tag] = flat(gl.vars.order_parameter)
+        # A from the device: after psi-only steps the reference's host mirror of A is
+        # not refreshed, though its device A has changed by the A_irr subtractions
+        out["ab_" + tag] = np.asarray(gl.vars._vp.get_d_obj().get()).reshape(-1)
+        out["vpi_" + tag] = device_vpi()
+        assert close(orc.psi, out["psi_" + tag], 1e-13) and close(orc.ab, out["ab_" + tag], 1e-13), (name, tag)
+        assert close(orc.vpi, out["vpi_" + tag], 1e-13), (name, tag)
+
+    gl.solve.td(dt=0.1, Nt=n0)
+    orc.td(dt=0.1, Nt=n0)
+    snap("td")
+    gl.solve.td(dt=0.1, Nt=n1, eqn="order_parameter")
+    orc.td(dt=0.1, Nt=n1, eqn="order_parameter")
+    snap("psi")
+    if n2:
+        gl.solve.td(dt=0.1, Nt=n2, eqn="vector_potential")
+        orc.td(dt=0.1, Nt=n2, eqn="vector_potential")
+        snap("A")
+    out["sweeps_psi"] = np.array(orc.sweeps_psi)
+    out["sweeps_A"] = np.array(orc.sweeps_A)
+    out["F"] = gl.observables.free_energy
+    assert abs(orc.free_energy() - out["F"]) <= 1e-12 * abs(out["F"]), name
+    vx, vy, vv = gl.vortex_detector.vortices
+    out["vx"], out["vy"], out["vv"] = np.asarray(vx), np.asarray(vy), np.asarray(vv)
+    # the detector reads the host mirror of A (not refreshed by the A_irr kernels)
+    a, b = gl.vars.vector_potential
+    out["ab_host"] = np.concatenate([flat(a), flat(b)])
+    ai_bi = (ai, bi)
+    ox, oy, ov = O.detect_vortices(orc.g, orc.psi, out["ab_host"], H, ai_bi=ai_bi)
+    assert np.array_equal(ox, out["vx"]) and np.array_equal(oy, out["vy"]) and np.array_equal(ov, out["vv"]), name
+    np.savez_compressed(os.path.join(HERE, "%s.npz" % name), **out)
+    return out
+
+
 def svirl_gpu(x):
     from pycuda import gpuarray  # the shim's
     return gpuarray.to_gpu(np.ascontiguousarray(x))
@@ -147,6 +222,9 @@ def main():
         for name, spec in CASES.items():
             make_case(svirl, name, spec)
             print("wrote case_%s.npz" % name)
+        for name, spec in FV_CASES.items():
+            make_fv_case(svirl, name, spec)
+            print("wrote %s.npz" % name)
 
 
 if __name__ == "__main__":

@@ -12,6 +12,7 @@ import pytest
 from oracle import gl_oracle as O
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "case_*.npz")))
+GOLDEN_FV = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fv_*.npz")))
 
 
 def load(path):
@@ -56,4 +57,34 @@ def test_oracle_reproduces_golden(path):
     tol = 1e-13 if np.isinf(f["kappa"]) else 1e-8
     assert rel(orc.cg_energies, f["cg_energies"]) < tol
     vx, vy, vv = O.detect_vortices(orc.g, f["psi_cg"], f["ab_cg"], float(f["H"]))
+    assert np.array_equal(vx, f["vx"]) and np.array_equal(vy, f["vy"]) and np.array_equal(vv, f["vv"])
+
+
+def test_fixed_vortex_fixtures_present():
+    assert len(GOLDEN_FV) >= 2
+
+
+@pytest.mark.parametrize("path", GOLDEN_FV, ids=lambda p: os.path.basename(p))
+def test_oracle_reproduces_fixed_vortex_golden(path):
+    """Fixed vortices: the irregular vector potential around the psi and A steps
+    (with the reference's element ranges), the phase lock, the three TD modes,
+    the A_irr drift, the energy and the vortex list."""
+    f = load(path)
+    mt = f["mt"] if f["mt"].size else None
+    abei = f["abei"] if f["abei"].size else None
+    orc = O.GLOracle(int(f["Nx"]), int(f["Ny"]), float(f["dx"]), float(f["dy"]), f["psi0"].copy(), f["ab0"].copy(),
+                     mt=mt, abei=abei, kappa=float(f["kappa"]), sigma=float(f["sigma"]), H=float(f["H"]),
+                     rand_t=int(f["seed"]), vpi=f["ai0"].copy(), lock_ns=f["lock"])
+    n0, n1, n2 = (int(x) for x in f["steps"])
+    for tag, eqn, nt in (("td", None, n0), ("psi", "order_parameter", n1), ("A", "vector_potential", n2)):
+        if nt == 0:
+            continue
+        orc.td(dt=0.1, Nt=nt, eqn=eqn)
+        assert rel(orc.psi, f["psi_" + tag]) < 1e-13 and rel(orc.ab, f["ab_" + tag]) < 1e-13, tag
+        assert rel(orc.vpi, f["vpi_" + tag]) < 1e-13, tag
+    assert list(orc.sweeps_psi) == list(f["sweeps_psi"]) and list(orc.sweeps_A) == list(f["sweeps_A"])
+    assert abs(orc.free_energy() - f["F"]) <= 1e-12 * abs(f["F"])
+    g = orc.g
+    ai = O.unflatten_ij(f["ai0"][:g.Na], g.Nx - 1, g.Ny), O.unflatten_ij(f["ai0"][g.Na:], g.Nx, g.Ny - 1)
+    vx, vy, vv = O.detect_vortices(g, orc.psi, f["ab_host"], float(f["H"]), ai_bi=ai)
     assert np.array_equal(vx, f["vx"]) and np.array_equal(vy, f["vy"]) and np.array_equal(vv, f["vv"])
