@@ -974,9 +974,7 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     return GLGPU_OK;
 }
 
-// CTAs of the persistent psi sweep: all SMs at full occupancy, or fewer if
-// there are fewer items than warps.
-// CTAs of the persistent sweep: one warp per item up to a full device.
+// CTAs of the persistent psi sweep: one warp per item, up to all SMs at full occupancy.
 int psi_sweep_grid(int dtype, int rows, int nitems) {
     int dev = 0, sms = 1, per_sm = 1;
     cudaGetDevice(&dev);

@@ -119,3 +119,18 @@ def test_release_moves_the_phase_into_psi():
     assert np.allclose(gl.vars.order_parameter, psi0 * np.exp(-1j * phase), rtol=0, atol=1e-13)
     assert fvs.fixed_vortices_x.size == 0 and fvs.phase_lock_radius is None
     assert not np.any(gl._h.get_irregular_vector_potential())
+
+
+@pytest.mark.parametrize("path", GOLDEN_FV, ids=lambda p: os.path.basename(p))
+def test_fixed_vortices_fp32_near_golden(path):
+    """The FP32 path with fixed vortices against the reference's FP64 states
+    (FP32 rounding only: 1e-4 after the combined and psi-only steps)."""
+    f = load(path)
+    gl = solver_of(f, np.float32)
+    n0, n1, _ = (int(x) for x in f["steps"])
+    gl.solve.td(dt=0.1, Nt=n0)
+    psi, ab = gpu_state(gl)
+    assert rel_err(psi, f["psi_td"]) < 1e-4 and rel_err(ab, f["ab_td"]) < 1e-4
+    gl.solve.td(dt=0.1, Nt=n1, eqn="order_parameter")
+    psi, ab = gpu_state(gl)
+    assert rel_err(psi, f["psi_psi"]) < 1e-4 and rel_err(ab, f["ab_psi"]) < 1e-4
