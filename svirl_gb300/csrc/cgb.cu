@@ -4,7 +4,7 @@
 // for (alpha_psi, alpha_A)), with the step length, beta and the stop test decided
 // on the device, so a whole CG run is one CUDA-graph launch for all instances.
 //
-// Per iteration three tile kernels (REP x 256 nodes of one instance per CTA) write
+// Per iteration three tile kernels (rep x 256 nodes of one instance per CTA) write
 // per-tile FP64 partial sums; in each, the CTA that finishes an instance's last
 // tile adds that instance's partials in tile order (one warp, deterministic) and
 // takes the instance's scalar decisions:
@@ -29,11 +29,27 @@
 namespace glgpu {
 
 constexpr int kPart = 17;  // doubles of per-tile partials
-// The CG kernels walk tiles of REP x 256 nodes of one instance: each thread
-// accumulates REP nodes in registers before the block reduction, so the
-// reduction's cost is shared by REP nodes.  REP is chosen per batch from
-// kCGReps (choose_cg_rep): the deepest tile that still gives every SM a tile.
-constexpr int kCGReps[] = {2, 4, 8};
+// The CG kernels walk tiles of rep x 256 nodes of one instance: each thread
+// accumulates rep nodes in registers before the block reduction, so the
+// reduction's cost is shared by rep nodes.  rep (2, 4 or 8) is a property of the
+// instance alone (cg_rep_of), so an instance's arithmetic, and with it its CG
+// run, does not depend on the batch it is in.
+constexpr int kCGRepMax = 8;
+struct CGTile {
+    int inst, n0, rep, pad;
+};
+
+// Tile depth of an instance of N nodes: the deepest of 8, 4, 2 that still cuts
+// it into at least kCGMinTiles tiles (so that an instance run alone spreads over
+// a quarter of the SMs), else 2.  Deeper tiles share each block reduction among
+// more nodes: 64 instances, 7.19M nodes: 0.77 ms per iteration with depth 4 for
+// all, 0.70 with 8 for all.
+constexpr int kCGMinTiles = 38;
+static int cg_rep_of(int N) {
+    for (int r = kCGRepMax; r > 2; r /= 2)
+        if ((N + kThreads * r - 1) / (kThreads * r) >= kCGMinTiles) return r;
+    return 2;
+}
 // Resident CTAs per SM asked of the compiler for the two stencil-heavy FP32 CG
 // kernels (caps their registers at 65536 / (kThreads * GLGPU_CG_MINB)).
 #ifndef GLGPU_CG_MINB
@@ -155,8 +171,8 @@ __device__ __forceinline__ bool last_cta_of_instance(CGState* cs, int ntiles) {
 // store a node's results after its loads.
 
 // gradient (new buffer), Polak-Ribiere sums and |g|^2 of one tile
-template <typename T, int REP>
-__device__ __forceinline__ void grad_tile(const Inst& I, int n0, const C2<T>* __restrict__ psi,
+template <typename T>
+__device__ __forceinline__ void grad_tile(const Inst& I, int n0, int rep, const C2<T>* __restrict__ psi,
                                           const T* __restrict__ ab, const T* __restrict__ abei,
                                           const C2<T>* __restrict__ U, C2<T>* __restrict__ G,
                                           const C2<T>* __restrict__ Gp, T* __restrict__ GA,
@@ -165,7 +181,8 @@ __device__ __forceinline__ void grad_tile(const Inst& I, int n0, const C2<T>* __
     const TableLinks<T> lk{U};
     const T eps0 = gsel<T>(I.epsilon, I.fepsilon), k2 = gsel<T>(I.kappa2, I.fkappa2), H = gsel<T>(I.H, I.fH);
 #pragma unroll
-    for (int r = 0; r < REP; ++r) {
+    for (int r = 0; r < kCGRepMax; ++r) {
+        if (r >= rep) break;
         const int n = n0 + threadIdx.x + r * kThreads;
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
@@ -198,16 +215,16 @@ __device__ __forceinline__ void grad_tile(const Inst& I, int n0, const C2<T>* __
     }
 }
 
-template <typename T, int REP>
+template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB : 1)
-kb_grad(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop) {
-    const Tile t = tiles[blockIdx.x];
+kb_grad(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop) {
+    const CGTile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
     CGState* cs = I.cg;
     if (*(volatile const int*)&cs->done) return;
     const int gi = cs->gi, pi = cs->pi;
     T v[5] = {T(0), T(0), T(0), T(0), T(0)};
-    grad_tile<T, REP>(I, t.n0, (const C2<T>*)I.psi[pi], (const T*)I.ab[I.solveA ? pi : 0], (const T*)I.abei,
+    grad_tile<T>(I, t.n0, t.rep, (const C2<T>*)I.psi[pi], (const T*)I.ab[I.solveA ? pi : 0], (const T*)I.abei,
                  (const C2<T>*)I.U, (C2<T>*)I.gpsi[1 - gi], (const C2<T>*)I.gpsi[gi], (T*)I.gA[1 - gi],
                  (const T*)I.gA[gi], v);
     double vs[5];
@@ -431,8 +448,8 @@ __device__ __noinline__ void inst_alpha(const Inst& I, CGState* cs, const double
 }
 
 // new direction (written) and the line-search coefficients of one tile
-template <typename T, int REP>
-__device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, T bp, T bA, const C2<T>* __restrict__ psi,
+template <typename T>
+__device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, int rep, T bp, T bA, const C2<T>* __restrict__ psi,
                                               const T* __restrict__ ab, const T* __restrict__ abei,
                                               const C2<T>* __restrict__ U, const C2<T>* __restrict__ G,
                                               const T* __restrict__ GA, const C2<T>* __restrict__ dO,
@@ -449,7 +466,7 @@ __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, T bp, T bA,
     auto phase = [&](int l) -> T { return link_phase(abei, ab, l); };
     const T eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
 #pragma unroll 1
-    for (int r = 0; r < REP; ++r) {
+    for (int r = 0; r < rep; ++r) {
         const int n = n0 + threadIdx.x + r * kThreads;
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
@@ -472,11 +489,11 @@ __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, T bp, T bA,
     }
 }
 
-template <typename T, int REP>
+template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB : 1)
-kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials,
+kb_dir_coef(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double* __restrict__ partials,
             CGLoop* loop) {
-    const Tile t = tiles[blockIdx.x];
+    const CGTile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
     CGState* cs = I.cg;
     if (*(volatile const int*)&cs->done) return;
@@ -484,7 +501,7 @@ kb_dir_coef(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, doub
     T c[17];
 #pragma unroll
     for (int k = 0; k < 17; ++k) c[k] = T(0);
-    dir_coef_tile<T, REP>(I, t.n0, (T)cs->beta_psi, (T)cs->beta_A, (const C2<T>*)I.psi[pi],
+    dir_coef_tile<T>(I, t.n0, t.rep, (T)cs->beta_psi, (T)cs->beta_A, (const C2<T>*)I.psi[pi],
                      (const T*)I.ab[I.solveA ? pi : 0], (const T*)I.abei, (const C2<T>*)I.U,
                      (const C2<T>*)I.gpsi[gi], (const T*)I.gA[gi], (const C2<T>*)I.dpsi[di], (const T*)I.dA[di],
                      (C2<T>*)I.dpsi[1 - di], (T*)I.dA[1 - di], c);
@@ -521,8 +538,8 @@ __device__ __noinline__ void inst_energy_stop(const Inst& I, CGState* cs, const 
 }
 
 // step and energy of the new state of one tile
-template <typename T, int REP>
-__device__ __forceinline__ void step_tile(const Inst& I, int n0, T ap, T aA, const C2<T>* __restrict__ psi,
+template <typename T>
+__device__ __forceinline__ void step_tile(const Inst& I, int n0, int rep, T ap, T aA, const C2<T>* __restrict__ psi,
                                           C2<T>* __restrict__ psiN, const C2<T>* __restrict__ dpsi,
                                           const T* __restrict__ ab, T* __restrict__ abN, const T* __restrict__ dA,
                                           const T* __restrict__ abei, C2<T>* __restrict__ U, T (&v)[1]) {
@@ -538,7 +555,8 @@ __device__ __forceinline__ void step_tile(const Inst& I, int n0, T ap, T aA, con
     const TableLinks<T> lk{U};
     const T k2 = gsel<T>(I.kappa2, I.fkappa2), eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
 #pragma unroll
-    for (int r = 0; r < REP; ++r) {
+    for (int r = 0; r < kCGRepMax; ++r) {
+        if (r >= rep) break;
         const int n = n0 + threadIdx.x + r * kThreads;
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
@@ -571,17 +589,17 @@ __device__ __forceinline__ void step_tile(const Inst& I, int n0, T ap, T aA, con
 // owners store, so the energy equals that of the stored state bit for bit.  The
 // last CTA of the launch counts the active instances and sets the WHILE
 // condition.
-template <typename T, int REP>
+template <typename T>
 __global__ void __launch_bounds__(kThreads)
-kb_step(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop,
+kb_step(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop,
         cudaGraphConditionalHandle cond, int use_cond) {
-    const Tile t = tiles[blockIdx.x];
+    const CGTile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
     CGState* cs = I.cg;
     if (!*(volatile const int*)&cs->done) {
         const int pi = cs->pi, di = cs->di;
         T v[1] = {T(0)};
-        step_tile<T, REP>(I, t.n0, (T)cs->alpha_psi, (T)cs->alpha_A, (const C2<T>*)I.psi[pi], (C2<T>*)I.psi[1 - pi],
+        step_tile<T>(I, t.n0, t.rep, (T)cs->alpha_psi, (T)cs->alpha_A, (const C2<T>*)I.psi[pi], (C2<T>*)I.psi[1 - pi],
                      (const C2<T>*)I.dpsi[di], (const T*)I.ab[I.solveA ? pi : 0], I.solveA ? (T*)I.ab[1 - pi] : nullptr,
                      (const T*)I.dA[di], (const T*)I.abei, (C2<T>*)I.U, v);
         double vs[1];
@@ -611,16 +629,18 @@ kb_step(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* 
 }
 
 // energy of the start state per tile (buffer 0)
-template <typename T, int REP>
+template <typename T>
 __global__ void __launch_bounds__(kThreads)
-kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double* __restrict__ partials) {
-    const Tile t = tiles[blockIdx.x];
+kb_energy(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double* __restrict__ partials) {
+    const CGTile t = tiles[blockIdx.x];
+    const int rep = t.rep;
     const Inst& I = insts[t.inst];
     const Geo g = I.g;
     const TableLinks<T> lk{(const C2<T>*)I.U};
     T v[1] = {T(0)};
 #pragma unroll
-    for (int r = 0; r < REP; ++r) {
+    for (int r = 0; r < kCGRepMax; ++r) {
+        if (r >= rep) break;
         const int n = t.n0 + threadIdx.x + r * kThreads;
         if (n < g.N)
             v[0] += energy_density<T>(g, gsel<T>(I.kappa2, I.fkappa2), gsel<T>(I.epsilon, I.fepsilon),
@@ -633,15 +653,17 @@ kb_energy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, double
 }
 
 // end of a CG call: the state is copied back to buffer 0 where it ended in buffer 1
-template <typename T, int REP>
+template <typename T>
 __global__ void __launch_bounds__(kThreads)
-kb_finish(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
-    const Tile t = tiles[blockIdx.x];
+kb_finish(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles) {
+    const CGTile t = tiles[blockIdx.x];
+    const int rep = t.rep;
     const Inst& I = insts[t.inst];
     if (I.cg->pi == 0) return;
     const Geo g = I.g;
 #pragma unroll
-    for (int r = 0; r < REP; ++r) {
+    for (int r = 0; r < kCGRepMax; ++r) {
+        if (r >= rep) break;
         const int n = t.n0 + threadIdx.x + r * kThreads;
         if (n >= g.N) break;
         ((C2<T>*)I.psi[0])[n] = ((const C2<T>*)I.psi[1])[n];
@@ -659,14 +681,16 @@ kb_finish(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
 // the iteration kernels read one byte instead of four mask cells), the
 // link-factor table of the start state (TableLinks), then the energy of the
 // start state
-template <typename T, int REP>
+template <typename T>
 __global__ void __launch_bounds__(kThreads)
-kb_zero_dir(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
-    const Tile t = tiles[blockIdx.x];
+kb_zero_dir(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles) {
+    const CGTile t = tiles[blockIdx.x];
+    const int rep = t.rep;
     const Inst& I = insts[t.inst];
     const Geo g = I.g;
 #pragma unroll
-    for (int r = 0; r < REP; ++r) {
+    for (int r = 0; r < kCGRepMax; ++r) {
+        if (r >= rep) break;
         const int n = t.n0 + threadIdx.x + r * kThreads;
         if (n >= g.N) break;
         ((C2<T>*)I.dpsi[0])[n] = cmk<T>(T(0), T(0));
@@ -732,35 +756,14 @@ kb_init(const Inst* __restrict__ insts, int ninst, const double* __restrict__ pa
 
 struct CGLaunch {
     const Inst* insts;
-    const Tile* tiles;
+    const CGTile* tiles;
     double* partials;
     CGLoop* loop;
-    int ninst, ntiles, dtype, rep;
+    int ninst, ntiles, dtype;
 };
 
-// Tile depth of a batch: the deepest of kCGReps that still gives every SM a
-// tile (deeper tiles share each block reduction among more nodes; measured on
-// 64 instances, 7.19M nodes: 0.77 ms per iteration at REP = 4, 0.70 at 8, and
-// 16 instances of 257²: 0.129 / 0.117 ms), else the shallowest.
-static int choose_cg_rep(const std::vector<glgpu_handle*>& hs) {
-    int dev = 0, sms = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    for (int v = (int)(sizeof(kCGReps) / sizeof(kCGReps[0])) - 1; v >= 0; --v) {
-        long long tiles = 0;
-        for (const glgpu_handle* h : hs) tiles += (h->g.N + kThreads * kCGReps[v] - 1) / (kThreads * kCGReps[v]);
-        if (tiles >= sms) return kCGReps[v];
-    }
-    return kCGReps[0];
-}
-
-// kernel of depth `rep` (one of kCGReps) and precision `dt`
-#define CG_FN(name)                                                                              \
-    static void* fn_##name(int dt, int rep) {                                                   \
-        if (rep == 2) return dt == 8 ? (void*)kb_##name<double, 2> : (void*)kb_##name<float, 2>; \
-        if (rep == 4) return dt == 8 ? (void*)kb_##name<double, 4> : (void*)kb_##name<float, 4>; \
-        return dt == 8 ? (void*)kb_##name<double, 8> : (void*)kb_##name<float, 8>;              \
-    }
+#define CG_FN(name) \
+    static void* fn_##name(int dt) { return dt == 8 ? (void*)kb_##name<double> : (void*)kb_##name<float>; }
 CG_FN(grad)
 CG_FN(dir_coef)
 CG_FN(step)
@@ -778,26 +781,26 @@ static cudaError_t cg_launch_body(const CGLaunch& L, cudaStream_t s) {
     cudaGraphConditionalHandle none = 0;
     int zero = 0;
     const Inst* insts = L.insts;
-    const Tile* tiles = L.tiles;
+    const CGTile* tiles = L.tiles;
     double* partials = L.partials;
     CGLoop* loop = L.loop;
     void* a[] = {&insts, &tiles, &partials, &loop};
     void* b[] = {&insts, &tiles, &partials, &loop, &none, &zero};
-    cudaError_t e = launch(fn_grad(L.dtype, L.rep), L.ntiles, kThreads, a, s);
-    if (e == cudaSuccess) e = launch(fn_dir_coef(L.dtype, L.rep), L.ntiles, kThreads, a, s);
-    if (e == cudaSuccess) e = launch(fn_step(L.dtype, L.rep), L.ntiles, kThreads, b, s);
+    cudaError_t e = launch(fn_grad(L.dtype), L.ntiles, kThreads, a, s);
+    if (e == cudaSuccess) e = launch(fn_dir_coef(L.dtype), L.ntiles, kThreads, a, s);
+    if (e == cudaSuccess) e = launch(fn_step(L.dtype), L.ntiles, kThreads, b, s);
     return e;
 }
 
 static cudaError_t cg_launch_prologue(const CGLaunch& L, cudaStream_t s) {
     const cudaGraphConditionalHandle none = 0;
     const Inst* insts = L.insts;
-    const Tile* tiles = L.tiles;
+    const CGTile* tiles = L.tiles;
     double* partials = L.partials;
     void* a[] = {&insts, &tiles};
     void* b[] = {&insts, &tiles, &partials};
-    cudaError_t e = launch(fn_zero_dir(L.dtype, L.rep), L.ntiles, kThreads, a, s);
-    if (e == cudaSuccess) e = launch(fn_energy(L.dtype, L.rep), L.ntiles, kThreads, b, s);
+    cudaError_t e = launch(fn_zero_dir(L.dtype), L.ntiles, kThreads, a, s);
+    if (e == cudaSuccess) e = launch(fn_energy(L.dtype), L.ntiles, kThreads, b, s);
     if (e != cudaSuccess) return e;
     kb_init<<<1, 1024, 0, s>>>(L.insts, L.ninst, L.partials, L.loop, none, 0);
     return cudaGetLastError();
@@ -805,9 +808,9 @@ static cudaError_t cg_launch_prologue(const CGLaunch& L, cudaStream_t s) {
 
 static cudaError_t cg_launch_epilogue(const CGLaunch& L, cudaStream_t s) {
     const Inst* insts = L.insts;
-    const Tile* tiles = L.tiles;
+    const CGTile* tiles = L.tiles;
     void* a[] = {&insts, &tiles};
-    return launch(fn_finish(L.dtype, L.rep), L.ntiles, kThreads, a, s);
+    return launch(fn_finish(L.dtype), L.ntiles, kThreads, a, s);
 }
 
 #define GCHK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { err = e_; goto fail; } } while (0)
@@ -822,7 +825,7 @@ static cudaError_t build_cg_graph(const CGLaunch& L, cudaGraphExec_t* exec) {
     int one = 1;
     const dim3 gt(L.ntiles), bt(kThreads), g1(1), b1(1024);
     const Inst* insts = L.insts;
-    const Tile* tiles = L.tiles;
+    const CGTile* tiles = L.tiles;
     double* partials = L.partials;
     CGLoop* loop = L.loop;
     int ninst = L.ninst;
@@ -831,12 +834,12 @@ static cudaError_t build_cg_graph(const CGLaunch& L, cudaGraphExec_t* exec) {
     GCHK(cudaGraphConditionalHandleCreate(&h, top, 0, cudaGraphCondAssignDefault));
     {
         void* a[] = {&insts, &tiles};
-        GCHK(add_kernel(top, &nd, nullptr, 0, fn_zero_dir(L.dtype, L.rep), gt, bt, a));
+        GCHK(add_kernel(top, &nd, nullptr, 0, fn_zero_dir(L.dtype), gt, bt, a));
         prev = nd;
     }
     {
         void* a[] = {&insts, &tiles, &partials};
-        GCHK(add_kernel(top, &nd, &prev, 1, fn_energy(L.dtype, L.rep), gt, bt, a));
+        GCHK(add_kernel(top, &nd, &prev, 1, fn_energy(L.dtype), gt, bt, a));
         prev = nd;
     }
     {
@@ -847,22 +850,22 @@ static cudaError_t build_cg_graph(const CGLaunch& L, cudaGraphExec_t* exec) {
     GCHK(add_while(top, &wh, &prev, 1, h, &body));
     {
         void* a[] = {&insts, &tiles};
-        GCHK(add_kernel(top, &nd, &wh, 1, fn_finish(L.dtype, L.rep), gt, bt, a));
+        GCHK(add_kernel(top, &nd, &wh, 1, fn_finish(L.dtype), gt, bt, a));
     }
     prev = nullptr;
     {
         void* a[] = {&insts, &tiles, &partials, &loop};
-        GCHK(add_kernel(body, &nd, nullptr, 0, fn_grad(L.dtype, L.rep), gt, bt, a));
+        GCHK(add_kernel(body, &nd, nullptr, 0, fn_grad(L.dtype), gt, bt, a));
         prev = nd;
     }
     {
         void* a[] = {&insts, &tiles, &partials, &loop};
-        GCHK(add_kernel(body, &nd, &prev, 1, fn_dir_coef(L.dtype, L.rep), gt, bt, a));
+        GCHK(add_kernel(body, &nd, &prev, 1, fn_dir_coef(L.dtype), gt, bt, a));
         prev = nd;
     }
     {
         void* a[] = {&insts, &tiles, &partials, &loop, &h, &one};
-        GCHK(add_kernel(body, &nd, &prev, 1, fn_step(L.dtype, L.rep), gt, bt, a));
+        GCHK(add_kernel(body, &nd, &prev, 1, fn_step(L.dtype), gt, bt, a));
     }
     GCHK(cudaGraphInstantiate(exec, top, 0));
     cudaGraphDestroy(top);
@@ -889,18 +892,17 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
              int32_t* status, double* elapsed_ms) {
     if (n_iter < 0 || !(rtol >= 0.0) || !(gtol >= 0.0)) return batch_error(b, GLGPU_E_ARG, "batch_cg: bad n_iter, rtol or gtol");
     std::vector<Inst> insts(b->ninst);
-    std::vector<Tile> cgtiles;
-    if (!b->cg_rep) b->cg_rep = choose_cg_rep(b->hs);
-    const int tile = kThreads * b->cg_rep;
+    std::vector<CGTile> cgtiles;
     for (int q = 0; q < b->ninst; ++q) {
         glgpu_handle* h = b->hs[q];
         const int rc = cg_ensure(h);
         if (rc) return batch_error(b, rc, "batch_cg: " + h->last_error);
         cudaStreamSynchronize(h->stream);
         insts[q] = h->inst_h;
-        // this copy of the descriptors indexes the CG tile table (`tile` nodes per tile)
+        // this copy of the descriptors indexes the CG tile table (rep x 256 nodes per tile)
         insts[q].tile0 = (int)cgtiles.size();
-        for (int n0 = 0; n0 < h->g.N; n0 += tile) cgtiles.push_back(Tile{q, n0});
+        const int rep = cg_rep_of(h->g.N);
+        for (int n0 = 0; n0 < h->g.N; n0 += kThreads * rep) cgtiles.push_back(CGTile{q, n0, rep, 0});
         insts[q].ntiles = (int)cgtiles.size() - insts[q].tile0;
         insts[q].cg_exact = (flags & GLGPU_CG_EXACT_BOUNDARY) ? 1 : 0;
         insts[q].cg_target = b->cg_targets.empty() ? NAN : b->cg_targets[q];
@@ -908,8 +910,8 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
     }
     if (!b->cg_tiles) {
         b->cg_ntiles = (int)cgtiles.size();
-        if (cudaMalloc(&b->cg_tiles, sizeof(Tile) * cgtiles.size()) != cudaSuccess ||
-            cudaMemcpy(b->cg_tiles, cgtiles.data(), sizeof(Tile) * cgtiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        if (cudaMalloc(&b->cg_tiles, sizeof(CGTile) * cgtiles.size()) != cudaSuccess ||
+            cudaMemcpy(b->cg_tiles, cgtiles.data(), sizeof(CGTile) * cgtiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
             return batch_error(b, GLGPU_E_OOM, "batch_cg: cannot place the tile table");
     }
     if (!b->cg_partials && cudaMalloc(&b->cg_partials, sizeof(double) * kPart * (size_t)b->cg_ntiles) != cudaSuccess)
@@ -929,13 +931,12 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
     if (e != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_cg: ") + cudaGetErrorString(e));
     CGLaunch L;
     L.insts = b->insts;
-    L.tiles = (const Tile*)b->cg_tiles;
+    L.tiles = (const CGTile*)b->cg_tiles;
     L.partials = b->cg_partials;
     L.loop = (CGLoop*)b->cg_loop;
     L.ninst = b->ninst;
     L.ntiles = b->cg_ntiles;
     L.dtype = b->dtype;
-    L.rep = b->cg_rep;
     if (b->use_graphs && !b->cg_graph_failed && !b->cg_exec && build_cg_graph(L, &b->cg_exec) != cudaSuccess) {
         b->cg_graph_failed = true;
         cudaGetLastError();

@@ -210,7 +210,6 @@ struct glgpu_batch {
     // batched device CG (allocated on first use)
     void* cg_tiles = nullptr;            // CG tile table (larger tiles than the TD one)
     int cg_ntiles = 0;
-    int cg_rep = 0;                      // CG tile depth (nodes per thread), chosen at the first call
     double* cg_partials = nullptr;       // cg_ntiles * 17 doubles
     void* cg_loop = nullptr;             // CGLoop
     cudaGraphExec_t cg_exec = nullptr;

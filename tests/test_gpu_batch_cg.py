@@ -118,3 +118,28 @@ def test_batch_cg_gradient_stop_and_zero_iterations():
     assert np.all(out["status"] == 1) and np.all(out["grad_rel"] <= 1e-6)
     assert np.all(out["iters"] < 5000)
     assert out["energy"][1] <= o_ref["energy"][0] + 1e-9 * abs(o_ref["energy"][0])
+
+
+def test_batch_cg_independent_of_batch_at_every_tile_depth():
+    """Instances large enough for each CG tile depth (2, 4, 8 nodes per thread),
+    in one batch and alone: the same iterations bitwise."""
+    from svirl_gb300 import learned as L
+    from svirl_gb300.relax import HandleCache
+    from svirl_gb300.batch import HandleBatch
+    rng = np.random.default_rng(11)
+    insts = [L.Instance.sample(n, rng, kappa_range=(4.0, 4.0)) for n in (129, 257, 385)]
+    cache = HandleCache()
+    try:
+        hs = [cache.get(it.n, np.float32) for it in insts]
+        for it, h in zip(insts, hs):
+            it.load_into(h)
+        together = HandleBatch(hs).cg_device(n_iter=20, rtol=0.0, gtol=0.0, exact_boundary=True)
+        states = [(h.get_psi(), h.get_ab()) for h in hs]
+        for q, it in enumerate(insts):
+            h = cache.get(it.n, np.float32)  # a second handle of the size (the first is still held)
+            it.load_into(h)
+            alone = HandleBatch([h]).cg_device(n_iter=20, rtol=0.0, gtol=0.0, exact_boundary=True)
+            assert alone["energy"][0] == together["energy"][q]
+            assert np.array_equal(h.get_psi(), states[q][0]) and np.array_equal(h.get_ab(), states[q][1])
+    finally:
+        cache.close()
