@@ -30,6 +30,21 @@ def test_psi_step_matches_oracle(mask, shape):
     assert gl.solve._td.last_stats.total_sweeps_psi == sum(orc.sweeps_psi)
 
 
+@pytest.mark.parametrize("shape", [(4, 4), (5, 70), (70, 5), (27, 18), (53, 35), (25, 16)])
+@pytest.mark.parametrize("mask", ["none", "random30"])
+def test_psi_step_at_strip_edges_matches_oracle(mask, shape):
+    """Domains at and around the psi sweep's strip width (26 columns) and heights
+    (8, 12, 17 rows), down to the smallest grid, at every compiled strip height."""
+    for rows in (8, 12, 17):
+        gl, orc = make_pair(Nx=shape[0], Ny=shape[1], kappa=np.inf, H=0.2, mask=mask, seed=shape[0] + shape[1])
+        gl._h.set_psi_strip_rows(rows)
+        gl.solve.td(dt=0.1, Nt=3, eqn="order_parameter")
+        orc.td(dt=0.1, Nt=3, eqn="order_parameter")
+        psi, _ = gpu_state(gl)
+        assert rel_err(psi, orc.psi) < 1e-12, rows
+        assert gl.solve._td.last_stats.total_sweeps_psi == sum(orc.sweeps_psi), rows
+
+
 @pytest.mark.parametrize("mask", ["none", "random30", "holes"])
 @pytest.mark.parametrize("kappa,sigma", [(5.0, 200.0), (2.0, 10.0), (1.0, 4.0)])
 def test_td_with_vector_potential_matches_oracle(mask, kappa, sigma):
