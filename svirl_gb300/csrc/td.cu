@@ -163,29 +163,52 @@ template <typename T> __device__ __forceinline__ C2<T> shfl_down_c(C2<T> v, int 
 // the link weights, which are fixed during a Jacobi loop, so its reciprocal is
 // formed once per node and launch (psi_diag_inv) and each sweep only forms the
 // neighbour sums (psi_node).  A node with neither a left nor a right link gets 0.
+// The link table holds U scaled by dt/dx^2 (x links) or dt/dy^2 (y links), and
+// 0 on links of weight 0, so the neighbour sum is one FMA chain per component
+// with no branch per link.
 template <typename T>
 __device__ __forceinline__ T psi_diag_inv(C2<T> rq, T eps, unsigned cd, T dt, T idx2, T idy2) {
-    const bool rm0 = cd & 1u, rp0 = cd & 2u, r0m = cd & 4u, r0p = cd & 8u;
-    const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
-    const T diag = T(1) + dt * (rq.x * rq.x + rq.y * rq.y - eps + (idx2 * wx + idy2 * wy));
-    return T(1) / diag;
+    // FP64: the link-count terms by selects, keeping conversions off the FP64 pipe
+    if constexpr (sizeof(T) == 8) {
+        const unsigned nx = (cd & 1u) + ((cd >> 1) & 1u), ny = ((cd >> 2) & 1u) + ((cd >> 3) & 1u);
+        const T cx = nx == 0u ? T(0) : (nx == 1u ? idx2 : idx2 + idx2);
+        const T cy = ny == 0u ? T(0) : (ny == 1u ? idy2 : idy2 + idy2);
+        const T diag = T(1) + dt * (rq.x * rq.x + rq.y * rq.y - eps + (cx + cy));
+        return T(1) / diag;
+    } else {
+        const bool rm0 = cd & 1u, rp0 = cd & 2u, r0m = cd & 4u, r0p = cd & 8u;
+        const T wx = T(rm0) + T(rp0), wy = T(r0m) + T(r0p);
+        const T diag = T(1) + dt * (rq.x * rq.x + rq.y * rq.y - eps + (idx2 * wx + idy2 * wy));
+        return T(1) / diag;
+    }
 }
 
+// rq + conj(ua_left) p_left + ua p_right + conj(ub_down) p_prev + ub p_next as one
+// FMA chain per component, the link factors already scaled; p_next, the row the
+// previous sweep produced last, enters at the end of the chain.
 template <typename T>
 __device__ __forceinline__ C2<T> psi_node(C2<T> p_left, C2<T> p_right, C2<T> p_prev, C2<T> p_next, C2<T> ua_left,
-                                          C2<T> ua, C2<T> ub_down, C2<T> ub, C2<T> rq, T inv, unsigned cd, T dt,
-                                          T idx2, T idy2) {
+                                          C2<T> ua, C2<T> ub_down, C2<T> ub, C2<T> rq, T inv, unsigned cd) {
     const C2<T> z = cmk<T>(T(0), T(0));
     C2<T> out = z;
-    if (cd & 3u) {
-        C2<T> sx = z, sy = z;
-        if (cd & 1u) sx = cadd(sx, cmul(cconj(ua_left), p_left));
-        if (cd & 2u) sx = cadd(sx, cmul(ua, p_right));
-        if (cd & 4u) sy = cadd(sy, cmul(cconj(ub_down), p_prev));
-        if (cd & 8u) sy = cadd(sy, cmul(ub, p_next));
-        out.x = (rq.x + dt * (idx2 * sx.x + idy2 * sy.x)) * inv;
-        out.y = (rq.y + dt * (idx2 * sx.y + idy2 * sy.y)) * inv;
-    }
+    T ax = fma(ua_left.x, p_left.x, rq.x);
+    ax = fma(ua_left.y, p_left.y, ax);
+    ax = fma(ua.x, p_right.x, ax);
+    ax = fma(-ua.y, p_right.y, ax);
+    T ay = fma(ua_left.x, p_left.y, rq.y);
+    ay = fma(-ua_left.y, p_left.x, ay);
+    ay = fma(ua.x, p_right.y, ay);
+    ay = fma(ua.y, p_right.x, ay);
+    ax = fma(ub_down.x, p_prev.x, ax);
+    ax = fma(ub_down.y, p_prev.y, ax);
+    ax = fma(ub.x, p_next.x, ax);
+    ax = fma(-ub.y, p_next.y, ax);
+    ay = fma(ub_down.x, p_prev.y, ay);
+    ay = fma(-ub_down.y, p_prev.x, ay);
+    ay = fma(ub.x, p_next.y, ay);
+    ay = fma(ub.y, p_next.x, ay);
+    const T vx = ax * inv, vy = ay * inv;
+    if (cd & 3u) out = cmk<T>(vx, vy);
     return out;
 }
 
@@ -352,15 +375,28 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
                     const C2<T> ual = shfl_up_c<T>(d.ua, 1);
                     const bool node = calc_lane && y >= 0 && y < Ny;
                     if (node) {
-                        out = psi_node<T>(pl, pr, wp[l - 1], newrow, ual, d.ua, D[l].ub, d.ub, d.rq, d.inv, d.cd, dt,
-                                          idx2, idy2);
+                        out = psi_node<T>(pl, pr, wp[l - 1], newrow, ual, d.ua, D[l].ub, d.ub, d.rq, d.inv, d.cd);
                         if (own_lane && y >= j0 && y < j0 + RR) {
                             outb[l - 1][i + Nx * y] = out;
                             // max(|d re|, |d im|); a NaN component counts as 0 (the reference's
-                            // int conversion), fmax drops NaN operands
-                            const T dr = fabs(out.x - pc.x), di = fabs(out.y - pc.y);
-                            if (!(dr + di == dr + di)) wnan[l - 1] = true;
-                            wmax[l - 1] = fmax(wmax[l - 1], fmax(dr, di));
+                            // int conversion).  FP64 compares the bit patterns (non-negative
+                            // doubles order as integers), off the FP64 pipe; FP32 uses fmax,
+                            // which drops NaN operands.
+                            if constexpr (sizeof(T) == 8) {
+                                const unsigned long long kAbs = 0x7fffffffffffffffull, kInf = 0x7ff0000000000000ull;
+                                unsigned long long bx = (unsigned long long)__double_as_longlong(out.x - pc.x) & kAbs;
+                                unsigned long long by = (unsigned long long)__double_as_longlong(out.y - pc.y) & kAbs;
+                                if ((bx > kInf) | (by > kInf)) wnan[l - 1] = true;
+                                bx = bx > kInf ? 0ull : bx;
+                                by = by > kInf ? 0ull : by;
+                                const unsigned long long m = bx > by ? bx : by;
+                                const unsigned long long w = (unsigned long long)__double_as_longlong(wmax[l - 1]);
+                                wmax[l - 1] = __longlong_as_double((long long)(w > m ? w : m));
+                            } else {
+                                const T dr = fabs(out.x - pc.x), di = fabs(out.y - pc.y);
+                                if (isnan(dr) | isnan(di)) wnan[l - 1] = true;
+                                wmax[l - 1] = fmax(wmax[l - 1], fmax(dr, di));
+                            }
                         }
                     }
                 }
@@ -493,7 +529,9 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
 }
 
 // Per-step tables of the psi Jacobi loop, during which A is fixed: the link
-// factors U = exp(-i d a) of the current A, and per node the Winecki-Adams
+// factors U = exp(-i d a) of the current A times dt/d^2 (0 on links whose
+// weight is 0; the CG fills the same buffer with its own unscaled factors
+// before each run), and per node the Winecki-Adams
 // link weights as a bit code (bit 0: left link r_m0, 1: right r_p0, 2: lower
 // r_0m, 3: upper r_0p; a node is updated iff it has a left or a right link).
 template <typename T>
@@ -513,13 +551,15 @@ k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int onl
     I.code[n] = (uint8_t)(rm0 | (rp0 << 1) | (r0m << 2) | (r0p << 3));
     const T* A = (const T*)I.ab[*(volatile int*)&I.st->rhsA];
     C2<T>* U = (C2<T>*)I.U;
+    const C2<T> z = cmk<T>(T(0), T(0));
+    const T dt = gsel<T>(I.dt, I.fdt), sx = dt * GT(g, idx2), sy = dt * GT(g, idy2);
     if (i < g.Nx - 1) {
         int na = i + (g.Nx - 1) * j;
-        U[na] = link_U<T>(GT(g, dx) * A[na]);
+        U[na] = rp0 ? cscale(sx, link_U<T>(GT(g, dx) * A[na])) : z;
     }
     if (j < g.Ny - 1) {
         int nb = g.Na + i + g.Nx * j;
-        U[nb] = link_U<T>(GT(g, dy) * A[nb]);
+        U[nb] = r0p ? cscale(sy, link_U<T>(GT(g, dy) * A[nb])) : z;
     }
 }
 
