@@ -373,10 +373,11 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
                     const C2<T> pl = shfl_up_c<T>(pc, 1), pr = shfl_down_c<T>(pc, 1);
                     const PsiRow<T>& d = D[l - 1];
                     const C2<T> ual = shfl_up_c<T>(d.ua, 1);
-                    const bool node = calc_lane && y >= 0 && y < Ny;
-                    if (node) {
+                    // every lane computes: outside the domain and on the edge lanes the
+                    // loaded inputs are zero with code 0, and psi_node returns 0 there
+                    {
                         out = psi_node<T>(pl, pr, wp[l - 1], newrow, ual, d.ua, D[l].ub, d.ub, d.rq, d.inv, d.cd);
-                        if (own_lane && y >= j0 && y < j0 + RR) {
+                        if (own_lane && y >= j0 && y < j0 + RR && y < Ny) {
                             outb[l - 1][i + Nx * y] = out;
                             // max(|d re|, |d im|); a NaN component counts as 0 (the reference's
                             // int conversion).  FP64 compares the bit patterns (non-negative
