@@ -1,6 +1,7 @@
 // C ABI of libglgpu: handle lifetime, state and parameter transfer, and the
 // extern "C" wrappers of the TD / CG / observable entry points.
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -156,7 +157,8 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (int q = 0; q < kPsiBufs && ok; ++q) ok = cudaMalloc(&h->psi[q], npsi) == cudaSuccess;
     for (int q = 0; q < 3 && ok; ++q) ok = cudaMalloc(&h->ab[q], nab) == cudaSuccess;
-    ok = ok && cudaMalloc(&h->U, (size_t)h->g.Nab * 2 * rs) == cudaSuccess;
+    // link factors: Nab complex for the CG, one (x link, y link) pair per node for the TD step
+    ok = ok && cudaMalloc(&h->U, std::max((size_t)h->g.Nab * 2, (size_t)h->g.N * 4) * rs) == cudaSuccess;
     ok = ok && cudaMalloc(&h->code, (size_t)h->g.N) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st_gather, sizeof(InstState)) == cudaSuccess;

@@ -310,7 +310,7 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
         const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
         const bool lang = I.lang_psi_on != 0;
         const T lc = gsel<T>(I.lang_psi, I.flang_psi);
-        const int Nx = g.Nx, Ny = g.Ny, Nxa = g.Nx - 1, Na = g.Na;
+        const int Nx = g.Nx, Ny = g.Ny;
         const int i = w.x0 - K + lane;
         const bool in_x = i >= 0 && i < Nx;
         const bool calc_lane = in_x && lane >= 1 && lane <= 30;        // lanes any sweep computes
@@ -323,8 +323,14 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             const bool row = y >= 0 && y < Ny;
             const int n = i + Nx * y;
             const bool ld = in_x && row, ldc = calc_lane && row;
-            q.ua = (ld && i < Nx - 1) ? __ldg(&U[i + Nxa * y]) : z;
-            q.ub = (ldc && y < Ny - 1) ? __ldg(&U[Na + n]) : z;
+            if constexpr (sizeof(T) == 4) {
+                const float4 v = ld ? __ldg((const float4*)U + n) : make_float4(0.f, 0.f, 0.f, 0.f);
+                q.ua = cmk<T>(v.x, v.y);
+                q.ub = cmk<T>(v.z, v.w);
+            } else {
+                q.ua = ld ? __ldg(&U[2 * n]) : z;
+                q.ub = ld ? __ldg(&U[2 * n + 1]) : z;
+            }
             q.cd = ldc ? (unsigned)__ldg(&code[n]) : 0u;
             q.rr = ldc ? __ldg(&rhs[n]) : z;
             q.eps = (ldc && eps_sp) ? __ldg(&eps_sp[n]) : eps0;
@@ -531,8 +537,9 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
 
 // Per-step tables of the psi Jacobi loop, during which A is fixed: the link
 // factors U = exp(-i d a) of the current A times dt/d^2 (0 on links whose
-// weight is 0; the CG fills the same buffer with its own unscaled factors
-// before each run), and per node the Winecki-Adams
+// weight is 0), stored per node as the pair (x link, y link) that starts there,
+// so a lane loads both with one 16-byte load (the CG fills the same buffer with
+// its own unscaled factors in link order before each run), and per node the Winecki-Adams
 // link weights as a bit code (bit 0: left link r_m0, 1: right r_p0, 2: lower
 // r_0m, 3: upper r_0p; a node is updated iff it has a left or a right link).
 template <typename T>
@@ -554,13 +561,14 @@ k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int onl
     C2<T>* U = (C2<T>*)I.U;
     const C2<T> z = cmk<T>(T(0), T(0));
     const T dt = gsel<T>(I.dt, I.fdt), sx = dt * GT(g, idx2), sy = dt * GT(g, idy2);
-    if (i < g.Nx - 1) {
-        int na = i + (g.Nx - 1) * j;
-        U[na] = rp0 ? cscale(sx, link_U<T>(GT(g, dx) * A[na])) : z;
-    }
-    if (j < g.Ny - 1) {
-        int nb = g.Na + i + g.Nx * j;
-        U[nb] = r0p ? cscale(sy, link_U<T>(GT(g, dy) * A[nb])) : z;
+    C2<T> ua = z, ub = z;
+    if (i < g.Nx - 1 && rp0) ua = cscale(sx, link_U<T>(GT(g, dx) * A[i + (g.Nx - 1) * j]));
+    if (j < g.Ny - 1 && r0p) ub = cscale(sy, link_U<T>(GT(g, dy) * A[g.Na + i + g.Nx * j]));
+    if constexpr (sizeof(T) == 4) {
+        ((float4*)U)[n] = make_float4(ua.x, ua.y, ub.x, ub.y);
+    } else {
+        U[2 * n] = ua;
+        U[2 * n + 1] = ub;
     }
 }
 
