@@ -70,6 +70,25 @@ def make_solver(n_side=N_SIDE, dtype=np.float32, seed=0, device=0):
     return gl
 
 
+def precision_check(n_side, steps=20, seed=0):
+    """FP32 against FP64 on the same workload: the same initial state (the FP64
+    state rounded to FP32), `steps` TD steps each; max |psi32 - psi64| and the
+    relative free-energy difference after them."""
+    g32 = make_solver(n_side, np.float32, seed=seed)
+    g64 = make_solver(n_side, np.float64, seed=seed)
+    try:
+        g32.solve.td(dt=DT, Nt=steps)
+        g64.solve.td(dt=DT, Nt=steps)
+        p32 = np.asarray(g32.vars.order_parameter).astype(np.complex128)
+        p64 = np.asarray(g64.vars.order_parameter)
+        f32, f64 = float(g32.observables.free_energy), float(g64.observables.free_energy)
+    finally:
+        g32.close()
+        g64.close()
+    return {"steps": steps, "max_abs_dpsi": float(np.max(np.abs(p32 - p64))),
+            "max_abs_psi": float(np.max(np.abs(p64))), "rel_dF": abs(f32 - f64) / abs(f64)}
+
+
 def make_oracle(n_side, seed=0):
     """The same workload for the CPU oracle (FP64), on an n_side x n_side domain."""
     from oracle import gl_oracle as O
@@ -610,6 +629,12 @@ def main():
 
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_baseline()
+        prec = None
+        if dtype == np.float32 and not args.no_cpu_baseline:
+            try:  # a side measurement: the bench line prints whatever happens here
+                prec = precision_check(args.size)
+            except Exception as e:  # noqa: BLE001
+                prec = {"error": "%s: %s" % (type(e).__name__, e)}
         # sweep launches counted on the device, plus per step the link table, the
         # loop begin/end and step-end kernels, plus the final copy and reset
         launches = int(st.sweep_launches) + 4 * args.steps + 3
@@ -634,6 +659,7 @@ def main():
             "gpu_launches": launches,
             "clocks": clk,
             "cpu_baseline": cpu,
+            "fp32_vs_fp64": prec,
         }
         print(json.dumps(line), flush=True)
     gl.close()
