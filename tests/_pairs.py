@@ -66,6 +66,8 @@ def oracle_of(gl, rand_t=1):
     return O.GLOracle(int(c.Nx), int(c.Ny), float(c.dx), float(c.dy), psi, ab, mt=mt, abei=abei,
                       kappa=float(gl.params.gl_parameter), sigma=float(gl.params.normal_conductivity),
                       epsilon=float(np.asarray(gl.params._epsilon)) if np.ndim(gl.params._epsilon) == 0 else 0.0,
+                      epsilon_spatial=(None if np.ndim(gl.params._epsilon) == 0
+                                       else flat(gl.params._epsilon).astype(np.float64)),
                       H=float(gl.params.homogeneous_external_field),
                       stop_psi=float(c.stop_criterion_order_parameter), stop_A=float(c.stop_criterion_vector_potential),
                       rand_t=rand_t, langevin_psi=float(gl.params.order_parameter_Langevin_coefficient),

@@ -9,7 +9,7 @@ the energy, and the minimisation reaches the oracle CG's converged energy."""
 import numpy as np
 import pytest
 
-from tests._pairs import gpu_state, make_pair, rel_err
+from tests._pairs import gpu_state, make_pair, oracle_of, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -71,6 +71,37 @@ def test_batch_cg_first_iterations_follow_oracle():
         if orc.solveA:
             assert rel_err(a, orc.ab) < tol, q
         assert abs(out["energy"][q] / orc.cg_energies[-1] - 1.0) < tol, q
+
+
+def test_batch_cg_spatial_linear_coefficient_follows_oracle():
+    """A per-node linear coefficient reaches the batched CG (each instance's
+    own field): first iterations against the oracle, and batch independence."""
+    from svirl_gb300.batch import GLBatch
+    cfgs = [CONFIGS[0], CONFIGS[1]]
+
+    def build():
+        sol, _ = _solvers(np.float64, cfgs)
+        for q, gl in enumerate(sol):
+            c = gl.cfg
+            gl.params.linear_coefficient = 1.0 + 0.2 * np.random.default_rng(20 + q).random((int(c.Nx), int(c.Ny)))
+        return sol
+
+    sol = build()
+    orcs = [oracle_of(gl, rand_t=1) for gl in sol]
+    n = 4
+    out = GLBatch(sol).cg(n_iter=n, rtol=0.0)
+    for q, (gl, orc) in enumerate(zip(sol, orcs)):
+        assert orc.epsilon_spatial is not None
+        orc.convergence_rtol = 0.0
+        orc.cg(n_iter=n)
+        tol = 1e-9 if np.isinf(cfgs[q]["kappa"]) else 1e-5
+        p, _ = gpu_state(gl)
+        assert rel_err(p, orc.psi) < tol, q
+        assert abs(out["energy"][q] / orc.cg_energies[-1] - 1.0) < tol, q
+    alone = build()
+    for q, gl in enumerate(alone):
+        o = GLBatch([gl]).cg(n_iter=n, rtol=0.0)
+        assert o["energy"][0] == out["energy"][q]
 
 
 def test_batch_cg_monotone_energy():

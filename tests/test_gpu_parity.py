@@ -68,6 +68,38 @@ def test_td_eqn_variants_and_langevin_match_oracle():
     assert int(gl.solve._td._random_t) == orc.rand_t
 
 
+def _eps_field(x, y):
+    return 1.0 - 0.3 * np.cos(0.7 * x) * np.sin(0.5 * y)
+
+
+@pytest.mark.parametrize("kappa,sigma,mask,form", [(3.0, 20.0, "random30", "callable"),
+                                                   (np.inf, 1.0, "holes", "array"),
+                                                   (2.0, 50.0, "none", "array")])
+def test_spatial_linear_coefficient_matches_oracle(kappa, sigma, mask, form):
+    """epsilon(x, y) (svirl/vars/params.py:56-83): the TD step, the energy and
+    the CG with a per-node linear coefficient."""
+    gl, _ = make_pair(Nx=15, Ny=12, kappa=kappa, sigma=sigma, H=0.2, mask=mask, seed=5)
+    if form == "callable":
+        gl.params.linear_coefficient = _eps_field
+    else:
+        gl.params.linear_coefficient = _eps_field(*gl.mesh.xy_grid) + 0.1 * np.random.default_rng(5).random((15, 12))
+    orc = oracle_of(gl, rand_t=5)
+    assert orc.epsilon_spatial is not None and orc.epsilon == 0.0
+    assert abs(gl.observables.free_energy - orc.free_energy()) <= 1e-12 * abs(orc.free_energy())
+    gl.solve.td(dt=0.1, Nt=8)
+    orc.td(dt=0.1, Nt=8)
+    psi, ab = gpu_state(gl)
+    assert rel_err(psi, orc.psi) < 1e-12 and rel_err(ab, orc.ab) < 1e-12
+    st = gl.solve._td.last_stats
+    assert st.total_sweeps_psi == sum(orc.sweeps_psi) and st.total_sweeps_A == sum(orc.sweeps_A)
+    gl.solve.cg(n_iter=30)
+    orc.cg(n_iter=30)
+    e_gpu, e_orc = np.array(gl.solve._cg.cg_energies), np.array(orc.cg_energies)
+    n = min(len(e_gpu), len(e_orc))
+    assert abs(len(e_gpu) - len(e_orc)) <= (0 if np.isinf(kappa) else 2)
+    assert np.max(np.abs(e_gpu[:n] - e_orc[:n]) / np.abs(e_orc[:n])) < (1e-10 if np.isinf(kappa) else 1e-6)
+
+
 @pytest.mark.parametrize("mask", ["none", "random30", "q1"])
 @pytest.mark.parametrize("kappa", [np.inf, 3.0])
 def test_observables_match_oracle(mask, kappa):

@@ -26,6 +26,8 @@ def oracle_from_ref(gl, rand_t=1):
     return O.GLOracle(cfg.Nx, cfg.Ny, cfg.dx, cfg.dy, psi, ab, mt=mt, abei=abei,
                       kappa=gl.params.gl_parameter, sigma=gl.params.normal_conductivity,
                       epsilon=float(np.asarray(gl.params.linear_coefficient_scalar_h()).reshape(-1)[0]),
+                      epsilon_spatial=(None if gl.params._epsilon.size == 1
+                                       else O.flatten_ij(gl.params.linear_coefficient)),
                       H=gl.params.homogeneous_external_field,
                       stop_psi=cfg.stop_criterion_order_parameter, stop_A=cfg.stop_criterion_vector_potential,
                       rand_t=rand_t, langevin_psi=gl.params.order_parameter_Langevin_coefficient,
@@ -99,6 +101,46 @@ def test_td_then_cg_matches_reference(kappa, sigma, H, masked, seed):
     sx, sy = gl.observables.supercurrent_density
     assert close(orc.supercurrent_density(), np.concatenate([O.flatten_ij(sx), O.flatten_ij(sy)]), 1e-12)
     assert close(orc.free_energy(), gl.observables.free_energy, 1e-12)
+
+
+@pytest.mark.parametrize("kappa,sigma,masked,form", [
+    (3.0, 20.0, True, "array"),
+    (np.inf, 1.0, True, "callable"),
+    (2.0, 10.0, False, "callable"),
+])
+def test_spatial_linear_coefficient_matches_reference(kappa, sigma, masked, form):
+    """epsilon(x, y) set as an (Nx, Ny) array (params.py:56-69): the kernels
+    then take epsilon_spatial and a scalar epsilon of 0 (params.py:72-83).  The
+    reference's callable form names an undefined `mesh` (params.py:59) and
+    raises NameError, so a callable is evaluated on the node grid here and
+    passed as the array."""
+    svirl = load_reference()
+    rng = np.random.default_rng(11)
+    mt = random_mask(rng, 10, 8) if masked else None
+    gl = svirl.GLSolver(Nx=11, Ny=9, dx=0.5, dy=0.45, order_parameter="random", random_seed=4,
+                        gl_parameter=kappa, normal_conductivity=sigma, homogeneous_external_field=0.2,
+                        material_tiling=mt)
+    if form == "array":
+        gl.params.linear_coefficient = 1.0 + 0.5 * rng.random((11, 9)) - 0.2
+    else:
+        f = lambda x, y: 1.0 - 0.3 * np.cos(0.7 * x) * np.sin(0.5 * y)  # noqa: E731
+        with pytest.raises(NameError):
+            gl.params.linear_coefficient = f
+        gl.params.linear_coefficient = f(*gl.mesh.xy_grid)
+    assert gl.params._epsilon.size > 1
+    orc = oracle_from_ref(gl, rand_t=4)
+    assert orc.epsilon == 0.0 and orc.epsilon_spatial is not None
+    assert close(orc.free_energy(), gl.observables.free_energy, 1e-13)
+    gl.solve.td(dt=0.1, Nt=8)
+    orc.td(dt=0.1, Nt=8)
+    psi, ab = ref_state(gl)
+    assert close(orc.psi, psi) and close(orc.ab, ab)
+    tol = 1e-13 if np.isinf(kappa) else 1e-8
+    gl.solve.cg(n_iter=15)
+    orc.cg(n_iter=15)
+    psi, ab = ref_state(gl)
+    assert close(orc.cg_energies, gl.solve._cg.cg_energies, tol)
+    assert close(orc.psi, psi, 10 * tol) and close(orc.ab, ab, 10 * tol)
 
 
 def test_langevin_and_eqn_variants_match_reference():
