@@ -11,7 +11,7 @@ the Jacobi sweep counts after TDGL; the CG energies and state after a few
 iterations; the vortex list of the final state).  The oracle recomputes every
 output from the inputs and must agree before a fixture is written.
 
-    python tests/golden/make_golden.py [reference_dir]
+    python tests/golden/make_golden.py [reference_dir]      (GOLDEN_ONLY=cases|fv|api: one group)
 """
 import os
 import sys
@@ -206,6 +206,65 @@ def make_fv_case(svirl, name, spec):
     return out
 
 
+API_CASE = dict(Nx=12, Ny=10, dx=0.5, dy=0.5, kappa=4.0, sigma=30.0, H=0.1, ext=0.03, eps=0.9, seed=5, level=0.7,
+                level2=0.5, seed2=8, dH=0.05, H_reset=0.2, dt=0.08, Nt=6)
+
+
+def make_api_case(svirl):
+    """The GLSolver surface around the hot path: random_level / random_seed at
+    construction, randomize_order_parameter, homogeneous_external_field_delta
+    and _reset (the vector potential they set), td with T given, and the
+    observables normalcurrent_density and superfluid_density."""
+    c = API_CASE
+    gl = svirl.GLSolver(Nx=c["Nx"], Ny=c["Ny"], dx=c["dx"], dy=c["dy"], order_parameter="random",
+                        random_seed=c["seed"], random_level=c["level"], gl_parameter=c["kappa"],
+                        normal_conductivity=c["sigma"], linear_coefficient=c["eps"],
+                        homogeneous_external_field=c["H"], external_field=c["ext"])
+    out = {k: np.asarray(v) for k, v in c.items()}
+
+    def ab():
+        a, b = gl.vars.vector_potential
+        return np.concatenate([flat(a), flat(b)])
+
+    out["psi0"], out["ab0"] = flat(gl.vars.order_parameter), ab()
+    ei = gl.params.external_irregular_vector_potential
+    out["abei"] = np.concatenate([flat(ei[0]), flat(ei[1])])
+    gl.vars.randomize_order_parameter(level=c["level2"], seed=c["seed2"])
+    out["psi1"] = flat(gl.vars.order_parameter)
+    gl.params.homogeneous_external_field_delta = c["dH"]
+    out["H2"], out["ab2"] = np.float64(gl.params.homogeneous_external_field), ab()
+    gl.params.homogeneous_external_field_reset = c["H_reset"]
+    out["H3"], out["ab3"] = np.float64(gl.params.homogeneous_external_field), ab()
+    try:
+        gl.solve.td(dt=c["dt"], Nt=c["Nt"], T=c["dt"] * c["Nt"] + 1.0)
+        raise RuntimeError("td accepted an end time that disagrees with dt * Nt")
+    except AssertionError:
+        pass
+    gl.solve.td(dt=c["dt"], Nt=c["Nt"], T=c["dt"] * c["Nt"])
+    out["psi4"], out["ab4"] = flat(gl.vars.order_parameter), ab()
+    out["F4"] = gl.observables.free_energy
+    out["B4"] = flat(gl.observables.magnetic_field)
+    jx, jy = gl.observables.current_density
+    out["j4"] = np.concatenate([flat(jx), flat(jy)])
+    sx, sy = gl.observables.supercurrent_density
+    out["js4"] = np.concatenate([flat(sx), flat(sy)])
+    nx_, ny_ = gl.observables.normalcurrent_density
+    out["jn4"] = np.concatenate([flat(nx_), flat(ny_)])
+    out["rho4"] = flat(gl.observables.superfluid_density)
+    # the oracle from the state after the field reset reproduces the TD step and the observables
+    orc = O.GLOracle(c["Nx"], c["Ny"], c["dx"], c["dy"], out["psi1"], out["ab3"], abei=out["abei"],
+                     kappa=c["kappa"], sigma=c["sigma"], epsilon=c["eps"], H=float(out["H3"]), rand_t=c["seed"])
+    orc.td(dt=c["dt"], Nt=c["Nt"])
+    assert close(orc.psi, out["psi4"], 1e-13) and close(orc.ab, out["ab4"], 1e-13)
+    assert abs(orc.free_energy() - out["F4"]) <= 1e-13 * abs(out["F4"])
+    assert close(orc.magnetic_field(), out["B4"], 1e-12) and close(orc.current_density(), out["j4"], 1e-12)
+    assert close(orc.supercurrent_density(), out["js4"], 1e-12)
+    assert close(orc.current_density() - orc.supercurrent_density(), out["jn4"], 1e-12)
+    assert close(np.abs(orc.psi) ** 2, out["rho4"], 1e-13)
+    np.savez_compressed(os.path.join(HERE, "api_k4.npz"), **out)
+    return out
+
+
 def svirl_gpu(x):
     from pycuda import gpuarray  # the shim's
     return gpuarray.to_gpu(np.ascontiguousarray(x))
@@ -219,12 +278,18 @@ def main():
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         import svirl
-        for name, spec in CASES.items():
-            make_case(svirl, name, spec)
-            print("wrote case_%s.npz" % name)
-        for name, spec in FV_CASES.items():
-            make_fv_case(svirl, name, spec)
-            print("wrote %s.npz" % name)
+        only = os.environ.get("GOLDEN_ONLY")  # e.g. "api": write that fixture alone
+        if only in (None, "cases"):
+            for name, spec in CASES.items():
+                make_case(svirl, name, spec)
+                print("wrote case_%s.npz" % name)
+        if only in (None, "fv"):
+            for name, spec in FV_CASES.items():
+                make_fv_case(svirl, name, spec)
+                print("wrote %s.npz" % name)
+        if only in (None, "api"):
+            make_api_case(svirl)
+            print("wrote api_k4.npz")
 
 
 if __name__ == "__main__":

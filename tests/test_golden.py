@@ -88,3 +88,24 @@ def test_oracle_reproduces_fixed_vortex_golden(path):
     ai = O.unflatten_ij(f["ai0"][:g.Na], g.Nx - 1, g.Ny), O.unflatten_ij(f["ai0"][g.Na:], g.Nx, g.Ny - 1)
     vx, vy, vv = O.detect_vortices(g, orc.psi, f["ab_host"], float(f["H"]), ai_bi=ai)
     assert np.array_equal(vx, f["vx"]) and np.array_equal(vy, f["vy"]) and np.array_equal(vv, f["vv"])
+
+
+API = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "api_k4.npz")
+
+
+def test_oracle_reproduces_api_golden():
+    """The API-surface fixture (field delta/reset, randomize_order_parameter, td
+    with an end time, normal current, superfluid density): the oracle's
+    initial-state helpers and its TD step from the state after the field reset."""
+    f = load(API)
+    Nx, Ny = int(f["Nx"]), int(f["Ny"])
+    assert rel(O.random_order_parameter(Nx * Ny, float(f["level"]), int(f["seed"])), f["psi0"]) < 1e-15
+    assert rel(O.random_order_parameter(Nx * Ny, float(f["level2"]), int(f["seed2"])), f["psi1"]) < 1e-15
+    orc = O.GLOracle(Nx, Ny, float(f["dx"]), float(f["dy"]), f["psi1"].copy(), f["ab3"].copy(), abei=f["abei"],
+                     kappa=float(f["kappa"]), sigma=float(f["sigma"]), epsilon=float(f["eps"]), H=float(f["H3"]),
+                     rand_t=int(f["seed"]))
+    orc.td(dt=float(f["dt"]), Nt=int(f["Nt"]))
+    assert rel(orc.psi, f["psi4"]) < 1e-13 and rel(orc.ab, f["ab4"]) < 1e-13
+    assert abs(orc.free_energy() / float(f["F4"]) - 1.0) < 1e-13
+    assert rel(orc.current_density() - orc.supercurrent_density(), f["jn4"]) < 1e-12
+    assert rel(np.abs(orc.psi) ** 2, f["rho4"]) < 1e-13
