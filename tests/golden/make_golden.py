@@ -210,17 +210,25 @@ API_CASE = dict(Nx=12, Ny=10, dx=0.5, dy=0.5, kappa=4.0, sigma=30.0, H=0.1, ext=
                 level2=0.5, seed2=8, dH=0.05, H_reset=0.2, dt=0.08, Nt=6)
 
 
+def api_material(x, y):
+    """Material tiling of the API case as a callable of the cell centres
+    (svirl/mesh/grid.py:102-120): the domain minus a disc and a strip."""
+    return ((x - 3.1) ** 2 + (y - 2.2) ** 2 > 1.2 ** 2) & ~((x > 4.0) & (y < 0.8))
+
+
 def make_api_case(svirl):
-    """The GLSolver surface around the hot path: random_level / random_seed at
-    construction, randomize_order_parameter, homogeneous_external_field_delta
+    """The GLSolver surface around the hot path: a callable material tiling,
+    random_level / random_seed at construction, randomize_order_parameter, homogeneous_external_field_delta
     and _reset (the vector potential they set), td with T given, and the
     observables normalcurrent_density and superfluid_density."""
     c = API_CASE
     gl = svirl.GLSolver(Nx=c["Nx"], Ny=c["Ny"], dx=c["dx"], dy=c["dy"], order_parameter="random",
                         random_seed=c["seed"], random_level=c["level"], gl_parameter=c["kappa"],
                         normal_conductivity=c["sigma"], linear_coefficient=c["eps"],
-                        homogeneous_external_field=c["H"], external_field=c["ext"])
+                        homogeneous_external_field=c["H"], external_field=c["ext"], material_tiling=api_material)
     out = {k: np.asarray(v) for k, v in c.items()}
+    out["mt"] = flat(gl.mesh.material_tiling)
+    assert 0 < out["mt"].sum() < out["mt"].size
 
     def ab():
         a, b = gl.vars.vector_potential
@@ -252,7 +260,7 @@ def make_api_case(svirl):
     out["jn4"] = np.concatenate([flat(nx_), flat(ny_)])
     out["rho4"] = flat(gl.observables.superfluid_density)
     # the oracle from the state after the field reset reproduces the TD step and the observables
-    orc = O.GLOracle(c["Nx"], c["Ny"], c["dx"], c["dy"], out["psi1"], out["ab3"], abei=out["abei"],
+    orc = O.GLOracle(c["Nx"], c["Ny"], c["dx"], c["dy"], out["psi1"], out["ab3"], mt=out["mt"], abei=out["abei"],
                      kappa=c["kappa"], sigma=c["sigma"], epsilon=c["eps"], H=float(out["H3"]), rand_t=c["seed"])
     orc.td(dt=c["dt"], Nt=c["Nt"])
     assert close(orc.psi, out["psi4"], 1e-13) and close(orc.ab, out["ab4"], 1e-13)

@@ -101,7 +101,8 @@ def test_oracle_reproduces_api_golden():
     Nx, Ny = int(f["Nx"]), int(f["Ny"])
     assert rel(O.random_order_parameter(Nx * Ny, float(f["level"]), int(f["seed"])), f["psi0"]) < 1e-15
     assert rel(O.random_order_parameter(Nx * Ny, float(f["level2"]), int(f["seed2"])), f["psi1"]) < 1e-15
-    orc = O.GLOracle(Nx, Ny, float(f["dx"]), float(f["dy"]), f["psi1"].copy(), f["ab3"].copy(), abei=f["abei"],
+    orc = O.GLOracle(Nx, Ny, float(f["dx"]), float(f["dy"]), f["psi1"].copy(), f["ab3"].copy(), mt=f["mt"],
+                     abei=f["abei"],
                      kappa=float(f["kappa"]), sigma=float(f["sigma"]), epsilon=float(f["eps"]), H=float(f["H3"]),
                      rand_t=int(f["seed"]))
     orc.td(dt=float(f["dt"]), Nt=int(f["Nt"]))

@@ -1,5 +1,6 @@
 """The GLSolver surface around the hot path against the golden fixture made by
-the reference's own host code (tests/golden/api_k4.npz): random_level and
+the reference's own host code (tests/golden/api_k4.npz): a callable material
+tiling (svirl/mesh/grid.py:102-120), random_level and
 random_seed at construction (svirl/vars/vars.py:93-109), randomize_order_parameter,
 homogeneous_external_field_delta and _reset (svirl/vars/params.py:135-170),
 td with an end time (svirl/solvers/td.py:75-107), and the observables
@@ -10,6 +11,7 @@ import numpy as np
 import pytest
 
 from tests._pairs import flat, rel_err
+from tests.golden.make_golden import api_material
 
 pytestmark = pytest.mark.gpu
 
@@ -23,7 +25,9 @@ def test_api_surface_matches_reference_golden():
     gl = GLSolver(Nx=int(f["Nx"]), Ny=int(f["Ny"]), dx=float(f["dx"]), dy=float(f["dy"]), order_parameter="random",
                   random_seed=int(f["seed"]), random_level=float(f["level"]), gl_parameter=float(f["kappa"]),
                   normal_conductivity=float(f["sigma"]), linear_coefficient=float(f["eps"]),
-                  homogeneous_external_field=float(f["H"]), external_field=float(f["ext"]), dtype=np.float64)
+                  homogeneous_external_field=float(f["H"]), external_field=float(f["ext"]), dtype=np.float64,
+                  material_tiling=api_material)
+    assert np.array_equal(flat(gl.mesh.material_tiling), f["mt"])
 
     def ab():
         a, b = gl.vars.vector_potential
