@@ -56,14 +56,15 @@ class Engine:
         self.cache = HandleCache(device=device)
         self.active = []   # dicts: req, h, phase ('td' | 'cg'), td_left, cg_done, admitted
         self.done = []
-        self.used_bytes = 0
 
     def _free_bytes(self):
+        """Free device memory as the CUDA runtime reports it through torch.  Where
+        torch cannot report it, admission rests on the active-node budget alone."""
         try:
             import torch
             free, _ = torch.cuda.mem_get_info()
             return free
-        except Exception:
+        except Exception:  # noqa: BLE001
             return 1 << 40
 
     def admit(self, req, now):
