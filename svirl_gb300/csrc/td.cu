@@ -945,10 +945,14 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
 }
 
 // Prepare one timed sweep: Jacobi sweep index k (k >= 1 reads a psi^(k) buffer
-// distinct from the right-hand side, as in a typical sweep), loop not done.
+// distinct from the right-hand side, as in a typical sweep), loop not done, and
+// the right-hand sides at buffer 0 as at rest (a timed launch that meets the stop
+// rule moves them, and the next launch would then write into buffer 0).
 __global__ void k_bench_prep(const Inst* __restrict__ insts, int ninst, LoopState* loop, int k) {
     for (int q = threadIdx.x; q < ninst; q += blockDim.x) {
         InstState* st = insts[q].st;
+        st->rhs = 0;
+        st->rhsA = 0;
         st->sweep = k;
         st->done = 0;
         st->blocks_done = 0u;
