@@ -60,6 +60,7 @@ void upload_inst(glgpu_handle* h) {
     I.eps_sp = h->eps_sp;
     I.U = h->U;
     I.code = h->code;
+    I.dinv = h->dinv;
     I.st = h->st;
     I.cg = h->cgst;
     I.cbits = h->cbits;
@@ -112,7 +113,7 @@ static void free_all(glgpu_handle* h) {
         if (h->dir_psi[q]) cudaFree(h->dir_psi[q]);
         if (h->dir_A[q]) cudaFree(h->dir_A[q]);
     }
-    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->code, h->st, h->inst, h->tiles, h->items, h->loop, h->partials, h->counter,
+    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->code, h->dinv, h->st, h->inst, h->tiles, h->items, h->loop, h->partials, h->counter,
                     h->dscal, h->out, h->vort, h->vort_n, h->flush};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -160,6 +161,7 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     // link factors: Nab complex for the CG, one (x link, y link) pair per node for the TD step
     ok = ok && cudaMalloc(&h->U, std::max((size_t)h->g.Nab * 2, (size_t)h->g.N * 4) * rs) == cudaSuccess;
     ok = ok && cudaMalloc(&h->code, (size_t)h->g.N) == cudaSuccess;
+    if (h->dtype == 8) ok = ok && cudaMalloc(&h->dinv, (size_t)h->g.N * rs) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st_gather, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->inst, sizeof(Inst)) == cudaSuccess;
@@ -198,6 +200,7 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(h->loop, 0, sizeof(LoopState), h->stream);
     for (int q = 0; q < kPsiBufs && e == cudaSuccess; ++q) e = cudaMemsetAsync(h->psi[q], 0, npsi, h->stream);
     for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = cudaMemsetAsync(h->ab[q], 0, nab, h->stream);
+    if (e == cudaSuccess && h->dinv) e = cudaMemsetAsync(h->dinv, 0, (size_t)h->g.N * rs, h->stream);
     if (e == cudaSuccess) {
         upload_inst(h);
         e = cudaStreamSynchronize(h->stream);

@@ -76,6 +76,7 @@ struct Inst {
     const void* eps_sp;       // spatial linear coefficient (nodes) or NULL
     void* U;                  // link factors exp(-i d a) of the psi loop, Nab complex
     uint8_t* code;            // per-node link-weight bits of the psi loop, N bytes
+    void* dinv;               // FP64: per-node reciprocal of the psi step's diagonal, N reals (NULL for FP32)
     uint8_t* cbits;           // per-node cell bits (cell_bits) for the batched CG, N bytes (NULL until CG)
     void* vpi;                // irregular vector potential of fixed vortices, Nab, or NULL
     const int32_t* lock;      // phase-lock node list or NULL
@@ -149,6 +150,7 @@ struct glgpu_handle {
     void* eps_sp = nullptr;
     void* U = nullptr;
     uint8_t* code = nullptr;
+    void* dinv = nullptr;
     glgpu::InstState* st = nullptr;
     glgpu::Inst* inst = nullptr;        // device copy of the descriptor
     glgpu::Inst inst_h;                 // host copy of the descriptor

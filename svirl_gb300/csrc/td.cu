@@ -256,6 +256,7 @@ template <typename T> struct PsiRow {
 #endif
 
 constexpr int kPsiThreads = GLGPU_PSI_THREADS, kPsiWarps = kPsiThreads / 32;
+template <typename T> constexpr bool kStoreInv = sizeof(T) == 8;
 template <typename T, int RR>
 __global__ void __launch_bounds__(kPsiThreads, GLGPU_PSI_MIN_CTAS)
 k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
@@ -278,6 +279,7 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
     C2<T>* outb[K];
     const C2<T>* U = nullptr;
     const uint8_t* code = nullptr;
+    T* dinv = nullptr;
     uint32_t rt = 0;
     for (int it = gw; it < nitems; it += nw) {
         const Item w = items[it];
@@ -300,6 +302,7 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             }
             U = (const C2<T>*)I.U;
             code = I.code;
+            dinv = (T*)I.dinv;
             count = 0;
         }
         if (done) continue;
@@ -316,6 +319,10 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
         const bool calc_lane = in_x && lane >= 1 && lane <= 30;        // lanes any sweep computes
         const bool own_lane = in_x && lane >= K && lane <= 31 - K;     // the strip's own columns
         const int j0 = w.j0;
+        // FP64: the first launch of a step stores the diagonal reciprocals of the
+        // strip's own nodes, later launches of the step load them (the diagonal is
+        // fixed during the Jacobi loop; the FP64 pipe binds this build)
+        const bool load_inv = kStoreInv<T> && k > 0, store_inv = kStoreInv<T> && k == 0;
         const C2<T> z = cmk<T>(T(0), T(0));
         auto load_psi = [&](int y) -> C2<T> { return (in_x && y >= 0 && y < Ny) ? __ldg(&cur[i + Nx * y]) : z; };
         auto load_side = [&](int y) -> PsiSide<T> {
@@ -333,7 +340,8 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             }
             q.cd = ldc ? (unsigned)__ldg(&code[n]) : 0u;
             q.rr = ldc ? __ldg(&rhs[n]) : z;
-            q.eps = (ldc && eps_sp) ? __ldg(&eps_sp[n]) : eps0;
+            if (load_inv) q.eps = ldc ? __ldg(&dinv[n]) : T(0);  // the stored reciprocal
+            else q.eps = (ldc && eps_sp) ? __ldg(&eps_sp[n]) : eps0;
             return q;
         };
         // window of sweep l-1 (l = 1..K) as seen by sweep l: rows y-1 and y
@@ -355,7 +363,12 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
                 r.rq.x += lc * (rand_1<T>(n, rt) - T(0.5));
                 r.rq.y += lc * (rand_2<T>(n, rt) - T(0.5));
             }
-            r.inv = (q.cd & 3u) ? psi_diag_inv<T>(r.rq, q.eps, q.cd, dt, idx2, idy2) : T(0);
+            if (load_inv) {
+                r.inv = q.eps;
+            } else {
+                r.inv = (q.cd & 3u) ? psi_diag_inv<T>(r.rq, q.eps, q.cd, dt, idx2, idy2) : T(0);
+                if (store_inv && own_lane && y >= j0 && y < j0 + RR && y < Ny) dinv[i + Nx * y] = r.inv;
+            }
             return r;
         };
         C2<T> nx_p = load_psi(j0 - K);
