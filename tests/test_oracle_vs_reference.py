@@ -180,3 +180,29 @@ def test_vortex_detector_matches_reference():
     ox, oy, ov = O.detect_vortices(g, psi, ab, 0.4)
     assert vx.size > 0
     assert np.array_equal(ox, vx) and np.array_equal(oy, vy) and np.array_equal(ov, vv)
+
+
+@pytest.mark.parametrize("Nx,Ny,mask", [(4, 4, "none"), (4, 40, "random"), (40, 4, "random"), (9, 7, "empty")])
+def test_edge_geometries_match_reference(Nx, Ny, mask):
+    """The smallest grid the reference accepts (4 x 4, svirl/__init__.py:97-98),
+    three-cell-wide strips in either direction, and a domain with every cell
+    removed (psi is then 0 after the first step): TD and the energy follow the
+    reference."""
+    svirl = load_reference()
+    rng = np.random.default_rng(Nx * 100 + Ny)
+    mt = None
+    if mask == "random":
+        mt = random_mask(rng, Nx - 1, Ny - 1, 0.2)
+    elif mask == "empty":
+        mt = np.zeros((Nx - 1, Ny - 1), dtype=bool)
+    gl = svirl.GLSolver(Nx=Nx, Ny=Ny, dx=0.5, dy=0.5, order_parameter="random", random_seed=2,
+                        gl_parameter=3.0, normal_conductivity=50.0, homogeneous_external_field=0.2,
+                        material_tiling=mt)
+    orc = oracle_from_ref(gl, rand_t=2)
+    assert close(orc.free_energy(), gl.observables.free_energy, 1e-13) or abs(gl.observables.free_energy) < 1e-300
+    gl.solve.td(dt=0.1, Nt=6)
+    orc.td(dt=0.1, Nt=6)
+    psi, ab = ref_state(gl)
+    assert close(orc.psi, psi) and close(orc.ab, ab)
+    if mask == "empty":
+        assert not np.any(psi)
