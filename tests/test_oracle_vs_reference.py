@@ -206,3 +206,27 @@ def test_edge_geometries_match_reference(Nx, Ny, mask):
     assert close(orc.psi, psi) and close(orc.ab, ab)
     if mask == "empty":
         assert not np.any(psi)
+
+
+@pytest.mark.parametrize("kappa,sigma", [(np.inf, 1.0), (4.0, 80.0)])
+def test_external_field_with_mask_matches_reference(kappa, sigma):
+    """An external field (the external irregular vector potential enters the link
+    phases of the energy, the gradients and the CG, params.py:224-303) on a
+    masked domain, for kappa = inf and finite kappa."""
+    svirl = load_reference()
+    rng = np.random.default_rng(21)
+    mt = random_mask(rng, 12, 10, 0.15)
+    gl = svirl.GLSolver(Nx=13, Ny=11, dx=0.5, dy=0.5, order_parameter="random", random_seed=6,
+                        gl_parameter=kappa, normal_conductivity=sigma, homogeneous_external_field=0.15,
+                        external_field=0.04, material_tiling=mt)
+    orc = oracle_from_ref(gl, rand_t=6)
+    assert orc.abei is not None
+    assert close(orc.free_energy(), gl.observables.free_energy, 1e-13)
+    gl.solve.td(dt=0.1, Nt=6)
+    orc.td(dt=0.1, Nt=6)
+    psi, ab = ref_state(gl)
+    assert close(orc.psi, psi) and close(orc.ab, ab)
+    tol = 1e-13 if np.isinf(kappa) else 1e-8
+    gl.solve.cg(n_iter=20)
+    orc.cg(n_iter=20)
+    assert close(orc.cg_energies, gl.solve._cg.cg_energies, tol)
