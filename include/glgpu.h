@@ -122,6 +122,14 @@ int glgpu_set_linear_coefficient_field(glgpu_handle* h, const void* eps);   /* N
  *     2 = vector potential only (td.py:444). */
 int glgpu_td(glgpu_handle* h, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats);
 int glgpu_set_use_graphs(glgpu_handle* h, int32_t enable);
+/* Safety net of the device-side Jacobi loops: a loop that has launched this many
+ * sweep kernels without meeting the stop rule ends, and the call returns
+ * GLGPU_E_TIMEOUT; a time step whose loop was cut keeps the state it started
+ * from (its sweeps are discarded).  0 (the default) = 1088 launches, above the
+ * reference's cap of 1024 sweeps per step (svirl/solvers/td.py:164,274), which
+ * the loop also applies, so by default the guard fires only if that cap fails.
+ * The reference's host loop has no guard. */
+int glgpu_set_loop_guard(glgpu_handle* h, int32_t launches);
 
 /* --- timing (CUDA events on the handle's stream; no counterpart in the reference,
  *     which has no timing code: its profiler calls are commented out,
@@ -183,6 +191,7 @@ int glgpu_batch_destroy(glgpu_batch* b);
 const char* glgpu_batch_last_error(const glgpu_batch* b);
 int glgpu_batch_td(glgpu_batch* b, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats, double* elapsed_ms);
 int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable);
+int glgpu_batch_set_loop_guard(glgpu_batch* b, int32_t launches);  /* as glgpu_set_loop_guard */
 /* Free-energy minimisation of every instance of the batch with the step
  * length, beta and stop test decided on the device (one graph launch for the
  * whole run).  No counterpart in the reference; each instance follows the

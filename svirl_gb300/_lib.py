@@ -66,6 +66,7 @@ _SIGNATURES = {
     "glgpu_set_linear_coefficient_field": (C.c_int, [_H, _P]),
     "glgpu_td": (C.c_int, [_H, C.c_double, C.c_int32, C.c_int32, C.POINTER(TDStats)]),
     "glgpu_set_use_graphs": (C.c_int, [_H, C.c_int32]),
+    "glgpu_set_loop_guard": (C.c_int, [_H, C.c_int32]),
     "glgpu_td_timed": (C.c_int, [_H, C.c_double, C.c_int32, C.c_int32, C.POINTER(TDStats), C.POINTER(C.c_double)]),
     "glgpu_time_sweeps": (C.c_int, [_H, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "glgpu_free_energy": (C.c_int, [_H, C.POINTER(C.c_double)]),
@@ -86,6 +87,7 @@ _SIGNATURES = {
     "glgpu_batch_last_error": (C.c_char_p, [_H]),
     "glgpu_batch_td": (C.c_int, [_H, C.c_double, C.c_int32, C.c_int32, C.POINTER(TDStats), C.POINTER(C.c_double)]),
     "glgpu_batch_set_use_graphs": (C.c_int, [_H, C.c_int32]),
+    "glgpu_batch_set_loop_guard": (C.c_int, [_H, C.c_int32]),
     "glgpu_batch_set_energy_targets": (C.c_int, [_H, _P, C.c_double]),
     "glgpu_batch_cg": (C.c_int, [_H, C.c_int32, C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
@@ -264,6 +266,9 @@ class Handle:
 
     def set_use_graphs(self, enable):
         check(self.lib.glgpu_set_use_graphs(self.h, 1 if enable else 0), self.h, "set_use_graphs")
+
+    def set_loop_guard(self, launches):
+        check(self.lib.glgpu_set_loop_guard(self.h, int(launches)), self.h, "set_loop_guard")
 
     # TD ------------------------------------------------------------------------
     def td(self, dt, Nt, eqn=0):

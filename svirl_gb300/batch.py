@@ -72,6 +72,10 @@ class HandleBatch:
     def set_use_graphs(self, enable):
         self._check(self.lib.glgpu_batch_set_use_graphs(self.b, 1 if enable else 0), "set_use_graphs")
 
+    def set_loop_guard(self, launches):
+        """Jacobi loop guard in sweep launches (0: the default of 1088)."""
+        self._check(self.lib.glgpu_batch_set_loop_guard(self.b, int(launches)), "set_loop_guard")
+
     def td_raw(self, dt, Nt, eqn=0, timed=False):
         """``glgpu_batch_td``: eqn 0 = both equations, 1 = psi only, 2 = A only."""
         st = _lib.TDStats()

@@ -317,6 +317,13 @@ int glgpu_set_use_graphs(glgpu_handle* h, int32_t enable) {
     return GLGPU_OK;
 }
 
+int glgpu_set_loop_guard(glgpu_handle* h, int32_t launches) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    if (launches < 0) return set_error(h, GLGPU_E_ARG, "set_loop_guard: launches must be >= 0");
+    h->loop_guard = launches;
+    return GLGPU_OK;
+}
+
 static void drop_td_graphs(glgpu_handle* h) {
     for (int q = 0; q < kTDGraphs; ++q)
         if (h->td_exec[q]) {
@@ -580,6 +587,13 @@ int glgpu_batch_set_energy_targets(glgpu_batch* b, const double* targets, double
 int glgpu_batch_set_use_graphs(glgpu_batch* b, int32_t enable) {
     if (!b) return GLGPU_E_ARG;
     b->use_graphs = enable != 0;
+    return GLGPU_OK;
+}
+
+int glgpu_batch_set_loop_guard(glgpu_batch* b, int32_t launches) {
+    if (!b) return GLGPU_E_ARG;
+    if (launches < 0) return batch_error(b, GLGPU_E_ARG, "batch_set_loop_guard: launches must be >= 0");
+    b->loop_guard = launches;
     return GLGPU_OK;
 }
 

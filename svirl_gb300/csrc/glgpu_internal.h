@@ -105,6 +105,7 @@ struct LoopState {
     int err;                  // error bits (kErr*)
     int ninst;
     long long total_launches;  // sweep kernel launches (psi and A) in the current call
+    int guard;                // launches after which a Jacobi loop is stopped with kErrLoopGuard
 };
 
 constexpr int kErrLoopGuard = 1;
@@ -185,6 +186,7 @@ struct glgpu_handle {
     glgpu::InstState* st_gather = nullptr;  // device copy target of the loop state
     bool td_graph_failed = false;
     bool use_graphs = true;
+    int loop_guard = 0;                 // Jacobi loop guard in sweep launches (0: kLoopGuard)
     std::string last_error;
     void* flush = nullptr;              // L2 flush buffer for kernel timing
     // host pinned staging for small results
@@ -209,6 +211,7 @@ struct glgpu_batch {
     std::vector<int> inst_items;         // psi sweep items of each instance (at strip_rows)
     cudaGraphExec_t td_exec[glgpu::kTDGraphs] = {};
     bool td_graph_failed = false, use_graphs = true;
+    int loop_guard = 0;                  // Jacobi loop guard in sweep launches (0: kLoopGuard)
     // batched device CG (allocated on first use)
     void* cg_tiles = nullptr;            // CG tile table (larger tiles than the TD one)
     int cg_ntiles = 0;

@@ -38,7 +38,7 @@ __device__ void finish_launch(LoopState* loop, cudaGraphConditionalHandle cond, 
     loop->total_launches += 1;
     int act = atomicAdd(&loop->active, 0);
     int cont = act > 0 ? 1 : 0;
-    if (cont && L >= kLoopGuard) {
+    if (cont && L >= loop->guard) {
         cont = 0;
         loop->err |= kErrLoopGuard;
     }
@@ -1096,7 +1096,7 @@ struct TDOutcome {
 // once per eqn mode and kappa mix) or the host-driven loop, then the instances'
 // loop states gathered to the host.
 static TDOutcome td_core(cudaStream_t s, const TDLaunch& L, int Nt, int eqn, cudaGraphExec_t* execs, bool* graph_failed,
-                         bool use_graphs, bool timed, InstState* gather_dev, InstState* gather_host) {
+                         bool use_graphs, int guard, bool timed, InstState* gather_dev, InstState* gather_host) {
     TDOutcome o = {cudaSuccess, 0, 0, 0, 0.f, 0};
     k_reset_counters<<<(L.ninst + 127) / 128, 128, 0, s>>>(L.insts, L.ninst);
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1111,6 +1111,7 @@ static TDOutcome td_core(cudaStream_t s, const TDLaunch& L, int Nt, int eqn, cud
         memset(&ls, 0, sizeof(ls));
         ls.Nt = Nt;
         ls.ninst = L.ninst;
+        ls.guard = guard > 0 ? guard : kLoopGuard;
         o.err = cudaMemcpyAsync(L.loop, &ls, sizeof(ls), cudaMemcpyHostToDevice, s);
         if (o.err != cudaSuccess) return o;
         const int slot = eqn * 4 + (L.any_solveA ? 2 : 0) + (L.any_fv ? 1 : 0);
@@ -1183,7 +1184,8 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     L.any_solveA = h->inst_h.solveA != 0;
     L.any_fv = h->vpi != nullptr || h->lock_n > 0;
     InstState hs;
-    TDOutcome o = td_core(h->stream, L, Nt, eqn, h->td_exec, &h->td_graph_failed, h->use_graphs, elapsed_ms != nullptr,
+    TDOutcome o = td_core(h->stream, L, Nt, eqn, h->td_exec, &h->td_graph_failed, h->use_graphs, h->loop_guard,
+                          elapsed_ms != nullptr,
                           h->st_gather, &hs);
     if (o.err != cudaSuccess) return cuda_check(h, o.err, "td");
     if (elapsed_ms) *elapsed_ms = o.ms;
@@ -1216,7 +1218,8 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
     L.strip_rows = b->strip_rows;
     L.any_solveA = any_solveA;
     L.any_fv = any_fv;
-    TDOutcome o = td_core(b->stream, L, Nt, eqn, b->td_exec, &b->td_graph_failed, b->use_graphs, elapsed_ms != nullptr,
+    TDOutcome o = td_core(b->stream, L, Nt, eqn, b->td_exec, &b->td_graph_failed, b->use_graphs, b->loop_guard,
+                          elapsed_ms != nullptr,
                           b->gather, b->gather_h.data());
     if (o.err != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_td: ") + cudaGetErrorString(o.err));
     if (elapsed_ms) *elapsed_ms = o.ms;
