@@ -102,7 +102,10 @@ class GLOracle:
     def __init__(self, Nx, Ny, dx, dy, psi, ab, mt=None, abei=None, kappa=np.inf, sigma=1.0,
                  epsilon=1.0, epsilon_spatial=None, H=0.0, stop_psi=1e-6, stop_A=1e-6,
                  rand_t=1, langevin_psi=0.0, langevin_A=0.0, convergence_rtol=1e-6,
-                 dtype=np.float64, vpi=None, lock_ns=None):
+                 dtype=np.float64, vpi=None, lock_ns=None, kernels=None):
+        # kernels: a module or object with kernels_np's functions; oracle.ref_gpu.RefKernels
+        # runs these host loops on the reference's own compiled kernels instead
+        self.K = K if kernels is None else kernels
         self.g = K.Grid(Nx, Ny, dx, dy)
         self.dtype = dtype
         self.psi = np.array(psi, dtype=np.complex128).reshape(-1).copy()
@@ -153,7 +156,7 @@ class GLOracle:
         cur = self.psi
         nsw = 0
         for j in range(1024):
-            nxt, code = K.iterate_order_parameter_jacobi_step(
+            nxt, code = self.K.iterate_order_parameter_jacobi_step(
                 g, dt, self.epsilon, self.epsilon_spatial, self.mt, self.ab, rhs, cur,
                 self.langevin_psi, j, self.rand_t, stop)
             cur = nxt
@@ -164,7 +167,7 @@ class GLOracle:
         self.rand_t = (self.rand_t + 1) & 0xFFFFFFFF
         self.sweeps_psi.append(nsw)
         if self.lock_ns is not None:  # td.py:206-216
-            K.order_parameter_phase_lock(self.psi, self.lock_ns)
+            self.K.order_parameter_phase_lock(self.psi, self.lock_ns)
 
     # fixed vortices around the psi step (td.py:120-154): xpy_r / xmy_r over the
     # first N elements of the link array
@@ -192,7 +195,7 @@ class GLOracle:
         rhs = self.ab.copy()
         nsw = 0
         for j in range(1024):
-            vals, code = K.iterate_vector_potential_jacobi_step(
+            vals, code = self.K.iterate_vector_potential_jacobi_step(
                 g, dt, self.kappa2, self.rho, self.H, self.mt, self.psi, X, rhs, cur,
                 self.langevin_A, j, self.rand_t, stop)
             nxt_buf[:] = vals
@@ -234,33 +237,33 @@ class GLOracle:
 
     # observables --------------------------------------------------------------
     def free_energy(self):
-        return K.free_energy(self.g, self.kappa2, self.epsilon, self.epsilon_spatial, self.H,
+        return self.K.free_energy(self.g, self.kappa2, self.epsilon, self.epsilon_spatial, self.H,
                              self.mt, self.psi, self.abei, self.ab)
 
     def magnetic_field(self):
-        return K.magnetic_field(self.g, self.abei, self.ab)
+        return self.K.magnetic_field(self.g, self.abei, self.ab)
 
     def supercurrent_density(self):
-        return K.supercurrent_density(self.g, self.mt, self.psi, self.abei, self.ab)
+        return self.K.supercurrent_density(self.g, self.mt, self.psi, self.abei, self.ab)
 
     def current_density(self):
         if not self.solveA:
             return self.supercurrent_density()
-        return K.current_density(self.g, self.kappa2, self.H, self.abei, self.ab)
+        return self.K.current_density(self.g, self.kappa2, self.H, self.abei, self.ab)
 
     def jacobian_psi(self):
-        return K.free_energy_jacobian_psi(self.g, self.kappa2, self.epsilon, self.epsilon_spatial, self.H,
+        return self.K.free_energy_jacobian_psi(self.g, self.kappa2, self.epsilon, self.epsilon_spatial, self.H,
                                           self.mt, self.psi, self.abei, self.ab)
 
     def jacobian_A(self):
-        return K.free_energy_jacobian_A(self.g, self.kappa2, self.H, self.mt, self.psi, self.abei, self.ab)
+        return self.K.free_energy_jacobian_A(self.g, self.kappa2, self.H, self.mt, self.psi, self.abei, self.ab)
 
     def coef_psi(self, dpsi):
-        return K.free_energy_conjgrad_coef_psi_total(self.g, self.kappa2, self.epsilon, self.epsilon_spatial,
+        return self.K.free_energy_conjgrad_coef_psi_total(self.g, self.kappa2, self.epsilon, self.epsilon_spatial,
                                                      self.H, self.mt, self.psi, dpsi, self.abei, self.ab)
 
     def coef(self, dpsi, dab):
-        return K.free_energy_conjgrad_coef_total(self.g, self.kappa2, self.epsilon, self.epsilon_spatial,
+        return self.K.free_energy_conjgrad_coef_total(self.g, self.kappa2, self.epsilon, self.epsilon_spatial,
                                                  self.H, self.mt, self.psi, dpsi, self.abei, self.ab, dab)
 
     # CG -----------------------------------------------------------------------

@@ -53,7 +53,7 @@ def make_pair(Nx=12, Ny=11, dx=0.5, dy=0.45, kappa=np.inf, sigma=1.0, H=0.1, mas
     return gl, orc
 
 
-def oracle_of(gl, rand_t=1):
+def oracle_of(gl, rand_t=1, kernels=None):
     c = gl.cfg
     psi = flat(gl.vars.order_parameter).astype(np.complex128)
     a, b = gl.vars.vector_potential
@@ -72,7 +72,7 @@ def oracle_of(gl, rand_t=1):
                       stop_psi=float(c.stop_criterion_order_parameter), stop_A=float(c.stop_criterion_vector_potential),
                       rand_t=rand_t, langevin_psi=float(gl.params.order_parameter_Langevin_coefficient),
                       langevin_A=float(gl.params.vector_potential_Langevin_coefficient),
-                      convergence_rtol=c.convergence_rtol, dtype=c.dtype)
+                      convergence_rtol=c.convergence_rtol, dtype=c.dtype, kernels=kernels)
 
 
 def gpu_state(gl):

@@ -279,7 +279,10 @@ def svirl_gpu(x):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SVIRL_REFERENCE", "/root/reference")
+    from oracle.ref_build import reference_root
+    ref = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    if ref is None:
+        raise SystemExit("reference sources not found: pass their directory or set SVIRL_REFERENCE")
     for p in (os.path.join(ROOT, "oracle", "fake_pycuda"), ref):
         sys.path.insert(0, p)
     import warnings

@@ -9,12 +9,13 @@ import sys
 
 import pytest
 
-REF = os.environ.get("SVIRL_REFERENCE", "/root/reference")
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def load_reference():
-    if not os.path.isdir(os.path.join(REF, "svirl")):
+    from oracle.ref_build import reference_root
+    REF = reference_root()
+    if REF is None:
         pytest.skip("reference sources not mounted")
     sys.dont_write_bytecode = True
     shim = os.path.join(ROOT, "oracle", "fake_pycuda")

@@ -5,7 +5,7 @@ FP64 tolerances (relative to the max |value| of the field):
   observables, gradients: 1e-12; line-search coefficients: 1e-11 of max |c|;
   CG with kappa=inf (polyroots line search): energies 1e-10;
   CG with finite kappa: energies 1e-6 (scipy BFGS with tol=1e-8 amplifies
-  1e-16 differences of the coefficients).
+  1e-16 differences of the coefficients into 1e-10..1e-8 changes of the step).
 Vortex lists: bit-exact for the same order parameter.
 """
 import numpy as np
