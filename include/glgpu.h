@@ -230,9 +230,13 @@ int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int
  *     Asynchronous: *energy is written when the stream reaches the kernel.  The
  *     reduction scratch is a static 256 KB device array in the library (held by
  *     every GPU that loads it until exit), so grids are limited to 8,388,608
- *     nodes (larger ones: GLGPU_E_ARG).  The first call on a device looks the
- *     array up (cudaGetSymbolAddress); make that first call before any stream
- *     capture.  All calls share the array: calls that overlap on the GPU race. */
+ *     nodes (larger ones: GLGPU_E_ARG).  Every call outside stream capture looks
+ *     the array up (cudaGetSymbolAddress; a device reset moves it); a call under
+ *     capture uses the address of the last call outside capture, so make the
+ *     first call on a device before any stream capture.  All calls share the
+ *     array: calls that overlap on the GPU race.  The energy uses the scalar
+ *     linear coefficient params->epsilon; a spatially varying one (a handle's
+ *     glgpu_set_linear_coefficient_field) is not supported by this call. */
 int glgpu_free_energy_noalloc(const glgpu_grid* grid, const glgpu_params* params, const void* psi, const void* ab,
                               const void* abei, const uint8_t* mt, double* energy, void* stream);
 

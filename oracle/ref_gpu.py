@@ -358,3 +358,61 @@ class RefKernels:
                  m.mask(mt), m.complex_t(psi), m.complex_t(dpsi), m.opt_real(abei), m.opt_real(ab),
                  m.real_t(dab), C)
         return _f64(m.gsum_v(C, grid, 17) if grid > 1 else C)[:17]
+
+
+def reference_td(dtype, g, psi0, ab, mt, dt, warmup, steps, stop=1e-6, rand_t=1):
+    """The reference's TD time loop at kappa = inf on its own kernels, driven as its
+    host code drives them (``svirl/solvers/td.py:157-200,342-377``): per time step a
+    device copy of psi into the right-hand side, then Jacobi sweeps, each preceded
+    by zeroing the residual word and followed by reading it back (a 4-byte
+    device-to-host copy, which synchronises), until ``1e-4*code < 1`` or 1024 sweeps;
+    psi and psi_next swap after every sweep.  Buffers stay on the device.
+
+    Returns the wall-clock seconds of ``steps`` steps after ``warmup`` untimed ones,
+    the mean sweeps per timed step, and the mean device time of one sweep kernel
+    (CUDA events around the timed steps' kernels)."""
+    import time
+    dt_ = np.dtype(dtype).type
+    stop = max(float(stop), 1e-6 if dt_ is np.float32 else 1e-12)  # td.py:52-66
+    m = RefModule.get(dt_, g.Nx, g.Ny, g.dx, g.dy, 5)
+    torch = m.torch
+    psi = m.complex_t(psi0)
+    nxt = m.zeros_complex(g.N)
+    rhs = m.zeros_complex(g.N)
+    abd = m.real_t(ab)
+    mtd = m.mask(mt)
+    r2 = torch.zeros(1, dtype=torch.int32, device="cuda")
+    grid = (g.N + BLOCK - 1) // BLOCK
+    state = {"psi": psi, "nxt": nxt, "t": rand_t}
+    ev = []
+
+    def step(record):
+        rhs.copy_(state["psi"])
+        n = 0
+        for j in range(1024):
+            r2.zero_()
+            if record:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+            m.launch("iterate_order_parameter_jacobi_step", grid, BLOCK, dt, 1.0, None, mtd, abd, rhs,
+                     state["psi"], state["nxt"], 0.0, j, state["t"], stop, r2)
+            if record:
+                e1.record()
+                ev.append((e0, e1))
+            state["psi"], state["nxt"] = state["nxt"], state["psi"]
+            n += 1
+            if 1.0e-4 * dt_(int(r2.item())) < 1.0:
+                break
+        state["t"] = (state["t"] + 1) & 0xFFFFFFFF
+        return n
+
+    for _ in range(warmup):
+        step(False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sweeps = [step(True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    kms = float(np.mean([a.elapsed_time(b) for a, b in ev])) if ev else 0.0
+    return {"wall_s": wall, "steps": steps, "mean_sweeps": float(np.mean(sweeps)) if sweeps else 0.0,
+            "sweep_kernel_ms": kms, "psi": state["psi"]}

@@ -142,25 +142,36 @@ constexpr int kNoAllocMaxBlocks = (int)(kNoAllocMaxNodes / kThreads);   // 32,76
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxBlocks + 1];  // partials, then the counter
 
 // Device address of g_noalloc_scratch for each device (host code cannot use the
-// symbol itself: on the host it names a stand-in, not device memory).  Filled on
-// the first call made with that device current.
+// symbol itself: on the host it names a stand-in, not device memory).  Looked up
+// again on every call that is not being captured into a graph, so that a device
+// reset (which reloads the module at another address) leaves no stale pointer;
+// a call under stream capture uses the address of the last call outside capture.
 static std::mutex g_noalloc_mutex;
 static double* g_noalloc_addr[256] = {nullptr};
 
-static double* noalloc_scratch(int dev, std::string* why) {
+static double* noalloc_scratch(int dev, cudaStream_t stream, std::string* why) {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (dev < 0 || dev >= 256) {
         *why = "device ordinal out of range";
         return nullptr;
     }
-    if (!g_noalloc_addr[dev]) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(stream, &cs);
+    if (e != cudaSuccess) {
+        *why = std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e);
+        return nullptr;
+    }
+    if (cs == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || p == nullptr) {
             *why = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
             return nullptr;
         }
         g_noalloc_addr[dev] = (double*)p;
+    } else if (!g_noalloc_addr[dev]) {
+        *why = "the first call on a device must come before any stream capture";
+        return nullptr;
     }
     return g_noalloc_addr[dev];
 }
@@ -179,7 +190,7 @@ int free_energy_noalloc(const glgpu_grid* grid, const glgpu_params* p, const voi
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(nullptr, GLGPU_E_CUDA, std::string("glgpu_free_energy_noalloc: ") + cudaGetErrorString(e));
     std::string why;
-    double* scratch = noalloc_scratch(dev, &why);
+    double* scratch = noalloc_scratch(dev, stream, &why);
     if (!scratch) return set_error(nullptr, GLGPU_E_CUDA, "glgpu_free_energy_noalloc: " + why);
     unsigned* counter = (unsigned*)(scratch + kNoAllocMaxBlocks);
     const Geo g = make_geo(grid->Nx, grid->Ny, grid->dx, grid->dy);

@@ -1,8 +1,11 @@
 """The learned warm start end to end on a small problem: relaxed states made by
 the batched device CG, the network trained by the library's kernels (its loss
 must fall), then what it gains: CG iterations from the random start and from
-the prediction to the energy F* of a tight relaxation from the random start
-(a prediction counts only where its CG reaches F*; the numbers are printed)."""
+the prediction to the energy F* of a tight relaxation from the random start.
+A run counts only where its CG reaches F* within 1e-6 (a lower-energy vortex
+state is another minimum and does not count); on the instances where both runs
+count, the median iteration count from the prediction must be below 0.8 of
+that from the random start."""
 import numpy as np
 import pytest
 
@@ -29,6 +32,10 @@ def test_trained_network_gain_is_measured():
         cache.close()
     assert res["reached_random"] >= 8
     assert 0 <= res["reached_warm"] <= res["n"]
+    # the gain: on the instances where the CG reaches F* (within 1e-6, from either
+    # side) from both starts, the prediction needs fewer iterations
+    assert res["reached_both"] >= 4, res
+    assert res["iters_warm_median_both"] < 0.8 * res["iters_random_median_both"], res
     # the throughput comparison counts states by the same criterion on both arms
     assert 0 <= thr["ok"] <= thr["n"] and 0 <= thr["plain"]["ok"] <= thr["plain"]["sample"]
     assert thr["wall_s"] > 0 and thr["plain"]["wall_s"] > 0

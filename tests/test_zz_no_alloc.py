@@ -3,9 +3,10 @@ computed without the library allocating anything (its reduction scratch is a
 static device array).  It exists for callers that cannot let a library call
 cudaMalloc, e.g. a host whose own allocator or fixed pre-sized arena owns all
 device memory.  Checked through the C ABI against the handle-based
-glgpu_free_energy on the same state, on two calls in a row (the shared scratch
-keeps the previous call's contents), in FP64 and FP32, plus the size limit.
-Kept in its own file, collected last."""
+glgpu_free_energy and against the oracle's energy of the same state, on two
+calls in a row (the shared scratch keeps the previous call's contents), in FP64
+and FP32; the second call must leave the device's free memory unchanged; plus
+the size limit.  Kept in its own file, collected last."""
 import ctypes as C
 
 import numpy as np
@@ -13,7 +14,10 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-12  # relative, as the FP64 observable parity tests
+TOL = 1e-12  # relative, against the handle path (the same kernel), as the FP64 observable parity tests
+# relative, against the oracle's FP64 energy of the same stored state: FP64 as the
+# parity tests; FP32 accumulates each node in FP32 (double-float partial sums)
+ORACLE_TOL = {np.float64: 1e-12, np.float32: 1e-5}
 
 
 def _state(dtype):
@@ -48,8 +52,16 @@ def test_noalloc_free_energy_matches_handle_path(dtype):
     assert psi.dtype == tdt
     grid = _lib.Grid(int(gl.cfg.Nx), int(gl.cfg.Ny), float(gl.cfg.dx), float(gl.cfg.dy), 8 if dtype == np.float64 else 4)
     params = h.get_params()
-    for _ in range(2):
+    # the oracle's energy of the same state (FP64 arithmetic on the stored values)
+    from oracle import kernels_np as K
+    g = K.Grid(int(gl.cfg.Nx), int(gl.cfg.Ny), float(gl.cfg.dx), float(gl.cfg.dy))
+    E_orc = K.free_energy(g, float(params.kappa) ** 2, float(params.epsilon), None, float(params.H),
+                          np.reshape(gl.mesh.material_tiling.T, -1), h.get_psi().astype(np.complex128),
+                          abei.cpu().numpy().astype(np.float64), h.get_ab().astype(np.float64))
+    free_after_first = None
+    for call in range(2):
         out.fill_(float("nan"))
+        torch.cuda.synchronize()
         rc = lib.glgpu_free_energy_noalloc(C.byref(grid), C.byref(params), C.c_void_p(psi.data_ptr()),
                                            C.c_void_p(ab.data_ptr()), C.c_void_p(abei.data_ptr()),
                                            C.c_void_p(mt.data_ptr()), C.c_void_p(out.data_ptr()), None)
@@ -57,6 +69,12 @@ def test_noalloc_free_energy_matches_handle_path(dtype):
         torch.cuda.synchronize()
         E = float(out.item())
         assert abs(E - ref) <= TOL * abs(ref), (E, ref)
+        assert abs(E - E_orc) <= ORACLE_TOL[dtype] * abs(E_orc), (E, E_orc)
+        if call == 0:
+            # the first call may load the kernel's code (lazy module loading);
+            # from then on the call takes no device memory
+            free_after_first = torch.cuda.mem_get_info()[0]
+    assert torch.cuda.mem_get_info()[0] == free_after_first
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch():
