@@ -90,6 +90,11 @@ int glgpu_psi_strip_rows(const glgpu_handle* h);
 /* Force the strip height (one of the compiled heights; 0 = the model's choice).
  * Results do not depend on it: every node gets the same arithmetic. */
 int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows);
+/* The FP32 psi sweep kernel: 0 (default) = the register-strip kernel (the FP64
+ * build always uses it); 1 = inputs staged in shared memory by bulk copies
+ * (TMA), four strips per CTA, measured slower on GB300 (172 against 89 us per
+ * launch on the 2049^2 workload).  Both compute the same values bitwise. */
+int glgpu_set_psi_sweep_kernel(glgpu_handle* h, int32_t select);
 
 /* --- fixed vortices (svirl/vars/fixed_vortices.py, svirl/solvers/td.py:120-154,
  *     204-216, 252-325): the irregular vector potential A_irr (Nab values, flat

@@ -49,6 +49,7 @@ _SIGNATURES = {
     "glgpu_psi_sweeps_per_launch": (C.c_int, []),
     "glgpu_psi_strip_rows": (C.c_int, [_H]),
     "glgpu_set_psi_strip_rows": (C.c_int, [_H, C.c_int32]),
+    "glgpu_set_psi_sweep_kernel": (C.c_int, [_H, C.c_int32]),
     "glgpu_set_irregular_vector_potential": (C.c_int, [_H, _P, C.c_int32]),
     "glgpu_get_irregular_vector_potential": (C.c_int, [_H, _P]),
     "glgpu_set_phase_lock": (C.c_int, [_H, _P, C.c_int32]),
@@ -263,6 +264,10 @@ class Handle:
 
     def set_psi_strip_rows(self, rows):
         check(self.lib.glgpu_set_psi_strip_rows(self.h, int(rows)), self.h, "set_psi_strip_rows")
+
+    def set_psi_sweep_kernel(self, select):
+        """FP32 psi sweep kernel: 0 = register strip (default), 1 = bulk-copy ring."""
+        check(self.lib.glgpu_set_psi_sweep_kernel(self.h, int(select)), self.h, "set_psi_sweep_kernel")
 
     def set_use_graphs(self, enable):
         check(self.lib.glgpu_set_use_graphs(self.h, 1 if enable else 0), self.h, "set_use_graphs")

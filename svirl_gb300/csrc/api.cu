@@ -75,7 +75,7 @@ void upload_inst(glgpu_handle* h) {
     }
     I.tile0 = 0;
     I.ntiles = h->ntiles;
-    I.nitems = h->nitems;
+    I.nitems = strip_items(h->g.Nx, h->g.Ny, h->strip_rows);  // strips (the table also has empty items)
     I.solveA = finite_kappa(h->p) ? 1 : 0;
     I.fepsilon = (float)I.epsilon;
     I.fkappa2 = (float)I.kappa2;
@@ -156,11 +156,13 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     h->ntiles = blocks_for(h->g.N);
     const int nblk = blocks_for(h->g.N);
     bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
-    for (int q = 0; q < kPsiBufs && ok; ++q) ok = cudaMalloc(&h->psi[q], npsi) == cudaSuccess;
+    // 64 bytes of slack after psi and the code table: the FP32 sweep copies whole
+    // 16-byte units, which can reach up to 15 bytes past a row's last node
+    for (int q = 0; q < kPsiBufs && ok; ++q) ok = cudaMalloc(&h->psi[q], npsi + 64) == cudaSuccess;
     for (int q = 0; q < 3 && ok; ++q) ok = cudaMalloc(&h->ab[q], nab) == cudaSuccess;
     // link factors: Nab complex for the CG, one (x link, y link) pair per node for the TD step
     ok = ok && cudaMalloc(&h->U, std::max((size_t)h->g.Nab * 2, (size_t)h->g.N * 4) * rs) == cudaSuccess;
-    ok = ok && cudaMalloc(&h->code, (size_t)h->g.N) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->code, (size_t)h->g.N + 64) == cudaSuccess;
     if (h->dtype == 8) ok = ok && cudaMalloc(&h->dinv, (size_t)h->g.N * rs) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->st_gather, sizeof(InstState)) == cudaSuccess;
@@ -170,7 +172,7 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
         const Geo* gp = &h->g;
         h->strip_rows = choose_strip_rows(h->dtype, &gp, 1);
     }
-    h->nitems = strip_items(h->g.Nx, h->g.Ny, h->strip_rows);
+    h->nitems = strip_table_len(h->g.Nx, h->g.Ny, h->strip_rows);
     ok = ok && cudaMalloc(&h->items, sizeof(Item) * (size_t)h->nitems) == cudaSuccess;
     ok = ok && cudaMalloc(&h->loop, sizeof(LoopState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->partials, sizeof(double) * 17 * (size_t)nblk) == cudaSuccess;
@@ -188,7 +190,7 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     std::vector<Tile> tiles(h->ntiles);
     for (int k = 0; k < h->ntiles; ++k) tiles[k] = Tile{0, k * kThreads};
     const std::vector<Item> items = make_items(h->g, 0, h->strip_rows);
-    h->psi_grid = psi_sweep_grid(h->dtype, h->strip_rows, h->nitems);
+    h->psi_grid = psi_sweep_grid(psi_kind(h->dtype, h->psi_select), h->strip_rows, h->nitems);
     InstState st;
     memset(&st, 0, sizeof(st));
     st.rand_t = h->p.rand_t;
@@ -332,6 +334,19 @@ static void drop_td_graphs(glgpu_handle* h) {
         }
 }
 
+int glgpu_set_psi_sweep_kernel(glgpu_handle* h, int32_t select) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    if (select < 0 || select > 1) return set_error(h, GLGPU_E_ARG, "set_psi_sweep_kernel: select is 0 or 1");
+    cudaSetDevice(h->device);
+    if (select == h->psi_select) return GLGPU_OK;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "set_psi_sweep_kernel");
+    h->psi_select = select;
+    h->psi_grid = psi_sweep_grid(psi_kind(h->dtype, h->psi_select), h->strip_rows, h->nitems);
+    drop_td_graphs(h);  // the TD graphs hold the kernel and its grid
+    return GLGPU_OK;
+}
+
 int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows) {
     if (check_handle(h)) return GLGPU_E_ARG;
     cudaSetDevice(h->device);
@@ -356,7 +371,7 @@ int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows) {
     h->items = buf;
     h->strip_rows = rows;
     h->nitems = (int)items.size();
-    h->psi_grid = psi_sweep_grid(h->dtype, rows, h->nitems);
+    h->psi_grid = psi_sweep_grid(psi_kind(h->dtype, h->psi_select), rows, h->nitems);
     drop_td_graphs(h);  // the TD graphs hold the old kernel, grid and table
     upload_inst(h);
     return cuda_check(h, cudaStreamSynchronize(h->stream), "set_psi_strip_rows");
@@ -523,12 +538,12 @@ int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** ou
     for (int q = 0; q < n; ++q) {
         for (int k = 0; k < handles[q]->ntiles; ++k) tiles.push_back(Tile{q, k * kThreads});
         const std::vector<Item> it = make_items(handles[q]->g, q, b->strip_rows);
-        b->inst_items[q] = (int)it.size();
+        b->inst_items[q] = strip_items(handles[q]->g.Nx, handles[q]->g.Ny, b->strip_rows);
         items.insert(items.end(), it.begin(), it.end());
     }
     b->ntiles = (int)tiles.size();
     b->nitems = (int)items.size();
-    b->psi_grid = psi_sweep_grid(b->dtype, b->strip_rows, b->nitems);
+    b->psi_grid = psi_sweep_grid(psi_kind(b->dtype, 0), b->strip_rows, b->nitems);
     b->gather_h.resize(n);
     bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && cudaMalloc(&b->insts, sizeof(Inst) * (size_t)n) == cudaSuccess;

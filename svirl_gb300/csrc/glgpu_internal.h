@@ -109,6 +109,7 @@ struct LoopState {
 };
 
 constexpr int kErrLoopGuard = 1;
+constexpr int kErrCopyWait = 2;  // a wait for a bulk copy into shared memory ran out (psi sweep)
 
 // A tile = 256 consecutive nodes of one instance.
 struct Tile {
@@ -130,8 +131,17 @@ constexpr int kStripCols = 32 - 2 * kFuse;
 inline int strip_items(int Nx, int Ny, int rows) {
     return ((Nx + kStripCols - 1) / kStripCols) * ((Ny + rows - 1) / rows);
 }
+// The FP32 sweep runs kPsiGroup adjacent strips of one row band per CTA (they
+// share one ring of rows in shared memory), so the item table lists each band's
+// strips in groups of kPsiGroup, the last group of a band padded with empty
+// items (inst = -1).  strip_table_len: entries of one instance's table.
+constexpr int kPsiGroup = 4;
+inline int strip_table_len(int Nx, int Ny, int rows) {
+    const int nstrips = (Nx + kStripCols - 1) / kStripCols;
+    return (nstrips + kPsiGroup - 1) / kPsiGroup * kPsiGroup * ((Ny + rows - 1) / rows);
+}
 struct Item {
-    int inst, x0, j0, pad;
+    int inst, x0, j0, pad;  // inst = -1: an empty item (group padding)
 };
 
 }  // namespace glgpu
@@ -187,6 +197,7 @@ struct glgpu_handle {
     bool td_graph_failed = false;
     bool use_graphs = true;
     int loop_guard = 0;                 // Jacobi loop guard in sweep launches (0: kLoopGuard)
+    int psi_select = 0;                 // psi sweep kernel (psi_kind)
     std::string last_error;
     void* flush = nullptr;              // L2 flush buffer for kernel timing
     // host pinned staging for small results
@@ -237,7 +248,11 @@ size_t real_size(const glgpu_handle* h);
 int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, double* elapsed_ms);
 int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms);
 int choose_strip_rows(int dtype, const Geo* const* geos, int n);
-int psi_sweep_grid(int dtype, int rows, int nitems);
+// psi sweep kernel of a dtype and a selection (0: register strip, the default;
+// 1: FP32 bulk-copy ring): 8 = FP64 register strip, 4 = FP32 register strip,
+// 5 = FP32 bulk-copy ring
+inline int psi_kind(int dtype, int select) { return dtype == 8 ? 8 : (select == 1 ? 5 : 4); }
+int psi_sweep_grid(int kind, int rows, int nitems);
 std::vector<Item> make_items(const Geo& g, int inst, int rows);
 // obs.cu
 int obs_free_energy(glgpu_handle* h, double* out);

@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include "glgpu_bulk.cuh"
 #include "glgpu_internal.h"
 
 namespace glgpu {
@@ -283,6 +284,7 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
     uint32_t rt = 0;
     for (int it = gw; it < nitems; it += nw) {
         const Item w = items[it];
+        if (w.inst < 0) continue;  // group padding
         if (w.inst != cur_inst) {
             if (cur_inst >= 0 && !done) warp_flush<T>(insts, cur_inst, k, wmax, wnan, count, loop);
             cur_inst = w.inst;
@@ -429,6 +431,241 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
         ++count;
     }
     if (cur_inst >= 0 && !done) warp_flush<T>(insts, cur_inst, k, wmax, wnan, count, loop);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned gdone = atomicAdd(&loop->blocks_done, 1u);
+        if (gdone == gridDim.x - 1u) finish_launch(loop, cond, use_cond);
+    }
+}
+
+// FP32 psi sweep with the inputs staged by bulk copies (TMA).  The same three
+// fused Jacobi sweeps per launch and the same register walk down a strip as
+// k_psi_sweep, bitwise the same values, but the rows a warp reads come from a
+// ring of shared-memory stages filled by the copy engine several rows ahead,
+// so the warps do not wait on global-memory latency.  A CTA runs kPsiGroup
+// adjacent strips of one row band (one group of the item table); one thread
+// (thread 0) copies, per row of the band, the group's columns x0 - 3 ..
+// x0_last + 28 of psi^(k), of the right-hand side, of the link table and of the
+// link-weight codes into the next free stage, each as one cp.async.bulk from the
+// 16-byte boundary at or below the row segment (the arrays' row pitch, 8 Nx
+// bytes, is not a multiple of 16 for odd Nx, so tensor maps cannot describe
+// them).  Per stage a "full" mbarrier (the copies' bytes) and an "empty" one
+// (one arrival per warp when the warp has read the stage).  Every wait is
+// bounded; a wait that runs out sets kErrCopyWait in the loop state (the host
+// reports it) and the CTA stops waiting.
+constexpr int kBulkStages = 8, kBulkAhead = 5;  // ring depth, rows copied ahead of the one being used
+static_assert(kBulkStages >= kBulkAhead + 3, "a stage is reused only after every warp released it");
+constexpr int kBulkCols = kPsiGroup * kStripCols + 2 * kFuse;      // columns of a group's row
+constexpr int kBulkPsiBytes = ((kBulkCols + 1) * 8 + 15) / 16 * 16;  // psi or rhs: one extra node of alignment
+constexpr int kBulkUBytes = kBulkCols * 16;                         // (x link, y link) per node
+constexpr int kBulkCodeBytes = (kBulkCols + 30) / 16 * 16;          // up to 15 bytes of alignment
+constexpr int kBulkOffRhs = kBulkPsiBytes, kBulkOffU = 2 * kBulkPsiBytes, kBulkOffCode = kBulkOffU + kBulkUBytes;
+constexpr int kBulkStageBytes = kBulkOffCode + kBulkCodeBytes;
+constexpr int kBulkThreads = kPsiGroup * 32;
+constexpr int kBulkSpins = 1 << 20;
+static_assert(kBulkStageBytes % 16 == 0 && kBulkOffU % 16 == 0 && kBulkOffCode % 16 == 0, "stage layout");
+
+#ifndef GLGPU_BULK_MIN_CTAS
+#define GLGPU_BULK_MIN_CTAS 4
+#endif
+template <int RR>
+__global__ void __launch_bounds__(kBulkThreads, GLGPU_BULK_MIN_CTAS)
+k_psi_sweep_bulk(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
+                 cudaGraphConditionalHandle cond, int use_cond) {
+    using T = float;
+    constexpr int K = kFuse, S = RR + 2 * kFuse, L = S + 1;  // row steps / rows copied per item
+    __shared__ __align__(128) unsigned char ring[kBulkStages * kBulkStageBytes];
+    __shared__ __align__(8) uint64_t full[kBulkStages], empty[kBulkStages];
+    __shared__ int broken;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const bool leader = threadIdx.x == 0;
+    if (leader) {
+        for (int q = 0; q < kBulkStages; ++q) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], kPsiGroup);
+        }
+        broken = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto wait_bar = [&](uint64_t* bar, unsigned parity) {
+        if (*(volatile int*)&broken) return;
+        if (!mbar_wait(bar, parity, kBulkSpins)) {
+            atomicOr(&loop->err, kErrCopyWait);
+            *(volatile int*)&broken = 1;
+        }
+    };
+    const int ngroups = nitems / kPsiGroup;
+    uint32_t qb = 0;      // row copies of this CTA so far (the same count in every thread)
+    uint32_t issued = 0;  // row copies issued (thread 0)
+    int cur_inst = -1, k = 0, count = 0;
+    T wmax[K];
+    bool wnan[K];
+#pragma unroll
+    for (int l = 0; l < K; ++l) {
+        wmax[l] = T(0);
+        wnan[l] = false;
+    }
+    C2<T>* outb[K];
+    uint32_t rt = 0;
+    for (int gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
+        const Item w0 = items[gi * kPsiGroup];
+        const Item w = items[gi * kPsiGroup + wid];
+        int last = 0;
+#pragma unroll
+        for (int t = 1; t < kPsiGroup; ++t)
+            if (items[gi * kPsiGroup + t].inst >= 0) last = t;
+        const int xl = items[gi * kPsiGroup + last].x0;
+        const Inst& I = insts[w0.inst];
+        const InstState* st = I.st;
+        if (*(volatile const int*)&st->done) continue;  // this instance's loop has stopped
+        const int kg = *(volatile const int*)&st->sweep;
+        const int R = *(volatile const int*)&st->rhs;
+        const Geo g = I.g;
+        const int Nx = g.Nx, Ny = g.Ny;
+        const C2<T>* cur = (const C2<T>*)I.psi[pbuf(R, kg)];
+        const C2<T>* rhs = (const C2<T>*)I.psi[R];
+        const float4* U = (const float4*)I.U;
+        const uint8_t* code = I.code;
+        const int ca = max(w0.x0 - K, 0), cb = min(xl + kStripCols + K - 1, Nx - 1);  // the group's columns
+        const int j0 = w0.j0;
+        // copy row r (0..L-1) of this item, row y = j0 - K - 1 + r, into the stage of copy number q
+        auto issue = [&](uint32_t q, int r) {
+            const int sidx = (int)(q % kBulkStages);
+            if (q >= (uint32_t)kBulkStages) wait_bar(&empty[sidx], ((q / kBulkStages) + 1u) & 1u);
+            const int y = j0 - K - 1 + r;
+            unsigned char* stg = ring + sidx * kBulkStageBytes;
+            if (y < 0 || y >= Ny) {
+                mbar_arrive(&full[sidx]);  // nothing to copy: the readers use zeros outside the domain
+                return;
+            }
+            const long long e0 = (long long)ca + (long long)Nx * y, e1 = (long long)cb + (long long)Nx * y;
+            const long long p0 = e0 & ~1LL, p1 = (e1 + 2) & ~1LL;   // psi, rhs: 16-byte units
+            const long long c0 = e0 & ~15LL, c1 = (e1 + 16) & ~15LL;  // codes: 16-byte units
+            const unsigned pb = (unsigned)(p1 - p0) * 8u, ub = (unsigned)(e1 - e0 + 1) * 16u, cbts = (unsigned)(c1 - c0);
+            mbar_arrive_expect_tx(&full[sidx], 2u * pb + ub + cbts);
+            bulk_g2s(stg, cur + p0, pb, &full[sidx]);
+            bulk_g2s(stg + kBulkOffRhs, rhs + p0, pb, &full[sidx]);
+            bulk_g2s(stg + kBulkOffU, U + e0, ub, &full[sidx]);
+            bulk_g2s(stg + kBulkOffCode, code + c0, cbts, &full[sidx]);
+        };
+        if (leader)
+            for (int r = 0; r <= kBulkAhead && r < L; ++r) issue(issued++, r);
+        const bool real = w.inst >= 0;
+        if (real && w.inst != cur_inst) {
+            if (cur_inst >= 0) warp_flush<T>(insts, cur_inst, k, wmax, wnan, count, loop);
+            cur_inst = w.inst;
+            k = kg;
+            rt = *(volatile const uint32_t*)&st->rand_t;
+#pragma unroll
+            for (int l = 0; l < K; ++l) {
+                outb[l] = (C2<T>*)I.psi[pbuf(R, k + 1 + l)];
+                wmax[l] = T(0);
+                wnan[l] = false;
+            }
+            count = 0;
+        }
+        const T* eps_sp = (const T*)I.eps_sp;
+        const T dt = I.fdt, eps0 = I.fepsilon;
+        const T idx2 = GT(g, idx2), idy2 = GT(g, idy2);
+        const bool lang = I.lang_psi_on != 0;
+        const T lc = I.flang_psi;
+        const int i = w.x0 - K + lane;
+        const bool in_x = real && i >= 0 && i < Nx;
+        const bool calc_lane = in_x && lane >= 1 && lane <= 30;
+        const bool own_lane = in_x && lane >= K && lane <= 31 - K;
+        const int jw = w.j0;
+        const int rel = i - ca;
+        const C2<T> z = cmk<T>(T(0), T(0));
+        auto psi_at = [&](const unsigned char* stg, int y) -> C2<T> {
+            return (in_x && y >= 0 && y < Ny) ? ((const float2*)stg)[rel + ((ca + Nx * y) & 1)] : z;
+        };
+        auto side_at = [&](const unsigned char* stg, int y) -> PsiSide<T> {
+            PsiSide<T> q;
+            const bool row = y >= 0 && y < Ny;
+            const bool ld = in_x && row, ldc = calc_lane && row;
+            if (ld) {
+                const float4 v = ((const float4*)(stg + kBulkOffU))[rel];
+                q.ua = cmk<T>(v.x, v.y);
+                q.ub = cmk<T>(v.z, v.w);
+            } else {
+                q.ua = q.ub = z;
+            }
+            q.cd = ldc ? (unsigned)stg[kBulkOffCode + rel + ((ca + Nx * y) & 15)] : 0u;
+            q.rr = ldc ? ((const float2*)(stg + kBulkOffRhs))[rel + ((ca + Nx * y) & 1)] : z;
+            q.eps = (ldc && eps_sp) ? __ldg(&eps_sp[i + Nx * y]) : eps0;
+            return q;
+        };
+        auto finish_side = [&](const PsiSide<T>& q, int y) -> PsiRow<T> {
+            PsiRow<T> r;
+            r.ua = q.ua;
+            r.ub = q.ub;
+            r.cd = q.cd;
+            r.rq = q.rr;
+            if (lang && calc_lane && y >= 0 && y < Ny) {
+                const uint32_t n = (uint32_t)(i + Nx * y);
+                r.rq.x += lc * (rand_1<T>(n, rt) - T(0.5));
+                r.rq.y += lc * (rand_2<T>(n, rt) - T(0.5));
+            }
+            r.inv = (q.cd & 3u) ? psi_diag_inv<T>(r.rq, q.eps, q.cd, dt, idx2, idy2) : T(0);
+            return r;
+        };
+        auto stage = [&](uint32_t q) -> const unsigned char* { return ring + (int)(q % kBulkStages) * kBulkStageBytes; };
+        auto parity = [&](uint32_t q) -> unsigned { return (q / kBulkStages) & 1u; };
+        auto release = [&](uint32_t q) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[q % kBulkStages]);
+        };
+        C2<T> wp[K], wc[K];
+        PsiRow<T> D[K + 1];
+#pragma unroll
+        for (int l = 0; l < K; ++l) wp[l] = wc[l] = z;
+#pragma unroll
+        for (int m = 0; m <= K; ++m) D[m] = PsiRow<T>{z, z, z, T(0), 0u};
+        wait_bar(&full[qb % kBulkStages], parity(qb));
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            if (leader && s + kBulkAhead + 1 < L) issue(issued++, s + kBulkAhead + 1);
+            wait_bar(&full[(qb + s + 1) % kBulkStages], parity(qb + s + 1));
+            C2<T> newrow = psi_at(stage(qb + s + 1), jw - K + s);  // psi^(k) on row jw - K + s
+            const PsiSide<T> sd = side_at(stage(qb + s), jw - K + s - 1);
+            release(qb + s);
+#pragma unroll
+            for (int m = K; m >= 1; --m) D[m] = D[m - 1];
+            D[0] = finish_side(sd, jw - K + s - 1);
+#pragma unroll
+            for (int l = 1; l <= K; ++l) {
+                C2<T> out = z;
+                if (s >= 2 * l) {
+                    const int y = jw - K + s - l;
+                    const C2<T> pc = wc[l - 1];
+                    const C2<T> pl = shfl_up_c<T>(pc, 1), pr = shfl_down_c<T>(pc, 1);
+                    const PsiRow<T>& d = D[l - 1];
+                    const C2<T> ual = shfl_up_c<T>(d.ua, 1);
+                    out = psi_node<T>(pl, pr, wp[l - 1], newrow, ual, d.ua, D[l].ub, d.ub, d.rq, d.inv, d.cd);
+                    if (own_lane && y >= jw && y < jw + RR && y < Ny) {
+                        outb[l - 1][i + Nx * y] = out;
+                        const T dr = fabs(out.x - pc.x), di = fabs(out.y - pc.y);
+                        if (isnan(dr) | isnan(di)) wnan[l - 1] = true;
+                        wmax[l - 1] = fmax(wmax[l - 1], fmax(dr, di));
+                    }
+                }
+                wp[l - 1] = wc[l - 1];
+                wc[l - 1] = newrow;
+                newrow = out;
+            }
+        }
+        release(qb + S);
+        qb += L;
+        if (real) ++count;
+    }
+    if (cur_inst >= 0) warp_flush<T>(insts, cur_inst, k, wmax, wnan, count, loop);
+    // every copy issued was waited for; after a wait that ran out, give the
+    // copies still in flight a bounded time to land before the CTA exits
+    if (leader && *(volatile int*)&broken)
+        for (uint32_t q = issued > (uint32_t)kBulkStages ? issued - kBulkStages : 0u; q < issued; ++q)
+            mbar_wait(&full[q % kBulkStages], (q / kBulkStages) & 1u, kBulkSpins);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -713,7 +950,7 @@ struct TDLaunch {
     const Tile* tiles;
     const Item* items;
     LoopState* loop;
-    int ninst, ntiles, nitems, psi_grid, dtype, strip_rows;
+    int ninst, ntiles, nitems, psi_grid, dtype, strip_rows, psi_kind;
     bool any_solveA;
     bool any_fv;  // an instance has fixed vortices (irregular potential or phase lock)
 };
@@ -722,25 +959,31 @@ static void* fv_psi_pre_fn(int dt) { return dt == 8 ? (void*)k_fv_psi_pre<double
 static void* fv_psi_post_fn(int dt) { return dt == 8 ? (void*)k_fv_psi_post<double> : (void*)k_fv_psi_post<float>; }
 static void* fv_A_fn(int dt) { return dt == 8 ? (void*)k_fv_A<double> : (void*)k_fv_A<float>; }
 
+// The psi sweep kernel of a kind (psi_kind): FP64 and FP32 register strip (the
+// default), FP32 bulk-copy ring (selected per handle).
+static bool psi_bulk(int kind) { return kind == 5; }
 template <int V>
-static void* psi_sweep_fn_v(int dtype, int rows) {
+static void* psi_sweep_fn_v(int kind, int rows) {
     if constexpr (V < kNumStripRows) {
         constexpr int R = kStripRowsSet[V];
-        if (rows == R) return dtype == 8 ? (void*)k_psi_sweep<double, R> : (void*)k_psi_sweep<float, R>;
-        return psi_sweep_fn_v<V + 1>(dtype, rows);
+        if (rows == R)
+            return kind == 8 ? (void*)k_psi_sweep<double, R>
+                             : (kind == 5 ? (void*)k_psi_sweep_bulk<R> : (void*)k_psi_sweep<float, R>);
+        return psi_sweep_fn_v<V + 1>(kind, rows);
     } else {
         return nullptr;
     }
 }
-// the sweep kernel compiled for strip height `rows` (one of kStripRowsSet)
-static void* psi_sweep_fn(int dtype, int rows) { return psi_sweep_fn_v<0>(dtype, rows); }
+// the sweep kernel compiled for strip height `rows` (one of kStripRowsSet), and its CTA size
+static void* psi_sweep_fn(int kind, int rows) { return psi_sweep_fn_v<0>(kind, rows); }
+static int psi_threads(int kind) { return psi_bulk(kind) ? kBulkThreads : kPsiThreads; }
 
-static cudaError_t launch_psi_sweep(int dtype, int rows, int grid, cudaStream_t s, const Inst* insts, const Item* items,
+static cudaError_t launch_psi_sweep(int kind, int rows, int grid, cudaStream_t s, const Inst* insts, const Item* items,
                                     int nitems, LoopState* loop) {
     cudaGraphConditionalHandle none = 0;
     int zero = 0;
     void* a[] = {&insts, &items, &nitems, &loop, &none, &zero};
-    return cudaLaunchKernel(psi_sweep_fn(dtype, rows), dim3(grid), dim3(kPsiThreads), a, 0, s);
+    return cudaLaunchKernel(psi_sweep_fn(kind, rows), dim3(grid), dim3(psi_threads(kind)), a, 0, s);
 }
 static void* A_sweep_fn(int dtype) {
     return dtype == 8 ? (void*)k_A_sweep<double> : (void*)k_A_sweep<float>;
@@ -837,8 +1080,8 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         {
             cudaGraphNode_t sw;
             void* a[] = {&insts, &items, &nitems, &loop, &hpsi, &one};
-            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.dtype, L.strip_rows), dim3(L.psi_grid),
-                            dim3(kPsiThreads), a));
+            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.psi_kind, L.strip_rows), dim3(L.psi_grid),
+                            dim3(psi_threads(L.psi_kind)), a));
         }
         {
             void* a[] = {&insts, &ninst, &zero};
@@ -933,7 +1176,7 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
             for (;;) {
                 for (int c = 0; c < chunk; ++c) {
                     if (part == 0) {
-                        launch_psi_sweep(L.dtype, L.strip_rows, L.psi_grid, s, L.insts, L.items, L.nitems, L.loop);
+                        launch_psi_sweep(L.psi_kind, L.strip_rows, L.psi_grid, s, L.insts, L.items, L.nitems, L.loop);
                     } else {
                         if (L.dtype == 8) k_A_sweep<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
                         else k_A_sweep<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
@@ -1019,7 +1262,8 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
         k_bench_prep<<<1, 32, 0, h->stream>>>(h->inst, 1, h->loop, 1);
         cudaEventRecord(e0, h->stream);
         if (which == 0) {
-            launch_psi_sweep(h->dtype, h->strip_rows, h->psi_grid, h->stream, h->inst, h->items, h->nitems, h->loop);
+            launch_psi_sweep(psi_kind(h->dtype, h->psi_select), h->strip_rows, h->psi_grid, h->stream, h->inst, h->items,
+                             h->nitems, h->loop);
         } else {
             if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
             else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
@@ -1034,20 +1278,27 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     cudaEventDestroy(e1);
     // leave the loop state as a finished loop; the state at rest (buffer 0) was not written
     k_canonical_reset<<<1, 32, 0, h->stream>>>(h->inst, 1);
+    LoopState hl;
+    memset(&hl, 0, sizeof(hl));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hl, h->loop, sizeof(hl), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_check(h, e, "time_sweeps");
+    if (hl.err & kErrCopyWait) return set_error(h, GLGPU_E_TIMEOUT, "time_sweeps: psi sweep: a bulk-copy wait ran out");
     *avg_ms = total / nrep;
     return GLGPU_OK;
 }
 
-// CTAs of the persistent psi sweep: one warp per item, up to all SMs at full occupancy.
-int psi_sweep_grid(int dtype, int rows, int nitems) {
+// CTAs of the persistent psi sweep (nitems: length of the item table): one warp
+// per item (register-strip kernel) or one CTA per group of kPsiGroup items
+// (bulk-copy kernel), up to all SMs at full occupancy.
+int psi_sweep_grid(int kind, int rows, int nitems) {
     int dev = 0, sms = 1, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void* fn = psi_sweep_fn(dtype, rows);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPsiThreads, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
-    const int need = (nitems + kPsiWarps - 1) / kPsiWarps;
+    void* fn = psi_sweep_fn(kind, rows);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, psi_threads(kind), 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const int need = psi_bulk(kind) ? nitems / kPsiGroup : (nitems + kPsiWarps - 1) / kPsiWarps;
     const int full = sms * per_sm;
     return need < full ? (need > 0 ? need : 1) : full;
 }
@@ -1063,10 +1314,14 @@ int choose_strip_rows(int dtype, const Geo* const* geos, int n) {
     long long best_cost = -1;
     for (int v = 0; v < kNumStripRows; ++v) {
         const int R = kStripRowsSet[v];
-        long long items = 0;
-        for (int q = 0; q < n; ++q) items += strip_items(geos[q]->Nx, geos[q]->Ny, R);
-        const long long warps = (long long)psi_sweep_grid(dtype, R, (int)items) * kPsiWarps;
-        const long long cost = (items + warps - 1) / warps * (3LL * R + 2LL * kFuse);
+        long long table = 0;
+        for (int q = 0; q < n; ++q) table += strip_table_len(geos[q]->Nx, geos[q]->Ny, R);
+        // work units: groups of kPsiGroup items per CTA (bulk-copy kernel) or items per warp
+        const int kind = psi_kind(dtype, 0);
+        const bool bulk = psi_bulk(kind);
+        const long long units = bulk ? table / kPsiGroup : table;
+        const long long slots = (long long)psi_sweep_grid(kind, R, (int)table) * (bulk ? 1 : kPsiWarps);
+        const long long cost = (units + slots - 1) / slots * (3LL * R + 2LL * kFuse);
         if (best_cost < 0 || cost < best_cost) {
             best_cost = cost;
             best = R;
@@ -1075,13 +1330,16 @@ int choose_strip_rows(int dtype, const Geo* const* geos, int n) {
     return best;
 }
 
-// Items of one instance, row-block major (concurrently running warps share halo rows in L2).
+// Items of one instance, row-block major (concurrently running warps share halo
+// rows in L2); each band's strips padded to a multiple of kPsiGroup with empty items.
 std::vector<Item> make_items(const Geo& g, int inst, int rows) {
     std::vector<Item> items;
     const int nstrips = (g.Nx + kStripCols - 1) / kStripCols, nrows = (g.Ny + rows - 1) / rows;
-    items.reserve((size_t)nstrips * nrows);
+    const int padded = (nstrips + kPsiGroup - 1) / kPsiGroup * kPsiGroup;
+    items.reserve((size_t)padded * nrows);
     for (int r = 0; r < nrows; ++r)
-        for (int s = 0; s < nstrips; ++s) items.push_back(Item{inst, kStripCols * s, rows * r, 0});
+        for (int s = 0; s < padded; ++s)
+            items.push_back(s < nstrips ? Item{inst, kStripCols * s, rows * r, 0} : Item{-1, 0, 0, 0});
     return items;
 }
 
@@ -1181,6 +1439,7 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     L.insts = h->inst; L.tiles = h->tiles; L.items = h->items; L.loop = h->loop;
     L.ninst = 1; L.ntiles = h->ntiles; L.nitems = h->nitems; L.psi_grid = h->psi_grid; L.dtype = h->dtype;
     L.strip_rows = h->strip_rows;
+    L.psi_kind = psi_kind(h->dtype, h->psi_select);
     L.any_solveA = h->inst_h.solveA != 0;
     L.any_fv = h->vpi != nullptr || h->lock_n > 0;
     InstState hs;
@@ -1192,6 +1451,7 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     h->p.rand_t = hs.rand_t;
     fill_stats(stats, &hs, 1, o);
     if (o.loop_err & kErrLoopGuard) return set_error(h, GLGPU_E_TIMEOUT, "td: Jacobi loop guard reached");
+    if (o.loop_err & kErrCopyWait) return set_error(h, GLGPU_E_TIMEOUT, "td: psi sweep: a bulk-copy wait ran out");
     if (hs.nan_seen) return set_error(h, GLGPU_E_NAN, "td: NaN residual (the state was updated as the reference does)");
     return GLGPU_OK;
 }
@@ -1216,6 +1476,7 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
     L.insts = b->insts; L.tiles = b->tiles; L.items = b->items; L.loop = b->loop;
     L.ninst = b->ninst; L.ntiles = b->ntiles; L.nitems = b->nitems; L.psi_grid = b->psi_grid; L.dtype = b->dtype;
     L.strip_rows = b->strip_rows;
+    L.psi_kind = psi_kind(b->dtype, 0);
     L.any_solveA = any_solveA;
     L.any_fv = any_fv;
     TDOutcome o = td_core(b->stream, L, Nt, eqn, b->td_exec, &b->td_graph_failed, b->use_graphs, b->loop_guard,
@@ -1230,6 +1491,7 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
     }
     fill_stats(stats, b->gather_h.data(), b->ninst, o);
     if (o.loop_err & kErrLoopGuard) return batch_error(b, GLGPU_E_TIMEOUT, "batch_td: Jacobi loop guard reached");
+    if (o.loop_err & kErrCopyWait) return batch_error(b, GLGPU_E_TIMEOUT, "batch_td: psi sweep: a bulk-copy wait ran out");
     if (nan) return batch_error(b, GLGPU_E_NAN, "batch_td: NaN residual in at least one instance");
     return GLGPU_OK;
 }
