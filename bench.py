@@ -70,23 +70,39 @@ def make_solver(n_side=N_SIDE, dtype=np.float32, seed=0, device=0):
     return gl
 
 
+def fp32_errors(g32, g64):
+    """Every result of a solver pair that ran the same steps in FP32 and FP64:
+    max |x32 - x64| and max |x64| of psi, A, the magnetic field B, the current
+    density j and the supercurrent density js, and the relative free-energy
+    difference."""
+    def pair(get):
+        a, b = get(g32), get(g64)
+        a = np.concatenate([np.ravel(x) for x in a]) if isinstance(a, tuple) else np.ravel(a)
+        b = np.concatenate([np.ravel(x) for x in b]) if isinstance(b, tuple) else np.ravel(b)
+        return {"max_abs_err": float(np.max(np.abs(a.astype(b.dtype) - b))), "max_abs": float(np.max(np.abs(b)))}
+    out = {"psi": pair(lambda g: g.vars.order_parameter), "A": pair(lambda g: g.vars.vector_potential),
+           "B": pair(lambda g: g.observables.magnetic_field), "j": pair(lambda g: g.observables.current_density),
+           "js": pair(lambda g: g.observables.supercurrent_density)}
+    f32, f64 = float(g32.observables.free_energy), float(g64.observables.free_energy)
+    out["F"] = {"rel_err": abs(f32 - f64) / abs(f64), "F64": f64}
+    return out
+
+
 def precision_check(n_side, steps=20, seed=0):
     """FP32 against FP64 on the same workload: the same initial state (the FP64
-    state rounded to FP32), `steps` TD steps each; max |psi32 - psi64| and the
-    relative free-energy difference after them."""
+    state rounded to FP32), `steps` TD steps each; the errors of every result
+    after them (fp32_errors), plus the summary keys of earlier lines."""
     g32 = make_solver(n_side, np.float32, seed=seed)
     g64 = make_solver(n_side, np.float64, seed=seed)
     try:
         g32.solve.td(dt=DT, Nt=steps)
         g64.solve.td(dt=DT, Nt=steps)
-        p32 = np.asarray(g32.vars.order_parameter).astype(np.complex128)
-        p64 = np.asarray(g64.vars.order_parameter)
-        f32, f64 = float(g32.observables.free_energy), float(g64.observables.free_energy)
+        err = fp32_errors(g32, g64)
     finally:
         g32.close()
         g64.close()
-    return {"steps": steps, "max_abs_dpsi": float(np.max(np.abs(p32 - p64))),
-            "max_abs_psi": float(np.max(np.abs(p64))), "rel_dF": abs(f32 - f64) / abs(f64)}
+    return {"steps": steps, "max_abs_dpsi": err["psi"]["max_abs_err"], "max_abs_psi": err["psi"]["max_abs"],
+            "rel_dF": err["F"]["rel_err"], "per_result": err}
 
 
 def make_oracle(n_side, seed=0):
@@ -384,10 +400,25 @@ def run_c1(args):
     from svirl_gb300 import GLSolver
     if int(os.environ.get("RANK", "0")) != 0:
         return
-    gl = GLSolver(dx=0.5, dy=0.5, Lx=64, Ly=64, order_parameter="random", random_seed=0, gl_parameter=5.0,
-                  normal_conductivity=200.0, homogeneous_external_field=0.1, dtype=np.float64)
-    ya = gl.mesh.xy_a_grid[1]
-    gl.vars.vector_potential = (-0.1 * ya, np.zeros((129, 128)))
+
+    def c1_solver(dtype):
+        g = GLSolver(dx=0.5, dy=0.5, Lx=64, Ly=64, order_parameter="random", random_seed=0, gl_parameter=5.0,
+                     normal_conductivity=200.0, homogeneous_external_field=0.1, dtype=dtype)
+        ya = g.mesh.xy_a_grid[1]
+        g.vars.vector_potential = ((-0.1 * ya).astype(dtype), np.zeros((129, 128), dtype=dtype))
+        return g
+
+    # FP32 against FP64 from the same start after the same TD steps and CG (untimed)
+    g32, g64 = c1_solver(np.float32), c1_solver(np.float64)
+    g32.solve.td(dt=0.1, Nt=args.steps)
+    g64.solve.td(dt=0.1, Nt=args.steps)
+    prec = {"after_td_steps": args.steps, "td": fp32_errors(g32, g64)}
+    g32.solve.cg(n_iter=200)
+    g64.solve.cg(n_iter=200)
+    prec["after_cg_200"] = fp32_errors(g32, g64)
+    g32.close()
+    g64.close()
+    gl = c1_solver(np.float64)
     gl.solve.td(dt=0.1, Nt=5)  # warm-up: graph build
     st, ms = gl._h.td_timed(0.1, args.steps, 0)
     t0 = time.perf_counter()
@@ -418,6 +449,7 @@ def run_c1(args):
                        "mean_sweeps_A": st.total_sweeps_A / args.steps},
             "cg": {"iterations": n_cg, "wall_s": t_cg, "ms_per_iteration": 1e3 * t_cg / max(n_cg, 1),
                    "how": "GLSolver.solve.cg(n_iter=1000): GPU phases, step length on the host (reference decisions)"},
+            "fp32_vs_fp64": prec,
             "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
 
@@ -557,11 +589,11 @@ def main():
     ap.add_argument("--workload", choices=["tdgl", "states", "serve", "learned", "c1", "conv"], default="tdgl",
                     help="tdgl: node-steps/s on the 2049^2 domain; states: relaxed states/s of a batched sweep; "
                          "serve: the serving loop; learned: the learned CG warm start")
-    ap.add_argument("--train-states", type=int, default=2048)
+    ap.add_argument("--train-states", type=int, default=20000)
     ap.add_argument("--epochs", type=int, default=10)
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
-    ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--cg-iters", type=int, default=12000)
     ap.add_argument("--gtol", type=float, default=1e-4)
     ap.add_argument("--plain-sample", type=int, default=8)
@@ -601,6 +633,9 @@ def main():
     dtype = np.float32 if args.dtype == "fp32" else np.float64
     gl = make_solver(args.size, dtype=dtype, seed=rank, device=local)
     h = gl._h
+    # the psi sweep's launch shape: measured (or read from the tuning cache)
+    from svirl_gb300 import autotune
+    tuned = autotune.tune(h)
     if args.no_graphs:
         h.set_use_graphs(False)
     N = args.size * args.size
@@ -676,10 +711,15 @@ def main():
                        "parallelism": "replica per GPU" if world > 1 else "single GPU",
                        "l2": "working set %.0f MB > 129 MB L2 (no flush between steps); sweep timing flushes L2"
                              % (N * (3 * (8 if dtype == np.float32 else 16) + (8 if dtype == np.float32 else 16)) / 1e6),
-                       "mean_sweeps_per_step": sweeps / args.steps},
+                       "mean_sweeps_per_step": sweeps / args.steps,
+                       "psi_sweep_shape": {"kernel": ["register strip", "bulk-copy ring"][tuned["kernel"]],
+                                           "strip_rows": tuned["rows"], "from_cache": tuned["cached"],
+                                           "measured_us": tuned["measured"]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": ncu_traffic(args.dtype, fuse, rows),
-                         "kernel": "k_psi_sweep", "sweeps_per_launch": fuse, "strip_rows": rows,
+                         "frac": achieved / peak,
+                         "traffic": ncu_traffic(args.dtype, fuse, rows) if tuned["kernel"] == 0 else None,
+                         "kernel": "k_psi_sweep" if tuned["kernel"] == 0 else "k_psi_sweep_bulk",
+                         "sweeps_per_launch": fuse, "strip_rows": rows,
                          "bytes_per_node_sweep": bytes_per_node_sweep, "bytes_per_launch": alg_bytes,
                          "launch_ms": sweep_ms, "peak_kind": peak_kind},
             "e2e": {"value": e2e_value, "unit": "node-steps/s",

@@ -205,6 +205,10 @@ class Handle:
         check(self.lib.glgpu_get_params(self.h, C.byref(p)), self.h, "get_params")
         return p
 
+    def kappa_finite(self):
+        k = float(self.get_params().kappa)
+        return k > 0.0 and np.isfinite(k)
+
     def set_params(self, **kw):
         p = self.get_params()
         for k, v in kw.items():

@@ -43,7 +43,7 @@ struct InstState {
     int last_sweeps_psi, last_sweeps_A, max_sweeps_psi, max_sweeps_A;
     long long total_sweeps_psi, total_sweeps_A;
     int steps;                // time steps done in the current call
-    int pad_;
+    int commitA;              // FP32 A loop: 1 + the buffer of A^(0) to add to the final offsets (0: none)
 };
 
 // Device-resident state of one instance in the batched device CG.

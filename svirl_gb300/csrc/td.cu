@@ -60,6 +60,8 @@ __device__ void finish_instance_A(const Inst& I, LoopState* loop, int k) {
     st->blocks_done = 0u;
     if (conv || s >= kMaxSweeps) {
         st->done = 1;
+        // FP32: the buffers hold offsets from A^(0) (k_A_sweep); k_A_commit adds A^(0)
+        if (sizeof(T) == 4) st->commitA = 1 + st->rhsA;
         st->rhsA = buf_of(st->rhsA, s);
         st->last_sweeps_A = s;
         st->total_sweeps_A += s;
@@ -248,21 +250,33 @@ template <typename T> struct PsiRow {
 #ifndef GLGPU_PSI_THREADS
 #define GLGPU_PSI_THREADS 64
 #endif
-#ifndef GLGPU_PSI_MIN_CTAS
-#define GLGPU_PSI_MIN_CTAS 1
+// CTAs per SM the register allocation must allow: FP32 at 8 (128 registers a
+// thread, 16 warps per SM), FP64 at 1 (its sweep needs about 190 registers)
+#ifndef GLGPU_PSI_MIN_CTAS_F32
+#define GLGPU_PSI_MIN_CTAS_F32 8
+#endif
+#ifndef GLGPU_PSI_MIN_CTAS_F64
+#define GLGPU_PSI_MIN_CTAS_F64 1
 #endif
 // Row steps of the strip walk unrolled together (0: the whole walk).
 #ifndef GLGPU_PSI_ROW_UNROLL
 #define GLGPU_PSI_ROW_UNROLL 0
 #endif
 
+// Rows of inputs loaded ahead of their use in the register-strip sweep: FP32 2
+// (measured on 2049^2: 75 us per launch against 88 with 1 row; 3 rows: 76-77 us),
+// FP64 1 (register bound).
+#ifndef GLGPU_PSI_PREFETCH_F32
+#define GLGPU_PSI_PREFETCH_F32 2
+#endif
+template <typename T> constexpr int kPFof = sizeof(T) == 4 ? GLGPU_PSI_PREFETCH_F32 : 1;
 constexpr int kPsiThreads = GLGPU_PSI_THREADS, kPsiWarps = kPsiThreads / 32;
 template <typename T> constexpr bool kStoreInv = sizeof(T) == 8;
 template <typename T, int RR>
-__global__ void __launch_bounds__(kPsiThreads, GLGPU_PSI_MIN_CTAS)
+__global__ void __launch_bounds__(kPsiThreads, sizeof(T) == 4 ? GLGPU_PSI_MIN_CTAS_F32 : GLGPU_PSI_MIN_CTAS_F64)
 k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int nitems, LoopState* loop,
             cudaGraphConditionalHandle cond, int use_cond) {
-    constexpr int K = kFuse, S = RR + 2 * kFuse;
+    constexpr int K = kFuse, S = RR + 2 * kFuse, kPF = kPFof<T>;
     constexpr int kRowUnroll = GLGPU_PSI_ROW_UNROLL > 0 ? GLGPU_PSI_ROW_UNROLL : S;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * kPsiWarps + (threadIdx.x >> 5), nw = gridDim.x * kPsiWarps;
@@ -373,17 +387,24 @@ k_psi_sweep(const Inst* __restrict__ insts, const Item* __restrict__ items, int 
             }
             return r;
         };
-        C2<T> nx_p = load_psi(j0 - K);
-        PsiSide<T> nx_s = load_side(j0 - K - 1);
+        // the rows' loads are issued kPF row steps ahead of their use (a ring of
+        // kPF rows in registers; the walk is unrolled, so the indexing is static)
+        C2<T> nx_p[kPF];
+        PsiSide<T> nx_s[kPF];
+#pragma unroll
+        for (int a = 0; a < kPF; ++a) {
+            nx_p[a] = load_psi(j0 - K + a);
+            nx_s[a] = load_side(j0 - K - 1 + a);
+        }
 #pragma unroll kRowUnroll
         for (int s = 0; s < S; ++s) {
-            C2<T> newrow = nx_p;  // psi^(k) on row j0 - K + s
+            C2<T> newrow = nx_p[s % kPF];  // psi^(k) on row j0 - K + s
 #pragma unroll
             for (int m = K; m >= 1; --m) D[m] = D[m - 1];
-            D[0] = finish_side(nx_s, j0 - K + s - 1);
-            if (s + 1 < S) {
-                nx_p = load_psi(j0 - K + s + 1);
-                nx_s = load_side(j0 - K + s);
+            D[0] = finish_side(nx_s[s % kPF], j0 - K + s - 1);
+            if (s + kPF < S) {
+                nx_p[s % kPF] = load_psi(j0 - K + s + kPF);
+                nx_s[s % kPF] = load_side(j0 - K - 1 + s + kPF);
             }
 #pragma unroll
             for (int l = 1; l <= K; ++l) {
@@ -624,7 +645,9 @@ k_psi_sweep_bulk(const Inst* __restrict__ insts, const Item* __restrict__ items,
 #pragma unroll
         for (int m = 0; m <= K; ++m) D[m] = PsiRow<T>{z, z, z, T(0), 0u};
         wait_bar(&full[qb % kBulkStages], parity(qb));
-#pragma unroll
+        // rolled: the stage index is dynamic anyway, and an unrolled walk with the
+        // copy issue inlined in every step overflowed the instruction cache
+#pragma unroll 1
         for (int s = 0; s < S; ++s) {
             if (leader && s + kBulkAhead + 1 < L) issue(issued++, s + kBulkAhead + 1);
             wait_bar(&full[(qb + s + 1) % kBulkStages], parity(qb + s + 1));
@@ -696,7 +719,10 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
     __syncthreads();
     if (!s_skip) {
         const int k = s_k, R = s_R;
-        const T* cur = (const T*)I.ab[buf_of(R, k)];
+        // FP32: the iterates are offsets delta = A - A^(0) from the loop's right-hand
+        // side (see the delta branch below); delta^(0) = 0
+        constexpr bool kDelta = sizeof(T) == 4;
+        const T* cur = (kDelta && k == 0) ? nullptr : (const T*)I.ab[buf_of(R, k)];
         const T* rhs = (const T*)I.ab[R];
         // with fixed vortices the supercurrent phases come from the irregular
         // potential buffer, which holds A_irr + A^(0) on its first N elements
@@ -708,11 +734,96 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
         const int n = t.n0 + tid;
         T res = T(0);
         bool nan = false;
+        T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
+        bool has_a = false, has_b = false;
+        int na = 0, nb = 0;
+        if constexpr (kDelta) {
+            // The same Jacobi iteration as the FP64 branch, written for delta: with
+            // A^(k) = A^(0) + delta^(k) the update of a link is
+            //   delta' = (noise + dt rho (js + rh) + dt rho k2 (dd nbs(A^(0)) - 2 d^-2 A^(0))
+            //            + dt rho k2 dd nbs(delta^(k))) / D,
+            // and the stop rule's |A^(k+1) - A^(k)| = |delta^(k+1) - delta^(k)|.  In FP32 the
+            // iterates of A itself differ by whole units in the last place once |A| > 8
+            // (the Landau gauge reaches H L), which the absolute stop rule of 1e-6
+            // (svirl/solvers/td.py:53-57) never accepts; delta is small, so the loop
+            // converges.  The supercurrent phase is that of A^(0) + delta^(2 floor(k/2)).
+            if (n < g.N) {
+                const int i = n % g.Nx, j = n / g.Nx;
+                const int Nxa = g.Nx - 1, Na = g.Na;
+                has_a = i < g.Nx - 1;
+                has_b = j < g.Ny - 1;
+                na = i + Nxa * j;
+                nb = Na + i + g.Nx * j;
+                const T* al = (I.vpi || k < 2) ? nullptr : (const T*)I.ab[(R + 2) % 3];  // delta of the phase
+                auto dl = [&](int m) -> T { return cur ? cur[m] : T(0); };
+                // read the phases before anything is stored (aliasing)
+                const T ph_a = has_a ? (I.vpi ? abi[na] : rhs[na] + (al ? al[na] : T(0))) : T(0);
+                const T ph_b = has_b ? (I.vpi ? abi[nb] : rhs[nb] + (al ? al[nb] : T(0))) : T(0);
+                const unsigned cb = cell_bits(g, I.mt, i, j);
+                const C2<T> psi0 = psi[n];
+                const T dx = GT(g, dx), dy = GT(g, dy);
+                const T idx = GT(g, idx), idy = GT(g, idy);
+                const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
+                const T k2 = I.fkappa2, H = I.fH;
+                const T dt_rho = I.fdt * I.frho;
+                const T dt_rho_k2 = dt_rho * k2;
+                const T lc = I.flang_A;
+                const bool lang = I.lang_A_on != 0;
+                if (has_a) {
+                    const T r0 = rhs[na];
+                    const T noise = lang ? lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5)) : T(0);
+                    T rh = T(0), dd = T(1);
+                    if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
+                    else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
+                    T jl = T(0);
+                    if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
+                    T nr = T(0), nd = T(0);
+                    if (j > 0) {
+                        const int m0 = i + Nxa * (j - 1), m1 = Na + i + g.Nx * (j - 1), m2 = Na + i + 1 + g.Nx * (j - 1);
+                        nr += idy2 * rhs[m0] - idxy * rhs[m1] + idxy * rhs[m2];
+                        nd += idy2 * dl(m0) - idxy * dl(m1) + idxy * dl(m2);
+                    }
+                    if (j < g.Ny - 1) {
+                        const int m0 = i + Nxa * (j + 1), m1 = Na + i + g.Nx * j, m2 = Na + i + 1 + g.Nx * j;
+                        nr += idy2 * rhs[m0] + idxy * rhs[m1] - idxy * rhs[m2];
+                        nd += idy2 * dl(m0) + idxy * dl(m1) - idxy * dl(m2);
+                    }
+                    va = (noise + dt_rho * (jl + rh) + dt_rho_k2 * (dd * nr - T(2) * idy2 * r0) + dt_rho_k2 * dd * nd) /
+                         (T(1) + T(2) * dt_rho_k2 * idy2);
+                    ca = dl(na);
+                }
+                if (has_b) {
+                    const T r0 = rhs[nb];
+                    const T noise = lang ? lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5)) : T(0);
+                    T rh = T(0), dd = T(1);
+                    if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
+                    else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
+                    T jl = T(0);
+                    if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
+                    T nr = T(0), nd = T(0);
+                    if (i > 0) {
+                        const int m0 = Na + (i - 1) + g.Nx * j, m1 = (i - 1) + Nxa * j, m2 = (i - 1) + Nxa * (j + 1);
+                        nr += idx2 * rhs[m0] - idxy * rhs[m1] + idxy * rhs[m2];
+                        nd += idx2 * dl(m0) - idxy * dl(m1) + idxy * dl(m2);
+                    }
+                    if (i < g.Nx - 1) {
+                        const int m0 = Na + (i + 1) + g.Nx * j, m1 = i + Nxa * j, m2 = i + Nxa * (j + 1);
+                        nr += idx2 * rhs[m0] + idxy * rhs[m1] - idxy * rhs[m2];
+                        nd += idx2 * dl(m0) + idxy * dl(m1) - idxy * dl(m2);
+                    }
+                    vb = (noise + dt_rho * (jl + rh) + dt_rho_k2 * (dd * nr - T(2) * idx2 * r0) + dt_rho_k2 * dd * nd) /
+                         (T(1) + T(2) * dt_rho_k2 * idx2);
+                    cbv = dl(nb);
+                }
+            }
+        } else
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
             const int Nxa = g.Nx - 1, Na = g.Na;
-            const bool has_a = i < g.Nx - 1, has_b = j < g.Ny - 1;
-            const int na = i + Nxa * j, nb = Na + i + g.Nx * j;
+            has_a = i < g.Nx - 1;
+            has_b = j < g.Ny - 1;
+            na = i + Nxa * j;
+            nb = Na + i + g.Nx * j;
             // read the supercurrent phases before anything is stored (aliasing, see top)
             const T ph_a = has_a ? abi[na] : T(0);
             const T ph_b = has_b ? abi[nb] : T(0);
@@ -726,7 +837,6 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
             const T dt_rho_k2 = dt_rho * k2;
             const T lc = gsel<T>(I.lang_A, I.flang_A);
             const bool lang = I.lang_A_on != 0;
-            T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
             if (has_a) {
                 T r = rhs[na];
                 if (lang) r += lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5));
@@ -755,6 +865,8 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
                 vb = (r + dt_rho * (jl + rh) + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idx2);
                 cbv = cur[nb];
             }
+        }
+        if (n < g.N) {
             if (has_a) {
                 nxt[na] = va;
                 T d = fabs(va - ca);
@@ -882,6 +994,7 @@ __global__ void k_loop_begin(const Inst* __restrict__ insts, int ninst, LoopStat
         const bool part = which == 0 || insts[q].solveA;
         st->sweep = 0;
         st->done = part ? 0 : 1;
+        if (which == 1) st->commitA = 0;
         st->blocks_done = 0u;
         st->res = 0ull;
         for (int l = 0; l < 4; ++l) st->resp[l] = 0ull;
@@ -899,10 +1012,36 @@ __global__ void k_loop_begin(const Inst* __restrict__ insts, int ninst, LoopStat
 }
 
 // End of a Jacobi loop: advance the Langevin seed of the instances that ran it
-// (td.py:204,313).
+// (td.py:204,313); after an A loop no commit is pending any more.
 __global__ void k_loop_end(const Inst* __restrict__ insts, int ninst, int which) {
-    for (int q = threadIdx.x; q < ninst; q += blockDim.x)
+    for (int q = threadIdx.x; q < ninst; q += blockDim.x) {
         if (which == 0 || insts[q].solveA) insts[q].st->rand_t += 1u;
+        if (which == 1) insts[q].st->commitA = 0;
+    }
+}
+
+// After an FP32 A loop: the state buffer holds the offsets delta = A - A^(0) of
+// the loop's last sweep (k_A_sweep); A = A^(0) + delta, in place.  A loop that
+// stopped on the guard leaves no commit pending and the state at A^(0).
+__global__ void __launch_bounds__(kThreads) k_A_commit(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    const int c = *(volatile const int*)&I.st->commitA;
+    if (c == 0) return;
+    const Geo g = I.g;
+    const int n = t.n0 + threadIdx.x;
+    if (n >= g.N) return;
+    const float* base = (const float*)I.ab[c - 1];
+    float* A = (float*)I.ab[*(volatile const int*)&I.st->rhsA];
+    const int i = n % g.Nx, j = n / g.Nx;
+    if (i < g.Nx - 1) {
+        const int na = i + (g.Nx - 1) * j;
+        A[na] = base[na] + A[na];
+    }
+    if (j < g.Ny - 1) {
+        const int nb = g.Na + i + g.Nx * j;
+        A[nb] = base[nb] + A[nb];
+    }
 }
 
 // End of a time step: count it and decide whether the time loop goes on.
@@ -938,6 +1077,7 @@ __global__ void k_canonical_reset(const Inst* __restrict__ insts, int ninst) {
     for (int q = threadIdx.x; q < ninst; q += blockDim.x) {
         insts[q].st->rhs = 0;
         insts[q].st->rhsA = 0;
+        insts[q].st->commitA = 0;
     }
 }
 
@@ -1109,6 +1249,10 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
             void* a[] = {&insts, &tiles, &loop, &hA, &one};
             GCHK(add_kernel(abody, &sw, nullptr, 0, A_sweep_fn(L.dtype), gt, bt, a));
         }
+        if (L.dtype == 4) {
+            void* a[] = {&insts, &tiles};
+            GCHK(chain(obody, (void*)k_A_commit, gt, bt, a));
+        }
         {
             void* a[] = {&insts, &ninst, &one};
             GCHK(chain(obody, (void*)k_loop_end, g1, b1, a));
@@ -1188,6 +1332,7 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
                 if (e != cudaSuccess) return e;
                 if (!cont) break;
             }
+            if (part == 1 && L.dtype == 4) k_A_commit<<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
             k_loop_end<<<1, 32, 0, s>>>(L.insts, L.ninst, part);
             if (part == 0 && L.any_fv) fv_psi(true);
             if (part == 1 && L.any_fv) fv_A(1);
