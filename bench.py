@@ -59,12 +59,14 @@ def holes_mask(n_side, dx, radius, frac, seed):
     return mt
 
 
-def make_solver(n_side=N_SIDE, dtype=np.float32, seed=0, device=0):
+def make_solver(n_side=N_SIDE, dtype=np.float32, seed=0, device=0, kappa=np.inf):
+    """The workload's solver; a finite `kappa` (normal conductivity 200) adds the
+    vector-potential equation (used to profile the A sweep on the same domain)."""
     from svirl_gb300 import GLSolver
     mt = holes_mask(n_side, DX, HOLE_R, HOLE_FRAC, seed)
     gl = GLSolver(Nx=n_side, Ny=n_side, dx=DX, dy=DX, order_parameter="random", random_seed=seed,
-                  gl_parameter=np.inf, homogeneous_external_field=H_FIELD, material_tiling=mt,
-                  dtype=dtype, device_id=device)
+                  gl_parameter=kappa, normal_conductivity=200.0, homogeneous_external_field=H_FIELD,
+                  material_tiling=mt, dtype=dtype, device_id=device)
     ya = gl.mesh.xy_a_grid[1]
     gl.vars.vector_potential = ((-H_FIELD * ya).astype(dtype), np.zeros((n_side, n_side - 1), dtype=dtype))
     return gl
@@ -499,6 +501,9 @@ def run_conv(args):
     bd = lambda: lib.glnn_conv3x3_bwd_data(P(dy), P(y), 1, P(wt), P(dx), cin, None, 0, n, h, w, cout, P(err), s)
     bw = lambda: lib.glnn_conv3x3_bwd_weight(P(dy), P(y), 1, P(x), cin, None, 0, P(dw), P(db), P(work), nwork, n, h, w,
                                             cout, s)
+    lib.glnn_set_conv_tma(0)
+    ms_f_gather = timed(f, args.steps)
+    lib.glnn_set_conv_tma(1)
     ms_f, ms_d, ms_w = timed(f, args.steps), timed(bd, args.steps), timed(bw, args.steps)
     assert int(err.item()) == 0
     peak = 1922.0
@@ -506,13 +511,16 @@ def run_conv(args):
     if os.path.exists(pth):
         peak = float(json.load(open(pth))["bf16_tflops"])
     tf = flop / (ms_f * 1e-3) / 1e12
-    line = {"metric": "3x3 conv TFLOP/s (tcgen05 forward, 32x128x128x64->64, bf16 in, fp32 accumulate)", "value": tf,
+    line = {"metric": "3x3 conv TFLOP/s (tcgen05 forward with TMA operands, 32x128x128x64->64, bf16 in, fp32 accumulate)",
+            "value": tf,
             "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": 3, "ms_per_step": ms_f,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
             "data": "synthetic (seeded)",
             "config": {"workload": "conv3x3_layer", "n": n, "h": h, "w": w, "cin": cin, "cout": cout},
             "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
                          "peak_kind": "measured bf16 burst"},
+            "forward_gather": {"ms": ms_f_gather, "tflops": flop / (ms_f_gather * 1e-3) / 1e12,
+                               "kernel": "tcgen05, operands gathered by the threads"},
             "data_grad": {"ms": ms_d, "tflops": flop / (ms_d * 1e-3) / 1e12, "kernel": "tcgen05"},
             "weight_grad": {"ms": ms_w, "tflops": flop / (ms_w * 1e-3) / 1e12, "kernel": "mma.sync"}}
     print(json.dumps(line), flush=True)
@@ -565,8 +573,9 @@ def run_learned(args):
                        "params": net.n_params(), "levels": list(L.LEVELS), "target_mode": "amplitude",
                        "train_loss_first_last": [hist[0], hist[-1]], "gen_s": t_gen, "train_s": t_train,
                        "cg_cap": args.learned_cap, "gtol_abs": args.gtol,
-                       "criterion": "|F - F*|/|F*| <= 1e-6, F* = FP64 relaxation from the random start (gradient "
-                                    "norm 1e-7, 20000 iterations)"},
+                       "criterion": "|F - F*|/|F*| <= 1e-6, F* = FP64 relaxation (gradient norm 1e-7, 20000 "
+                                    "iterations) of the same instance from the same initial state: the random start "
+                                    "(plain arm), the prediction (learned arm)"},
             "speedup_vs_plain": t["speedup_vs_plain"], "throughput": thr, "eval": evals,
             "e2e": {"value": t["states_per_s"], "unit": "states/s", "h2d_bytes_per_step": nodes * 8 * 2,
                     "d2h_bytes_per_step": nodes * 4 * 4,
@@ -584,6 +593,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, default=N_SIDE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kappa", type=float, default=float("inf"),
+                    help="GL parameter of the TDGL workload (inf: the headline workload; finite: adds the A step)")
+    ap.add_argument("--psi-kernel", type=int, choices=[0, 1], default=None,
+                    help="FP32 psi sweep kernel (0 register strip, 1 bulk-copy ring); default: the autotuner's choice")
     ap.add_argument("--no-graphs", action="store_true",
                     help="host-driven Jacobi loop (same kernels); ncu cannot profile kernels inside conditional graphs")
     ap.add_argument("--workload", choices=["tdgl", "states", "serve", "learned", "c1", "conv"], default="tdgl",
@@ -631,11 +644,17 @@ def main():
         dist.init_process_group("nccl")
 
     dtype = np.float32 if args.dtype == "fp32" else np.float64
-    gl = make_solver(args.size, dtype=dtype, seed=rank, device=local)
+    kinf = not np.isfinite(args.kappa)
+    gl = make_solver(args.size, dtype=dtype, seed=rank, device=local, kappa=args.kappa)
     h = gl._h
-    # the psi sweep's launch shape: measured (or read from the tuning cache)
+    # the psi sweep's launch shape: measured (or read from the tuning cache),
+    # or the kernel forced by --psi-kernel (at the model's strip height)
     from svirl_gb300 import autotune
-    tuned = autotune.tune(h)
+    if args.psi_kernel is None:
+        tuned = autotune.tune(h)
+    else:
+        h.set_psi_sweep_kernel(args.psi_kernel)
+        tuned = {"kernel": args.psi_kernel, "rows": h.psi_strip_rows(), "cached": False, "measured": None}
     if args.no_graphs:
         h.set_use_graphs(False)
     N = args.size * args.size
@@ -670,6 +689,17 @@ def main():
     alg_bytes = N * bytes_per_node_sweep * fuse
     peak, peak_kind = peaks()
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
+    # finite kappa: the A sweep timed alone as well (pairs of sweeps 0 and 1, L2
+    # flushed before each pair); algorithmic bytes per node-sweep: psi, the
+    # right-hand side, the supercurrent argument, A^(k), the write (8 B each in FP32,
+    # 16 B in FP64, two links per node), +1 B mask
+    a_sweep = None
+    if not kinf:
+        a_ms = h.time_sweeps(1, 10)
+        a_bytes = (40 if dtype == np.float32 else 80) + 1
+        a_gbs = N * a_bytes / (a_ms * 1e-3) / 1e9
+        a_sweep = {"kernel": "k_A_sweep", "launch_ms": a_ms, "bytes_per_node_sweep": a_bytes,
+                   "achieved_GBps": a_gbs, "frac": a_gbs / peak}
 
     # end to end through the C ABI with pinned host buffers: H2D psi, one TD step, D2H psi
     import torch
@@ -694,7 +724,7 @@ def main():
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_baseline(sweeps / args.steps)
         prec = None
-        if dtype == np.float32 and not args.no_cpu_baseline:
+        if dtype == np.float32 and not args.no_cpu_baseline and kinf:
             try:  # a side measurement: the bench line prints whatever happens here
                 prec = precision_check(args.size)
             except Exception as e:  # noqa: BLE001
@@ -703,15 +733,18 @@ def main():
         # loop begin/end and step-end kernels, plus the final copy and reset
         launches = int(st.sweep_launches) + 4 * args.steps + 3
         line = {
-            "metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
+            "metric": METRIC if kinf else METRIC.replace("kappa=inf", "kappa=%g" % args.kappa),
+            "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if dtype == np.float32 else "f64", "data": "synthetic (seeded)",
-            "config": {"workload": "tdgl_2049_kinf_holes5", "Nx": args.size, "Ny": args.size, "dx": DX,
-                       "kappa": "inf", "H": H_FIELD, "dt": DT, "hole_radius": HOLE_R, "hole_fraction": HOLE_FRAC,
+            "config": {"workload": "tdgl_2049_kinf_holes5" if kinf else "tdgl_2049_k%g_holes5" % args.kappa,
+                       "Nx": args.size, "Ny": args.size, "dx": DX,
+                       "kappa": "inf" if kinf else args.kappa, "H": H_FIELD, "dt": DT, "hole_radius": HOLE_R, "hole_fraction": HOLE_FRAC,
                        "parallelism": "replica per GPU" if world > 1 else "single GPU",
                        "l2": "working set %.0f MB > 129 MB L2 (no flush between steps); sweep timing flushes L2"
                              % (N * (3 * (8 if dtype == np.float32 else 16) + (8 if dtype == np.float32 else 16)) / 1e6),
                        "mean_sweeps_per_step": sweeps / args.steps,
+                       "mean_A_sweeps_per_step": st.total_sweeps_A / args.steps,
                        "psi_sweep_shape": {"kernel": ["register strip", "bulk-copy ring"][tuned["kernel"]],
                                            "strip_rows": tuned["rows"], "from_cache": tuned["cached"],
                                            "measured_us": tuned["measured"]}},
@@ -730,6 +763,8 @@ def main():
             "cpu_baseline": cpu,
             "fp32_vs_fp64": prec,
         }
+        if a_sweep is not None:
+            line["A_sweep"] = a_sweep
         print(json.dumps(line), flush=True)
     gl.close()
     if dist is not None:

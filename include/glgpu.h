@@ -95,6 +95,16 @@ int glgpu_set_psi_strip_rows(glgpu_handle* h, int32_t rows);
  * (TMA), four strips per CTA, measured slower on GB300 (172 against 89 us per
  * launch on the 2049^2 workload).  Both compute the same values bitwise. */
 int glgpu_set_psi_sweep_kernel(glgpu_handle* h, int32_t select);
+/* Time stepping of the order parameter: 0 (default) = backward Euler, the
+ * reference's scheme (svirl/cuda/td.h:4-133); 1 = Crank-Nicolson of the
+ * reference's commented-out kernel (iterate_order_parameter_jacobi_step_CN,
+ * svirl/cuda/td.h:136-292, which no host code of the reference launches) with
+ * the explicit half of every link from the step's start (the trapezoidal rule);
+ * 2 = that kernel exactly as written (the explicit half of three links from the
+ * current iterate, which counts them twice).  Same Jacobi loop and stop rule
+ * (on the squared change, as the kernel computes it).  Single handles only
+ * (glgpu_batch_td rejects them). */
+int glgpu_set_psi_scheme(glgpu_handle* h, int32_t scheme);
 
 /* --- fixed vortices (svirl/vars/fixed_vortices.py, svirl/solvers/td.py:120-154,
  *     204-216, 252-325): the irregular vector potential A_irr (Nab values, flat
@@ -141,7 +151,9 @@ int glgpu_set_loop_guard(glgpu_handle* h, int32_t launches);
  *     svirl/solvers/cg.py:473,546):
  *   glgpu_td_timed:    glgpu_td, plus the device time of the whole TD run;
  *   glgpu_time_sweeps: average device time of one Jacobi sweep kernel launch
- *                      (which 0 = psi, 1 = A), L2 flushed before each launch;
+ *                      (which 0 = psi; 1 = A, timed as pairs of sweeps 0 and 1,
+ *                      since the second of a pair reuses the first's link terms),
+ *                      L2 flushed before each launch (A: before each pair);
  *                      leaves the state at rest unchanged. */
 int glgpu_td_timed(glgpu_handle* h, double dt, int32_t Nt, int32_t eqn, glgpu_td_stats* stats, double* elapsed_ms);
 int glgpu_time_sweeps(glgpu_handle* h, int32_t which, int32_t nrep, double* avg_ms);

@@ -37,6 +37,12 @@ extern "C" {
 int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
                      void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, int32_t* err, void* stream);
 
+/* Operand loads of glnn_conv3x3_fwd: 1 (default) = by TMA (cp.async.bulk.tensor
+ * from 4-D / 2-D tensor maps, 4-stage pipeline) for the shapes it takes
+ * (c1, c2, cout multiples of 64; w a multiple of 128 or a divisor of 128; h*w a
+ * multiple of 128), the thread gather otherwise; 0 = always the thread gather.
+ * Process-wide. */
+int glnn_set_conv_tma(int32_t enable);
 /* [dx1|dx2] = conv3x3^T(dy * relu'(y), Wt), on tcgen05 like the forward.  y may be
  * NULL when relu = 0. */
 int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const void* wt, void* dx1, int32_t c1,

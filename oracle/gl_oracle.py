@@ -106,6 +106,10 @@ class GLOracle:
         # kernels: a module or object with kernels_np's functions; oracle.ref_gpu.RefKernels
         # runs these host loops on the reference's own compiled kernels instead
         self.K = K if kernels is None else kernels
+        # psi time stepping: "backward_euler" (the reference's), "crank_nicolson" or
+        # "crank_nicolson_as_written" (the reference's commented-out kernel,
+        # td.h:136-292, see kernels_np), with the same host loop
+        self.scheme = "backward_euler"
         self.g = K.Grid(Nx, Ny, dx, dy)
         self.dtype = dtype
         self.psi = np.array(psi, dtype=np.complex128).reshape(-1).copy()
@@ -155,8 +159,13 @@ class GLOracle:
         rhs = self.psi.copy()
         cur = self.psi
         nsw = 0
+        if self.scheme == "backward_euler":
+            sweep = self.K.iterate_order_parameter_jacobi_step
+        else:
+            aw = self.scheme == "crank_nicolson_as_written"
+            sweep = lambda *a: self.K.iterate_order_parameter_jacobi_step_cn(*a, as_written=aw)  # noqa: E731
         for j in range(1024):
-            nxt, code = self.K.iterate_order_parameter_jacobi_step(
+            nxt, code = sweep(
                 g, dt, self.epsilon, self.epsilon_spatial, self.mt, self.ab, rhs, cur,
                 self.langevin_psi, j, self.rand_t, stop)
             cur = nxt

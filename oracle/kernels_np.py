@@ -223,6 +223,71 @@ def iterate_order_parameter_jacobi_step(g, dt, epsilon, epsilon_spatial, mt, ab_
     return nxt.reshape(-1), r2_max
 
 
+def iterate_order_parameter_jacobi_step_cn(g, dt, epsilon, epsilon_spatial, mt, ab_abi,
+                                           psi_rhs, psi, langevin_c, jstep, rand_t, stop_eps, as_written=False):
+    """One Jacobi sweep of the Crank-Nicolson psi step of the reference's
+    commented-out kernel (``svirl/cuda/td.h:136-292``, never launched by
+    ``svirl/solvers/td.py``): c_lhs = c_rhs = 1/2, Du link weights
+    (``td.h:209-212``) with ig = 4 / (sum of the four), the diagonal from
+    |psi_rhs|^2, and the residual code from the SQUARED change
+    ``1e4 (dre^2 + dim^2) / stop`` (``td.h:285-291``).  The explicit part of the
+    links: from psi_rhs on all four (the trapezoidal rule the kernel's variable
+    names describe), or with ``as_written`` from psi_rhs on the left x link only
+    and from psi on the other three, as ``td.h:238-251`` writes it (which counts
+    those neighbours twice: not a Crank-Nicolson step).  Returns
+    ``(psi_next, r2_max)``; ``psi_rhs`` gets the Langevin term in sweep 0 as in the
+    backward-Euler kernel."""
+    Nx, Ny = g.Nx, g.Ny
+    mm, mp, pm, pp = _cells_at_nodes(g, mt)
+    active = mm | mp | pm | pp
+    r_m0, r_p0, r_0m, r_0p, _ = _du_weights(mm, mp, pm, pp)
+    P = g.psi2(psi)
+    rhs = g.psi2(psi_rhs).copy()
+    if jstep == 0 and langevin_c > 1.0e-32:
+        n = np.arange(g.N, dtype=np.uint32).reshape(Ny, Nx)
+        noise = langevin_c * ((rand_1(n, rand_t) - 0.5) + 1j * (rand_2(n, rand_t) - 0.5))
+        rhs = np.where(active, rhs + noise, rhs)
+        psi_rhs[:] = rhs.reshape(-1)
+    a, b = (np.zeros((g.Nya, g.Nxa)), np.zeros((g.Nyb, g.Nxb))) if ab_abi is None else (g.a2(ab_abi), g.b2(ab_abi))
+    z = lambda: np.zeros((Ny, Nx), complex)  # noqa: E731
+    u_m0, u_p0, u_0m, u_0p = z(), z(), z(), z()
+    u_m0[:, 1:] = U(-g.dx * a)
+    u_p0[:, :-1] = U(g.dx * a)
+    u_0m[1:, :] = U(-g.dy * b)
+    u_0p[:-1, :] = U(g.dy * b)
+    nb_m0, nb_p0, nb_0m, nb_0p = z(), z(), z(), z()   # psi at the four neighbours
+    nr_m0, nr_p0, nr_0m, nr_0p = z(), z(), z(), z()   # the explicit part's neighbours
+    Q = P if as_written else rhs
+    nb_m0[:, 1:], nr_m0[:, 1:] = P[:, :-1], rhs[:, :-1]
+    nb_p0[:, :-1], nr_p0[:, :-1] = P[:, 1:], Q[:, 1:]
+    nb_0m[1:, :], nr_0m[1:, :] = P[:-1, :], Q[:-1, :]
+    nb_0p[:-1, :], nr_0p[:-1, :] = P[1:, :], Q[1:, :]
+    on_m0, on_p0, on_0m, on_0p = (mm | mp), (pm | pp), (mm | pm), (mp | pp)
+    rU_m0 = np.where(on_m0, r_m0 * u_m0, 0.0)
+    rU_p0 = np.where(on_p0, r_p0 * u_p0, 0.0)
+    rU_0m = np.where(on_0m, r_0m * u_0m, 0.0)
+    rU_0p = np.where(on_0p, r_0p * u_0p, 0.0)
+    psi_m0, psi_p0, psi_0m, psi_0p = rU_m0 * nb_m0, rU_p0 * nb_p0, rU_0m * nb_0m, rU_0p * nb_0p
+    rhs_m0, rhs_p0, rhs_0m, rhs_0p = rU_m0 * nr_m0, rU_p0 * nr_p0, rU_0m * nr_0m, rU_0p * nr_0p
+    wsum = r_m0 + r_p0 + r_0m + r_0p
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ig = np.where(active, 4.0 / np.where(wsum > 0, wsum, 1.0), 0.0)
+        eps = epsilon if epsilon_spatial is None else g.psi2(epsilon_spatial)
+        c_lhs = c_rhs = 0.5
+        a2 = rhs.real * rhs.real + rhs.imag * rhs.imag
+        lap_w = g.idx2 * (r_m0 + r_p0) + g.idy2 * (r_0m + r_0p)
+        num = (rhs * (1.0 - c_rhs * dt * (a2 - eps))
+               + c_rhs * dt * ig * (g.idx2 * (rhs_m0 + rhs_p0) + g.idy2 * (rhs_0m + rhs_0p) - lap_w * rhs)
+               + c_lhs * dt * ig * (g.idx2 * (psi_m0 + psi_p0) + g.idy2 * (psi_0m + psi_0p)))
+        den = 1.0 + c_lhs * dt * (a2 - eps + ig * lap_w)
+        nxt = num / den
+    nxt = np.where(active, nxt, 0.0)
+    dre, dim = nxt.real - P.real, nxt.imag - P.imag
+    r2 = dre * dre + dim * dim
+    r2_max = int(residual_code(r2, stop_eps).max())
+    return nxt.reshape(-1), r2_max
+
+
 def order_parameter_phase_lock(psi, lock_ns):
     """psi[n] = |psi[n]| at phase-lock nodes (``svirl/cuda/td.h:295-307``)."""
     psi[lock_ns] = np.abs(psi[lock_ns])

@@ -32,6 +32,7 @@ BLOCK = 128
 # argument kinds per kernel: r = real_t, p = pointer (None -> NULL), i = int32, u = uint32
 SIGNATURES = {
     "iterate_order_parameter_jacobi_step": "rrppppppruurp",   # td.h:4-19
+    "iterate_order_parameter_jacobi_step_CN": "rrppppppruurp",  # td.h:136-150 (commented out in the reference)
     "order_parameter_phase_lock": "pip",                        # td.h:295-300
     "iterate_vector_potential_jacobi_step": "rrrrppppppruurp",  # td.h:310-326
     "magnetic_field": "ppp",                                    # observables.h:4-9
@@ -169,7 +170,9 @@ class RefModule:
                 holders.append(ctypes.c_void_p(0 if a is None else a.data_ptr()))
         params = (ctypes.c_void_p * len(holders))(*[ctypes.cast(ctypes.pointer(h), ctypes.c_void_p) for h in holders])
         stream = ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
-        _check(self.lib, self.lib.cuLaunchKernel(self._fn(name), int(grid), 1, 1, int(block), 1, 1, 0, stream,
+        gx, gy = (grid if isinstance(grid, tuple) else (grid, 1))
+        bx, by = (block if isinstance(block, tuple) else (block, 1))
+        _check(self.lib, self.lib.cuLaunchKernel(self._fn(name), int(gx), int(gy), 1, int(bx), int(by), 1, 0, stream,
                                                  params, None), "cuLaunchKernel(%s)" % name)
 
     # device buffers -----------------------------------------------------------
@@ -259,6 +262,27 @@ class RefKernels:
         nxt = m.zeros_complex(g.N)
         r2 = m.torch.zeros(1, dtype=m.torch.int32, device="cuda")
         m.launch("iterate_order_parameter_jacobi_step", self._grid(g.N), BLOCK, dt, epsilon,
+                 m.opt_real(epsilon_spatial), m.mask(mt), m.opt_real(ab_abi), rhs, m.complex_t(psi), nxt,
+                 langevin_c, jstep, rand_t, stop_eps, r2)
+        psi_rhs[:] = _c128(rhs)
+        return _c128(nxt), int(r2.cpu().item())
+
+    def iterate_order_parameter_jacobi_step_cn(self, g, dt, epsilon, epsilon_spatial, mt, ab_abi,
+                                               psi_rhs, psi, langevin_c, jstep, rand_t, stop_eps, as_written=True):
+        """The reference's commented-out Crank-Nicolson kernel (``td.h:136-292``),
+        compiled live by the recipe.  Its threads index (i, j) =
+        (blockIdx.x*blockDim.x + threadIdx.x, blockIdx.y*blockDim.y + threadIdx.y);
+        no host code of the reference launches it, so the launch is 16 x 8 blocks
+        over the node grid.  Only the kernel as written exists in the reference."""
+        if not as_written:
+            raise RefUnavailable("the reference has only the Crank-Nicolson kernel as written")
+        m = self._m(g)
+        if ab_abi is None:  # read without a NULL test (td.h:239-251)
+            ab_abi = np.zeros(g.Nab)
+        rhs = m.complex_t(psi_rhs)
+        nxt = m.zeros_complex(g.N)
+        r2 = m.torch.zeros(1, dtype=m.torch.int32, device="cuda")
+        m.launch("iterate_order_parameter_jacobi_step_CN", ((g.Nx + 15) // 16, (g.Ny + 7) // 8), (16, 8), dt, epsilon,
                  m.opt_real(epsilon_spatial), m.mask(mt), m.opt_real(ab_abi), rhs, m.complex_t(psi), nxt,
                  langevin_c, jstep, rand_t, stop_eps, r2)
         psi_rhs[:] = _c128(rhs)

@@ -50,6 +50,7 @@ _SIGNATURES = {
     "glgpu_psi_strip_rows": (C.c_int, [_H]),
     "glgpu_set_psi_strip_rows": (C.c_int, [_H, C.c_int32]),
     "glgpu_set_psi_sweep_kernel": (C.c_int, [_H, C.c_int32]),
+    "glgpu_set_psi_scheme": (C.c_int, [_H, C.c_int32]),
     "glgpu_set_irregular_vector_potential": (C.c_int, [_H, _P, C.c_int32]),
     "glgpu_get_irregular_vector_potential": (C.c_int, [_H, _P]),
     "glgpu_set_phase_lock": (C.c_int, [_H, _P, C.c_int32]),
@@ -93,6 +94,7 @@ _SIGNATURES = {
     "glgpu_batch_cg": (C.c_int, [_H, C.c_int32, C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     # learned warm start (include/glgpu_nn.h)
+    "glnn_set_conv_tma": (C.c_int, [C.c_int32]),
     "glnn_conv3x3_fwd": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_int32, _P, _P]),
     "glnn_conv3x3_bwd_data": (C.c_int, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32,
@@ -268,6 +270,11 @@ class Handle:
 
     def set_psi_strip_rows(self, rows):
         check(self.lib.glgpu_set_psi_strip_rows(self.h, int(rows)), self.h, "set_psi_strip_rows")
+
+    def set_psi_scheme(self, scheme):
+        """psi time stepping: 0 backward Euler (the reference's), 1 Crank-Nicolson,
+        2 the reference's Crank-Nicolson kernel as written."""
+        check(self.lib.glgpu_set_psi_scheme(self.h, int(scheme)), self.h, "set_psi_scheme")
 
     def set_psi_sweep_kernel(self, select):
         """FP32 psi sweep kernel: 0 = register strip (default), 1 = bulk-copy ring."""

@@ -334,6 +334,18 @@ static void drop_td_graphs(glgpu_handle* h) {
         }
 }
 
+int glgpu_set_psi_scheme(glgpu_handle* h, int32_t scheme) {
+    if (check_handle(h)) return GLGPU_E_ARG;
+    if (scheme < 0 || scheme > 2) return set_error(h, GLGPU_E_ARG, "set_psi_scheme: scheme is 0, 1 or 2");
+    cudaSetDevice(h->device);
+    if (scheme == h->psi_scheme) return GLGPU_OK;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_check(h, e, "set_psi_scheme");
+    h->psi_scheme = scheme;
+    drop_td_graphs(h);  // the TD graphs hold the sweep kernel
+    return GLGPU_OK;
+}
+
 int glgpu_set_psi_sweep_kernel(glgpu_handle* h, int32_t select) {
     if (check_handle(h)) return GLGPU_E_ARG;
     if (select < 0 || select > 1) return set_error(h, GLGPU_E_ARG, "set_psi_sweep_kernel: select is 0 or 1");

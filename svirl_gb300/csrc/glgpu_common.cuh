@@ -48,6 +48,11 @@ template <typename T> __device__ __forceinline__ C2<T> link_U(T ph) {
 }
 
 // Im(conj(psi0) U(ph) psi1) (svirl/cuda/common.h:66-73).
+// a * b rounded once, never fused into a neighbouring add
+__device__ __forceinline__ float mul_rn_t(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn_t(double a, double b) { return __dmul_rn(a, b); }
+template <typename T> __device__ __forceinline__ T mul_rn(T a, T b) { return mul_rn_t(a, b); }
+
 template <typename T> __device__ __forceinline__ T js_of(C2<T> p0, T ph, C2<T> p1) {
     T s, c;
     sincos_t(ph, &s, &c);

@@ -74,7 +74,8 @@ struct Inst {
     const void* abei;         // external+irregular vector potential or NULL
     const uint8_t* mt;        // material tiling (cells) or NULL
     const void* eps_sp;       // spatial linear coefficient (nodes) or NULL
-    void* U;                  // link factors exp(-i d a) of the psi loop, Nab complex
+    void* U;                  // link factors of the psi loop (Nab complex); during the A loop the
+                              // fixed parts of the link updates (k_A_sweep), 2 Nab reals
     uint8_t* code;            // per-node link-weight bits of the psi loop, N bytes
     void* dinv;               // FP64: per-node reciprocal of the psi step's diagonal, N reals (NULL for FP32)
     uint8_t* cbits;           // per-node cell bits (cell_bits) for the batched CG, N bytes (NULL until CG)
@@ -198,6 +199,7 @@ struct glgpu_handle {
     bool use_graphs = true;
     int loop_guard = 0;                 // Jacobi loop guard in sweep launches (0: kLoopGuard)
     int psi_select = 0;                 // psi sweep kernel (psi_kind)
+    int psi_scheme = 0;                 // psi time stepping: 0 backward Euler, 1 Crank-Nicolson, 2 as written
     std::string last_error;
     void* flush = nullptr;              // L2 flush buffer for kernel timing
     // host pinned staging for small results

@@ -14,8 +14,10 @@
 // bias, applies the ReLU and stores bfloat16.  Every wait is bounded; on a
 // timeout the kernel records an error, skips its stores and still frees its
 // tensor memory.  The weight gradient (K = pixels) is in nn.cu.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
 
 #include "../../include/glgpu.h"
@@ -272,6 +274,165 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Forward 3x3 convolution with the operands loaded by TMA (cp.async.bulk.tensor).
+// For layers whose input and output channel counts are multiples of 64 and whose
+// 128-pixel tiles are whole image rows (W a multiple of 128) or whole groups of
+// rows (128 a multiple of W), the A operand of tap (dy, dx) and channel chunk
+// c0..c0+63 is one box of the input viewed as the 4-D tensor [n][h][w][c]: the
+// tile's rows shifted by (dy, dx); the copy engine writes zeros where the box
+// leaves the image, which is the "same" padding.  B (the weights [cout][9 cin])
+// is a 64 x 64 box of a 2-D tensor.  Both land in shared memory in the 128-byte
+// swizzled K-major layout the MMA descriptors name (layout type 2).  Thread 0
+// issues the copies into a 4-stage ring (full barrier: the stage's bytes),
+// thread 32 issues four 128x64x16 tcgen05 MMAs per chunk and commits them to the
+// stage's empty barrier; all four warps then read the accumulator (TMEM lane =
+// output pixel) for the bias + ReLU epilogue.  Waits are bounded.
+// ---------------------------------------------------------------------------
+constexpr int TMA_STAGES = 4;
+constexpr int TMA_SMEM = TMA_STAGES * STAGE_BYTES + 1024 + 128;  // stages, 1024-byte alignment slack, barriers
+constexpr uint32_t kStageTx = (uint32_t)STAGE_BYTES;
+
+// SM100 shared-memory matrix descriptor, K-major with the 128-byte swizzle:
+// start >> 4 (bits 0-13), leading offset 16 B (unused for this layout), stride
+// offset 1024 B between 8-row groups (32-45), version 1 (46-47), layout type
+// 2 = 128-byte swizzle (61-63).  A K step of 16 elements advances the start by 32 B.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t start) {
+    uint64_t d = (uint64_t)((start >> 4) & 0x3FFFu);
+    d |= (uint64_t)1u << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1u << 46;
+    d |= (uint64_t)2u << 61;
+    return d;
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(dst),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            dst),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
+template <int RELU>
+__global__ void __launch_bounds__(NTH)
+k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ CUtensorMap ta2,
+               const __grid_constant__ CUtensorMap tb, const float* __restrict__ bias, bf16* __restrict__ y, int Cout,
+               int C1, int C2, int H, int W, int* err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + TMA_STAGES * STAGE_BYTES);
+    uint64_t* empty = full + TMA_STAGES;
+    uint64_t* done = empty + TMA_STAGES;
+    uint32_t* tslot = (uint32_t*)(done + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
+    const int img = m0 / (H * W), rem = m0 - img * H * W, y0 = rem / W, x0 = rem - y0 * W;
+    const int nck = (C1 + C2) / TK, nk = 9 * nck;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int q = 0; q < TMA_STAGES; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(full + q)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(empty + q)) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(done)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (tid == 0) {
+        // producer: chunk kc = tap * nck + cc, A = input box shifted by the tap, B = weights
+        for (int kc = 0; kc < nk && ok; ++kc) {
+            const int st = kc % TMA_STAGES, use = kc / TMA_STAGES;
+            if (use > 0 && !wait_parity(saddr(empty + st), (uint32_t)((use + 1) & 1))) ok = false;
+            if (!ok) break;
+            const int tap = kc / nck, cc = kc - tap * nck;
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            const int c = cc * TK;
+            const uint32_t a_dst = saddr(smem + st * STAGE_BYTES), b_dst = a_dst + A_BYTES;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(full + st)), "r"(kStageTx)
+                         : "memory");
+            if (c < C1) tma_load_4d(a_dst, &ta1, c, x0 + dx, y0 + dy, img, saddr(full + st));
+            else tma_load_4d(a_dst, &ta2, c - C1, x0 + dx, y0 + dy, img, saddr(full + st));
+            tma_load_2d(b_dst, &tb, tap * (C1 + C2) + c, n0, saddr(full + st));
+        }
+    } else if (tid == 32) {
+        // MMA issuer
+        for (int kc = 0; kc < nk && ok; ++kc) {
+            const int st = kc % TMA_STAGES, use = kc / TMA_STAGES;
+            if (!wait_parity(saddr(full + st), (uint32_t)(use & 1))) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t a0 = saddr(smem + st * STAGE_BYTES), b0 = a0 + A_BYTES;
+#pragma unroll
+            for (int j = 0; j < TK / 16; ++j)
+                mma_f16(tmem, smem_desc_sw128(a0 + 32 * j), smem_desc_sw128(b0 + 32 * j), kIdesc,
+                        (kc > 0 || j > 0) ? 1u : 0u);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             saddr(empty + st))
+                         : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(done))
+                     : "memory");
+    }
+    // everyone: the accumulator is complete when `done` fires (the issuer commits it
+    // even after a failed wait, so this wait ends)
+    if (!wait_parity(saddr(done), 0u)) ok = false;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (__syncthreads_or(ok ? 0 : 1)) ok = false;
+    if (ok) {
+        const int p = m0 + warp * 32 + lane;  // TMEM lane = tile row = pixel
+#pragma unroll
+        for (int c = 0; c < TN; c += 16) {
+            uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 16; q += 2) {
+                const int col = n0 + c + q;
+                float v0 = __uint_as_float(r[q]) + bias[col], v1 = __uint_as_float(r[q + 1]) + bias[col + 1];
+                if (RELU) {
+                    v0 = fmaxf(v0, 0.f);
+                    v1 = fmaxf(v1, 0.f);
+                }
+                *(__nv_bfloat162*)(y + (size_t)p * Cout + col) = __floats2bfloat162_rn(v0, v1);
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
 }  // namespace glnn_tc
 
 using namespace glnn_tc;
@@ -283,12 +444,95 @@ template <int MODE, int RELU> static cudaError_t conv_tc_smem_attr() {
     return e;
 }
 
+// --- TMA forward: tensor maps and the shapes it takes -------------------------
+static int g_conv_tma = 1;  // glnn_set_conv_tma
+
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// activations [n][h][w][c] (bf16), box = 64 channels x one 128-pixel tile
+static bool act_map(CUtensorMap* m, const void* base, int c, int n, int h, int w) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) return false;
+    const int wb = w < TM ? w : TM, hb = TM / wb;
+    cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
+    cuuint32_t box[4] = {(cuuint32_t)TK, (cuuint32_t)wb, (cuuint32_t)hb, 1u};
+    cuuint32_t es[4] = {1u, 1u, 1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// weights [rows][k] (bf16, k contiguous), box = 64 k x 64 rows
+static bool weight_map(CUtensorMap* m, const void* base, long long k, long long rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)k * 2};
+    cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)TN};
+    cuuint32_t es[2] = {1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// the shapes the TMA forward takes: 64-channel chunks, 64-channel output tiles,
+// 128-pixel tiles that are whole rows or whole groups of rows of one image
+static bool conv_tma_shape_ok(int c1, int c2, int h, int w, int cout) {
+    return c1 % TK == 0 && c2 % TK == 0 && cout % TN == 0 && ((long long)h * w) % TM == 0 && (w % TM == 0 || TM % w == 0);
+}
+
+template <int RELU> static cudaError_t conv_tma_smem_attr() {
+    static cudaError_t e =
+        cudaFuncSetAttribute(k_conv_fwd_tma<RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, TMA_SMEM);
+    return e;
+}
+
+// 1: launched; 0: shape or tensor maps not available (the caller uses the gather kernel)
+static int conv_fwd_tma(const void* x1, int c1, const void* x2, int c2, const void* wb, const float* bias, void* y, int n,
+                        int h, int w, int cout, int relu, int* err, cudaStream_t s) {
+    if (!g_conv_tma || !conv_tma_shape_ok(c1, c2, h, w, cout)) return 0;
+    CUtensorMap t1, t2, tb;
+    if (!act_map(&t1, x1, c1, n, h, w)) return 0;
+    if (c2 > 0) {
+        if (!act_map(&t2, x2, c2, n, h, w)) return 0;
+    } else {
+        t2 = t1;
+    }
+    if (!weight_map(&tb, wb, 9LL * (c1 + c2), cout)) return 0;
+    if ((relu ? conv_tma_smem_attr<1>() : conv_tma_smem_attr<0>()) != cudaSuccess) return 0;
+    const long long P = (long long)n * h * w;
+    dim3 grid((unsigned)(P / TM), (unsigned)(cout / TN));
+    if (relu)
+        k_conv_fwd_tma<1><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, c1, c2, h, w, err);
+    else
+        k_conv_fwd_tma<0><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, c1, c2, h, w, err);
+    return 1;
+}
+
 static int conv_tc_args_ok(int c1, int c2, int n, int h, int w, int cout) {
     return n > 0 && h > 0 && w > 0 && c1 > 0 && c1 % 8 == 0 && c2 >= 0 && c2 % 8 == 0 && cout > 0 && cout % 8 == 0 &&
            (long long)n * h * w < (1LL << 31);
 }
 
 extern "C" {
+
+int glnn_set_conv_tma(int32_t enable) {
+    g_conv_tma = enable ? 1 : 0;
+    return GLGPU_OK;
+}
 
 int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
                         void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, int32_t* err,
@@ -298,6 +542,8 @@ int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, con
     const long long P = (long long)n * h * w;
     dim3 grid((unsigned)((P + TM - 1) / TM), (unsigned)((cout + TN - 1) / TN));
     cudaStream_t s = (cudaStream_t)stream;
+    if (conv_fwd_tma(x1, c1, x2, c2, wb, bias, y, n, h, w, cout, relu, err, s))
+        return cudaGetLastError() == cudaSuccess ? GLGPU_OK : GLGPU_E_CUDA;
     if ((relu ? conv_tc_smem_attr<0, 1>() : conv_tc_smem_attr<0, 0>()) != cudaSuccess) return GLGPU_E_CUDA;
     if (relu)
         k_conv_tc<0, 1><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)x1, c1, (const bf16*)x2, c2, nullptr, (const bf16*)wb,

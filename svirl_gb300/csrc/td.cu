@@ -697,6 +697,153 @@ k_psi_sweep_bulk(const Inst* __restrict__ insts, const Item* __restrict__ items,
     }
 }
 
+// Called by the CTA that finishes the last tile of an instance in a
+// Crank-Nicolson psi sweep (one sweep per launch): the loop state keeps the max of
+// the squared change, which the reference's Crank-Nicolson kernel puts into its
+// residual code (svirl/cuda/td.h:285-291), so the usual stop predicate applies.
+template <typename T>
+__device__ void finish_instance_cn(const Inst& I, LoopState* loop, int k) {
+    InstState* st = I.st;
+    __threadfence();
+    const T r2 = res_from_bits<T>(atomicExch(&st->res, 0ull));
+    const bool conv = jacobi_converged(r2, I.stop_psi);
+    const int s = k + 1;
+    st->sweep = s;
+    st->blocks_done = 0u;
+    if (conv || s >= kMaxSweeps) {
+        st->done = 1;
+        st->rhs = pbuf(st->rhs, s);
+        st->last_sweeps_psi = s;
+        st->total_sweeps_psi += s;
+        if (s > st->max_sweeps_psi) st->max_sweeps_psi = s;
+        atomicSub(&loop->active, 1);
+    }
+}
+
+// One Jacobi sweep of the Crank-Nicolson psi step of the reference's
+// commented-out kernel (svirl/cuda/td.h:136-292; no host code of the reference
+// launches it): half explicit, half implicit (c_lhs = c_rhs = 1/2), Du link
+// weights r = (cell + cell) / 2 with ig = 4 / (r_m0 + r_p0 + r_0m + r_0p), the
+// nonlinear coefficient |psi_rhs|^2 in both halves, and the squared change as the
+// residual.  The explicit part of the links comes from the right-hand side on all
+// four (the trapezoidal rule, `as_written` = 0) or, as the kernel writes it, on
+// the left x link only and from psi^(k) on the other three (`as_written` = 1).  One thread per node;
+// psi^(k) -> psi^(k+1) in the same rotating buffers as the backward-Euler sweep.
+// The Langevin term of sweep 0 is recomputed from its hash for the node and its
+// left neighbour in every sweep (the reference stores it into psi_rhs at sweep 0,
+// where a thread may read its neighbour's value before or after that store).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_psi_sweep_cn(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopState* loop,
+               cudaGraphConditionalHandle cond, int use_cond, int as_written) {
+    const Tile t = tiles[blockIdx.x];
+    const Inst& I = insts[t.inst];
+    InstState* st = I.st;
+    const int tid = threadIdx.x;
+    __shared__ int s_skip, s_k, s_R, s_RA;
+    __shared__ uint32_t s_rt;
+    if (tid == 0) {
+        s_skip = *(volatile int*)&st->done;
+        s_k = *(volatile int*)&st->sweep;
+        s_R = *(volatile int*)&st->rhs;
+        s_RA = *(volatile int*)&st->rhsA;
+        s_rt = *(volatile uint32_t*)&st->rand_t;
+    }
+    __syncthreads();
+    if (!s_skip) {
+        const int k = s_k, R = s_R;
+        const C2<T>* __restrict__ cur = (const C2<T>*)I.psi[pbuf(R, k)];
+        const C2<T>* __restrict__ rhs = (const C2<T>*)I.psi[R];
+        C2<T>* nxt = (C2<T>*)I.psi[pbuf(R, k + 1)];
+        const T* __restrict__ A = (const T*)I.ab[s_RA];
+        const Geo g = I.g;
+        const int n = t.n0 + tid;
+        T res = T(0);
+        bool nan = false;
+        if (n < g.N) {
+            const int i = n % g.Nx, j = n / g.Nx;
+            const unsigned cb = cell_bits(g, I.mt, i, j);
+            const bool mm = GL_MM(cb), mp = GL_MP(cb), pm = GL_PM(cb), pp = GL_PP(cb);
+            const C2<T> p00 = cur[n];
+            C2<T> v = cmk<T>(T(0), T(0));
+            if (mm || mp || pm || pp) {
+                const bool lang = I.lang_psi_on != 0;
+                const T lc = gsel<T>(I.lang_psi, I.flang_psi);
+                auto rq_at = [&](int m) -> C2<T> {
+                    C2<T> r = rhs[m];
+                    if (lang) {
+                        r.x += lc * (rand_1<T>((uint32_t)m, s_rt) - T(0.5));
+                        r.y += lc * (rand_2<T>((uint32_t)m, s_rt) - T(0.5));
+                    }
+                    return r;
+                };
+                const C2<T> rq = rq_at(n);
+                const T dt = gsel<T>(I.dt, I.fdt);
+                const T dx = GT(g, dx), dy = GT(g, dy), idx2 = GT(g, idx2), idy2 = GT(g, idy2);
+                const T eps = I.eps_sp ? ((const T*)I.eps_sp)[n] : gsel<T>(I.epsilon, I.fepsilon);
+                const T r_m0 = T(0.5) * (T(mm) + T(mp)), r_p0 = T(0.5) * (T(pm) + T(pp));
+                const T r_0m = T(0.5) * (T(mm) + T(pm)), r_0p = T(0.5) * (T(mp) + T(pp));
+                const T ig = T(4) / (r_m0 + r_p0 + r_0m + r_0p);
+                const C2<T> z = cmk<T>(T(0), T(0));
+                // r U psi^(k) on the links (implicit part) and r U psi_rhs (explicit part)
+                C2<T> pm0 = z, pp0 = z, p0m = z, p0p = z, rm0 = z, rp0 = z, r0m = z, r0p = z;
+                if (mm || mp) {
+                    const C2<T> rU = cscale(r_m0, link_U<T>(-dx * A[(i - 1) + (g.Nx - 1) * j]));
+                    pm0 = cmul(rU, cur[n - 1]);
+                    rm0 = cmul(rU, rq_at(n - 1));
+                }
+                if (pm || pp) {
+                    const C2<T> rU = cscale(r_p0, link_U<T>(dx * A[i + (g.Nx - 1) * j]));
+                    pp0 = cmul(rU, cur[n + 1]);
+                    rp0 = as_written ? pp0 : cmul(rU, rq_at(n + 1));
+                }
+                if (mm || pm) {
+                    const C2<T> rU = cscale(r_0m, link_U<T>(-dy * A[g.Na + i + g.Nx * (j - 1)]));
+                    p0m = cmul(rU, cur[n - g.Nx]);
+                    r0m = as_written ? p0m : cmul(rU, rq_at(n - g.Nx));
+                }
+                if (mp || pp) {
+                    const C2<T> rU = cscale(r_0p, link_U<T>(dy * A[g.Na + i + g.Nx * j]));
+                    p0p = cmul(rU, cur[n + g.Nx]);
+                    r0p = as_written ? p0p : cmul(rU, rq_at(n + g.Nx));
+                }
+                const T c = T(0.5);  // c_lhs = c_rhs
+                const T a2 = rq.x * rq.x + rq.y * rq.y;
+                const T lw = idx2 * (r_m0 + r_p0) + idy2 * (r_0m + r_0p);
+                // explicit part: psi_rhs (1 - c dt (|psi_rhs|^2 - eps)) + c dt ig (idx2 (rhs_m0 + psi_p0)
+                //   + idy2 (psi_0m + psi_0p) - lw psi_rhs); implicit part: c dt ig (idx2 (psi_m0 + psi_p0)
+                //   + idy2 (psi_0m + psi_0p))
+                const T e = T(1) - c * dt * (a2 - eps);
+                const C2<T> ex = csub(cadd(cscale(idx2, cadd(rm0, rp0)), cscale(idy2, cadd(r0m, r0p))), cscale(lw, rq));
+                const C2<T> im = cadd(cscale(idx2, cadd(pm0, pp0)), cscale(idy2, cadd(p0m, p0p)));
+                const C2<T> num = cadd(cadd(cscale(e, rq), cscale(c * dt * ig, ex)), cscale(c * dt * ig, im));
+                const T den = T(1) + c * dt * (a2 - eps + ig * lw);
+                v = cmk<T>(num.x / den, num.y / den);
+            }
+            nxt[n] = v;
+            const T dr = v.x - p00.x, di = v.y - p00.y;
+            const T r2 = dr * dr + di * di;
+            if (r2 == r2) res = r2; else nan = true;
+        }
+        T bmax = block_max_res<T>(res, nan);
+        if (tid == 0) {
+            if (bmax < T(0)) {
+                atomicOr(&st->nan_seen, 1);
+                bmax = -(bmax + T(1));
+            }
+            atomicMax(&st->res, res_bits(bmax));
+            __threadfence();
+            unsigned prev = atomicAdd(&st->blocks_done, 1u);
+            if (prev == (unsigned)I.ntiles - 1u) finish_instance_cn<T>(I, loop, k);
+        }
+    }
+    if (tid == 0) {
+        __threadfence();
+        unsigned gdone = atomicAdd(&loop->blocks_done, 1u);
+        if (gdone == gridDim.x - 1u) finish_launch(loop, cond, use_cond);
+    }
+}
+
 // One Jacobi sweep of the A step (svirl/cuda/td.h:310-463): each thread owns the
 // x link and the y link that start at its node.
 template <typename T>
@@ -732,6 +879,19 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
         const C2<T>* __restrict__ psi = (const C2<T>*)I.psi[s_P];
         const Geo g = I.g;
         const int n = t.n0 + tid;
+        // Per link, the update is (X + dt rho k2 dd nbs(A^(k))) / D, where the fixed part
+        // X (right-hand side, noise, boundary field, supercurrent) depends on k only
+        // through the supercurrent argument A^(2 floor(k/2)) (the fixed-vortex potential
+        // with fixed vortices, constant over the loop).  Sweeps that start a pair
+        // (`fresh`) compute X and store it; the other sweeps of the pair read it back,
+        // so the sincos, the psi loads and the right-hand side's neighbour loads are paid
+        // once per two sweeps.  X (and in FP32 the A^(0) part G of X, constant over the
+        // loop) live in the link-factor buffer U, which the A loop does not read and
+        // k_link_U rebuilds before the next psi loop.  Both are stored rounded (mul_rn
+        // keeps G out of a fused multiply-add), so a pair's two sweeps use equal values.
+        const bool fresh = k == 0 || (!I.vpi && (k & 1) == 0);
+        T* Xc = (T*)I.U;
+        T* Gc = Xc + g.Nab;
         T res = T(0);
         bool nan = false;
         T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
@@ -754,65 +914,86 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
                 has_b = j < g.Ny - 1;
                 na = i + Nxa * j;
                 nb = Na + i + g.Nx * j;
-                const T* al = (I.vpi || k < 2) ? nullptr : (const T*)I.ab[(R + 2) % 3];  // delta of the phase
                 auto dl = [&](int m) -> T { return cur ? cur[m] : T(0); };
-                // read the phases before anything is stored (aliasing)
-                const T ph_a = has_a ? (I.vpi ? abi[na] : rhs[na] + (al ? al[na] : T(0))) : T(0);
-                const T ph_b = has_b ? (I.vpi ? abi[nb] : rhs[nb] + (al ? al[nb] : T(0))) : T(0);
-                const unsigned cb = cell_bits(g, I.mt, i, j);
-                const C2<T> psi0 = psi[n];
-                const T dx = GT(g, dx), dy = GT(g, dy);
-                const T idx = GT(g, idx), idy = GT(g, idy);
                 const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
-                const T k2 = I.fkappa2, H = I.fH;
-                const T dt_rho = I.fdt * I.frho;
-                const T dt_rho_k2 = dt_rho * k2;
-                const T lc = I.flang_A;
-                const bool lang = I.lang_A_on != 0;
+                const T k2 = I.fkappa2;
+                const T dt_rho_k2 = I.fdt * I.frho * k2;
+                T xa = T(0), xb = T(0);
+                if (fresh) {
+                    const T* al = (I.vpi || k < 2) ? nullptr : (const T*)I.ab[(R + 2) % 3];  // delta of the phase
+                    const T ph_a = has_a ? (I.vpi ? abi[na] : rhs[na] + (al ? al[na] : T(0))) : T(0);
+                    const T ph_b = has_b ? (I.vpi ? abi[nb] : rhs[nb] + (al ? al[nb] : T(0))) : T(0);
+                    const unsigned cb = cell_bits(g, I.mt, i, j);
+                    const C2<T> psi0 = psi[n];
+                    const T dx = GT(g, dx), dy = GT(g, dy);
+                    const T idx = GT(g, idx), idy = GT(g, idy);
+                    const T H = I.fH;
+                    const T dt_rho = I.fdt * I.frho;
+                    const T lc = I.flang_A;
+                    const bool lang = I.lang_A_on != 0;
+                    if (has_a) {
+                        const T noise = lang ? lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5)) : T(0);
+                        T rh = T(0), dd = T(1);
+                        if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
+                        else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
+                        T jl = T(0);
+                        if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
+                        T ga;
+                        if (k == 0) {
+                            T nr = T(0);
+                            if (j > 0)
+                                nr += idy2 * rhs[i + Nxa * (j - 1)] - idxy * rhs[Na + i + g.Nx * (j - 1)] +
+                                      idxy * rhs[Na + i + 1 + g.Nx * (j - 1)];
+                            if (j < g.Ny - 1)
+                                nr += idy2 * rhs[i + Nxa * (j + 1)] + idxy * rhs[Na + i + g.Nx * j] - idxy * rhs[Na + i + 1 + g.Nx * j];
+                            ga = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idy2 * rhs[na]);
+                            Gc[na] = ga;
+                        } else {
+                            ga = Gc[na];
+                        }
+                        xa = noise + dt_rho * (jl + rh) + ga;
+                        Xc[na] = xa;
+                    }
+                    if (has_b) {
+                        const T noise = lang ? lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5)) : T(0);
+                        T rh = T(0), dd = T(1);
+                        if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
+                        else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
+                        T jl = T(0);
+                        if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
+                        T gb;
+                        if (k == 0) {
+                            T nr = T(0);
+                            if (i > 0)
+                                nr += idx2 * rhs[Na + (i - 1) + g.Nx * j] - idxy * rhs[(i - 1) + Nxa * j] + idxy * rhs[(i - 1) + Nxa * (j + 1)];
+                            if (i < g.Nx - 1)
+                                nr += idx2 * rhs[Na + (i + 1) + g.Nx * j] + idxy * rhs[i + Nxa * j] - idxy * rhs[i + Nxa * (j + 1)];
+                            gb = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idx2 * rhs[nb]);
+                            Gc[nb] = gb;
+                        } else {
+                            gb = Gc[nb];
+                        }
+                        xb = noise + dt_rho * (jl + rh) + gb;
+                        Xc[nb] = xb;
+                    }
+                } else {
+                    if (has_a) xa = Xc[na];
+                    if (has_b) xb = Xc[nb];
+                }
                 if (has_a) {
-                    const T r0 = rhs[na];
-                    const T noise = lang ? lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5)) : T(0);
-                    T rh = T(0), dd = T(1);
-                    if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
-                    else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
-                    T jl = T(0);
-                    if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
-                    T nr = T(0), nd = T(0);
-                    if (j > 0) {
-                        const int m0 = i + Nxa * (j - 1), m1 = Na + i + g.Nx * (j - 1), m2 = Na + i + 1 + g.Nx * (j - 1);
-                        nr += idy2 * rhs[m0] - idxy * rhs[m1] + idxy * rhs[m2];
-                        nd += idy2 * dl(m0) - idxy * dl(m1) + idxy * dl(m2);
-                    }
-                    if (j < g.Ny - 1) {
-                        const int m0 = i + Nxa * (j + 1), m1 = Na + i + g.Nx * j, m2 = Na + i + 1 + g.Nx * j;
-                        nr += idy2 * rhs[m0] + idxy * rhs[m1] - idxy * rhs[m2];
-                        nd += idy2 * dl(m0) + idxy * dl(m1) - idxy * dl(m2);
-                    }
-                    va = (noise + dt_rho * (jl + rh) + dt_rho_k2 * (dd * nr - T(2) * idy2 * r0) + dt_rho_k2 * dd * nd) /
-                         (T(1) + T(2) * dt_rho_k2 * idy2);
+                    const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
+                    T nd = T(0);
+                    if (j > 0) nd += idy2 * dl(i + Nxa * (j - 1)) - idxy * dl(Na + i + g.Nx * (j - 1)) + idxy * dl(Na + i + 1 + g.Nx * (j - 1));
+                    if (j < g.Ny - 1) nd += idy2 * dl(i + Nxa * (j + 1)) + idxy * dl(Na + i + g.Nx * j) - idxy * dl(Na + i + 1 + g.Nx * j);
+                    va = (xa + dt_rho_k2 * dd * nd) / (T(1) + T(2) * dt_rho_k2 * idy2);
                     ca = dl(na);
                 }
                 if (has_b) {
-                    const T r0 = rhs[nb];
-                    const T noise = lang ? lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5)) : T(0);
-                    T rh = T(0), dd = T(1);
-                    if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
-                    else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
-                    T jl = T(0);
-                    if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
-                    T nr = T(0), nd = T(0);
-                    if (i > 0) {
-                        const int m0 = Na + (i - 1) + g.Nx * j, m1 = (i - 1) + Nxa * j, m2 = (i - 1) + Nxa * (j + 1);
-                        nr += idx2 * rhs[m0] - idxy * rhs[m1] + idxy * rhs[m2];
-                        nd += idx2 * dl(m0) - idxy * dl(m1) + idxy * dl(m2);
-                    }
-                    if (i < g.Nx - 1) {
-                        const int m0 = Na + (i + 1) + g.Nx * j, m1 = i + Nxa * j, m2 = i + Nxa * (j + 1);
-                        nr += idx2 * rhs[m0] + idxy * rhs[m1] - idxy * rhs[m2];
-                        nd += idx2 * dl(m0) + idxy * dl(m1) - idxy * dl(m2);
-                    }
-                    vb = (noise + dt_rho * (jl + rh) + dt_rho_k2 * (dd * nr - T(2) * idx2 * r0) + dt_rho_k2 * dd * nd) /
-                         (T(1) + T(2) * dt_rho_k2 * idx2);
+                    const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
+                    T nd = T(0);
+                    if (i > 0) nd += idx2 * dl(Na + (i - 1) + g.Nx * j) - idxy * dl((i - 1) + Nxa * j) + idxy * dl((i - 1) + Nxa * (j + 1));
+                    if (i < g.Nx - 1) nd += idx2 * dl(Na + (i + 1) + g.Nx * j) + idxy * dl(i + Nxa * j) - idxy * dl(i + Nxa * (j + 1));
+                    vb = (xb + dt_rho_k2 * dd * nd) / (T(1) + T(2) * dt_rho_k2 * idx2);
                     cbv = dl(nb);
                 }
             }
@@ -824,45 +1005,62 @@ k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopSt
             has_b = j < g.Ny - 1;
             na = i + Nxa * j;
             nb = Na + i + g.Nx * j;
-            // read the supercurrent phases before anything is stored (aliasing, see top)
-            const T ph_a = has_a ? abi[na] : T(0);
-            const T ph_b = has_b ? abi[nb] : T(0);
-            const unsigned cb = cell_bits(g, I.mt, i, j);
-            const C2<T> psi0 = psi[n];
-            const T dx = GT(g, dx), dy = GT(g, dy);
-            const T idx = GT(g, idx), idy = GT(g, idy);
             const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
-            const T k2 = gsel<T>(I.kappa2, I.fkappa2), H = gsel<T>(I.H, I.fH);
+            const T k2 = gsel<T>(I.kappa2, I.fkappa2);
             const T dt_rho = gsel<T>(I.dt, I.fdt) * gsel<T>(I.rho, I.frho);
             const T dt_rho_k2 = dt_rho * k2;
-            const T lc = gsel<T>(I.lang_A, I.flang_A);
-            const bool lang = I.lang_A_on != 0;
+            T xa = T(0), xb = T(0);
+            if (fresh) {
+                // read the supercurrent phases before anything is stored (aliasing, see top)
+                const T ph_a = has_a ? abi[na] : T(0);
+                const T ph_b = has_b ? abi[nb] : T(0);
+                const unsigned cb = cell_bits(g, I.mt, i, j);
+                const C2<T> psi0 = psi[n];
+                const T dx = GT(g, dx), dy = GT(g, dy);
+                const T idx = GT(g, idx), idy = GT(g, idy);
+                const T H = gsel<T>(I.H, I.fH);
+                const T lc = gsel<T>(I.lang_A, I.flang_A);
+                const bool lang = I.lang_A_on != 0;
+                if (has_a) {
+                    T r = rhs[na];
+                    if (lang) r += lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5));
+                    T rh = T(0);
+                    if (j == 0) rh = T(2) * k2 * H * idy;
+                    else if (j == g.Ny - 1) rh = -T(2) * k2 * H * idy;
+                    T jl = T(0);
+                    if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
+                    xa = r + dt_rho * (jl + rh);
+                    Xc[na] = xa;
+                }
+                if (has_b) {
+                    T r = rhs[nb];
+                    if (lang) r += lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5));
+                    T rh = T(0);
+                    if (i == 0) rh = -T(2) * k2 * H * idx;
+                    else if (i == g.Nx - 1) rh = T(2) * k2 * H * idx;
+                    T jl = T(0);
+                    if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
+                    xb = r + dt_rho * (jl + rh);
+                    Xc[nb] = xb;
+                }
+            } else {
+                if (has_a) xa = Xc[na];
+                if (has_b) xb = Xc[nb];
+            }
             if (has_a) {
-                T r = rhs[na];
-                if (lang) r += lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5));
-                T rh = T(0), dd = T(1);
-                if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
-                else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
-                T jl = T(0);
-                if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
+                const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
                 T nbs = T(0);
                 if (j > 0) nbs += idy2 * cur[i + Nxa * (j - 1)] - idxy * cur[Na + i + g.Nx * (j - 1)] + idxy * cur[Na + i + 1 + g.Nx * (j - 1)];
                 if (j < g.Ny - 1) nbs += idy2 * cur[i + Nxa * (j + 1)] + idxy * cur[Na + i + g.Nx * j] - idxy * cur[Na + i + 1 + g.Nx * j];
-                va = (r + dt_rho * (jl + rh) + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idy2);
+                va = (xa + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idy2);
                 ca = cur[na];
             }
             if (has_b) {
-                T r = rhs[nb];
-                if (lang) r += lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5));
-                T rh = T(0), dd = T(1);
-                if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
-                else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
-                T jl = T(0);
-                if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
+                const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
                 T nbs = T(0);
                 if (i > 0) nbs += idx2 * cur[Na + (i - 1) + g.Nx * j] - idxy * cur[(i - 1) + Nxa * j] + idxy * cur[(i - 1) + Nxa * (j + 1)];
                 if (i < g.Nx - 1) nbs += idx2 * cur[Na + (i + 1) + g.Nx * j] + idxy * cur[i + Nxa * j] - idxy * cur[i + Nxa * (j + 1)];
-                vb = (r + dt_rho * (jl + rh) + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idx2);
+                vb = (xb + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idx2);
                 cbv = cur[nb];
             }
         }
@@ -1091,6 +1289,7 @@ struct TDLaunch {
     const Item* items;
     LoopState* loop;
     int ninst, ntiles, nitems, psi_grid, dtype, strip_rows, psi_kind;
+    int psi_cn;       // psi time stepping: 0 backward Euler, 1 Crank-Nicolson, 2 its kernel as written
     bool any_solveA;
     bool any_fv;  // an instance has fixed vortices (irregular potential or phase lock)
 };
@@ -1127,6 +1326,9 @@ static cudaError_t launch_psi_sweep(int kind, int rows, int grid, cudaStream_t s
 }
 static void* A_sweep_fn(int dtype) {
     return dtype == 8 ? (void*)k_A_sweep<double> : (void*)k_A_sweep<float>;
+}
+static void* cn_fn(int dtype) {
+    return dtype == 8 ? (void*)k_psi_sweep_cn<double> : (void*)k_psi_sweep_cn<float>;
 }
 static void* link_fn(int dtype) {
     return dtype == 8 ? (void*)k_link_U<double> : (void*)k_link_U<float>;
@@ -1219,9 +1421,15 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         prev = nd;
         {
             cudaGraphNode_t sw;
-            void* a[] = {&insts, &items, &nitems, &loop, &hpsi, &one};
-            GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.psi_kind, L.strip_rows), dim3(L.psi_grid),
-                            dim3(psi_threads(L.psi_kind)), a));
+            if (L.psi_cn) {
+                int aw = L.psi_cn == 2 ? 1 : 0;
+                void* a[] = {&insts, &tiles, &loop, &hpsi, &one, &aw};
+                GCHK(add_kernel(pbody, &sw, nullptr, 0, cn_fn(L.dtype), gt, bt, a));
+            } else {
+                void* a[] = {&insts, &items, &nitems, &loop, &hpsi, &one};
+                GCHK(add_kernel(pbody, &sw, nullptr, 0, psi_sweep_fn(L.psi_kind, L.strip_rows), dim3(L.psi_grid),
+                                dim3(psi_threads(L.psi_kind)), a));
+            }
         }
         {
             void* a[] = {&insts, &ninst, &zero};
@@ -1319,7 +1527,13 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
             k_loop_begin<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0, part);
             for (;;) {
                 for (int c = 0; c < chunk; ++c) {
-                    if (part == 0) {
+                    if (part == 0 && L.psi_cn) {
+                        const int aw = L.psi_cn == 2 ? 1 : 0;
+                        if (L.dtype == 8)
+                            k_psi_sweep_cn<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0, aw);
+                        else
+                            k_psi_sweep_cn<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0, aw);
+                    } else if (part == 0) {
                         launch_psi_sweep(L.psi_kind, L.strip_rows, L.psi_grid, s, L.insts, L.items, L.nitems, L.loop);
                     } else {
                         if (L.dtype == 8) k_A_sweep<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
@@ -1402,22 +1616,27 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     if (h->dtype == 8) k_link_U<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, 0);
     else k_link_U<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, 0);
     double total = 0.0;
+    // A sweeps come in pairs (sweep 0 computes the links' fixed parts, sweep 1 reuses
+    // them), so an A repetition times both and the average is over sweeps
+    const int per_rep = which == 0 ? 1 : 2;
     for (int r = 0; r < nrep && e == cudaSuccess; ++r) {
         cudaMemsetAsync(h->flush, r & 0xff, flush_bytes, h->stream);
-        k_bench_prep<<<1, 32, 0, h->stream>>>(h->inst, 1, h->loop, 1);
-        cudaEventRecord(e0, h->stream);
-        if (which == 0) {
-            launch_psi_sweep(psi_kind(h->dtype, h->psi_select), h->strip_rows, h->psi_grid, h->stream, h->inst, h->items,
-                             h->nitems, h->loop);
-        } else {
-            if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
-            else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+        for (int q = 0; q < per_rep && e == cudaSuccess; ++q) {
+            k_bench_prep<<<1, 32, 0, h->stream>>>(h->inst, 1, h->loop, which == 0 ? 1 : q);
+            cudaEventRecord(e0, h->stream);
+            if (which == 0) {
+                launch_psi_sweep(psi_kind(h->dtype, h->psi_select), h->strip_rows, h->psi_grid, h->stream, h->inst, h->items,
+                                 h->nitems, h->loop);
+            } else {
+                if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+                else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+            }
+            cudaEventRecord(e1, h->stream);
+            e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            total += ms;
         }
-        cudaEventRecord(e1, h->stream);
-        e = cudaEventSynchronize(e1);
-        float ms = 0.f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-        total += ms;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1429,7 +1648,7 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_check(h, e, "time_sweeps");
     if (hl.err & kErrCopyWait) return set_error(h, GLGPU_E_TIMEOUT, "time_sweeps: psi sweep: a bulk-copy wait ran out");
-    *avg_ms = total / nrep;
+    *avg_ms = total / (nrep * per_rep);
     return GLGPU_OK;
 }
 
@@ -1585,6 +1804,7 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     L.ninst = 1; L.ntiles = h->ntiles; L.nitems = h->nitems; L.psi_grid = h->psi_grid; L.dtype = h->dtype;
     L.strip_rows = h->strip_rows;
     L.psi_kind = psi_kind(h->dtype, h->psi_select);
+    L.psi_cn = h->psi_scheme;
     L.any_solveA = h->inst_h.solveA != 0;
     L.any_fv = h->vpi != nullptr || h->lock_n > 0;
     InstState hs;
@@ -1605,6 +1825,9 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
     if (eqn < 0 || eqn > 2 || Nt < 0) return batch_error(b, GLGPU_E_ARG, "batch_td: bad eqn or Nt");
     std::vector<Inst> insts(b->ninst);
     bool any_solveA = false, any_fv = false;
+    for (int q = 0; q < b->ninst; ++q)
+        if (b->hs[q]->psi_scheme != 0)
+            return batch_error(b, GLGPU_E_ARG, "batch_td: Crank-Nicolson instances run on their own handle");
     for (int q = 0; q < b->ninst; ++q) {
         glgpu_handle* h = b->hs[q];
         cudaStreamSynchronize(h->stream);
@@ -1622,6 +1845,7 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
     L.ninst = b->ninst; L.ntiles = b->ntiles; L.nitems = b->nitems; L.psi_grid = b->psi_grid; L.dtype = b->dtype;
     L.strip_rows = b->strip_rows;
     L.psi_kind = psi_kind(b->dtype, 0);
+    L.psi_cn = 0;
     L.any_solveA = any_solveA;
     L.any_fv = any_fv;
     TDOutcome o = td_core(b->stream, L, Nt, eqn, b->td_exec, &b->td_graph_failed, b->use_graphs, b->loop_guard,

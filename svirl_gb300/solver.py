@@ -702,11 +702,30 @@ class TD:
     """TDGL driver (``svirl/solvers/td.py``): the time loop and the Jacobi loops
     run on the device in one CUDA-graph launch per call."""
 
+    SCHEMES = ("backward_euler", "crank_nicolson", "crank_nicolson_as_written")
+
     def __init__(self, gl):
         self._gl = gl
         self.dt = self.Nt = self.T = None
         self.dtA = self.NtA = self.TA = None
         self.last_stats = None
+        self._scheme = "backward_euler"
+
+    @property
+    def scheme(self):
+        """Time stepping of the order parameter: "backward_euler" (the reference's,
+        the default), "crank_nicolson" (the reference's commented-out sweep,
+        svirl/cuda/td.h:136-292, with the explicit half of every link from the
+        step's start) or "crank_nicolson_as_written" (that sweep as written), with
+        the same Jacobi loop and stop rule."""
+        return self._scheme
+
+    @scheme.setter
+    def scheme(self, value):
+        if value not in self.SCHEMES:
+            raise ValueError("scheme must be one of %s" % (self.SCHEMES,))
+        self._gl._h.set_psi_scheme(self.SCHEMES.index(value))
+        self._scheme = value
 
     @property
     def _random_t(self):
@@ -881,6 +900,20 @@ class Solvers:
         self._init_cg()
         self._cg._solve(n_iter)
         self.vortices_detected = False
+
+    @property
+    def td_scheme(self):
+        """The order parameter's time stepping in ``td``: "backward_euler" (the
+        reference's, default), "crank_nicolson" or "crank_nicolson_as_written"
+        (see TD.scheme; the reference cannot reach them: its kernel is commented
+        out, svirl/cuda/td.h:136-292)."""
+        self._init_td()
+        return self._td.scheme
+
+    @td_scheme.setter
+    def td_scheme(self, value):
+        self._init_td()
+        self._td.scheme = value
 
     @property
     def vortices_detected(self):

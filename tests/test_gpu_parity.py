@@ -260,3 +260,10 @@ def test_sweep_timer_runs_and_keeps_state():
     after = gpu_state(gl)
     assert ms_psi > 0 and ms_A > 0
     assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
+    # the A timing leaves its link terms in the link-factor buffer; the next TD call
+    # rebuilds the table, so it continues exactly as an untimed twin does
+    twin, _ = make_pair(Nx=200, Ny=150, kappa=3.0, sigma=100.0, seed=3)
+    for x in (gl, twin):
+        x.solve.td(dt=0.1, Nt=3)
+    a, b = gpu_state(gl), gpu_state(twin)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
