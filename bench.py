@@ -500,9 +500,10 @@ def run_conv(args):
     f = lambda: lib.glnn_conv3x3_fwd(P(x), cin, None, 0, P(wb), P(b), P(y), n, h, w, cout, 1, P(err), s)
     bd = lambda: lib.glnn_conv3x3_bwd_data(P(dy), P(y), 1, P(wt), P(dx), cin, None, 0, n, h, w, cout, P(err), s)
     bw = lambda: lib.glnn_conv3x3_bwd_weight(P(dy), P(y), 1, P(x), cin, None, 0, P(dw), P(db), P(work), nwork, n, h, w,
-                                            cout, s)
+                                            cout, P(err), s)
     lib.glnn_set_conv_tma(0)
     ms_f_gather = timed(f, args.steps)
+    ms_w_mma = timed(bw, args.steps)
     lib.glnn_set_conv_tma(1)
     ms_f, ms_d, ms_w = timed(f, args.steps), timed(bd, args.steps), timed(bw, args.steps)
     assert int(err.item()) == 0
@@ -522,7 +523,10 @@ def run_conv(args):
             "forward_gather": {"ms": ms_f_gather, "tflops": flop / (ms_f_gather * 1e-3) / 1e12,
                                "kernel": "tcgen05, operands gathered by the threads"},
             "data_grad": {"ms": ms_d, "tflops": flop / (ms_d * 1e-3) / 1e12, "kernel": "tcgen05"},
-            "weight_grad": {"ms": ms_w, "tflops": flop / (ms_w * 1e-3) / 1e12, "kernel": "mma.sync"}}
+            "weight_grad": {"ms": ms_w, "tflops": flop / (ms_w * 1e-3) / 1e12,
+                            "kernel": "tcgen05, MN-major operands loaded by TMA, split-K (with the dy * relu'(y) "
+                                      "pass and the bias gradient)"},
+            "weight_grad_mma": {"ms": ms_w_mma, "tflops": flop / (ms_w_mma * 1e-3) / 1e12, "kernel": "mma.sync"}}
     print(json.dumps(line), flush=True)
 
 
@@ -563,22 +567,23 @@ def run_learned(args):
             evals["%d" % n] = L.evaluate(net, insts, cache=cache, Estar=Estar)
         finally:
             cache.close()
-    t = thr["128"]
+    t = thr["128"]["by_dtype"]["float64"]
     nodes = 128 * 128 * 64
-    line = {"metric": "GL states/s to dF/F<=1e-6, learned warm start + batched FP32 CG (128^2, 64 instances)",
+    line = {"metric": "GL states/s to dF/F<=1e-6, learned warm start + batched FP64 CG (128^2, 64 instances)",
             "value": t["states_per_s"], "unit": "states/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": 1e3 * t["wall_s"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16 net (f32 accumulate), f32 CG stencils, f64 reductions", "data": "synthetic (solver-generated)",
+            "dtype": "bf16 net (f32 accumulate), f64 CG (the f32 CG arm under throughput.*.by_dtype.float32)",
+            "data": "synthetic (solver-generated)",
             "config": {"workload": "learned_warm_start", "train_states": args.train_states, "epochs": args.epochs,
                        "params": net.n_params(), "levels": list(L.LEVELS), "target_mode": "amplitude",
                        "train_loss_first_last": [hist[0], hist[-1]], "gen_s": t_gen, "train_s": t_train,
-                       "cg_cap": args.learned_cap, "gtol_abs": args.gtol,
+                       "cg_cap": args.learned_cap, "gtol_abs": args.gtol, "plain": thr["128"]["plain"],
                        "criterion": "|F - F*|/|F*| <= 1e-6, F* = FP64 relaxation (gradient norm 1e-7, 20000 "
                                     "iterations) of the same instance from the same initial state: the random start "
                                     "(plain arm), the prediction (learned arm)"},
             "speedup_vs_plain": t["speedup_vs_plain"], "throughput": thr, "eval": evals,
-            "e2e": {"value": t["states_per_s"], "unit": "states/s", "h2d_bytes_per_step": nodes * 8 * 2,
-                    "d2h_bytes_per_step": nodes * 4 * 4,
+            "e2e": {"value": t["states_per_s"], "unit": "states/s", "h2d_bytes_per_step": nodes * 16 * 2,
+                    "d2h_bytes_per_step": nodes * 8 * 4,
                     "how": "wall time of features to the device, prediction, decoding to host, states into the "
                            "handles, batched CG, states back"}}
     print(json.dumps(line), flush=True)

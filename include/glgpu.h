@@ -222,7 +222,8 @@ int glgpu_batch_set_loop_guard(glgpu_batch* b, int32_t launches);  /* as glgpu_s
  * with GLGPU_CG_GTOL_ABS: |grad F| <= gtol, tested before the first update too).
  * Per-instance outputs (each may be NULL): iterations done, final energy,
  * final |grad F| relative to the first, status (1 gradient stop, 2 energy stop,
- * 3 n_iter reached, 4 energy target reached, -1 no descent step; then
+ * 3 n_iter reached, 4 energy target reached, 5 energy window (see
+ * glgpu_batch_set_cg_window), -1 no descent step; then
  * GLGPU_E_NOROOT is returned).
  * flags: GLGPU_CG_EXACT_BOUNDARY makes dF/dA the exact derivative of the free
  * energy on the boundary links too; the reference's formula (cg.h:174-300)
@@ -233,6 +234,12 @@ int glgpu_batch_set_loop_guard(glgpu_batch* b, int32_t launches);  /* as glgpu_s
  * such stop; targets = NULL clears them).  Measures the iterations a start needs
  * to reach a known minimum energy. */
 int glgpu_batch_set_energy_targets(glgpu_batch* b, const double* targets, double rel_tol);
+/* Energy-window stop for the next glgpu_batch_cg calls: every `window` iterations
+ * an instance compares its energy with the energy `window` iterations before and
+ * stops (status 5) unless it fell by more than rel_tol |E| (window = 0: off).
+ * For FP32 batches, whose gradient norm has a rounding floor above tight
+ * gradient tolerances: the run ends once the energy has stopped improving. */
+int glgpu_batch_set_cg_window(glgpu_batch* b, int32_t window, double rel_tol);
 #define GLGPU_CG_EXACT_BOUNDARY 1
 #define GLGPU_CG_GTOL_ABS 2
 int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int32_t flags, int32_t* iters,

@@ -10,8 +10,8 @@
  *    W[cout][3][3][cin]; the kernels read bfloat16 copies made by
  *    glnn_prep_weights (Wb: same layout, Wt: [3][3][cin][cout]).  Weight and
  *    bias gradients, optimiser state: float32.  Products are accumulated in
- *    float32 on the tensor cores (tcgen05 for the forward pass and the data
- *    gradient, mma for the weight gradient).
+ *    float32 on the tensor cores (tcgen05; the weight gradient of shapes the
+ *    tcgen05 kernel does not take runs on mma).
  *  - "Same" padding (zeros), stride 1.  A convolution may read the channel
  *    concatenation [x1 | x2] of two tensors (x2 may be NULL with c2 = 0), so the
  *    decoder's skip connections need no copy; the data gradient is written split
@@ -41,6 +41,7 @@ int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, con
  * from 4-D / 2-D tensor maps, 4-stage pipeline) for the shapes it takes
  * (c1, c2, cout multiples of 64; w a multiple of 128 or a divisor of 128; h*w a
  * multiple of 128), the thread gather otherwise; 0 = always the thread gather.
+ * The same switch selects the tcgen05 weight gradient (1) or the mma.sync one (0).
  * Process-wide. */
 int glnn_set_conv_tma(int32_t enable);
 /* [dx1|dx2] = conv3x3^T(dy * relu'(y), Wt), on tcgen05 like the forward.  y may be
@@ -51,11 +52,17 @@ int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const voi
 
 /* dW[cout][9*cin] and db[cout] (float32, overwritten) from dy * relu'(y) and
  * the input [x1|x2].  work: float32 scratch of glnn_conv3x3_bwd_weight_work()
- * floats (split-K partial sums, reduced in a fixed order: deterministic). */
+ * floats, 16-byte aligned (split-K partial sums, reduced in a fixed order:
+ * deterministic).  With glnn_set_conv_tma(1) and c1, c2, cout multiples of 64,
+ * w a multiple or a divisor of 64 and h*w a multiple of 64, it runs on tcgen05
+ * (M = two taps x 64 input channels, N = 64 output channels, K = pixels, both
+ * operands MN-major boxes loaded by TMA, FP32 accumulator in tensor memory); else
+ * on mma.sync.  *err (a device int) is set to 1 if a CTA's bounded wait ran out
+ * (its partial sums are then NaN). */
 int64_t glnn_conv3x3_bwd_weight_work(int32_t n, int32_t h, int32_t w, int32_t cin, int32_t cout);
 int glnn_conv3x3_bwd_weight(const void* dy, const void* y, int32_t relu, const void* x1, int32_t c1, const void* x2,
                             int32_t c2, float* dw, float* db, float* work, int64_t work_floats, int32_t n, int32_t h,
-                            int32_t w, int32_t cout, void* stream);
+                            int32_t w, int32_t cout, int32_t* err, void* stream);
 
 /* bfloat16 copies of a float32 weight W[cout][9][cin]: wb (same layout) and
  * wt[9][cin][cout] (for the data gradient); either may be NULL. */

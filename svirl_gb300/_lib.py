@@ -91,6 +91,7 @@ _SIGNATURES = {
     "glgpu_batch_set_use_graphs": (C.c_int, [_H, C.c_int32]),
     "glgpu_batch_set_loop_guard": (C.c_int, [_H, C.c_int32]),
     "glgpu_batch_set_energy_targets": (C.c_int, [_H, _P, C.c_double]),
+    "glgpu_batch_set_cg_window": (C.c_int, [_H, C.c_int32, C.c_double]),
     "glgpu_batch_cg": (C.c_int, [_H, C.c_int32, C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     # learned warm start (include/glgpu_nn.h)
@@ -101,7 +102,7 @@ _SIGNATURES = {
                                         C.c_int32, C.c_int32, _P, _P]),
     "glnn_conv3x3_bwd_weight_work": (C.c_int64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "glnn_conv3x3_bwd_weight": (C.c_int, [_P, _P, C.c_int32, _P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int64,
-                                          C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+                                          C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P]),
     "glnn_prep_weights": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, _P]),
     "glnn_pool2_fwd": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
     "glnn_pool2_bwd": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),

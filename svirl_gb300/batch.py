@@ -95,6 +95,12 @@ class HandleBatch:
         self._check(self.lib.glgpu_batch_set_energy_targets(self.b, t.ctypes.data_as(C.c_void_p), float(rel_tol)),
                     "set_energy_targets")
 
+    def set_cg_window(self, window, rel_tol=0.0):
+        """Energy-window stop for the next device CG calls: every `window`
+        iterations an instance stops, with status 5, unless its energy fell by more
+        than rel_tol |E| since `window` iterations before (window 0: off)."""
+        self._check(self.lib.glgpu_batch_set_cg_window(self.b, int(window), float(rel_tol)), "set_cg_window")
+
     def cg_device(self, n_iter=1000, rtol=1e-6, gtol=0.0, exact_boundary=False, gtol_abs=False, timed=False):
         """``glgpu_batch_cg``; returns per-instance arrays (see ``GLBatch.cg``)."""
         n = len(self.handles)

@@ -606,6 +606,11 @@ int glgpu_batch_cg(glgpu_batch* b, int32_t n_iter, double rtol, double gtol, int
     return batch_cg(b, n_iter, rtol, gtol, flags, iters, energies, grad_rel, status, elapsed_ms);
 }
 
+int glgpu_batch_set_cg_window(glgpu_batch* b, int32_t window, double rel_tol) {
+    if (!b) return GLGPU_E_ARG;
+    return batch_set_cg_window(b, window, rel_tol);
+}
+
 int glgpu_batch_set_energy_targets(glgpu_batch* b, const double* targets, double rel_tol) {
     if (!b) return GLGPU_E_ARG;
     return batch_set_energy_targets(b, targets, rel_tol);

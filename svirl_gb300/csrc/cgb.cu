@@ -64,6 +64,9 @@ struct CGLoop {
     double rtol, gtol;
     int flags;     // GLGPU_CG_* bits
     int ticket;    // CTAs finished in the running launch of the step kernel
+    int window;    // energy-window stop: every `window` iterations (0: off) ...
+    int pad2_;
+    double wtol;   // ... stop unless E fell by more than wtol |E| since the last mark
 };
 
 template <typename T>
@@ -511,8 +514,14 @@ kb_dir_coef(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, do
     if (last_cta_of_instance(cs, I.ntiles)) inst_alpha<sizeof(T) == 8>(I, cs, partials, loop);
 }
 
-// energy-ratio stop, target stop and iteration cap of one instance, by the CTA
-// that finished its last tile
+// energy-ratio stop, target stop, energy-window stop and iteration cap of one
+// instance, by the CTA that finished its last tile.  The energy window: every
+// `window` iterations the energy is compared with the last mark; if it fell by no
+// more than wtol |E| over the window the instance stops (status 5), else the mark
+// moves.  It ends runs whose gradient cannot reach its tolerance because the
+// arithmetic's rounding floor is above it (FP32 stencils) once the energy has
+// stopped improving.  No counterpart in the reference (its CG stops on the
+// per-iteration energy ratio, cg.py:315-318).
 __device__ __noinline__ void inst_energy_stop(const Inst& I, CGState* cs, const double* partials, CGLoop* loop) {
     __shared__ double e1[1];
     cta_tile_sums<1>(partials, I.tile0, I.ntiles, I.g.dxdy, e1);
@@ -522,17 +531,23 @@ __device__ __noinline__ void inst_energy_stop(const Inst& I, CGState* cs, const 
     cs->E = E;
     const int it = cs->iter;
     cs->iter = it + 1;
+    int stop = 0;
     if (it > 0 && fabs(E / cs->E_prev - 1.0) < loop->rtol) {
-        cs->done = 1;
-        cs->status = 2;
-        atomicSub(&loop->active, 1);
+        stop = 2;
     } else if (I.cg_target == I.cg_target && E <= I.cg_target + I.cg_target_tol * fabs(I.cg_target)) {
+        stop = 4;
+    } else if (loop->window > 0 && cs->iter - cs->it_mark >= loop->window) {
+        if (cs->E_mark - E <= loop->wtol * fabs(E)) {
+            stop = 5;
+        } else {
+            cs->E_mark = E;
+            cs->it_mark = cs->iter;
+        }
+    }
+    if (!stop && cs->iter >= loop->n_iter) stop = 3;
+    if (stop) {
         cs->done = 1;
-        cs->status = 4;
-        atomicSub(&loop->active, 1);
-    } else if (cs->iter >= loop->n_iter) {
-        cs->done = 1;
-        cs->status = 3;
+        cs->status = stop;
         atomicSub(&loop->active, 1);
     }
 }
@@ -730,6 +745,8 @@ kb_init(const Inst* __restrict__ insts, int ninst, const double* __restrict__ pa
         cs->alpha_psi = cs->alpha_A = 0.0;
         cs->E = E;
         cs->E_prev = E;
+        cs->E_mark = E;
+        cs->it_mark = 0;
         cs->g2 = cs->g2_0 = 0.0;
         cs->iter = 0;
         cs->done = 0;
@@ -888,6 +905,13 @@ int batch_set_energy_targets(glgpu_batch* b, const double* targets, double rel_t
     return GLGPU_OK;
 }
 
+int batch_set_cg_window(glgpu_batch* b, int window, double rel_tol) {
+    if (window < 0 || !(rel_tol >= 0.0)) return batch_error(b, GLGPU_E_ARG, "batch_set_cg_window: window < 0 or rel_tol < 0");
+    b->cg_window = window;
+    b->cg_window_tol = rel_tol;
+    return GLGPU_OK;
+}
+
 int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, int32_t* iters, double* energies, double* grad_rel,
              int32_t* status, double* elapsed_ms) {
     if (n_iter < 0 || !(rtol >= 0.0) || !(gtol >= 0.0)) return batch_error(b, GLGPU_E_ARG, "batch_cg: bad n_iter, rtol or gtol");
@@ -925,6 +949,8 @@ int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, in
     lp.rtol = rtol;
     lp.gtol = gtol;
     lp.flags = flags;
+    lp.window = b->cg_window;
+    lp.wtol = b->cg_window_tol;
     cudaError_t e = cudaMemcpyAsync(b->insts, insts.data(), sizeof(Inst) * insts.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->cg_loop, &lp, sizeof(lp), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -54,10 +54,12 @@ struct CGState {
     double E, E_prev;         // energy after the last / the previous update
     double g2, g2_0;          // |gradient|^2 now and at the first iteration
     int iter, done, gi, di;   // iterations done, finished, current gradient / direction buffer
-    int status;               // 0 ok, 1 gradient-norm stop, 2 energy stop, 3 n_iter, -1 no step found
+    int status;               // 0 ok, 1 gradient-norm stop, 2 energy stop, 3 n_iter, 4 energy target,
+                              // 5 energy window (stagnation), -1 no step found
     int pi;                   // buffer (psi[pi], ab[pi]) holding the current state during a CG call
     int ticket;               // CTAs of this instance finished in the running launch
-    int pad_;
+    int it_mark;              // iteration of the last energy-window mark
+    double E_mark;            // energy at that mark
 };
 
 // Everything a kernel needs to process one instance.  Lives in device memory,
@@ -234,6 +236,8 @@ struct glgpu_batch {
     bool cg_graph_failed = false;
     std::vector<double> cg_targets;      // per-instance energy targets (empty: none)
     double cg_target_tol = 0.0;
+    int cg_window = 0;                   // energy-window stop: iterations (0: off) and relative decrease
+    double cg_window_tol = 0.0;
     std::string last_error;
 };
 
@@ -275,6 +279,7 @@ int cg_read_gradient(glgpu_handle* h, void* gpsi_host, void* gA_host);
 int cg_coef_for(glgpu_handle* h, const void* dpsi_host, const void* dab_host, double* c_out);
 // cgb.cu
 int batch_set_energy_targets(glgpu_batch* b, const double* targets, double rel_tol);
+int batch_set_cg_window(glgpu_batch* b, int window, double rel_tol);
 int batch_cg(glgpu_batch* b, int n_iter, double rtol, double gtol, int flags, int32_t* iters, double* energies, double* grad_rel,
              int32_t* status, double* elapsed_ms);
 // td.cu graph helpers

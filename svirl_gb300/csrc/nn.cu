@@ -1,12 +1,13 @@
-// Kernels of the learned CG warm start: the weight gradient of the 3x3
-// convolution as an implicit GEMM on the tensor cores (mma bf16 -> f32),
-// pooling/upsampling, a weighted squared-error loss and Adam.  The forward
-// convolution and its data gradient run on tcgen05 (nn_tc.cu).  No counterpart in
-// the reference (its only minimiser is the CG of svirl/solvers/cg.py).
+// Kernels of the learned CG warm start: the fallback weight gradient of the 3x3
+// convolution as an implicit GEMM on mma.sync (bf16 -> f32), pooling/upsampling,
+// a weighted squared-error loss and Adam.  The forward convolution, its data
+// gradient and, for channel counts that are multiples of 64, the weight gradient
+// run on tcgen05 (nn_tc.cu).  No counterpart in the reference (its only minimiser
+// is the CG of svirl/solvers/cg.py).
 //
-// Weight gradient: M = cout, N = 9 cin, K = pixels; A = dy^T (with the layer's
-// ReLU derivative applied while gathering), B = the input shifted by the tap.
-// A CTA of 4 warps computes a 64 x 64 tile, each warp 32 x 32 (2 x 4
+// Fallback weight gradient: M = cout, N = 9 cin, K = pixels; A = dy^T (with the
+// layer's ReLU derivative applied while gathering), B = the input shifted by the
+// tap.  A CTA of 4 warps computes a 64 x 64 tile, each warp 32 x 32 (2 x 4
 // mma.m16n8k16), over K chunks of 32 staged in shared memory with register
 // prefetch of the next chunk; the pixel range is split over CTAs (split-K) and
 // the partial sums are reduced in a fixed order (deterministic).
@@ -459,36 +460,69 @@ static WPlan wplan(int n, int h, int w, int cin, int cout) {
 
 using namespace glnn;
 
+// nn_tc.cu: the weight gradient on tcgen05 with TMA operands (its split plan, and
+// the launch: 1 when enqueued, 0 when the shape or the TMA switch rule it out)
+void glnn_tc_wgrad_plan(int n, int h, int w, int cin, int cout, int* nz, int* chunk);
+int glnn_tc_wgrad(const void* dy, const void* y, int relu, const void* x1, int c1, const void* x2, int c2, float* ws,
+                  void* dy_masked, int n, int h, int w, int cout, int* err, cudaStream_t s);
+
+// work layout: [split partial sums (the larger of the two plans)][bias partials]
+// [dy * relu'(y) in bf16, for the tcgen05 path], each part 256-byte aligned
+struct WLayout {
+    long long ws, bias_off, dym_off, total;
+};
+static WLayout wlayout(int n, int h, int w, int cin, int cout) {
+    const WPlan q = wplan(n, h, w, cin, cout);
+    int nz_tc = 0, chunk_tc = 0;
+    glnn_tc_wgrad_plan(n, h, w, cin, cout, &nz_tc, &chunk_tc);
+    auto up = [](long long v) { return (v + 63) / 64 * 64; };
+    WLayout L;
+    L.ws = up(std::max(q.ws_floats, (long long)nz_tc * cout * 9 * cin));
+    L.bias_off = L.ws;
+    L.dym_off = L.bias_off + up(q.bias_floats);
+    L.total = L.dym_off + up(((long long)n * h * w * cout + 1) / 2);
+    return L;
+}
+
 extern "C" {
 
 int64_t glnn_conv3x3_bwd_weight_work(int32_t n, int32_t h, int32_t w, int32_t cin, int32_t cout) {
     if (n <= 0 || h <= 0 || w <= 0 || cin <= 0 || cout <= 0) return 0;
-    const WPlan q = wplan(n, h, w, cin, cout);
-    return q.ws_floats + q.bias_floats;
+    return wlayout(n, h, w, cin, cout).total;
 }
 
 int glnn_conv3x3_bwd_weight(const void* dy, const void* y, int32_t relu, const void* x1, int32_t c1, const void* x2,
                             int32_t c2, float* dw, float* db, float* work, int64_t work_floats, int32_t n, int32_t h,
-                            int32_t w, int32_t cout, void* stream) {
-    if (!dy || !x1 || !dw || !db || !work || (relu && !y) || (c2 > 0 && !x2) || !conv_shape_ok(c1, c2, n, h, w, cout))
+                            int32_t w, int32_t cout, int32_t* err, void* stream) {
+    if (!dy || !x1 || !dw || !db || !work || !err || (relu && !y) || (c2 > 0 && !x2) ||
+        !conv_shape_ok(c1, c2, n, h, w, cout))
         return GLGPU_E_ARG;
-    if (!aligned16(dy) || (y && !aligned16(y)) || !aligned16(x1) || (x2 && !aligned16(x2))) return GLGPU_E_ARG;
+    if (!aligned16(dy) || (y && !aligned16(y)) || !aligned16(x1) || (x2 && !aligned16(x2)) || !aligned16(work))
+        return GLGPU_E_ARG;
     const int cin = c1 + c2;
     const WPlan q = wplan(n, h, w, cin, cout);
-    if (work_floats < q.ws_floats + q.bias_floats) return GLGPU_E_ARG;
+    const WLayout L = wlayout(n, h, w, cin, cout);
+    if (work_floats < L.total) return GLGPU_E_ARG;
     const long long P = (long long)n * h * w;
     cudaStream_t s = (cudaStream_t)stream;
-    dim3 grid((unsigned)((cout + BM - 1) / BM), (unsigned)((9 * cin + BN - 1) / BN), (unsigned)q.nz);
-    float* bias_part = work + q.ws_floats;
-    if (relu) {
-        k_conv_bwd_weight<1><<<grid, NT, 0, s>>>((const bf16*)dy, (const bf16*)y, (const bf16*)x1, c1, (const bf16*)x2, c2, work, n, h, w, cout, q.chunk);
-        k_bias_partial<1><<<q.nbias, 256, 0, s>>>((const bf16*)dy, (const bf16*)y, (int)P, cout, bias_part);
+    float* bias_part = work + L.bias_off;
+    int nz = q.nz;
+    if (glnn_tc_wgrad(dy, y, relu, x1, c1, x2, c2, work, work + L.dym_off, n, h, w, cout, err, s)) {
+        int chunk_tc = 0;
+        glnn_tc_wgrad_plan(n, h, w, cin, cout, &nz, &chunk_tc);
     } else {
-        k_conv_bwd_weight<0><<<grid, NT, 0, s>>>((const bf16*)dy, (const bf16*)y, (const bf16*)x1, c1, (const bf16*)x2, c2, work, n, h, w, cout, q.chunk);
-        k_bias_partial<0><<<q.nbias, 256, 0, s>>>((const bf16*)dy, (const bf16*)y, (int)P, cout, bias_part);
+        dim3 grid((unsigned)((cout + BM - 1) / BM), (unsigned)((9 * cin + BN - 1) / BN), (unsigned)q.nz);
+        if (relu)
+            k_conv_bwd_weight<1><<<grid, NT, 0, s>>>((const bf16*)dy, (const bf16*)y, (const bf16*)x1, c1, (const bf16*)x2, c2, work, n, h, w, cout, q.chunk);
+        else
+            k_conv_bwd_weight<0><<<grid, NT, 0, s>>>((const bf16*)dy, (const bf16*)y, (const bf16*)x1, c1, (const bf16*)x2, c2, work, n, h, w, cout, q.chunk);
     }
+    if (relu)
+        k_bias_partial<1><<<q.nbias, 256, 0, s>>>((const bf16*)dy, (const bf16*)y, (int)P, cout, bias_part);
+    else
+        k_bias_partial<0><<<q.nbias, 256, 0, s>>>((const bf16*)dy, (const bf16*)y, (int)P, cout, bias_part);
     const long long size = (long long)cout * 9 * cin;
-    k_sum_splits<<<grid_for(size, 256), 256, 0, s>>>(work, q.nz, size, dw);
+    k_sum_splits<<<grid_for(size, 256), 256, 0, s>>>(work, nz, size, dw);
     k_bias_reduce<<<(cout + 127) / 128, 128, 0, s>>>(bias_part, q.nbias, cout, db);
     return ret(cudaGetLastError());
 }

@@ -433,6 +433,174 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+
+// ---------------------------------------------------------------------------
+// Weight gradient on tcgen05 with TMA operands: dW[co][tap][ci] =
+// sum_p dy'[p][co] x[p + off(tap)][ci] (dy' = dy * relu'(y), formed by
+// k_relu_mask_dy beforehand), as D[m][co] = sum_k A[m][k] B[k][co] with
+// M = 128 rows = (two taps, 64 input channels), N = 64 output channels and
+// K = pixels.  A K chunk of 64 pixels is three boxes of the 4-D activation
+// tensors, each 64 pixels x 64 channels: the input shifted by the pair's first
+// tap, the input shifted by its second tap, and dy'.  They land as pixel rows of
+// 128 bytes (64 channels) with the 128-byte swizzle, which is the MN-major
+// operand layout (M, resp. N, contiguous within a row; K = the row index): both
+// operands are MN-major in the instruction descriptor, the two tap boxes are the
+// two 64-row atoms of A along M (leading byte offset 8 KB), 8-row groups along K
+// are 1024 bytes apart, and a K step of 16 pixels advances the start by 2 KB.
+// Tap pairs (0,1) (2,3) (4,5) (6,7) (8,-): the last pair's second half is not
+// stored.  The pixel range is split over blockIdx.y (split-K); every CTA writes
+// its tile of partial sums to ws[split][co][tap][ci], which k_sum_splits reduces
+// in a fixed order.  Thread 0 issues the copies into a 4-stage ring, thread 32
+// the MMAs; every wait is bounded, and a CTA whose wait ran out writes NaN
+// partials (and sets *err), so the failure reaches dW.
+// ---------------------------------------------------------------------------
+constexpr int WG_PX = 64;                          // pixels per K chunk
+constexpr int WG_BOX = WG_PX * 64 * 2;             // one 64 x 64 bf16 box: 8 KB
+constexpr int WG_STAGE = 3 * WG_BOX;               // two tap boxes + dy': 24 KB
+constexpr int WG_STAGES = 4;
+constexpr int WG_SMEM = WG_STAGES * WG_STAGE + 1024 + 128;
+// kIdesc (M = 128, N = 64, bf16 -> f32) with A and B MN-major (bits 15, 16)
+constexpr uint32_t kIdescMN = kIdesc | (1u << 15) | (1u << 16);
+
+// SM100 shared-memory matrix descriptor, MN-major with the 128-byte swizzle:
+// leading byte offset = distance between 64-element atoms along M or N, stride
+// byte offset = distance between 8-row groups along K (1024 B here).
+__device__ __forceinline__ uint64_t smem_desc_sw128_mn(uint32_t start, uint32_t lbo) {
+    uint64_t d = (uint64_t)((start >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1u << 46;
+    d |= (uint64_t)2u << 61;
+    return d;
+}
+
+__global__ void __launch_bounds__(NTH)
+k_conv_wgrad_tma(const __grid_constant__ CUtensorMap tx1, const __grid_constant__ CUtensorMap tx2,
+                 const __grid_constant__ CUtensorMap tdy, float* __restrict__ ws, int C1, int C2, int Cout, int H,
+                 int W, int P, int chunk, int* err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + WG_STAGES * WG_STAGE);
+    uint64_t* empty = full + WG_STAGES;
+    uint64_t* done = empty + WG_STAGES;
+    uint32_t* tslot = (uint32_t*)(done + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int Cin = C1 + C2, nco = Cout / 64, nci = Cin / 64;
+    int t = blockIdx.x;
+    const int oc = t % nco;
+    t /= nco;
+    const int cc = t % nci, g = t / nci;  // input-channel chunk, tap pair
+    const int tap0 = 2 * g, tap1 = g < 4 ? 2 * g + 1 : 8;
+    const int pbeg = blockIdx.y * chunk, pend = min(P, pbeg + chunk);
+    const int nk = pend > pbeg ? (pend - pbeg) / WG_PX : 0;
+    const int c = cc * 64;
+    const CUtensorMap* xm = c < C1 ? &tx1 : &tx2;
+    const int cx = c < C1 ? c : c - C1;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int q = 0; q < WG_STAGES; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(full + q)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(empty + q)) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(done)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (nk > 0) {
+        if (tid == 0) {
+            const int dy0 = tap0 / 3 - 1, dx0 = tap0 % 3 - 1, dy1 = tap1 / 3 - 1, dx1 = tap1 % 3 - 1;
+            for (int kc = 0; kc < nk && ok; ++kc) {
+                const int st = kc % WG_STAGES, use = kc / WG_STAGES;
+                if (use > 0 && !wait_parity(saddr(empty + st), (uint32_t)((use + 1) & 1))) ok = false;
+                if (!ok) break;
+                const int p0 = pbeg + kc * WG_PX;
+                const int img = p0 / (H * W), rem = p0 - img * H * W, y0 = rem / W, x0 = rem - y0 * W;
+                const uint32_t dst = saddr(smem + st * WG_STAGE);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(full + st)),
+                             "r"((uint32_t)WG_STAGE)
+                             : "memory");
+                tma_load_4d(dst, xm, cx, x0 + dx0, y0 + dy0, img, saddr(full + st));
+                tma_load_4d(dst + WG_BOX, xm, cx, x0 + dx1, y0 + dy1, img, saddr(full + st));
+                tma_load_4d(dst + 2 * WG_BOX, &tdy, oc * 64, x0, y0, img, saddr(full + st));
+            }
+        } else if (tid == 32) {
+            for (int kc = 0; kc < nk && ok; ++kc) {
+                const int st = kc % WG_STAGES, use = kc / WG_STAGES;
+                if (!wait_parity(saddr(full + st), (uint32_t)(use & 1))) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t a0 = saddr(smem + st * WG_STAGE), b0 = a0 + 2 * WG_BOX;
+#pragma unroll
+                for (int j = 0; j < WG_PX / 16; ++j)
+                    mma_f16(tmem, smem_desc_sw128_mn(a0 + 2048 * j, WG_BOX), smem_desc_sw128_mn(b0 + 2048 * j, WG_BOX),
+                            kIdescMN, (kc > 0 || j > 0) ? 1u : 0u);
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 saddr(empty + st))
+                             : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             saddr(done))
+                         : "memory");
+        }
+        if (!wait_parity(saddr(done), 0u)) ok = false;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    }
+    if (__syncthreads_or(ok ? 0 : 1)) ok = false;
+    // TMEM lane m = warp * 32 + lane: tap (m < 64 ? tap0 : tap1), input channel c + m % 64
+    const int m = warp * 32 + lane;
+    const int tap = m < 64 ? tap0 : tap1;
+    const bool store = m < 64 || g < 4;
+    float* out = ws + (size_t)blockIdx.y * Cout * 9 * Cin + (size_t)tap * Cin + c + (m & 63);
+#pragma unroll
+    for (int col = 0; col < 64; col += 16) {
+        uint32_t r[16];
+        if (nk > 0) {
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)col)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        } else {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) r[q] = 0u;
+        }
+        if (store) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+                out[(size_t)(oc * 64 + col + q) * 9 * Cin] = ok ? __uint_as_float(r[q]) : __int_as_float(0x7fc00000);
+        }
+    }
+    if (!ok && tid == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+// dy' = dy * (y > 0), 8 bf16 per thread step
+__global__ void k_relu_mask_dy(const uint4* __restrict__ dy, const uint4* __restrict__ y, uint4* __restrict__ out,
+                               long long n8) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n8; i += (long long)gridDim.x * blockDim.x) {
+        const uint4 d = dy[i], v = y[i];
+        out[i] = make_uint4(relu_mask2(d.x, v.x), relu_mask2(d.y, v.y), relu_mask2(d.z, v.z), relu_mask2(d.w, v.w));
+    }
+}
+
 }  // namespace glnn_tc
 
 using namespace glnn_tc;
@@ -461,11 +629,12 @@ static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
     return fn;
 }
 
-// activations [n][h][w][c] (bf16), box = 64 channels x one 128-pixel tile
-static bool act_map(CUtensorMap* m, const void* base, int c, int n, int h, int w) {
+// activations [n][h][w][c] (bf16), box = 64 channels x one tile of `px` pixels
+// (whole rows or a run of one row)
+static bool act_map(CUtensorMap* m, const void* base, int c, int n, int h, int w, int px = TM) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
     if (!enc) return false;
-    const int wb = w < TM ? w : TM, hb = TM / wb;
+    const int wb = w < px ? w : px, hb = px / wb;
     cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
     cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
     cuuint32_t box[4] = {(cuuint32_t)TK, (cuuint32_t)wb, (cuuint32_t)hb, 1u};
@@ -519,6 +688,57 @@ static int conv_fwd_tma(const void* x1, int c1, const void* x2, int c2, const vo
         k_conv_fwd_tma<1><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, c1, c2, h, w, err);
     else
         k_conv_fwd_tma<0><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, c1, c2, h, w, err);
+    return 1;
+}
+
+// --- weight gradient on tcgen05 -----------------------------------------------
+// the shapes it takes: 64-channel chunks in and out, 64-pixel chunks that are runs
+// of one row (w a multiple of 64) or whole groups of rows (64 a multiple of w)
+static bool wgrad_tma_shape_ok(int c1, int c2, int h, int w, int cout) {
+    return c1 % 64 == 0 && c2 % 64 == 0 && cout % 64 == 0 && ((long long)h * w) % WG_PX == 0 &&
+           (w % WG_PX == 0 || WG_PX % w == 0);
+}
+
+// split-K plan: splits of whole 64-pixel chunks, about two CTAs per SM in all
+void glnn_tc_wgrad_plan(int n, int h, int w, int cin, int cout, int* nz, int* chunk) {
+    const long long P = (long long)n * h * w;
+    const long long tiles = 5LL * (cin / 64) * (cout / 64);
+    const long long nchunks = (P + WG_PX - 1) / WG_PX;
+    long long z = (2 * 152 + tiles - 1) / tiles;
+    z = z < 1 ? 1 : (z > nchunks ? nchunks : z);
+    const long long per = (nchunks + z - 1) / z;
+    *chunk = (int)(per * WG_PX);
+    *nz = (int)((P + *chunk - 1) / *chunk);
+}
+
+// 1: launched (dy' and the partial sums enqueued on s); 0: shape, tensor maps or
+// the switch rule it out (the caller runs the mma kernel)
+int glnn_tc_wgrad(const void* dy, const void* y, int relu, const void* x1, int c1, const void* x2, int c2, float* ws,
+                  void* dy_masked, int n, int h, int w, int cout, int* err, cudaStream_t s) {
+    if (!g_conv_tma || !err || !wgrad_tma_shape_ok(c1, c2, h, w, cout)) return 0;
+    const long long P = (long long)n * h * w;
+    const void* dsrc = dy;
+    if (relu) {
+        if (!dy_masked) return 0;
+        const long long n8 = P * cout / 8;
+        const long long blocks = (n8 + 255) / 256;
+        k_relu_mask_dy<<<(unsigned)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, s>>>(
+            (const uint4*)dy, (const uint4*)y, (uint4*)dy_masked, n8);
+        dsrc = dy_masked;
+    }
+    CUtensorMap t1, t2, td;
+    if (!act_map(&t1, x1, c1, n, h, w, WG_PX) || !act_map(&td, dsrc, cout, n, h, w, WG_PX)) return 0;
+    if (c2 > 0) {
+        if (!act_map(&t2, x2, c2, n, h, w, WG_PX)) return 0;
+    } else {
+        t2 = t1;
+    }
+    static cudaError_t attr = cudaFuncSetAttribute(k_conv_wgrad_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, WG_SMEM);
+    if (attr != cudaSuccess) return 0;
+    int nz = 0, chunk = 0;
+    glnn_tc_wgrad_plan(n, h, w, c1 + c2, cout, &nz, &chunk);
+    dim3 grid((unsigned)(5 * ((c1 + c2) / 64) * (cout / 64)), (unsigned)nz);
+    k_conv_wgrad_tma<<<grid, NTH, WG_SMEM, s>>>(t1, t2, td, ws, c1, c2, cout, h, w, (int)P, chunk, err);
     return 1;
 }
 

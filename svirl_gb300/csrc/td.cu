@@ -845,248 +845,266 @@ k_psi_sweep_cn(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, L
 }
 
 // One Jacobi sweep of the A step (svirl/cuda/td.h:310-463): each thread owns the
-// x link and the y link that start at its node.
+// x link and the y link that start at its node.  A CTA takes kARep consecutive
+// tiles (kThreads nodes each); tiles of one instance form a run that shares one
+// prologue, one block reduction and one set of atomics, so the fixed latency of a
+// CTA's life (the dependent loads of its descriptors, the atomics of the residual
+// and of the completion counts) is paid once per run instead of once per tile.
+constexpr int kARep = 4;
+__host__ __device__ inline int a_sweep_blocks(int ntiles) { return (ntiles + kARep - 1) / kARep; }
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, LoopState* loop,
+k_A_sweep(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int ntiles, LoopState* loop,
           cudaGraphConditionalHandle cond, int use_cond) {
-    const Tile t = tiles[blockIdx.x];
-    const Inst& I = insts[t.inst];
-    InstState* st = I.st;
     const int tid = threadIdx.x;
-    __shared__ int s_skip, s_k, s_R, s_P;
+    __shared__ int s_skip, s_k, s_R, s_P, s_run;
     __shared__ uint32_t s_rt;
-    if (tid == 0) {
-        s_skip = *(volatile int*)&st->done;
-        s_k = *(volatile int*)&st->sweep;
-        s_R = *(volatile int*)&st->rhsA;
-        s_P = *(volatile int*)&st->rhs;
-        s_rt = *(volatile uint32_t*)&st->rand_t;
-    }
-    __syncthreads();
-    if (!s_skip) {
-        const int k = s_k, R = s_R;
-        // FP32: the iterates are offsets delta = A - A^(0) from the loop's right-hand
-        // side (see the delta branch below); delta^(0) = 0
-        constexpr bool kDelta = sizeof(T) == 4;
-        const T* cur = (kDelta && k == 0) ? nullptr : (const T*)I.ab[buf_of(R, k)];
-        const T* rhs = (const T*)I.ab[R];
-        // with fixed vortices the supercurrent phases come from the irregular
-        // potential buffer, which holds A_irr + A^(0) on its first N elements
-        // (td.py:256-270), so there is no aliasing
-        const T* abi = I.vpi ? (const T*)I.vpi : (const T*)I.ab[k < 2 ? R : (R + 2) % 3];
-        T* nxt = (T*)I.ab[(R + 1 + (k & 1)) % 3];
-        const C2<T>* __restrict__ psi = (const C2<T>*)I.psi[s_P];
-        const Geo g = I.g;
-        const int n = t.n0 + tid;
-        // Per link, the update is (X + dt rho k2 dd nbs(A^(k))) / D, where the fixed part
-        // X (right-hand side, noise, boundary field, supercurrent) depends on k only
-        // through the supercurrent argument A^(2 floor(k/2)) (the fixed-vortex potential
-        // with fixed vortices, constant over the loop).  Sweeps that start a pair
-        // (`fresh`) compute X and store it; the other sweeps of the pair read it back,
-        // so the sincos, the psi loads and the right-hand side's neighbour loads are paid
-        // once per two sweeps.  X (and in FP32 the A^(0) part G of X, constant over the
-        // loop) live in the link-factor buffer U, which the A loop does not read and
-        // k_link_U rebuilds before the next psi loop.  Both are stored rounded (mul_rn
-        // keeps G out of a fused multiply-add), so a pair's two sweeps use equal values.
-        const bool fresh = k == 0 || (!I.vpi && (k & 1) == 0);
-        T* Xc = (T*)I.U;
-        T* Gc = Xc + g.Nab;
-        T res = T(0);
-        bool nan = false;
-        T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
-        bool has_a = false, has_b = false;
-        int na = 0, nb = 0;
-        if constexpr (kDelta) {
-            // The same Jacobi iteration as the FP64 branch, written for delta: with
-            // A^(k) = A^(0) + delta^(k) the update of a link is
-            //   delta' = (noise + dt rho (js + rh) + dt rho k2 (dd nbs(A^(0)) - 2 d^-2 A^(0))
-            //            + dt rho k2 dd nbs(delta^(k))) / D,
-            // and the stop rule's |A^(k+1) - A^(k)| = |delta^(k+1) - delta^(k)|.  In FP32 the
-            // iterates of A itself differ by whole units in the last place once |A| > 8
-            // (the Landau gauge reaches H L), which the absolute stop rule of 1e-6
-            // (svirl/solvers/td.py:53-57) never accepts; delta is small, so the loop
-            // converges.  The supercurrent phase is that of A^(0) + delta^(2 floor(k/2)).
-            if (n < g.N) {
-                const int i = n % g.Nx, j = n / g.Nx;
-                const int Nxa = g.Nx - 1, Na = g.Na;
-                has_a = i < g.Nx - 1;
-                has_b = j < g.Ny - 1;
-                na = i + Nxa * j;
-                nb = Na + i + g.Nx * j;
-                auto dl = [&](int m) -> T { return cur ? cur[m] : T(0); };
-                const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
-                const T k2 = I.fkappa2;
-                const T dt_rho_k2 = I.fdt * I.frho * k2;
-                T xa = T(0), xb = T(0);
-                if (fresh) {
-                    const T* al = (I.vpi || k < 2) ? nullptr : (const T*)I.ab[(R + 2) % 3];  // delta of the phase
-                    const T ph_a = has_a ? (I.vpi ? abi[na] : rhs[na] + (al ? al[na] : T(0))) : T(0);
-                    const T ph_b = has_b ? (I.vpi ? abi[nb] : rhs[nb] + (al ? al[nb] : T(0))) : T(0);
-                    const unsigned cb = cell_bits(g, I.mt, i, j);
-                    const C2<T> psi0 = psi[n];
-                    const T dx = GT(g, dx), dy = GT(g, dy);
-                    const T idx = GT(g, idx), idy = GT(g, idy);
-                    const T H = I.fH;
-                    const T dt_rho = I.fdt * I.frho;
-                    const T lc = I.flang_A;
-                    const bool lang = I.lang_A_on != 0;
-                    if (has_a) {
-                        const T noise = lang ? lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5)) : T(0);
-                        T rh = T(0), dd = T(1);
-                        if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
-                        else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
-                        T jl = T(0);
-                        if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
-                        T ga;
-                        if (k == 0) {
-                            T nr = T(0);
-                            if (j > 0)
-                                nr += idy2 * rhs[i + Nxa * (j - 1)] - idxy * rhs[Na + i + g.Nx * (j - 1)] +
-                                      idxy * rhs[Na + i + 1 + g.Nx * (j - 1)];
-                            if (j < g.Ny - 1)
-                                nr += idy2 * rhs[i + Nxa * (j + 1)] + idxy * rhs[Na + i + g.Nx * j] - idxy * rhs[Na + i + 1 + g.Nx * j];
-                            ga = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idy2 * rhs[na]);
-                            Gc[na] = ga;
+    const int tb = blockIdx.x * kARep;
+    for (int r = 0; r < kARep && tb + r < ntiles;) {
+        const Tile t = tiles[tb + r];
+        const Inst& I = insts[t.inst];
+        InstState* st = I.st;
+        if (tid == 0) {
+            int run = 1;
+            while (r + run < kARep && tb + r + run < ntiles && tiles[tb + r + run].inst == t.inst) ++run;
+            s_run = run;
+            s_skip = *(volatile int*)&st->done;
+            s_k = *(volatile int*)&st->sweep;
+            s_R = *(volatile int*)&st->rhsA;
+            s_P = *(volatile int*)&st->rhs;
+            s_rt = *(volatile uint32_t*)&st->rand_t;
+        }
+        __syncthreads();
+        const int run = s_run;
+        if (!s_skip) {
+            const int k = s_k, R = s_R;
+            // FP32: the iterates are offsets delta = A - A^(0) from the loop's right-hand
+            // side (see the delta branch below); delta^(0) = 0
+            constexpr bool kDelta = sizeof(T) == 4;
+            const T* cur = (kDelta && k == 0) ? nullptr : (const T*)I.ab[buf_of(R, k)];
+            const T* rhs = (const T*)I.ab[R];
+            // with fixed vortices the supercurrent phases come from the irregular
+            // potential buffer, which holds A_irr + A^(0) on its first N elements
+            // (td.py:256-270), so there is no aliasing
+            const T* abi = I.vpi ? (const T*)I.vpi : (const T*)I.ab[k < 2 ? R : (R + 2) % 3];
+            T* nxt = (T*)I.ab[(R + 1 + (k & 1)) % 3];
+            const C2<T>* __restrict__ psi = (const C2<T>*)I.psi[s_P];
+            const Geo g = I.g;
+            // Per link, the update is (X + dt rho k2 dd nbs(A^(k))) / D, where the fixed part
+            // X (right-hand side, noise, boundary field, supercurrent) depends on k only
+            // through the supercurrent argument A^(2 floor(k/2)) (the fixed-vortex potential
+            // with fixed vortices, constant over the loop).  Sweeps that start a pair
+            // (`fresh`) compute X and store it; the other sweeps of the pair read it back,
+            // so the sincos, the psi loads and the right-hand side's neighbour loads are paid
+            // once per two sweeps.  X (and in FP32 the A^(0) part G of X, constant over the
+            // loop) live in the link-factor buffer U, which the A loop does not read and
+            // k_link_U rebuilds before the next psi loop.  Both are stored rounded (mul_rn
+            // keeps G out of a fused multiply-add), so a pair's two sweeps use equal values.
+            const bool fresh = k == 0 || (!I.vpi && (k & 1) == 0);
+            T* Xc = (T*)I.U;
+            T* Gc = Xc + g.Nab;
+            T res = T(0);
+            bool nan = false;
+            for (int q = 0; q < run; ++q) {
+                const int n = t.n0 + tid + kThreads * q;
+                T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
+                bool has_a = false, has_b = false;
+                int na = 0, nb = 0;
+                if constexpr (kDelta) {
+                    // The same Jacobi iteration as the FP64 branch, written for delta: with
+                    // A^(k) = A^(0) + delta^(k) the update of a link is
+                    //   delta' = (noise + dt rho (js + rh) + dt rho k2 (dd nbs(A^(0)) - 2 d^-2 A^(0))
+                    //            + dt rho k2 dd nbs(delta^(k))) / D,
+                    // and the stop rule's |A^(k+1) - A^(k)| = |delta^(k+1) - delta^(k)|.  In FP32 the
+                    // iterates of A itself differ by whole units in the last place once |A| > 8
+                    // (the Landau gauge reaches H L), which the absolute stop rule of 1e-6
+                    // (svirl/solvers/td.py:53-57) never accepts; delta is small, so the loop
+                    // converges.  The supercurrent phase is that of A^(0) + delta^(2 floor(k/2)).
+                    if (n < g.N) {
+                        const int i = n % g.Nx, j = n / g.Nx;
+                        const int Nxa = g.Nx - 1, Na = g.Na;
+                        has_a = i < g.Nx - 1;
+                        has_b = j < g.Ny - 1;
+                        na = i + Nxa * j;
+                        nb = Na + i + g.Nx * j;
+                        auto dl = [&](int m) -> T { return cur ? cur[m] : T(0); };
+                        const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
+                        const T k2 = I.fkappa2;
+                        const T dt_rho_k2 = I.fdt * I.frho * k2;
+                        T xa = T(0), xb = T(0);
+                        if (fresh) {
+                            const T* al = (I.vpi || k < 2) ? nullptr : (const T*)I.ab[(R + 2) % 3];  // delta of the phase
+                            const T ph_a = has_a ? (I.vpi ? abi[na] : rhs[na] + (al ? al[na] : T(0))) : T(0);
+                            const T ph_b = has_b ? (I.vpi ? abi[nb] : rhs[nb] + (al ? al[nb] : T(0))) : T(0);
+                            const unsigned cb = cell_bits(g, I.mt, i, j);
+                            const C2<T> psi0 = psi[n];
+                            const T dx = GT(g, dx), dy = GT(g, dy);
+                            const T idx = GT(g, idx), idy = GT(g, idy);
+                            const T H = I.fH;
+                            const T dt_rho = I.fdt * I.frho;
+                            const T lc = I.flang_A;
+                            const bool lang = I.lang_A_on != 0;
+                            if (has_a) {
+                                const T noise = lang ? lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5)) : T(0);
+                                T rh = T(0), dd = T(1);
+                                if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
+                                else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
+                                T jl = T(0);
+                                if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
+                                T ga;
+                                if (k == 0) {
+                                    T nr = T(0);
+                                    if (j > 0)
+                                        nr += idy2 * rhs[i + Nxa * (j - 1)] - idxy * rhs[Na + i + g.Nx * (j - 1)] +
+                                              idxy * rhs[Na + i + 1 + g.Nx * (j - 1)];
+                                    if (j < g.Ny - 1)
+                                        nr += idy2 * rhs[i + Nxa * (j + 1)] + idxy * rhs[Na + i + g.Nx * j] - idxy * rhs[Na + i + 1 + g.Nx * j];
+                                    ga = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idy2 * rhs[na]);
+                                    Gc[na] = ga;
+                                } else {
+                                    ga = Gc[na];
+                                }
+                                xa = noise + dt_rho * (jl + rh) + ga;
+                                Xc[na] = xa;
+                            }
+                            if (has_b) {
+                                const T noise = lang ? lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5)) : T(0);
+                                T rh = T(0), dd = T(1);
+                                if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
+                                else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
+                                T jl = T(0);
+                                if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
+                                T gb;
+                                if (k == 0) {
+                                    T nr = T(0);
+                                    if (i > 0)
+                                        nr += idx2 * rhs[Na + (i - 1) + g.Nx * j] - idxy * rhs[(i - 1) + Nxa * j] + idxy * rhs[(i - 1) + Nxa * (j + 1)];
+                                    if (i < g.Nx - 1)
+                                        nr += idx2 * rhs[Na + (i + 1) + g.Nx * j] + idxy * rhs[i + Nxa * j] - idxy * rhs[i + Nxa * (j + 1)];
+                                    gb = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idx2 * rhs[nb]);
+                                    Gc[nb] = gb;
+                                } else {
+                                    gb = Gc[nb];
+                                }
+                                xb = noise + dt_rho * (jl + rh) + gb;
+                                Xc[nb] = xb;
+                            }
                         } else {
-                            ga = Gc[na];
+                            if (has_a) xa = Xc[na];
+                            if (has_b) xb = Xc[nb];
                         }
-                        xa = noise + dt_rho * (jl + rh) + ga;
-                        Xc[na] = xa;
+                        if (has_a) {
+                            const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
+                            T nd = T(0);
+                            if (j > 0) nd += idy2 * dl(i + Nxa * (j - 1)) - idxy * dl(Na + i + g.Nx * (j - 1)) + idxy * dl(Na + i + 1 + g.Nx * (j - 1));
+                            if (j < g.Ny - 1) nd += idy2 * dl(i + Nxa * (j + 1)) + idxy * dl(Na + i + g.Nx * j) - idxy * dl(Na + i + 1 + g.Nx * j);
+                            va = (xa + dt_rho_k2 * dd * nd) / (T(1) + T(2) * dt_rho_k2 * idy2);
+                            ca = dl(na);
+                        }
+                        if (has_b) {
+                            const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
+                            T nd = T(0);
+                            if (i > 0) nd += idx2 * dl(Na + (i - 1) + g.Nx * j) - idxy * dl((i - 1) + Nxa * j) + idxy * dl((i - 1) + Nxa * (j + 1));
+                            if (i < g.Nx - 1) nd += idx2 * dl(Na + (i + 1) + g.Nx * j) + idxy * dl(i + Nxa * j) - idxy * dl(i + Nxa * (j + 1));
+                            vb = (xb + dt_rho_k2 * dd * nd) / (T(1) + T(2) * dt_rho_k2 * idx2);
+                            cbv = dl(nb);
+                        }
+                    }
+                } else
+                if (n < g.N) {
+                    const int i = n % g.Nx, j = n / g.Nx;
+                    const int Nxa = g.Nx - 1, Na = g.Na;
+                    has_a = i < g.Nx - 1;
+                    has_b = j < g.Ny - 1;
+                    na = i + Nxa * j;
+                    nb = Na + i + g.Nx * j;
+                    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
+                    const T k2 = gsel<T>(I.kappa2, I.fkappa2);
+                    const T dt_rho = gsel<T>(I.dt, I.fdt) * gsel<T>(I.rho, I.frho);
+                    const T dt_rho_k2 = dt_rho * k2;
+                    T xa = T(0), xb = T(0);
+                    if (fresh) {
+                        // read the supercurrent phases before anything is stored (aliasing, see top)
+                        const T ph_a = has_a ? abi[na] : T(0);
+                        const T ph_b = has_b ? abi[nb] : T(0);
+                        const unsigned cb = cell_bits(g, I.mt, i, j);
+                        const C2<T> psi0 = psi[n];
+                        const T dx = GT(g, dx), dy = GT(g, dy);
+                        const T idx = GT(g, idx), idy = GT(g, idy);
+                        const T H = gsel<T>(I.H, I.fH);
+                        const T lc = gsel<T>(I.lang_A, I.flang_A);
+                        const bool lang = I.lang_A_on != 0;
+                        if (has_a) {
+                            T r = rhs[na];
+                            if (lang) r += lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5));
+                            T rh = T(0);
+                            if (j == 0) rh = T(2) * k2 * H * idy;
+                            else if (j == g.Ny - 1) rh = -T(2) * k2 * H * idy;
+                            T jl = T(0);
+                            if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
+                            xa = r + dt_rho * (jl + rh);
+                            Xc[na] = xa;
+                        }
+                        if (has_b) {
+                            T r = rhs[nb];
+                            if (lang) r += lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5));
+                            T rh = T(0);
+                            if (i == 0) rh = -T(2) * k2 * H * idx;
+                            else if (i == g.Nx - 1) rh = T(2) * k2 * H * idx;
+                            T jl = T(0);
+                            if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
+                            xb = r + dt_rho * (jl + rh);
+                            Xc[nb] = xb;
+                        }
+                    } else {
+                        if (has_a) xa = Xc[na];
+                        if (has_b) xb = Xc[nb];
+                    }
+                    if (has_a) {
+                        const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
+                        T nbs = T(0);
+                        if (j > 0) nbs += idy2 * cur[i + Nxa * (j - 1)] - idxy * cur[Na + i + g.Nx * (j - 1)] + idxy * cur[Na + i + 1 + g.Nx * (j - 1)];
+                        if (j < g.Ny - 1) nbs += idy2 * cur[i + Nxa * (j + 1)] + idxy * cur[Na + i + g.Nx * j] - idxy * cur[Na + i + 1 + g.Nx * j];
+                        va = (xa + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idy2);
+                        ca = cur[na];
                     }
                     if (has_b) {
-                        const T noise = lang ? lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5)) : T(0);
-                        T rh = T(0), dd = T(1);
-                        if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
-                        else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
-                        T jl = T(0);
-                        if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
-                        T gb;
-                        if (k == 0) {
-                            T nr = T(0);
-                            if (i > 0)
-                                nr += idx2 * rhs[Na + (i - 1) + g.Nx * j] - idxy * rhs[(i - 1) + Nxa * j] + idxy * rhs[(i - 1) + Nxa * (j + 1)];
-                            if (i < g.Nx - 1)
-                                nr += idx2 * rhs[Na + (i + 1) + g.Nx * j] + idxy * rhs[i + Nxa * j] - idxy * rhs[i + Nxa * (j + 1)];
-                            gb = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idx2 * rhs[nb]);
-                            Gc[nb] = gb;
-                        } else {
-                            gb = Gc[nb];
-                        }
-                        xb = noise + dt_rho * (jl + rh) + gb;
-                        Xc[nb] = xb;
+                        const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
+                        T nbs = T(0);
+                        if (i > 0) nbs += idx2 * cur[Na + (i - 1) + g.Nx * j] - idxy * cur[(i - 1) + Nxa * j] + idxy * cur[(i - 1) + Nxa * (j + 1)];
+                        if (i < g.Nx - 1) nbs += idx2 * cur[Na + (i + 1) + g.Nx * j] + idxy * cur[i + Nxa * j] - idxy * cur[i + Nxa * (j + 1)];
+                        vb = (xb + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idx2);
+                        cbv = cur[nb];
                     }
-                } else {
-                    if (has_a) xa = Xc[na];
-                    if (has_b) xb = Xc[nb];
                 }
-                if (has_a) {
-                    const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
-                    T nd = T(0);
-                    if (j > 0) nd += idy2 * dl(i + Nxa * (j - 1)) - idxy * dl(Na + i + g.Nx * (j - 1)) + idxy * dl(Na + i + 1 + g.Nx * (j - 1));
-                    if (j < g.Ny - 1) nd += idy2 * dl(i + Nxa * (j + 1)) + idxy * dl(Na + i + g.Nx * j) - idxy * dl(Na + i + 1 + g.Nx * j);
-                    va = (xa + dt_rho_k2 * dd * nd) / (T(1) + T(2) * dt_rho_k2 * idy2);
-                    ca = dl(na);
-                }
-                if (has_b) {
-                    const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
-                    T nd = T(0);
-                    if (i > 0) nd += idx2 * dl(Na + (i - 1) + g.Nx * j) - idxy * dl((i - 1) + Nxa * j) + idxy * dl((i - 1) + Nxa * (j + 1));
-                    if (i < g.Nx - 1) nd += idx2 * dl(Na + (i + 1) + g.Nx * j) + idxy * dl(i + Nxa * j) - idxy * dl(i + Nxa * (j + 1));
-                    vb = (xb + dt_rho_k2 * dd * nd) / (T(1) + T(2) * dt_rho_k2 * idx2);
-                    cbv = dl(nb);
+                if (n < g.N) {
+                    if (has_a) {
+                        nxt[na] = va;
+                        T d = fabs(va - ca);
+                        if (d == d) { if (d > res) res = d; } else nan = true;
+                    }
+                    if (has_b) {
+                        nxt[nb] = vb;
+                        T d = fabs(vb - cbv);
+                        if (d == d) { if (d > res) res = d; } else nan = true;
+                    }
                 }
             }
-        } else
-        if (n < g.N) {
-            const int i = n % g.Nx, j = n / g.Nx;
-            const int Nxa = g.Nx - 1, Na = g.Na;
-            has_a = i < g.Nx - 1;
-            has_b = j < g.Ny - 1;
-            na = i + Nxa * j;
-            nb = Na + i + g.Nx * j;
-            const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
-            const T k2 = gsel<T>(I.kappa2, I.fkappa2);
-            const T dt_rho = gsel<T>(I.dt, I.fdt) * gsel<T>(I.rho, I.frho);
-            const T dt_rho_k2 = dt_rho * k2;
-            T xa = T(0), xb = T(0);
-            if (fresh) {
-                // read the supercurrent phases before anything is stored (aliasing, see top)
-                const T ph_a = has_a ? abi[na] : T(0);
-                const T ph_b = has_b ? abi[nb] : T(0);
-                const unsigned cb = cell_bits(g, I.mt, i, j);
-                const C2<T> psi0 = psi[n];
-                const T dx = GT(g, dx), dy = GT(g, dy);
-                const T idx = GT(g, idx), idy = GT(g, idy);
-                const T H = gsel<T>(I.H, I.fH);
-                const T lc = gsel<T>(I.lang_A, I.flang_A);
-                const bool lang = I.lang_A_on != 0;
-                if (has_a) {
-                    T r = rhs[na];
-                    if (lang) r += lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5));
-                    T rh = T(0);
-                    if (j == 0) rh = T(2) * k2 * H * idy;
-                    else if (j == g.Ny - 1) rh = -T(2) * k2 * H * idy;
-                    T jl = T(0);
-                    if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
-                    xa = r + dt_rho * (jl + rh);
-                    Xc[na] = xa;
+            T bmax = block_max_res<T>(res, nan);
+            if (tid == 0) {
+                if (bmax < T(0)) {
+                    atomicOr(&st->nan_seen, 1);
+                    bmax = -(bmax + T(1));
                 }
-                if (has_b) {
-                    T r = rhs[nb];
-                    if (lang) r += lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5));
-                    T rh = T(0);
-                    if (i == 0) rh = -T(2) * k2 * H * idx;
-                    else if (i == g.Nx - 1) rh = T(2) * k2 * H * idx;
-                    T jl = T(0);
-                    if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
-                    xb = r + dt_rho * (jl + rh);
-                    Xc[nb] = xb;
-                }
-            } else {
-                if (has_a) xa = Xc[na];
-                if (has_b) xb = Xc[nb];
-            }
-            if (has_a) {
-                const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
-                T nbs = T(0);
-                if (j > 0) nbs += idy2 * cur[i + Nxa * (j - 1)] - idxy * cur[Na + i + g.Nx * (j - 1)] + idxy * cur[Na + i + 1 + g.Nx * (j - 1)];
-                if (j < g.Ny - 1) nbs += idy2 * cur[i + Nxa * (j + 1)] + idxy * cur[Na + i + g.Nx * j] - idxy * cur[Na + i + 1 + g.Nx * j];
-                va = (xa + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idy2);
-                ca = cur[na];
-            }
-            if (has_b) {
-                const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
-                T nbs = T(0);
-                if (i > 0) nbs += idx2 * cur[Na + (i - 1) + g.Nx * j] - idxy * cur[(i - 1) + Nxa * j] + idxy * cur[(i - 1) + Nxa * (j + 1)];
-                if (i < g.Nx - 1) nbs += idx2 * cur[Na + (i + 1) + g.Nx * j] + idxy * cur[i + Nxa * j] - idxy * cur[i + Nxa * (j + 1)];
-                vb = (xb + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idx2);
-                cbv = cur[nb];
+                atomicMax(&st->res, res_bits(bmax));
+                __threadfence();
+                unsigned prev = atomicAdd(&st->blocks_done, (unsigned)run);
+                if (prev + (unsigned)run == (unsigned)I.ntiles) finish_instance_A<T>(I, loop, k);
             }
         }
-        if (n < g.N) {
-            if (has_a) {
-                nxt[na] = va;
-                T d = fabs(va - ca);
-                if (d == d) res = d; else nan = true;
-            }
-            if (has_b) {
-                nxt[nb] = vb;
-                T d = fabs(vb - cbv);
-                if (d == d) { if (d > res) res = d; } else nan = true;
-            }
-        }
-        T bmax = block_max_res<T>(res, nan);
-        if (tid == 0) {
-            if (bmax < T(0)) {
-                atomicOr(&st->nan_seen, 1);
-                bmax = -(bmax + T(1));
-            }
-            atomicMax(&st->res, res_bits(bmax));
-            __threadfence();
-            unsigned prev = atomicAdd(&st->blocks_done, 1u);
-            if (prev == (unsigned)I.ntiles - 1u) finish_instance_A<T>(I, loop, k);
-        }
+        r += run;
+        __syncthreads();  // the run's shared values are read before the next run sets them
     }
     if (tid == 0) {
         __threadfence();
@@ -1454,8 +1472,9 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         prev = nd;
         {
             cudaGraphNode_t sw;
-            void* a[] = {&insts, &tiles, &loop, &hA, &one};
-            GCHK(add_kernel(abody, &sw, nullptr, 0, A_sweep_fn(L.dtype), gt, bt, a));
+            int ntiles = L.ntiles;
+            void* a[] = {&insts, &tiles, &ntiles, &loop, &hA, &one};
+            GCHK(add_kernel(abody, &sw, nullptr, 0, A_sweep_fn(L.dtype), dim3(a_sweep_blocks(L.ntiles)), bt, a));
         }
         if (L.dtype == 4) {
             void* a[] = {&insts, &tiles};
@@ -1536,8 +1555,9 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
                     } else if (part == 0) {
                         launch_psi_sweep(L.psi_kind, L.strip_rows, L.psi_grid, s, L.insts, L.items, L.nitems, L.loop);
                     } else {
-                        if (L.dtype == 8) k_A_sweep<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
-                        else k_A_sweep<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, L.loop, none, 0);
+                        const int ab = a_sweep_blocks(L.ntiles);
+                        if (L.dtype == 8) k_A_sweep<double><<<ab, kThreads, 0, s>>>(L.insts, L.tiles, L.ntiles, L.loop, none, 0);
+                        else k_A_sweep<float><<<ab, kThreads, 0, s>>>(L.insts, L.tiles, L.ntiles, L.loop, none, 0);
                     }
                 }
                 cudaError_t e = cudaMemcpyAsync(&cont, &L.loop->cont, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -1628,8 +1648,9 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
                 launch_psi_sweep(psi_kind(h->dtype, h->psi_select), h->strip_rows, h->psi_grid, h->stream, h->inst, h->items,
                                  h->nitems, h->loop);
             } else {
-                if (h->dtype == 8) k_A_sweep<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
-                else k_A_sweep<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->loop, none, 0);
+                const int ab = a_sweep_blocks(h->ntiles);
+                if (h->dtype == 8) k_A_sweep<double><<<ab, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->ntiles, h->loop, none, 0);
+                else k_A_sweep<float><<<ab, kThreads, 0, h->stream>>>(h->inst, h->tiles, h->ntiles, h->loop, none, 0);
             }
             cudaEventRecord(e1, h->stream);
             e = cudaEventSynchronize(e1);

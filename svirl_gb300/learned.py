@@ -7,8 +7,9 @@ svirl/solvers/cg.py).
 
 Compute: every convolution, pooling/upsampling, the loss and the optimiser step
 run in the hand-written kernels of ``include/glgpu_nn.h`` (BF16 implicit GEMMs
-on the tensor cores with FP32 accumulation: tcgen05 with tensor memory for the
-forward pass and the data gradient, mma for the weight gradient); PyTorch
+on the tensor cores with FP32 accumulation: tcgen05 with tensor memory, the
+operands of the forward pass and the weight gradient loaded by TMA; mma.sync for
+weight gradients of shapes the tcgen05 kernel does not take); PyTorch
 supplies device tensors, the stream and the autograd bookkeeping
 (``torch.autograd.Function`` wrappers).
 
@@ -119,7 +120,8 @@ class Conv3x3(torch.autograd.Function):
         nwork = int(lib.glnn_conv3x3_bwd_weight_work(n, h, wd, c1 + c2, cout))
         work = torch.empty((nwork,), dtype=torch.float32, device=dy.device)
         _ok(lib.glnn_conv3x3_bwd_weight(_ptr(dy), _ptr(y), relu, _ptr(x1), c1, _ptr(x2), c2, _ptr(dw), _ptr(db),
-                                        _ptr(work), nwork, n, h, wd, cout, s), "conv3x3_bwd_weight")
+                                        _ptr(work), nwork, n, h, wd, cout, _ptr(_err_flag(dy.device)), s),
+            "conv3x3_bwd_weight")
         return dx1, dx2, dw, db, None
 
 
@@ -522,36 +524,30 @@ def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=
 
 
 def states_throughput(net, insts, Estar, cache, cap=4000, gtol=1e-4, tol=1e-6, plain_sample=8, mode="amplitude",
-                      rtol=0.0, gtol_abs=True):
+                      rtol=0.0, gtol_abs=True, dtypes=(np.float32, np.float64)):
     """Relaxed states per second, the learned + batched method against the plain
     one, with one stop rule for both (gradient norm `gtol`, absolute or relative to
     the first iteration's, energy ratio `rtol`, or `cap` iterations) and one
     criterion: a state counts when |F - F*|/|F*| <= tol, F* the FP64 energy of a
     tight relaxation of the same instance from the same initial state (the random
     start for the plain arm, `Estar`; the network's prediction for the learned arm,
-    computed here before the timed run).  Against the random start's F* the
+    computed here before the timed runs).  Against the random start's F* the
     learned states are also counted (`ok_vs_random_start`), and those that end
     below it, in another (lower) vortex minimum, reported (`lower_energy`).
-    Learned + batched (timed end to end): features to the device, the network's
-    prediction, decoding, the predicted states into the handles, the batched FP32
-    device CG of all instances, the states back to the host.  Plain: the same
-    device CG on one instance at a time in FP64 from its random start, on the
-    first `plain_sample` instances."""
+    Learned + batched (timed end to end), once per CG precision in `dtypes`:
+    features to the device, the network's prediction, decoding, the predicted
+    states into the handles, the batched device CG of all instances, the states
+    back to the host.  FP32 trajectories leave the FP64 one of the same start at
+    bifurcations and can end in another minimum; the FP64 arm follows the
+    arithmetic of F*.  Plain: the same device CG on one instance at a time in FP64
+    from its random start, on the first `plain_sample` instances.  Returns the
+    first precision's numbers at the top level and every precision under
+    "by_dtype"."""
     import time as _time
     from .relax import energies_fp64, relax
     # untimed: F* of each predicted start (the prediction is deterministic)
     starts0 = decode(insts, net.predict(features(insts)), mode=mode)
     Estar_pred = reference_energies(insts, cache, starts=starts0)
-    torch.cuda.synchronize()
-    t0 = _time.perf_counter()
-    pred = net.predict(features(insts))
-    starts = decode(insts, pred, mode=mode)
-    out, states, _ = relax(insts, cache, np.float32, starts=starts, n_iter=cap, gtol=gtol, gtol_abs=gtol_abs, rtol=rtol)
-    wall = _time.perf_counter() - t0
-    E = energies_fp64(insts, states, cache)
-    rel_pred = (E - Estar_pred) / np.abs(Estar_pred)
-    rel = (E - Estar) / np.abs(Estar)
-    ok = int((np.abs(rel_pred) <= tol).sum())
     t_plain, ok_plain, low_plain = 0.0, 0, 0
     for q, it in enumerate(insts[:plain_sample]):
         t1 = _time.perf_counter()
@@ -560,14 +556,29 @@ def states_throughput(net, insts, Estar, cache, cap=4000, gtol=1e-4, tol=1e-6, p
         r1 = (energies_fp64([it], st, cache)[0] - Estar[q]) / abs(Estar[q])
         ok_plain += int(abs(r1) <= tol)
         low_plain += int(r1 < -tol)
-    rate = ok / wall
     plain_rate = ok_plain / t_plain if t_plain > 0 else 0.0
-    return {"states_per_s": rate, "ok": ok, "n": len(insts), "wall_s": wall, "cg_ms": out["ms"],
+    plain = {"states_per_s": plain_rate, "ok": ok_plain, "sample": min(plain_sample, len(insts)),
+             "lower_energy": low_plain, "wall_s": t_plain}
+    by = {}
+    for dt in dtypes:
+        torch.cuda.synchronize()
+        t0 = _time.perf_counter()
+        pred = net.predict(features(insts))
+        starts = decode(insts, pred, mode=mode)
+        out, states, _ = relax(insts, cache, dt, starts=starts, n_iter=cap, gtol=gtol, gtol_abs=gtol_abs, rtol=rtol)
+        wall = _time.perf_counter() - t0
+        E = energies_fp64(insts, states, cache)
+        rel_pred = (E - Estar_pred) / np.abs(Estar_pred)
+        rel = (E - Estar) / np.abs(Estar)
+        ok = int((np.abs(rel_pred) <= tol).sum())
+        rate = ok / wall
+        by[np.dtype(dt).name] = {
+            "states_per_s": rate, "ok": ok, "n": len(insts), "wall_s": wall, "cg_ms": out["ms"],
             "cg_iters_median": float(np.median(out["iters"])),
             "ok_vs_random_start": int((np.abs(rel) <= tol).sum()), "lower_energy": int((rel < -tol).sum()),
             "rel_err_quantiles": np.quantile(rel_pred, [0, 0.5, 0.9, 1]).tolist(),
             "rel_err_vs_random_start_quantiles": np.quantile(rel, [0, 0.5, 0.9, 1]).tolist(),
-            "plain": {"states_per_s": plain_rate, "ok": ok_plain, "sample": min(plain_sample, len(insts)),
-                      "lower_energy": low_plain, "wall_s": t_plain},
-            "speedup_vs_plain": rate / plain_rate if plain_rate > 0 else None,
-            "cap": cap, "gtol": gtol, "gtol_abs": gtol_abs, "rtol": rtol}
+            "speedup_vs_plain": rate / plain_rate if plain_rate > 0 else None}
+    first = dict(by[np.dtype(dtypes[0]).name])
+    first.update({"plain": plain, "by_dtype": by, "cap": cap, "gtol": gtol, "gtol_abs": gtol_abs, "rtol": rtol})
+    return first

@@ -174,3 +174,44 @@ def test_batch_cg_independent_of_batch_at_every_tile_depth():
             assert np.array_equal(h.get_psi(), states[q][0]) and np.array_equal(h.get_ab(), states[q][1])
     finally:
         cache.close()
+
+
+def test_batch_cg_energy_window_stop():
+    """FP32 instances with an unreachable gradient tolerance: the energy-window
+    stop ends each run at a multiple of the window (status 5) before the cap, and
+    the state it returns is the state of a run capped at the same iteration count
+    (bitwise); with the window off the runs reach the cap (status 3)."""
+    from svirl_gb300 import learned as L
+    from svirl_gb300.batch import HandleBatch
+    from svirl_gb300.relax import HandleCache
+    rng = np.random.default_rng(3)
+    insts = [L.Instance.sample(n, rng, kappa_range=(4.0, 4.0)) for n in (48, 64)]
+    cache = HandleCache()
+    try:
+        def run(n_iter, window):
+            hs = [cache.get(it.n, np.float32) for it in insts]
+            try:
+                for it, h in zip(insts, hs):
+                    it.load_into(h)
+                b = HandleBatch(hs)
+                b.set_cg_window(window, 1e-7)
+                o = b.cg_device(n_iter=n_iter, rtol=0.0, gtol=1e-12, exact_boundary=True)
+                st = [(h.get_psi(), h.get_ab()) for h in hs]
+                b.close()
+                return o, st
+            finally:
+                for h in hs:
+                    cache.put(h)
+        cap = 20000
+        ow, sw = run(cap, 100)
+        assert np.all(ow["status"] == 5), ow["status"]
+        assert np.all(ow["iters"] % 100 == 0) and np.all(ow["iters"] < cap)
+        for q in range(len(insts)):
+            oc, sc = run(int(ow["iters"][q]), 0)
+            assert oc["status"][q] == 3 and oc["iters"][q] == ow["iters"][q]
+            assert oc["energy"][q] == ow["energy"][q]
+            assert np.array_equal(sc[q][0], sw[q][0]) and np.array_equal(sc[q][1], sw[q][1])
+        o0, _ = run(300, 0)
+        assert np.all(o0["status"] == 3) and np.all(o0["iters"] == 300)
+    finally:
+        cache.close()

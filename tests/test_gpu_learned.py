@@ -39,5 +39,7 @@ def test_trained_network_gain_is_measured():
     # the throughput comparison counts states by the same criterion on both arms
     assert 0 <= thr["ok"] <= thr["n"] and 0 <= thr["plain"]["ok"] <= thr["plain"]["sample"]
     assert thr["wall_s"] > 0 and thr["plain"]["wall_s"] > 0
+    # the FP64 arm follows the arithmetic of F* (FP64 from the same predicted start)
+    assert thr["by_dtype"]["float64"]["ok"] >= thr["n"] // 2, thr["by_dtype"]["float64"]
     print("learned warm start (64^2):", res)
     print("learned + batched states/s (64^2):", thr)
