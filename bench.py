@@ -369,6 +369,37 @@ def run_states(args):
     cache.close()
 
 
+def run_cg(args):
+    """Batched device CG iterations of the field sweep's first `instances`
+    instances (FP32 stencils, FP64 reductions, exact-boundary gradient), `steps`
+    iterations from the random start with every stop test off: device time per
+    iteration and node-iterations/s.  Algorithmic bytes per node-iteration (FP32):
+    gradient (read psi 8, A 8, write g 16), direction and line-search sums (read g
+    16, previous direction 16, psi 8, A 8, write the direction 16), update and
+    energy (read psi 8, A 8, direction 16, write psi 8, A 8) = 144 B."""
+    from svirl_gb300 import relax as RX
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    insts = states_instances(args.instances)
+    nodes = sum(it.n * it.n for it in insts)
+    cache = RX.HandleCache()
+    RX.relax(insts, cache, np.float32, n_iter=max(args.warmup, 3), gtol=0.0, fetch=False, graphs=not args.no_graphs)
+    out, _, _ = RX.relax(insts, cache, np.float32, n_iter=args.steps, gtol=0.0, fetch=False, graphs=not args.no_graphs)
+    cache.close()
+    ms_it = out["ms"] / args.steps
+    peak, peak_kind = peaks()
+    alg = nodes * 144 / (ms_it * 1e-3) / 1e9
+    line = {"metric": "batched CG node-iterations/s (FP32, field sweep)", "value": nodes / (ms_it * 1e-3),
+            "unit": "node-iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": ms_it, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 stencils, f64 reductions", "data": "synthetic (seeded)",
+            "config": {"workload": "batched_cg_iterations", "instances": len(insts), "nodes_total": nodes,
+                       "graphs": not args.no_graphs},
+            "roofline": {"bound": "hbm", "achieved": alg, "peak": peak, "unit": "GB/s", "frac": alg / peak,
+                         "bytes_per_node_iteration": 144, "peak_kind": peak_kind, "traffic": None}}
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args):
     """Poisson-arriving requests (mean 200/s), n ~ U{64..512}, kappa finite or inf,
     fp32 or fp64, TDGL 500 steps then CG; throughput and latency percentiles."""
@@ -604,7 +635,7 @@ def main():
                     help="FP32 psi sweep kernel (0 register strip, 1 bulk-copy ring); default: the autotuner's choice")
     ap.add_argument("--no-graphs", action="store_true",
                     help="host-driven Jacobi loop (same kernels); ncu cannot profile kernels inside conditional graphs")
-    ap.add_argument("--workload", choices=["tdgl", "states", "serve", "learned", "c1", "conv"], default="tdgl",
+    ap.add_argument("--workload", choices=["tdgl", "states", "serve", "learned", "c1", "conv", "cg"], default="tdgl",
                     help="tdgl: node-steps/s on the 2049^2 domain; states: relaxed states/s of a batched sweep; "
                          "serve: the serving loop; learned: the learned CG warm start")
     ap.add_argument("--train-states", type=int, default=20000)
@@ -636,6 +667,9 @@ def main():
         return
     if args.workload == "conv":
         run_conv(args)
+        return
+    if args.workload == "cg":
+        run_cg(args)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -51,10 +51,22 @@ static int cg_rep_of(int N) {
     return 2;
 }
 // Resident CTAs per SM asked of the compiler for the two stencil-heavy FP32 CG
-// kernels (caps their registers at 65536 / (kThreads * GLGPU_CG_MINB)).
+// kernels (caps their registers at 65536 / (kThreads * minimum CTAs)), per kernel.
 #ifndef GLGPU_CG_MINB
 #define GLGPU_CG_MINB 4
 #endif
+#ifndef GLGPU_CG_MINB_GRAD
+#define GLGPU_CG_MINB_GRAD GLGPU_CG_MINB
+#endif
+#ifndef GLGPU_CG_MINB_COEF
+#define GLGPU_CG_MINB_COEF GLGPU_CG_MINB
+#endif
+// nodes of a tile whose line-search terms one thread computes together (1: one
+// node at a time)
+#ifndef GLGPU_CG_COEF_UNROLL
+#define GLGPU_CG_COEF_UNROLL 1
+#endif
+constexpr int kCoefUnroll = GLGPU_CG_COEF_UNROLL;
 
 struct CGLoop {
     int active;
@@ -219,7 +231,7 @@ __device__ __forceinline__ void grad_tile(const Inst& I, int n0, int rep, const 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB : 1)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB_GRAD : 1)
 kb_grad(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop) {
     const CGTile t = tiles[blockIdx.x];
     const Inst& I = insts[t.inst];
@@ -468,7 +480,7 @@ __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, int rep, T 
     auto psi_at = [&](int m) -> C2<T> { return psi[m]; };
     auto phase = [&](int l) -> T { return link_phase(abei, ab, l); };
     const T eps0 = gsel<T>(I.epsilon, I.fepsilon), H = gsel<T>(I.H, I.fH);
-#pragma unroll 1
+#pragma unroll kCoefUnroll
     for (int r = 0; r < rep; ++r) {
         const int n = n0 + threadIdx.x + r * kThreads;
         if (n < g.N) {
@@ -493,7 +505,7 @@ __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, int rep, T 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB : 1)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB_COEF : 1)
 kb_dir_coef(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double* __restrict__ partials,
             CGLoop* loop) {
     const CGTile t = tiles[blockIdx.x];

@@ -206,30 +206,68 @@ __global__ void k_sum_splits(const float* __restrict__ ws, int nz, long long siz
     }
 }
 
-// bias gradient, stage 1: per block of kBiasRows pixels and per channel
-constexpr int kBiasRows = 256;
+// bias gradient, stage 1: per block of kBiasRows pixels, per channel.  Thread
+// (lane of pixels pl, channel group cg) adds 8 channels (one 16-byte load of dy,
+// and of y for the ReLU derivative) of pixels pl, pl + lanes, ...; the pixel
+// lanes' sums are then added in a fixed order in shared memory.
+constexpr int kBiasRows = 512;
+constexpr int kBiasThreads = 256;
 template <int RELU>
-__global__ void k_bias_partial(const bf16* __restrict__ dy, const bf16* __restrict__ yv, int P, int Cout,
-                               float* __restrict__ part) {
+__global__ void __launch_bounds__(kBiasThreads)
+k_bias_partial(const bf16* __restrict__ dy, const bf16* __restrict__ yv, int P, int Cout, float* __restrict__ part) {
+    __shared__ float red[kBiasThreads * 8];
+    const int groups = Cout / 8;
+    const int G = groups < kBiasThreads ? groups : kBiasThreads;
+    const int lanes = kBiasThreads / G;
+    const int cg0 = threadIdx.x % G, pl = threadIdx.x / G;
     const int p0 = blockIdx.x * kBiasRows, p1 = min(P, p0 + kBiasRows);
-    for (int co = threadIdx.x; co < Cout; co += blockDim.x) {
-        float s = 0.f;
-        for (int p = p0; p < p1; ++p) {
-            const size_t q = (size_t)p * Cout + co;
-            float d = __bfloat162float(dy[q]);
-            if (RELU && !(__bfloat162float(yv[q]) > 0.f)) d = 0.f;
-            s += d;
+    for (int cb = 0; cb < groups; cb += G) {
+        const int cg = cb + cg0;
+        float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (pl < lanes && cg < groups) {
+            for (int p = p0 + pl; p < p1; p += lanes) {
+                const size_t q = (size_t)p * Cout + cg * 8;
+                uint4 d = *(const uint4*)(dy + q);
+                if (RELU) d = relu_mask8(d, *(const uint4*)(yv + q));
+                const __nv_bfloat162* h = (const __nv_bfloat162*)&d;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float2 f = __bfloat1622float2(h[k]);
+                    s[2 * k] += f.x;
+                    s[2 * k + 1] += f.y;
+                }
+            }
         }
-        part[(size_t)blockIdx.x * Cout + co] = s;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) red[threadIdx.x * 8 + k] = s[k];
+        __syncthreads();
+        for (int e = threadIdx.x; e < G * 8; e += kBiasThreads) {
+            const int g = e / 8, k = e % 8;
+            if (cb + g < groups) {
+                float t = 0.f;
+                for (int l = 0; l < lanes; ++l) t += red[(l * G + g) * 8 + k];
+                part[(size_t)blockIdx.x * Cout + (cb + g) * 8 + k] = t;
+            }
+        }
+        __syncthreads();
     }
 }
 
-__global__ void k_bias_reduce(const float* __restrict__ part, int nblk, int Cout, float* __restrict__ db) {
-    const int co = blockIdx.x * blockDim.x + threadIdx.x;
-    if (co >= Cout) return;
+// bias gradient, stage 2: one block per channel adds the blocks' partial sums
+// (strided per thread, then a fixed tree)
+__global__ void __launch_bounds__(256) k_bias_reduce(const float* __restrict__ part, int nblk, int Cout,
+                                                     float* __restrict__ db) {
+    __shared__ float red[256];
+    const int co = blockIdx.x;
     float s = 0.f;
-    for (int b = 0; b < nblk; ++b) s += part[(size_t)b * Cout + co];
-    db[co] = s;
+    for (int b = threadIdx.x; b < nblk; b += 256) s += part[(size_t)b * Cout + co];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[co] = red[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -518,12 +556,12 @@ int glnn_conv3x3_bwd_weight(const void* dy, const void* y, int32_t relu, const v
             k_conv_bwd_weight<0><<<grid, NT, 0, s>>>((const bf16*)dy, (const bf16*)y, (const bf16*)x1, c1, (const bf16*)x2, c2, work, n, h, w, cout, q.chunk);
     }
     if (relu)
-        k_bias_partial<1><<<q.nbias, 256, 0, s>>>((const bf16*)dy, (const bf16*)y, (int)P, cout, bias_part);
+        k_bias_partial<1><<<q.nbias, kBiasThreads, 0, s>>>((const bf16*)dy, (const bf16*)y, (int)P, cout, bias_part);
     else
-        k_bias_partial<0><<<q.nbias, 256, 0, s>>>((const bf16*)dy, (const bf16*)y, (int)P, cout, bias_part);
+        k_bias_partial<0><<<q.nbias, kBiasThreads, 0, s>>>((const bf16*)dy, (const bf16*)y, (int)P, cout, bias_part);
     const long long size = (long long)cout * 9 * cin;
     k_sum_splits<<<grid_for(size, 256), 256, 0, s>>>(work, nz, size, dw);
-    k_bias_reduce<<<(cout + 127) / 128, 128, 0, s>>>(bias_part, q.nbias, cout, db);
+    k_bias_reduce<<<cout, 256, 0, s>>>(bias_part, q.nbias, cout, db);
     return ret(cudaGetLastError());
 }
 

@@ -359,7 +359,11 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
     const uint32_t tmem = *tslot;
     bool ok = true;
 
-    if (tid == 0) {
+    // warp 0, lane 0: producer; warp 1, lane 0: MMA issuer.  The other lanes of those
+    // two warps wait at __syncwarp, so they take no issue slots from the role lane
+    // (spinning in the same warp on the accumulator barrier halved the pipeline).
+    if (warp == 0) {
+        if (lane == 0) {
         // producer: chunk kc = tap * nck + cc, A = input box shifted by the tap, B = weights
         for (int kc = 0; kc < nk && ok; ++kc) {
             const int st = kc % TMA_STAGES, use = kc / TMA_STAGES;
@@ -375,7 +379,10 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
             else tma_load_4d(a_dst, &ta2, c - C1, x0 + dx, y0 + dy, img, saddr(full + st));
             tma_load_2d(b_dst, &tb, tap * (C1 + C2) + c, n0, saddr(full + st));
         }
-    } else if (tid == 32) {
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
         // MMA issuer
         for (int kc = 0; kc < nk && ok; ++kc) {
             const int st = kc % TMA_STAGES, use = kc / TMA_STAGES;
@@ -395,6 +402,8 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(done))
                      : "memory");
+        }
+        __syncwarp();
     }
     // everyone: the accumulator is complete when `done` fires (the issuer commits it
     // even after a failed wait, so this wait ends)
@@ -518,7 +527,10 @@ k_conv_wgrad_tma(const __grid_constant__ CUtensorMap tx1, const __grid_constant_
     bool ok = true;
 
     if (nk > 0) {
-        if (tid == 0) {
+        // warp 0, lane 0: producer; warp 1, lane 0: MMA issuer; their other lanes wait
+        // at __syncwarp (as in k_conv_fwd_tma)
+        if (warp == 0) {
+            if (lane == 0) {
             const int dy0 = tap0 / 3 - 1, dx0 = tap0 % 3 - 1, dy1 = tap1 / 3 - 1, dx1 = tap1 % 3 - 1;
             for (int kc = 0; kc < nk && ok; ++kc) {
                 const int st = kc % WG_STAGES, use = kc / WG_STAGES;
@@ -534,7 +546,10 @@ k_conv_wgrad_tma(const __grid_constant__ CUtensorMap tx1, const __grid_constant_
                 tma_load_4d(dst + WG_BOX, xm, cx, x0 + dx1, y0 + dy1, img, saddr(full + st));
                 tma_load_4d(dst + 2 * WG_BOX, &tdy, oc * 64, x0, y0, img, saddr(full + st));
             }
-        } else if (tid == 32) {
+            }
+            __syncwarp();
+        } else if (warp == 1) {
+            if (lane == 0) {
             for (int kc = 0; kc < nk && ok; ++kc) {
                 const int st = kc % WG_STAGES, use = kc / WG_STAGES;
                 if (!wait_parity(saddr(full + st), (uint32_t)(use & 1))) {
@@ -554,6 +569,8 @@ k_conv_wgrad_tma(const __grid_constant__ CUtensorMap tx1, const __grid_constant_
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                              saddr(done))
                          : "memory");
+            }
+            __syncwarp();
         }
         if (!wait_parity(saddr(done), 0u)) ok = false;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");

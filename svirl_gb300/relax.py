@@ -37,13 +37,15 @@ class HandleCache:
 
 
 def relax(insts, cache, dtype=np.float32, starts=None, n_iter=4000, gtol=1e-4, gtol_abs=True, rtol=0.0,
-          td_steps=0, td_dt=0.1, fetch=True, timed=True, targets=None, target_tol=1e-6, window=0, window_tol=0.0):
+          td_steps=0, td_dt=0.1, fetch=True, timed=True, targets=None, target_tol=1e-6, window=0, window_tol=0.0,
+          graphs=True):
     """Load `insts` (learned.Instance, any sizes) into handles, optionally run
     `td_steps` TDGL steps, then the device CG (exact boundary gradient) of all of
     them in one batch; with `targets`, an instance also stops once its energy is
     within `target_tol` of its target; with `window` > 0, once its energy fell by
-    no more than `window_tol` |E| over `window` iterations.  Returns (cg dict with
-    per-instance arrays and 'ms', [(psi, ab)] if fetch, td_ms)."""
+    no more than `window_tol` |E| over `window` iterations; graphs=False runs the
+    host-driven loop (the same kernels).  Returns (cg dict with per-instance arrays
+    and 'ms', [(psi, ab)] if fetch, td_ms)."""
     hs = [cache.get(it.n, dtype) for it in insts]
     try:
         for q, (it, h) in enumerate(zip(insts, hs)):
@@ -58,6 +60,8 @@ def relax(insts, cache, dtype=np.float32, starts=None, n_iter=4000, gtol=1e-4, g
                 batch.set_energy_targets(targets, target_tol)
             if window > 0:
                 batch.set_cg_window(window, window_tol)
+            if not graphs:
+                batch.set_use_graphs(False)
             if td_steps > 0:
                 _, td_ms = batch.td_raw(td_dt, td_steps, 0, timed=True)
             out = batch.cg_device(n_iter=n_iter, rtol=rtol, gtol=gtol, exact_boundary=True, gtol_abs=gtol_abs,
