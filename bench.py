@@ -488,9 +488,12 @@ def run_c1(args):
 
 
 def run_conv(args):
-    """The learned warm start's hottest kernels: the tcgen05 3x3 convolution (forward
-    and data gradient) and the mma weight gradient on a 32 x 128 x 128 x 64 -> 64
-    layer, timed with CUDA events; FLOP rate against the measured bf16 peak."""
+    """The learned warm start's hottest kernels on a 32 x 128 x 128 x 64 -> 64 layer,
+    timed with CUDA events: the tcgen05 3x3 convolution forward (TMA operands; the
+    value) and its backward as the library's autograd wrapper runs it (dy masked once
+    by the ReLU derivative, the data gradient and the weight gradient from the masked
+    dy, TMA operands), beside the thread-gather forward and data gradient and the
+    mma.sync weight gradient; FLOP rate against the measured bf16 peak."""
     import ctypes as C
     import torch
     from svirl_gb300 import learned as L
@@ -506,6 +509,7 @@ def run_conv(args):
     wt = torch.empty((3, 3, cin, cout), dtype=torch.bfloat16, device="cuda")
     y = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
     dy = torch.randn((n, h, w, cout), generator=g).to("cuda", torch.bfloat16)
+    dym = torch.empty_like(dy)
     dx = torch.empty_like(x)
     dw = torch.empty_like(W)
     db = torch.empty_like(b)
@@ -529,14 +533,18 @@ def run_conv(args):
         return e0.elapsed_time(e1) / reps
 
     f = lambda: lib.glnn_conv3x3_fwd(P(x), cin, None, 0, P(wb), P(b), P(y), n, h, w, cout, 1, P(err), s)
-    bd = lambda: lib.glnn_conv3x3_bwd_data(P(dy), P(y), 1, P(wt), P(dx), cin, None, 0, n, h, w, cout, P(err), s)
-    bw = lambda: lib.glnn_conv3x3_bwd_weight(P(dy), P(y), 1, P(x), cin, None, 0, P(dw), P(db), P(work), nwork, n, h, w,
-                                            cout, P(err), s)
+    mk = lambda: lib.glnn_relu_mask(P(dy), P(y), P(dym), dy.numel(), s)
+    bd_gather = lambda: lib.glnn_conv3x3_bwd_data(P(dy), P(y), 1, P(wt), P(dx), cin, None, 0, n, h, w, cout, P(err), s)
+    bd = lambda: lib.glnn_conv3x3_bwd_data(P(dym), None, 0, P(wt), P(dx), cin, None, 0, n, h, w, cout, P(err), s)
+    bw = lambda: lib.glnn_conv3x3_bwd_weight(P(dym), None, 0, P(x), cin, None, 0, P(dw), P(db), P(work), nwork, n, h,
+                                            w, cout, P(err), s)
+    f(); mk()
     lib.glnn_set_conv_tma(0)
     ms_f_gather = timed(f, args.steps)
+    ms_d_gather = timed(bd_gather, args.steps)
     ms_w_mma = timed(bw, args.steps)
     lib.glnn_set_conv_tma(1)
-    ms_f, ms_d, ms_w = timed(f, args.steps), timed(bd, args.steps), timed(bw, args.steps)
+    ms_f, ms_mk, ms_d, ms_w = timed(f, args.steps), timed(mk, args.steps), timed(bd, args.steps), timed(bw, args.steps)
     assert int(err.item()) == 0
     peak = 1922.0
     pth = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -553,11 +561,15 @@ def run_conv(args):
                          "peak_kind": "measured bf16 burst"},
             "forward_gather": {"ms": ms_f_gather, "tflops": flop / (ms_f_gather * 1e-3) / 1e12,
                                "kernel": "tcgen05, operands gathered by the threads"},
-            "data_grad": {"ms": ms_d, "tflops": flop / (ms_d * 1e-3) / 1e12, "kernel": "tcgen05"},
+            "relu_mask": {"ms": ms_mk, "kernel": "dy * relu'(y), once per backward"},
+            "data_grad": {"ms": ms_d, "tflops": flop / (ms_d * 1e-3) / 1e12,
+                          "kernel": "tcgen05, operands loaded by TMA (masked dy)"},
+            "data_grad_gather": {"ms": ms_d_gather, "tflops": flop / (ms_d_gather * 1e-3) / 1e12,
+                                 "kernel": "tcgen05, operands gathered by the threads (ReLU derivative while gathering)"},
             "weight_grad": {"ms": ms_w, "tflops": flop / (ms_w * 1e-3) / 1e12,
-                            "kernel": "tcgen05, MN-major operands loaded by TMA, split-K (with the dy * relu'(y) "
-                                      "pass and the bias gradient)"},
-            "weight_grad_mma": {"ms": ms_w_mma, "tflops": flop / (ms_w_mma * 1e-3) / 1e12, "kernel": "mma.sync"}}
+                            "kernel": "tcgen05, MN-major operands loaded by TMA, split-K (with the bias gradient)"},
+            "weight_grad_mma": {"ms": ms_w_mma, "tflops": flop / (ms_w_mma * 1e-3) / 1e12, "kernel": "mma.sync"},
+            "layer_fwd_bwd_ms": ms_f + ms_mk + ms_d + ms_w}
     print(json.dumps(line), flush=True)
 
 
@@ -598,12 +610,13 @@ def run_learned(args):
             evals["%d" % n] = L.evaluate(net, insts, cache=cache, Estar=Estar)
         finally:
             cache.close()
-    t = thr["128"]["by_dtype"]["float64"]
+    t = thr["128"]["by_dtype"]["float32"]
     nodes = 128 * 128 * 64
-    line = {"metric": "GL states/s to dF/F<=1e-6, learned warm start + batched FP64 CG (128^2, 64 instances)",
+    line = {"metric": "GL states/s to dF/F<=1e-6, learned warm start + batched FP32 CG (128^2, 64 instances)",
             "value": t["states_per_s"], "unit": "states/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": 1e3 * t["wall_s"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16 net (f32 accumulate), f64 CG (the f32 CG arm under throughput.*.by_dtype.float32)",
+            "dtype": "bf16 net (f32 accumulate), f32 CG stencils, f64 reductions (the f64 CG arm under "
+                     "throughput.*.by_dtype.float64)",
             "data": "synthetic (solver-generated)",
             "config": {"workload": "learned_warm_start", "train_states": args.train_states, "epochs": args.epochs,
                        "params": net.n_params(), "levels": list(L.LEVELS), "target_mode": "amplitude",
@@ -613,8 +626,8 @@ def run_learned(args):
                                     "iterations) of the same instance from the same initial state: the random start "
                                     "(plain arm), the prediction (learned arm)"},
             "speedup_vs_plain": t["speedup_vs_plain"], "throughput": thr, "eval": evals,
-            "e2e": {"value": t["states_per_s"], "unit": "states/s", "h2d_bytes_per_step": nodes * 16 * 2,
-                    "d2h_bytes_per_step": nodes * 8 * 4,
+            "e2e": {"value": t["states_per_s"], "unit": "states/s", "h2d_bytes_per_step": nodes * 8 * 2,
+                    "d2h_bytes_per_step": nodes * 4 * 4,
                     "how": "wall time of features to the device, prediction, decoding to host, states into the "
                            "handles, batched CG, states back"}}
     print(json.dumps(line), flush=True)

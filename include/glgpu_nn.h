@@ -45,7 +45,12 @@ int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, con
  * Process-wide. */
 int glnn_set_conv_tma(int32_t enable);
 /* [dx1|dx2] = conv3x3^T(dy * relu'(y), Wt), on tcgen05 like the forward.  y may be
- * NULL when relu = 0. */
+ * NULL when relu = 0.  With relu = 0 and the shapes of the TMA forward (roles of
+ * input and output channels exchanged) the operands are loaded by TMA (dy as the
+ * 4-D activation tensor, Wt as the 3-D tensor [9][cin][cout]); else the threads
+ * gather them (and apply the ReLU derivative).  Callers that have both gradients
+ * to compute mask dy once with glnn_relu_mask and pass relu = 0. */
+int glnn_relu_mask(const void* dy, const void* y, void* out, int64_t count, void* stream); /* out = dy * (y > 0), bf16, count % 8 == 0 */
 int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const void* wt, void* dx1, int32_t c1,
                           void* dx2, int32_t c2, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t* err,
                           void* stream);

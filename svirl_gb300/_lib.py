@@ -98,6 +98,7 @@ _SIGNATURES = {
     "glnn_set_conv_tma": (C.c_int, [C.c_int32]),
     "glnn_conv3x3_fwd": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_int32, _P, _P]),
+    "glnn_relu_mask": (C.c_int, [_P, _P, _P, C.c_int64, _P]),
     "glnn_conv3x3_bwd_data": (C.c_int, [_P, _P, C.c_int32, _P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32,
                                         C.c_int32, C.c_int32, _P, _P]),
     "glnn_conv3x3_bwd_weight_work": (C.c_int64, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),

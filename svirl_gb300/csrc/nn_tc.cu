@@ -323,11 +323,25 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
-template <int RELU>
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(dst),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
+// MODE 0 (forward): A = [x1 | x2] (C1 + C2 channels) shifted by +tap, B = Wb as the
+// 2-D tensor [cout][9 cin] (box: 64 rows of 64 k), out = y (Co1 = cout channels,
+// + bias, ReLU).  MODE 1 (data gradient): A = dy' (C1 = cout channels, C2 = 0: dy
+// with the ReLU derivative already applied) shifted by -tap, B = Wt as the 3-D
+// tensor [9][cin][cout] (box: 64 cin rows of 64 cout, one tap), out = [o1 | o2]
+// (Co1 + Co2 = cin channels), no bias.
+template <int MODE, int RELU>
 __global__ void __launch_bounds__(NTH)
 k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ CUtensorMap ta2,
                const __grid_constant__ CUtensorMap tb, const float* __restrict__ bias, bf16* __restrict__ y, int Cout,
-               int C1, int C2, int H, int W, int* err) {
+               bf16* __restrict__ o2, int Co2, int C1, int C2, int H, int W, int* err) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* full = (uint64_t*)(smem + TMA_STAGES * STAGE_BYTES);
@@ -370,14 +384,16 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
             if (use > 0 && !wait_parity(saddr(empty + st), (uint32_t)((use + 1) & 1))) ok = false;
             if (!ok) break;
             const int tap = kc / nck, cc = kc - tap * nck;
-            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            const int sgn = MODE == 0 ? 1 : -1;
+            const int dy = sgn * (tap / 3 - 1), dx = sgn * (tap % 3 - 1);
             const int c = cc * TK;
             const uint32_t a_dst = saddr(smem + st * STAGE_BYTES), b_dst = a_dst + A_BYTES;
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(full + st)), "r"(kStageTx)
                          : "memory");
             if (c < C1) tma_load_4d(a_dst, &ta1, c, x0 + dx, y0 + dy, img, saddr(full + st));
             else tma_load_4d(a_dst, &ta2, c - C1, x0 + dx, y0 + dy, img, saddr(full + st));
-            tma_load_2d(b_dst, &tb, tap * (C1 + C2) + c, n0, saddr(full + st));
+            if (MODE == 0) tma_load_2d(b_dst, &tb, tap * (C1 + C2) + c, n0, saddr(full + st));
+            else tma_load_3d(b_dst, &tb, c, n0, tap, saddr(full + st));
         }
         }
         __syncwarp();
@@ -422,15 +438,23 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
                 : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (MODE == 0) {
 #pragma unroll
-            for (int q = 0; q < 16; q += 2) {
-                const int col = n0 + c + q;
-                float v0 = __uint_as_float(r[q]) + bias[col], v1 = __uint_as_float(r[q + 1]) + bias[col + 1];
-                if (RELU) {
-                    v0 = fmaxf(v0, 0.f);
-                    v1 = fmaxf(v1, 0.f);
+                for (int q = 0; q < 16; q += 2) {
+                    const int col = n0 + c + q;
+                    float v0 = __uint_as_float(r[q]) + bias[col], v1 = __uint_as_float(r[q + 1]) + bias[col + 1];
+                    if (RELU) {
+                        v0 = fmaxf(v0, 0.f);
+                        v1 = fmaxf(v1, 0.f);
+                    }
+                    *(__nv_bfloat162*)(y + (size_t)p * Cout + col) = __floats2bfloat162_rn(v0, v1);
                 }
-                *(__nv_bfloat162*)(y + (size_t)p * Cout + col) = __floats2bfloat162_rn(v0, v1);
+            } else {
+                // output channel tile n0 lies in [o1 | o2]: both channel counts are multiples of TN
+                bf16* out = n0 < Cout ? y + (size_t)p * Cout + n0 : o2 + (size_t)p * Co2 + (n0 - Cout);
+#pragma unroll
+                for (int q = 0; q < 16; q += 2)
+                    *(__nv_bfloat162*)(out + c + q) = __floats2bfloat162_rn(__uint_as_float(r[q]), __uint_as_float(r[q + 1]));
             }
         }
     } else if (tid == 0) {
@@ -680,10 +704,37 @@ static bool conv_tma_shape_ok(int c1, int c2, int h, int w, int cout) {
     return c1 % TK == 0 && c2 % TK == 0 && cout % TN == 0 && ((long long)h * w) % TM == 0 && (w % TM == 0 || TM % w == 0);
 }
 
-template <int RELU> static cudaError_t conv_tma_smem_attr() {
+template <int MODE, int RELU> static cudaError_t conv_tma_smem_attr() {
     static cudaError_t e =
-        cudaFuncSetAttribute(k_conv_fwd_tma<RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, TMA_SMEM);
+        cudaFuncSetAttribute(k_conv_fwd_tma<MODE, RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, TMA_SMEM);
     return e;
+}
+
+// Wt [9][cin][cout] (bf16, cout contiguous), box = 64 cout x 64 cin x one tap
+static bool weight_t_map(CUtensorMap* m, const void* base, int cin, int cout) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)cout, (cuuint64_t)cin, 9u};
+    cuuint64_t strides[2] = {(cuuint64_t)cout * 2, (cuuint64_t)cin * cout * 2};
+    cuuint32_t box[3] = {(cuuint32_t)TK, (cuuint32_t)TN, 1u};
+    cuuint32_t es[3] = {1u, 1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// data gradient without a ReLU derivative (dy already masked) by TMA: 1 launched, 0 not taken
+static int conv_bwd_data_tma(const void* dy, const void* wt, void* dx1, int c1, void* dx2, int c2, int n, int h, int w,
+                             int cout, int* err, cudaStream_t s) {
+    if (!g_conv_tma || !conv_tma_shape_ok(c1, c2, h, w, cout)) return 0;
+    CUtensorMap ta, tb;
+    if (!act_map(&ta, dy, cout, n, h, w) || !weight_t_map(&tb, wt, c1 + c2, cout)) return 0;
+    if (conv_tma_smem_attr<1, 0>() != cudaSuccess) return 0;
+    const long long P = (long long)n * h * w;
+    dim3 grid((unsigned)(P / TM), (unsigned)((c1 + c2) / TN));
+    k_conv_fwd_tma<1, 0><<<grid, NTH, TMA_SMEM, s>>>(ta, ta, tb, nullptr, (bf16*)dx1, c1, (bf16*)dx2, c2, cout, 0, h, w,
+                                                     err);
+    return 1;
 }
 
 // 1: launched; 0: shape or tensor maps not available (the caller uses the gather kernel)
@@ -698,13 +749,13 @@ static int conv_fwd_tma(const void* x1, int c1, const void* x2, int c2, const vo
         t2 = t1;
     }
     if (!weight_map(&tb, wb, 9LL * (c1 + c2), cout)) return 0;
-    if ((relu ? conv_tma_smem_attr<1>() : conv_tma_smem_attr<0>()) != cudaSuccess) return 0;
+    if ((relu ? conv_tma_smem_attr<0, 1>() : conv_tma_smem_attr<0, 0>()) != cudaSuccess) return 0;
     const long long P = (long long)n * h * w;
     dim3 grid((unsigned)(P / TM), (unsigned)(cout / TN));
     if (relu)
-        k_conv_fwd_tma<1><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, c1, c2, h, w, err);
+        k_conv_fwd_tma<0, 1><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2, h, w, err);
     else
-        k_conv_fwd_tma<0><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, c1, c2, h, w, err);
+        k_conv_fwd_tma<0, 0><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2, h, w, err);
     return 1;
 }
 
@@ -791,6 +842,17 @@ int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, con
     return cudaGetLastError() == cudaSuccess ? GLGPU_OK : GLGPU_E_CUDA;
 }
 
+int glnn_relu_mask(const void* dy, const void* y, void* out, int64_t count, void* stream) {
+    if (!dy || !y || !out || count < 0 || count % 8 != 0) return GLGPU_E_ARG;
+    if (((uintptr_t)dy | (uintptr_t)y | (uintptr_t)out) & 15u) return GLGPU_E_ARG;
+    const long long n8 = count / 8;
+    if (n8 == 0) return GLGPU_OK;
+    const long long blocks = (n8 + 255) / 256;
+    k_relu_mask_dy<<<(unsigned)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, (cudaStream_t)stream>>>(
+        (const uint4*)dy, (const uint4*)y, (uint4*)out, n8);
+    return cudaGetLastError() == cudaSuccess ? GLGPU_OK : GLGPU_E_CUDA;
+}
+
 int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const void* wt, void* dx1, int32_t c1,
                              void* dx2, int32_t c2, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t* err,
                              void* stream) {
@@ -800,6 +862,8 @@ int glnn_conv3x3_bwd_data(const void* dy, const void* y, int32_t relu, const voi
     const long long P = (long long)n * h * w;
     dim3 grid((unsigned)((P + TM - 1) / TM), (unsigned)((c1 + c2 + TN - 1) / TN));
     cudaStream_t s = (cudaStream_t)stream;
+    if (!relu && conv_bwd_data_tma(dy, wt, dx1, c1, dx2, c2, n, h, w, cout, err, s))
+        return cudaGetLastError() == cudaSuccess ? GLGPU_OK : GLGPU_E_CUDA;
     if ((relu ? conv_tc_smem_attr<1, 1>() : conv_tc_smem_attr<1, 0>()) != cudaSuccess) return GLGPU_E_CUDA;
     if (relu)
         k_conv_tc<1, 1><<<grid, NTH, SMEM_BYTES, s>>>((const bf16*)dy, cout, nullptr, 0, (const bf16*)y, (const bf16*)wt,

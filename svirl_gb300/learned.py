@@ -108,7 +108,12 @@ class Conv3x3(torch.autograd.Function):
         c2 = 0 if x2 is None else x2.shape[3]
         cout = y.shape[3]
         s = _stream()
-        relu = 1 if ctx.relu else 0
+        relu = 0
+        if ctx.relu:
+            # dy * relu'(y) once, for both gradients (their TMA kernels load it as is)
+            dym = torch.empty_like(dy)
+            _ok(lib.glnn_relu_mask(_ptr(dy), _ptr(y), _ptr(dym), dy.numel(), s), "relu_mask")
+            dy = dym
         dx1 = dx2 = None
         if ctx.needs_input_grad[0] or ctx.needs_input_grad[1]:
             dx1 = torch.empty_like(x1)
@@ -484,10 +489,21 @@ def reference_energies(insts, cache, n_iter=20000, gtol=1e-7, starts=None):
 
 def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=1e-7, tol=1e-6, cache=None,
              Estar=None):
-    """CG iterations and device time to reach F* within `tol` from the random start
-    and from the network's prediction; F* = the energy of a tight relaxation from
-    the random start (gradient norm `gtol`).  A prediction counts only where its
-    CG reaches that energy (status 4)."""
+    """What the network gains, in CG iterations and device time, measured two ways.
+
+    Own minimum (the states/s criterion): the CG from the random start run until it
+    is within `tol` of F*_random (a tight FP64 relaxation from the random start), the
+    CG from the prediction until it is within `tol` of F*_pred (a tight FP64
+    relaxation from the prediction).  The CG is monotone in the energy and F* is
+    where the same arithmetic ends, so reaching the band means the run reached its
+    minimum: `iters_*_own_median`, `reached_*_own`.
+
+    The random start's minimum (strict): a prediction reaches F*_random only if its
+    own minimum is F*_random (|F*_pred - F*_random| <= tol |F*_random|); its
+    iterations are those to enter the band.  An energy that passes through the band
+    on the way to a lower minimum does not count.  `reached_warm`, `reached_both`,
+    `iters_*_median_both`; `warm_lower_energy` counts the predictions whose minimum
+    is lower than F*_random (another vortex configuration)."""
     import time as _time
     from .relax import HandleCache, relax
     own = cache is None
@@ -502,25 +518,29 @@ def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=
         torch.cuda.synchronize()
         t_net = _time.perf_counter() - t0
         starts = decode(insts, pred, mode=mode)
+        Epred = reference_energies(insts, cache, n_iter=n_iter, gtol=gtol, starts=starts)
         w, _, _ = relax(insts, cache, dtype, starts=starts, n_iter=n_iter, gtol=0.0, fetch=False, targets=Estar,
                         target_tol=tol)
+        wo, _, _ = relax(insts, cache, dtype, starts=starts, n_iter=n_iter, gtol=0.0, fetch=False, targets=Epred,
+                         target_tol=tol)
     finally:
         if own:
             cache.close()
-    # status 4: the energy fell to F* + tol |F*|; the state reached F* only if it did
-    # not go below F* - tol |F*| (a lower-energy vortex state is another minimum)
     lo = Estar - tol * np.abs(Estar)
     ok_r = (r["status"] == 4) & (r["energy"] >= lo)
-    ok_w = (w["status"] == 4) & (w["energy"] >= lo)
+    same_min = np.abs(Epred - Estar) <= tol * np.abs(Estar)
+    ok_w = (w["status"] == 4) & same_min
     both = ok_r & ok_w
+    ok_wo = (wo["status"] == 4) & (wo["energy"] >= Epred - tol * np.abs(Epred))
     med = lambda x: float(np.median(x)) if x.size else float("nan")  # noqa: E731
-    return {"n": len(insts), "size": insts[0].n, "reached_random": int(ok_r.sum()), "reached_warm": int(ok_w.sum()),
-            "reached_both": int(both.sum()),
+    return {"n": len(insts), "size": insts[0].n,
+            "reached_random_own": int(ok_r.sum()), "reached_warm_own": int(ok_wo.sum()),
+            "iters_random_own_median": med(r["iters"][ok_r]), "iters_warm_own_median": med(wo["iters"][ok_wo]),
+            "cg_ms_random_own": r["ms"], "cg_ms_warm_own": wo["ms"],
+            "reached_random": int(ok_r.sum()), "reached_warm": int(ok_w.sum()), "reached_both": int(both.sum()),
             "iters_random_median_both": med(r["iters"][both]), "iters_warm_median_both": med(w["iters"][both]),
-            "iters_random_median": float(np.median(r["iters"])), "iters_warm_median": float(np.median(w["iters"])),
-            "iters_random_mean": float(r["iters"].mean()), "iters_warm_mean": float(w["iters"].mean()),
-            "cg_ms_random": r["ms"], "cg_ms_warm": w["ms"], "net_ms": 1e3 * t_net,
-            "warm_lower_energy": int((w["energy"] < lo).sum()), "random_lower_energy": int((r["energy"] < lo).sum())}
+            "net_ms": 1e3 * t_net,
+            "warm_lower_energy": int((Epred < lo).sum()), "warm_higher_energy": int((Epred > Estar + tol * np.abs(Estar)).sum())}
 
 
 def states_throughput(net, insts, Estar, cache, cap=4000, gtol=1e-4, tol=1e-6, plain_sample=8, mode="amplitude",

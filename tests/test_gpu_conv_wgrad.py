@@ -1,12 +1,16 @@
-"""The weight gradient of the 3x3 convolution on tcgen05 (M = two taps x 64 input
-channels, N = 64 output channels, K = pixels; both operands MN-major boxes loaded
-by TMA, split-K partial sums reduced in a fixed order) against the NumPy reference
-(oracle/nn_np.py) on bfloat16-rounded operands (5e-3 of the gradient's max, as the
-other weight-gradient tests) and against the mma.sync kernel on the same inputs
-(1e-4 of max: the same bf16 products, summed in FP32 in another order); on the
-shapes the tcgen05 path takes: pixel chunks that are runs of one row (w = 64, 128)
-or groups of rows (w = 16, 32), channel concatenation, several channel tiles, a
-pixel count that gives a single split.  No bounded wait may run out."""
+"""The backward pass of the 3x3 convolution with TMA operands.  Weight gradient on
+tcgen05 (M = two taps x 64 input channels, N = 64 output channels, K = pixels; both
+operands MN-major boxes loaded by TMA, split-K partial sums reduced in a fixed
+order) against the NumPy reference (oracle/nn_np.py) on bfloat16-rounded operands
+(5e-3 of the gradient's max, as the other weight-gradient tests) and against the
+mma.sync kernel on the same inputs (1e-4 of max: the same bf16 products, summed in
+FP32 in another order).  Data gradient from the TMA kernel (dy masked once by
+glnn_relu_mask, shifted boxes of dy, Wt as a 3-D tensor) against the reference
+(2e-2 of max: bf16 outputs) and against the thread-gather kernel (bitwise: the same
+products in the same order).  Shapes: pixel chunks that are runs of one row
+(w = 64, 128) or groups of rows (w = 16, 32), channel concatenation, several
+channel tiles, a pixel count that gives a single split.  No bounded wait may run
+out."""
 import numpy as np
 import pytest
 
@@ -21,15 +25,17 @@ def _grads(L, x1, x2, W, b, dy, relu, tma):
     lib = L._lib_nn()
     lib.glnn_set_conv_tma(1 if tma else 0)
     try:
-        tx1 = torch.from_numpy(x1).to("cuda", torch.bfloat16)
-        tx2 = torch.from_numpy(x2).to("cuda", torch.bfloat16) if x2 is not None else None
+        tx1 = torch.from_numpy(x1).to("cuda", torch.bfloat16).requires_grad_()
+        tx2 = torch.from_numpy(x2).to("cuda", torch.bfloat16).requires_grad_() if x2 is not None else None
         tW = torch.from_numpy(W).cuda().requires_grad_()
         tb = torch.from_numpy(b).cuda().requires_grad_()
         y = L.Conv3x3.apply(tx1, tx2, tW, tb, relu)
-        gw, gb = torch.autograd.grad(y, [tW, tb], grad_outputs=torch.from_numpy(dy).to("cuda", torch.bfloat16))
+        ins = [tW, tb, tx1] + ([tx2] if tx2 is not None else [])
+        g = torch.autograd.grad(y, ins, grad_outputs=torch.from_numpy(dy).to("cuda", torch.bfloat16))
         torch.cuda.synchronize()
         f = lambda t: t.detach().float().cpu().numpy().astype(np.float64)
-        return f(y), f(gw), f(gb)
+        dx = f(g[2]) if tx2 is None else np.concatenate([f(g[2]), f(g[3])], axis=3)
+        return f(y), f(g[0]), f(g[1]), dx
     finally:
         lib.glnn_set_conv_tma(1)
 
@@ -47,10 +53,14 @@ def test_tcgen05_weight_gradient(shape, relu):
     b = (rng.standard_normal(cout) * 0.1).astype(np.float32)
     dy = R.bf16_round(rng.standard_normal((n, h, w, cout)).astype(np.float32))
     xc = x1 if x2 is None else np.concatenate([x1, x2], axis=3)
-    y_t, gw_t, gb_t = _grads(L, x1, x2, W, b, dy, relu, True)
+    y_t, gw_t, gb_t, dx_t = _grads(L, x1, x2, W, b, dy, relu, True)
     L.check_kernel_errors()
-    y_m, gw_m, gb_m = _grads(L, x1, x2, W, b, dy, relu, False)
-    _, dw_ref, db_ref = R.conv3x3_bwd(xc, R.bf16_round(W), y_t, dy, relu)
+    y_m, gw_m, gb_m, dx_m = _grads(L, x1, x2, W, b, dy, relu, False)
+    dx_ref, dw_ref, db_ref = R.conv3x3_bwd(xc, R.bf16_round(W), y_t, dy, relu)
+    e_dx = np.abs(dx_t - dx_ref).max() / np.abs(dx_ref).max()
+    print("shape %s relu %d: TMA dx vs reference %.2e, vs gather max |diff| %.2e"
+          % (shape, relu, e_dx, np.abs(dx_t - dx_m).max()))
+    assert e_dx < 2e-2 and np.array_equal(dx_t, dx_m)
     scale = np.abs(dw_ref).max()
     e_ref = np.abs(gw_t - dw_ref).max() / scale
     e_mma = np.abs(gw_t - gw_m).max() / scale
