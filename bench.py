@@ -772,6 +772,23 @@ def main():
     e2e_s = time.perf_counter() - t0
     barrier()
     e2e_value = world * N * e2e_steps / e2e_s
+    # where the end-to-end step's time goes: the same three calls timed apart
+    t_parts = [0.0, 0.0, 0.0]
+    for _ in range(e2e_steps):
+        t1 = time.perf_counter()
+        h.set_psi(psi_in)
+        t2 = time.perf_counter()
+        h.td(DT, 1, 0)
+        t3 = time.perf_counter()
+        assert h.lib.glgpu_get_order_parameter(h.h, psi_out.ctypes.data_as(__import__("ctypes").c_void_p)) == 0
+        t4 = time.perf_counter()
+        t_parts[0] += t2 - t1
+        t_parts[1] += t3 - t2
+        t_parts[2] += t4 - t3
+    e2e_parts = {"h2d_ms": 1e3 * t_parts[0] / e2e_steps, "td_step_ms": 1e3 * t_parts[1] / e2e_steps,
+                 "d2h_ms": 1e3 * t_parts[2] / e2e_steps,
+                 "h2d_GBps": psi_in.nbytes / (t_parts[0] / e2e_steps) / 1e9,
+                 "d2h_GBps": psi_out.nbytes / (t_parts[2] / e2e_steps) / 1e9}
 
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_baseline(sweeps / args.steps)
@@ -809,7 +826,8 @@ def main():
                          "launch_ms": sweep_ms, "peak_kind": peak_kind},
             "e2e": {"value": e2e_value, "unit": "node-steps/s",
                     "h2d_bytes_per_step": int(psi_in.nbytes), "d2h_bytes_per_step": int(psi_out.nbytes),
-                    "how": "per step: H2D psi from pinned memory, glgpu_td (1 step), D2H psi, via the C ABI"},
+                    "how": "per step: H2D psi from pinned memory, glgpu_td (1 step), D2H psi, via the C ABI",
+                    "parts": e2e_parts},
             "gpu_launches": launches,
             "clocks": clk,
             "cpu_baseline": cpu,

@@ -185,6 +185,128 @@ __device__ __forceinline__ bool last_cta_of_instance(CGState* cs, int ntiles) {
 // distinct), so the compiler may keep loaded values across the stores, and they
 // store a node's results after its loads.
 
+// Prefetch (to L2) of what the gradient of node n reads, issued GLGPU_CG_PREFETCH
+// nodes of the tile ahead (0: off) so that a node's loads find their lines on
+// chip: the node's psi row neighbourhood, its link factors and cell bits, its
+// previous gradient and the vector potential of the links around it.  No effect on
+// the results.  At the first node of a tile the next GLGPU_CG_PREFETCH nodes are
+// prefetched together.
+#ifndef GLGPU_CG_PREFETCH
+#define GLGPU_CG_PREFETCH 1
+#endif
+constexpr int kCGPrefetch = GLGPU_CG_PREFETCH;
+// calls pf(q) for the tile positions to prefetch at position r of a tile of rep
+template <typename PF> __device__ __forceinline__ void cg_prefetch_ahead(int r, int rep, const PF& pf) {
+    if (kCGPrefetch <= 0) return;
+    if (r == 0) {
+#pragma unroll
+        for (int q = 1; q <= kCGPrefetch; ++q)
+            if (q < rep) pf(q);
+    } else if (r + kCGPrefetch < rep) {
+        pf(r + kCGPrefetch);
+    }
+}
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+template <typename T>
+__device__ __forceinline__ void grad_prefetch(const Inst& I, const Geo& g, int n, const C2<T>* psi, const C2<T>* U,
+                                              const C2<T>* Gp, const T* ab, const T* GAp) {
+    if (n >= g.N) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    prefetch_l2(I.cbits + n);
+    prefetch_l2(psi + n);
+    if (j > 0) prefetch_l2(psi + n - g.Nx);
+    if (j + 1 < g.Ny) prefetch_l2(psi + n + g.Nx);
+    prefetch_l2(Gp + n);
+    const int la = i + (g.Nx - 1) * j, lb = g.Na + i + g.Nx * j;
+    if (i + 1 < g.Nx) prefetch_l2(U + la);
+    if (j + 1 < g.Ny) prefetch_l2(U + lb);
+    if (j > 0) prefetch_l2(U + lb - g.Nx);
+    if (I.solveA && ab) {
+        if (i + 1 < g.Nx) {
+            prefetch_l2(ab + la);
+            prefetch_l2(GAp + la);
+            if (j > 0) prefetch_l2(ab + la - (g.Nx - 1));
+            if (j + 1 < g.Ny) prefetch_l2(ab + la + (g.Nx - 1));
+        }
+        if (j + 1 < g.Ny) {
+            prefetch_l2(ab + lb);
+            prefetch_l2(GAp + lb);
+        }
+        if (j > 0) prefetch_l2(ab + lb - g.Nx);
+    }
+}
+
+// The same one node ahead for the direction / line-search kernel (state, previous
+// direction and new gradient at the node and its +x / +y neighbours, links) and
+// for the step kernel (state and direction at the node and its +y neighbour,
+// links of the node's cell).
+template <typename T>
+__device__ __forceinline__ void coef_prefetch(const Inst& I, const Geo& g, int n, const C2<T>* psi, const C2<T>* U,
+                                              const C2<T>* G, const C2<T>* dO, const T* ab, const T* GA,
+                                              const T* dAO) {
+    if (n >= g.N) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    prefetch_l2(I.cbits + n);
+    prefetch_l2(psi + n);
+    prefetch_l2(G + n);
+    prefetch_l2(dO + n);
+    if (j + 1 < g.Ny) {
+        prefetch_l2(psi + n + g.Nx);
+        prefetch_l2(G + n + g.Nx);
+        prefetch_l2(dO + n + g.Nx);
+    }
+    const int la = i + (g.Nx - 1) * j, lb = g.Na + i + g.Nx * j;
+    if (i + 1 < g.Nx) prefetch_l2(U + la);
+    if (j + 1 < g.Ny) prefetch_l2(U + lb);
+    if (I.solveA && ab) {
+        if (i + 1 < g.Nx) {
+            prefetch_l2(ab + la);
+            prefetch_l2(GA + la);
+            prefetch_l2(dAO + la);
+            if (j + 1 < g.Ny) {
+                prefetch_l2(ab + la + (g.Nx - 1));
+                prefetch_l2(GA + la + (g.Nx - 1));
+                prefetch_l2(dAO + la + (g.Nx - 1));
+            }
+        }
+        if (j + 1 < g.Ny) {
+            prefetch_l2(ab + lb);
+            prefetch_l2(GA + lb);
+            prefetch_l2(dAO + lb);
+        }
+    }
+}
+template <typename T>
+__device__ __forceinline__ void step_prefetch(const Inst& I, const Geo& g, int n, const C2<T>* psi, const C2<T>* dpsi,
+                                              const T* ab, const T* dA) {
+    if (n >= g.N) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    prefetch_l2(I.cbits + n);
+    prefetch_l2(psi + n);
+    prefetch_l2(dpsi + n);
+    if (j + 1 < g.Ny) {
+        prefetch_l2(psi + n + g.Nx);
+        prefetch_l2(dpsi + n + g.Nx);
+    }
+    if (I.solveA && ab) {
+        const int la = i + (g.Nx - 1) * j, lb = g.Na + i + g.Nx * j;
+        if (i + 1 < g.Nx) {
+            prefetch_l2(ab + la);
+            prefetch_l2(dA + la);
+            if (j + 1 < g.Ny) {
+                prefetch_l2(ab + la + (g.Nx - 1));
+                prefetch_l2(dA + la + (g.Nx - 1));
+            }
+        }
+        if (j + 1 < g.Ny) {
+            prefetch_l2(ab + lb);
+            prefetch_l2(dA + lb);
+        }
+    }
+}
+
 // gradient (new buffer), Polak-Ribiere sums and |g|^2 of one tile
 template <typename T>
 __device__ __forceinline__ void grad_tile(const Inst& I, int n0, int rep, const C2<T>* __restrict__ psi,
@@ -199,6 +321,7 @@ __device__ __forceinline__ void grad_tile(const Inst& I, int n0, int rep, const 
     for (int r = 0; r < kCGRepMax; ++r) {
         if (r >= rep) break;
         const int n = n0 + threadIdx.x + r * kThreads;
+        cg_prefetch_ahead(r, rep, [&](int q) { grad_prefetch<T>(I, g, n0 + threadIdx.x + q * kThreads, psi, U, Gp, ab, GAp); });
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
             const unsigned cb = I.cbits[n];
@@ -483,6 +606,7 @@ __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, int rep, T 
 #pragma unroll kCoefUnroll
     for (int r = 0; r < rep; ++r) {
         const int n = n0 + threadIdx.x + r * kThreads;
+        cg_prefetch_ahead(r, rep, [&](int q) { coef_prefetch<T>(I, g, n0 + threadIdx.x + q * kThreads, psi, U, G, dO, ab, GA, dAO); });
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
             const unsigned cb = I.cbits[n];
@@ -585,6 +709,7 @@ __device__ __forceinline__ void step_tile(const Inst& I, int n0, int rep, T ap, 
     for (int r = 0; r < kCGRepMax; ++r) {
         if (r >= rep) break;
         const int n = n0 + threadIdx.x + r * kThreads;
+        cg_prefetch_ahead(r, rep, [&](int q) { step_prefetch<T>(I, g, n0 + threadIdx.x + q * kThreads, psi, dpsi, ab, dA); });
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
             if (I.solveA) {

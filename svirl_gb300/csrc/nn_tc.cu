@@ -289,9 +289,15 @@ k_conv_tc(const bf16* __restrict__ a1, int Ca1, const bf16* __restrict__ a2, int
 // stage's empty barrier; all four warps then read the accumulator (TMEM lane =
 // output pixel) for the bias + ReLU epilogue.  Waits are bounded.
 // ---------------------------------------------------------------------------
-constexpr int TMA_STAGES = 4;
-constexpr int TMA_SMEM = TMA_STAGES * STAGE_BYTES + 1024 + 128;  // stages, 1024-byte alignment slack, barriers
+#ifndef GLNN_TMA_STAGES
+#define GLNN_TMA_STAGES 2
+#endif
+constexpr int TMA_STAGES = GLNN_TMA_STAGES;  // operand stages of the TMA forward / data gradient
+// stages, 1024-byte alignment slack, then the barriers (full and empty per stage, done)
+// and the TMEM address slot
+constexpr int TMA_SMEM = TMA_STAGES * STAGE_BYTES + 1024 + (2 * TMA_STAGES + 2) * 8;
 constexpr uint32_t kStageTx = (uint32_t)STAGE_BYTES;
+static_assert(TMA_STAGES >= 1 && TMA_SMEM <= 227 * 1024, "TMA conv stages exceed shared memory");
 
 // SM100 shared-memory matrix descriptor, K-major with the 128-byte swizzle:
 // start >> 4 (bits 0-13), leading offset 16 B (unused for this layout), stride
@@ -490,8 +496,12 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
 constexpr int WG_PX = 64;                          // pixels per K chunk
 constexpr int WG_BOX = WG_PX * 64 * 2;             // one 64 x 64 bf16 box: 8 KB
 constexpr int WG_STAGE = 3 * WG_BOX;               // two tap boxes + dy': 24 KB
-constexpr int WG_STAGES = 4;
-constexpr int WG_SMEM = WG_STAGES * WG_STAGE + 1024 + 128;
+#ifndef GLNN_WG_STAGES
+#define GLNN_WG_STAGES 3
+#endif
+constexpr int WG_STAGES = GLNN_WG_STAGES;
+constexpr int WG_SMEM = WG_STAGES * WG_STAGE + 1024 + (2 * WG_STAGES + 2) * 8;
+static_assert(WG_STAGES >= 1 && WG_SMEM <= 227 * 1024, "weight-gradient stages exceed shared memory");
 // kIdesc (M = 128, N = 64, bf16 -> f32) with A and B MN-major (bits 15, 16)
 constexpr uint32_t kIdescMN = kIdesc | (1u << 15) | (1u << 16);
 

@@ -503,7 +503,11 @@ def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=
     iterations are those to enter the band.  An energy that passes through the band
     on the way to a lower minimum does not count.  `reached_warm`, `reached_both`,
     `iters_*_median_both`; `warm_lower_energy` counts the predictions whose minimum
-    is lower than F*_random (another vortex configuration)."""
+    is lower than F*_random (another vortex configuration).
+
+    The random start's energy level: iterations until the energy first falls to
+    F*_random + tol |F*_random| (any state), from both starts, on the instances where
+    both get there: `iters_*_level_median`."""
     import time as _time
     from .relax import HandleCache, relax
     own = cache is None
@@ -532,6 +536,7 @@ def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=
     ok_w = (w["status"] == 4) & same_min
     both = ok_r & ok_w
     ok_wo = (wo["status"] == 4) & (wo["energy"] >= Epred - tol * np.abs(Epred))
+    lvl = (r["status"] == 4) & (w["status"] == 4)
     med = lambda x: float(np.median(x)) if x.size else float("nan")  # noqa: E731
     return {"n": len(insts), "size": insts[0].n,
             "reached_random_own": int(ok_r.sum()), "reached_warm_own": int(ok_wo.sum()),
@@ -539,6 +544,8 @@ def evaluate(net, insts, mode="amplitude", dtype=np.float64, n_iter=20000, gtol=
             "cg_ms_random_own": r["ms"], "cg_ms_warm_own": wo["ms"],
             "reached_random": int(ok_r.sum()), "reached_warm": int(ok_w.sum()), "reached_both": int(both.sum()),
             "iters_random_median_both": med(r["iters"][both]), "iters_warm_median_both": med(w["iters"][both]),
+            "reached_level_both": int(lvl.sum()), "iters_random_level_median": med(r["iters"][lvl]),
+            "iters_warm_level_median": med(w["iters"][lvl]),
             "net_ms": 1e3 * t_net,
             "warm_lower_energy": int((Epred < lo).sum()), "warm_higher_energy": int((Epred > Estar + tol * np.abs(Estar)).sum())}
 
