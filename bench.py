@@ -544,6 +544,8 @@ def run_conv(args):
     ms_d_gather = timed(bd_gather, args.steps)
     ms_w_mma = timed(bw, args.steps)
     lib.glnn_set_conv_tma(1)
+    ms_f_tile, ms_d_tile = timed(f, args.steps), timed(bd, args.steps)
+    lib.glnn_set_conv_tma(2)
     ms_f, ms_mk, ms_d, ms_w = timed(f, args.steps), timed(mk, args.steps), timed(bd, args.steps), timed(bw, args.steps)
     assert int(err.item()) == 0
     peak = 1922.0
@@ -551,7 +553,7 @@ def run_conv(args):
     if os.path.exists(pth):
         peak = float(json.load(open(pth))["bf16_tflops"])
     tf = flop / (ms_f * 1e-3) / 1e12
-    line = {"metric": "3x3 conv TFLOP/s (tcgen05 forward with TMA operands, 32x128x128x64->64, bf16 in, fp32 accumulate)",
+    line = {"metric": "3x3 conv TFLOP/s (tcgen05 forward with TMA operands, persistent CTAs, 32x128x128x64->64, bf16 in, fp32 accumulate)",
             "value": tf,
             "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": 3, "ms_per_step": ms_f,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
@@ -561,6 +563,9 @@ def run_conv(args):
                          "peak_kind": "measured bf16 burst"},
             "forward_gather": {"ms": ms_f_gather, "tflops": flop / (ms_f_gather * 1e-3) / 1e12,
                                "kernel": "tcgen05, operands gathered by the threads"},
+            "forward_tma_per_tile": {"ms": ms_f_tile, "tflops": flop / (ms_f_tile * 1e-3) / 1e12,
+                                     "kernel": "tcgen05, TMA operands, one output tile per CTA"},
+            "data_grad_tma_per_tile": {"ms": ms_d_tile, "tflops": flop / (ms_d_tile * 1e-3) / 1e12},
             "relu_mask": {"ms": ms_mk, "kernel": "dy * relu'(y), once per backward"},
             "data_grad": {"ms": ms_d, "tflops": flop / (ms_d * 1e-3) / 1e12,
                           "kernel": "tcgen05, operands loaded by TMA (masked dy)"},
@@ -774,11 +779,12 @@ def main():
     e2e_value = world * N * e2e_steps / e2e_s
     # where the end-to-end step's time goes: the same three calls timed apart
     t_parts = [0.0, 0.0, 0.0]
+    dev_ms = 0.0
     for _ in range(e2e_steps):
         t1 = time.perf_counter()
         h.set_psi(psi_in)
         t2 = time.perf_counter()
-        h.td(DT, 1, 0)
+        dev_ms += h.td_timed(DT, 1, 0)[1]
         t3 = time.perf_counter()
         assert h.lib.glgpu_get_order_parameter(h.h, psi_out.ctypes.data_as(__import__("ctypes").c_void_p)) == 0
         t4 = time.perf_counter()
@@ -786,6 +792,7 @@ def main():
         t_parts[1] += t3 - t2
         t_parts[2] += t4 - t3
     e2e_parts = {"h2d_ms": 1e3 * t_parts[0] / e2e_steps, "td_step_ms": 1e3 * t_parts[1] / e2e_steps,
+                 "td_step_graph_ms": dev_ms / e2e_steps,
                  "d2h_ms": 1e3 * t_parts[2] / e2e_steps,
                  "h2d_GBps": psi_in.nbytes / (t_parts[0] / e2e_steps) / 1e9,
                  "d2h_GBps": psi_out.nbytes / (t_parts[2] / e2e_steps) / 1e9}

@@ -37,11 +37,14 @@ extern "C" {
 int glnn_conv3x3_fwd(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* wb, const float* bias,
                      void* y, int32_t n, int32_t h, int32_t w, int32_t cout, int32_t relu, int32_t* err, void* stream);
 
-/* Operand loads of glnn_conv3x3_fwd: 1 (default) = by TMA (cp.async.bulk.tensor
- * from 4-D / 2-D tensor maps, 4-stage pipeline) for the shapes it takes
- * (c1, c2, cout multiples of 64; w a multiple of 128 or a divisor of 128; h*w a
- * multiple of 128), the thread gather otherwise; 0 = always the thread gather.
- * The same switch selects the tcgen05 weight gradient (1) or the mma.sync one (0).
+/* Operand loads of glnn_conv3x3_fwd (and of glnn_conv3x3_bwd_data with relu = 0):
+ * 2 (default) = by TMA (cp.async.bulk.tensor from 4-D / 2-D / 3-D tensor maps) in a
+ * persistent kernel (CTAs loop over output tiles, two tensor-memory accumulators,
+ * the epilogue of one tile under the MMAs of the next); 1 = by TMA, one output tile
+ * per CTA; both for the shapes they take (c1, c2, cout multiples of 64; w a multiple
+ * of 128 or a divisor of 128; h*w a multiple of 128), the thread gather otherwise;
+ * 0 = always the thread gather.  Every setting computes the same values bitwise.
+ * Nonzero also selects the tcgen05 weight gradient (0: the mma.sync one).
  * Process-wide. */
 int glnn_set_conv_tma(int32_t enable);
 /* [dx1|dx2] = conv3x3^T(dy * relu'(y), Wt), on tcgen05 like the forward.  y may be

@@ -474,6 +474,189 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
 
 
 // ---------------------------------------------------------------------------
+// Persistent form of k_conv_fwd_tma (same MODEs, operands, stage layout and MMA
+// order per tile, so the same values bitwise): a CTA loops over output tiles
+// (tile t = n-tile * m-tiles + m-tile, t += gridDim.x) with one operand ring that
+// runs across tile boundaries and two accumulators in tensor memory, so the
+// epilogue of one tile runs while the MMAs of the next are issued.  Warp 0 lane 0
+// issues the TMA copies, warp 1 lane 0 the MMAs; warps 2-5 are the epilogue (warp w
+// reads TMEM lanes 32 (w % 4) .. + 31).  Barriers: full / empty per stage, acc_full
+// per accumulator (the MMAs of a tile committed), acc_empty per accumulator (the
+// four epilogue warps have read it).  Every wait is bounded; a role that gives up
+// records the error and stops, the others then run out their own bounded waits.
+// ---------------------------------------------------------------------------
+constexpr int P_THREADS = 192;
+constexpr int P_STAGES = TMA_STAGES + 1;
+constexpr int P_SMEM = P_STAGES * STAGE_BYTES + 1024 + (2 * P_STAGES + 4) * 8 + 16;
+constexpr uint32_t kTmemColsP = 2 * TN;  // two FP32 accumulators of TN columns
+static_assert(P_SMEM <= 227 * 1024, "persistent conv stages exceed shared memory");
+
+template <int MODE, int RELU>
+__global__ void __launch_bounds__(P_THREADS)
+k_conv_tma_persist(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ CUtensorMap ta2,
+                   const __grid_constant__ CUtensorMap tb, const float* __restrict__ bias, bf16* __restrict__ y,
+                   int Cout, bf16* __restrict__ o2, int Co2, int C1, int C2, int H, int W, int nmt, int ntiles,
+                   int* err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + P_STAGES * STAGE_BYTES);
+    uint64_t* empty = full + P_STAGES;
+    uint64_t* acc_full = empty + P_STAGES;
+    uint64_t* acc_empty = acc_full + 2;
+    uint32_t* tslot = (uint32_t*)(acc_empty + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nck = (C1 + C2) / TK, nk = 9 * nck;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)),
+                     "r"(kTmemColsP)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int q = 0; q < P_STAGES; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(full + q)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(empty + q)) : "memory");
+        }
+        for (int q = 0; q < 2; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(acc_full + q)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(saddr(acc_empty + q)) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int g = 0;  // chunks issued by this CTA, across its tiles
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int m0 = (t % nmt) * TM, n0 = (t / nmt) * TN;
+                const int img = m0 / (H * W), rem = m0 - img * H * W, y0 = rem / W, x0 = rem - y0 * W;
+                for (int kc = 0; kc < nk; ++kc, ++g) {
+                    const int st = g % P_STAGES, use = g / P_STAGES;
+                    if (use > 0 && !wait_parity(saddr(empty + st), (uint32_t)((use + 1) & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    const int tap = kc / nck, cc = kc - tap * nck;
+                    const int sgn = MODE == 0 ? 1 : -1;
+                    const int dy = sgn * (tap / 3 - 1), dx = sgn * (tap % 3 - 1);
+                    const int c = cc * TK;
+                    const uint32_t a_dst = saddr(smem + st * STAGE_BYTES), b_dst = a_dst + A_BYTES;
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(full + st)),
+                                 "r"(kStageTx)
+                                 : "memory");
+                    if (c < C1) tma_load_4d(a_dst, &ta1, c, x0 + dx, y0 + dy, img, saddr(full + st));
+                    else tma_load_4d(a_dst, &ta2, c - C1, x0 + dx, y0 + dy, img, saddr(full + st));
+                    if (MODE == 0) tma_load_2d(b_dst, &tb, tap * (C1 + C2) + c, n0, saddr(full + st));
+                    else tma_load_3d(b_dst, &tb, c, n0, tap, saddr(full + st));
+                }
+            }
+            // copies still in flight land before the CTA leaves: wait (bounded) for the
+            // last stages issued
+            for (int q = 0; q < P_STAGES && q < g; ++q) {
+                const int gg = g - 1 - q, st = gg % P_STAGES, use = gg / P_STAGES;
+                wait_parity(saddr(full + st), (uint32_t)(use & 1));
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int g = 0, lt = 0;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
+                const int acc = lt & 1, ause = lt >> 1;
+                if (ause > 0 && !wait_parity(saddr(acc_empty + acc), (uint32_t)((ause + 1) & 1))) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)(acc * TN);
+                for (int kc = 0; kc < nk; ++kc, ++g) {
+                    const int st = g % P_STAGES, use = g / P_STAGES;
+                    if (!wait_parity(saddr(full + st), (uint32_t)(use & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t a0 = saddr(smem + st * STAGE_BYTES), b0 = a0 + A_BYTES;
+#pragma unroll
+                    for (int j = 0; j < TK / 16; ++j)
+                        mma_f16(d, smem_desc_sw128(a0 + 32 * j), smem_desc_sw128(b0 + 32 * j), kIdesc,
+                                (kc > 0 || j > 0) ? 1u : 0u);
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                     saddr(empty + st))
+                                 : "memory");
+                }
+                // the tile's accumulator is complete once its MMAs are (committed even
+                // after a failed wait, so the epilogue's wait ends)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 saddr(acc_full + acc))
+                             : "memory");
+            }
+        }
+        __syncwarp();
+    } else {
+        // epilogue warps 2..5: TMEM lane quarter w % 4
+        const int quarter = warp & 3;
+        int lt = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+            const int acc = lt & 1, ause = lt >> 1;
+            const bool got = wait_parity(saddr(acc_full + acc), (uint32_t)(ause & 1));
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (!got) {
+                ok = false;
+                break;
+            }
+            const int m0 = (t % nmt) * TM, n0 = (t / nmt) * TN;
+            const int p = m0 + quarter * 32 + lane;  // TMEM lane = tile row = pixel
+#pragma unroll
+            for (int c = 0; c < TN; c += 16) {
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                    : "r"(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TN + c))
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (MODE == 0) {
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        const int col = n0 + c + q;
+                        float v0 = __uint_as_float(r[q]) + bias[col], v1 = __uint_as_float(r[q + 1]) + bias[col + 1];
+                        if (RELU) {
+                            v0 = fmaxf(v0, 0.f);
+                            v1 = fmaxf(v1, 0.f);
+                        }
+                        *(__nv_bfloat162*)(y + (size_t)p * Cout + col) = __floats2bfloat162_rn(v0, v1);
+                    }
+                } else {
+                    bf16* out = n0 < Cout ? y + (size_t)p * Cout + n0 : o2 + (size_t)p * Co2 + (n0 - Cout);
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2)
+                        *(__nv_bfloat162*)(out + c + q) =
+                            __floats2bfloat162_rn(__uint_as_float(r[q]), __uint_as_float(r[q + 1]));
+                }
+            }
+            // this warp has read the accumulator: the MMAs of the tile after next may use it
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(saddr(acc_empty + acc)) : "memory");
+        }
+    }
+    if (!ok) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemColsP) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Weight gradient on tcgen05 with TMA operands: dW[co][tap][ci] =
 // sum_p dy'[p][co] x[p + off(tap)][ci] (dy' = dy * relu'(y), formed by
 // k_relu_mask_dy beforehand), as D[m][co] = sum_k A[m][k] B[k][co] with
@@ -664,7 +847,7 @@ template <int MODE, int RELU> static cudaError_t conv_tc_smem_attr() {
 }
 
 // --- TMA forward: tensor maps and the shapes it takes -------------------------
-static int g_conv_tma = 1;  // glnn_set_conv_tma
+static int g_conv_tma = 2;  // glnn_set_conv_tma: 0 thread gather, 1 TMA per tile, 2 TMA persistent
 
 static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -733,14 +916,41 @@ static bool weight_t_map(CUtensorMap* m, const void* base, int cin, int cout) {
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+template <int MODE, int RELU> static cudaError_t conv_persist_smem_attr() {
+    static cudaError_t e =
+        cudaFuncSetAttribute(k_conv_tma_persist<MODE, RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, P_SMEM);
+    return e;
+}
+
+// grid of the persistent kernel: its resident CTAs on every SM, at most one per tile
+static int persist_grid(int ntiles) {
+    static int ctas = 0;
+    if (!ctas) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        conv_persist_smem_attr<0, 0>();  // the occupancy query needs the kernel's shared-memory limit raised
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv_tma_persist<0, 0>, P_THREADS, P_SMEM);
+        ctas = (sms > 0 ? sms : 152) * (per > 0 ? per : 1);
+    }
+    return ntiles < ctas ? ntiles : ctas;
+}
+
 // data gradient without a ReLU derivative (dy already masked) by TMA: 1 launched, 0 not taken
 static int conv_bwd_data_tma(const void* dy, const void* wt, void* dx1, int c1, void* dx2, int c2, int n, int h, int w,
                              int cout, int* err, cudaStream_t s) {
     if (!g_conv_tma || !conv_tma_shape_ok(c1, c2, h, w, cout)) return 0;
     CUtensorMap ta, tb;
     if (!act_map(&ta, dy, cout, n, h, w) || !weight_t_map(&tb, wt, c1 + c2, cout)) return 0;
-    if (conv_tma_smem_attr<1, 0>() != cudaSuccess) return 0;
     const long long P = (long long)n * h * w;
+    if (g_conv_tma == 2) {
+        if (conv_persist_smem_attr<1, 0>() != cudaSuccess) return 0;
+        const int nmt = (int)(P / TM), ntiles = nmt * ((c1 + c2) / TN);
+        k_conv_tma_persist<1, 0><<<persist_grid(ntiles), P_THREADS, P_SMEM, s>>>(
+            ta, ta, tb, nullptr, (bf16*)dx1, c1, (bf16*)dx2, c2, cout, 0, h, w, nmt, ntiles, err);
+        return 1;
+    }
+    if (conv_tma_smem_attr<1, 0>() != cudaSuccess) return 0;
     dim3 grid((unsigned)(P / TM), (unsigned)((c1 + c2) / TN));
     k_conv_fwd_tma<1, 0><<<grid, NTH, TMA_SMEM, s>>>(ta, ta, tb, nullptr, (bf16*)dx1, c1, (bf16*)dx2, c2, cout, 0, h, w,
                                                      err);
@@ -759,8 +969,20 @@ static int conv_fwd_tma(const void* x1, int c1, const void* x2, int c2, const vo
         t2 = t1;
     }
     if (!weight_map(&tb, wb, 9LL * (c1 + c2), cout)) return 0;
-    if ((relu ? conv_tma_smem_attr<0, 1>() : conv_tma_smem_attr<0, 0>()) != cudaSuccess) return 0;
     const long long P = (long long)n * h * w;
+    if (g_conv_tma == 2) {
+        if ((relu ? conv_persist_smem_attr<0, 1>() : conv_persist_smem_attr<0, 0>()) != cudaSuccess) return 0;
+        const int nmt = (int)(P / TM), ntiles = nmt * (cout / TN);
+        const int gs = persist_grid(ntiles);
+        if (relu)
+            k_conv_tma_persist<0, 1><<<gs, P_THREADS, P_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2,
+                                                                   h, w, nmt, ntiles, err);
+        else
+            k_conv_tma_persist<0, 0><<<gs, P_THREADS, P_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2,
+                                                                   h, w, nmt, ntiles, err);
+        return 1;
+    }
+    if ((relu ? conv_tma_smem_attr<0, 1>() : conv_tma_smem_attr<0, 0>()) != cudaSuccess) return 0;
     dim3 grid((unsigned)(P / TM), (unsigned)(cout / TN));
     if (relu)
         k_conv_fwd_tma<0, 1><<<grid, NTH, TMA_SMEM, s>>>(t1, t2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2, h, w, err);
@@ -828,7 +1050,7 @@ static int conv_tc_args_ok(int c1, int c2, int n, int h, int w, int cout) {
 extern "C" {
 
 int glnn_set_conv_tma(int32_t enable) {
-    g_conv_tma = enable ? 1 : 0;
+    g_conv_tma = enable <= 0 ? 0 : (enable == 1 ? 1 : 2);
     return GLGPU_OK;
 }
 

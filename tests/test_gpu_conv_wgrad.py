@@ -21,9 +21,9 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def _grads(L, x1, x2, W, b, dy, relu, tma):
+def _grads(L, x1, x2, W, b, dy, relu, mode):
     lib = L._lib_nn()
-    lib.glnn_set_conv_tma(1 if tma else 0)
+    lib.glnn_set_conv_tma(mode)
     try:
         tx1 = torch.from_numpy(x1).to("cuda", torch.bfloat16).requires_grad_()
         tx2 = torch.from_numpy(x2).to("cuda", torch.bfloat16).requires_grad_() if x2 is not None else None
@@ -37,7 +37,7 @@ def _grads(L, x1, x2, W, b, dy, relu, tma):
         dx = f(g[2]) if tx2 is None else np.concatenate([f(g[2]), f(g[3])], axis=3)
         return f(y), f(g[0]), f(g[1]), dx
     finally:
-        lib.glnn_set_conv_tma(1)
+        lib.glnn_set_conv_tma(2)
 
 
 @pytest.mark.parametrize("shape", [(2, 16, 16, 64, 0, 64), (1, 32, 128, 64, 64, 128), (1, 8, 64, 128, 0, 64),
@@ -53,9 +53,13 @@ def test_tcgen05_weight_gradient(shape, relu):
     b = (rng.standard_normal(cout) * 0.1).astype(np.float32)
     dy = R.bf16_round(rng.standard_normal((n, h, w, cout)).astype(np.float32))
     xc = x1 if x2 is None else np.concatenate([x1, x2], axis=3)
-    y_t, gw_t, gb_t, dx_t = _grads(L, x1, x2, W, b, dy, relu, True)
+    y_t, gw_t, gb_t, dx_t = _grads(L, x1, x2, W, b, dy, relu, 2)
     L.check_kernel_errors()
-    y_m, gw_m, gb_m, dx_m = _grads(L, x1, x2, W, b, dy, relu, False)
+    y_1, gw_1, gb_1, dx_1 = _grads(L, x1, x2, W, b, dy, relu, 1)
+    L.check_kernel_errors()
+    y_m, gw_m, gb_m, dx_m = _grads(L, x1, x2, W, b, dy, relu, 0)
+    # one tile per CTA and persistent: the same values
+    assert np.array_equal(y_t, y_1) and np.array_equal(dx_t, dx_1) and np.array_equal(gw_t, gw_1)
     dx_ref, dw_ref, db_ref = R.conv3x3_bwd(xc, R.bf16_round(W), y_t, dy, relu)
     e_dx = np.abs(dx_t - dx_ref).max() / np.abs(dx_ref).max()
     print("shape %s relu %d: TMA dx vs reference %.2e, vs gather max |diff| %.2e"
