@@ -241,7 +241,10 @@ def run_reference(args):
     split into row blocks over all host cores (oracle/parallel_np.py, bitwise the
     single-process result), `warmup` untimed TD steps, then `steps` timed ones
     (steps warmup+1 .. warmup+steps, as the GPU run times); value = nodes x steps /
-    wall time of the timed steps."""
+    wall time of the timed steps.  A run stays within a few minutes: at most 20
+    warm-up and 100 timed steps (about 0.8 s each on 16 cores) are run, a bounded
+    sample of the GPU run's steps; the line states the sample and its mean sweeps
+    per step, and node-sweeps/s beside node-steps/s."""
     from oracle.parallel_np import SharedTD, timed_steps
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -250,22 +253,27 @@ def run_reference(args):
     orc = make_oracle(N_SIDE, seed=0)
     td = SharedTD(N_SIDE, N_SIDE, DX, DX, orc.psi, orc.ab, mt=orc.mt, dt=DT, processes=cores)
     del orc
+    warm, steps = min(args.warmup, 20), min(args.steps, 100)
     try:
-        wall = timed_steps(td, args.warmup, args.steps)
-        sweeps = td.sweeps[args.warmup:]
+        wall = timed_steps(td, warm, steps)
+        sweeps = td.sweeps[warm:]
     finally:
         td.close()
-    value = N_SIDE * N_SIDE * args.steps / wall
+    value = N_SIDE * N_SIDE * steps / wall
     line = {"metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "impl": "reference",
             "config": {"workload": "tdgl_2049_kinf_holes5", "Nx": N_SIDE, "Ny": N_SIDE, "same_config": True,
-                       "processes": td.P, "mean_sweeps_per_step": float(np.mean(sweeps))},
+                       "processes": td.P, "mean_sweeps_per_step": float(np.mean(sweeps)),
+                       "timed_steps": steps, "warmup_steps": warm,
+                       "node_sweeps_per_s": N_SIDE * N_SIDE * float(np.sum(sweeps)) / wall},
             "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": td.P, "kind": "port",
                              "sample": "the whole %dx%d workload (seed 0), one trajectory, %d untimed then %d timed "
-                                       "TD steps; NumPy FP64 oracle split into %d row blocks, one process per core"
-                                       % (N_SIDE, N_SIDE, args.warmup, args.steps, td.P)},
+                                       "TD steps (steps %d..%d; at most 20 + 100 of the requested %d + %d); NumPy "
+                                       "FP64 oracle split into %d row blocks, one process per core"
+                                       % (N_SIDE, N_SIDE, warm, steps, warm + 1, warm + steps, args.warmup,
+                                          args.steps, td.P)},
             "e2e": {"value": value, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     try:
         line["reference_kernels_gb300"] = reference_kernels_gpu(args)
