@@ -486,7 +486,10 @@ k_conv_fwd_tma(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ 
 // records the error and stops, the others then run out their own bounded waits.
 // ---------------------------------------------------------------------------
 constexpr int P_THREADS = 192;
-constexpr int P_STAGES = TMA_STAGES + 1;
+#ifndef GLNN_P_STAGES
+#define GLNN_P_STAGES 3
+#endif
+constexpr int P_STAGES = GLNN_P_STAGES;  // operand stages of the persistent kernel (the ring runs across tiles)
 constexpr int P_SMEM = P_STAGES * STAGE_BYTES + 1024 + (2 * P_STAGES + 4) * 8 + 16;
 constexpr uint32_t kTmemColsP = 2 * TN;  // two FP32 accumulators of TN columns
 static_assert(P_SMEM <= 227 * 1024, "persistent conv stages exceed shared memory");
