@@ -118,6 +118,7 @@ static void free_all(glgpu_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->hscal) cudaFreeHost(h->hscal);
+    if (h->pin) cudaFreeHost(h->pin);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -181,6 +182,7 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     ok = ok && cudaMalloc(&h->out, nab > (size_t)h->g.Nxc * h->g.Nyc * rs ? nab : (size_t)h->g.Nxc * h->g.Nyc * rs) == cudaSuccess;
     ok = ok && cudaMalloc(&h->vort_n, sizeof(int)) == cudaSuccess;
     ok = ok && cudaMallocHost(&h->hscal, sizeof(double) * 32) == cudaSuccess;
+    ok = ok && cudaMallocHost(&h->pin, sizeof(PinStage)) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         free_all(h);
@@ -563,6 +565,9 @@ int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** ou
     ok = ok && cudaMalloc(&b->tiles, sizeof(Tile) * tiles.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&b->items, sizeof(Item) * items.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&b->loop, sizeof(LoopState)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&b->gather_pin, sizeof(InstState) * (size_t)n) == cudaSuccess;
+    ok = ok && cudaMallocHost(&b->loop_pin, sizeof(LoopState)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&b->insts_pin, sizeof(Inst) * (size_t)n) == cudaSuccess;
     cudaError_t e = ok ? cudaSuccess : cudaErrorMemoryAllocation;
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->items, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice, b->stream);
@@ -586,6 +591,9 @@ int glgpu_batch_destroy(glgpu_batch* b) {
     void* ptrs[] = {b->insts, b->gather, b->tiles, b->items, b->loop, b->cg_partials, b->cg_loop, b->cg_tiles};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    void* pins[] = {b->gather_pin, b->loop_pin, b->insts_pin};
+    for (void* p : pins)
+        if (p) cudaFreeHost(p);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return GLGPU_OK;

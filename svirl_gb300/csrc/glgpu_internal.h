@@ -206,12 +206,21 @@ struct glgpu_handle {
     void* flush = nullptr;              // L2 flush buffer for kernel timing
     // host pinned staging for small results
     double* hscal = nullptr;
+    void* pin = nullptr;                // PinStage (pinned host memory)
 };
 
 // A batch: several handles (instances of any sizes and parameters, one dtype,
 // one device) advanced together.  Their descriptors, item and tile tables are
 // concatenated, so one sweep launch covers every instance and each instance
 // keeps its own Jacobi stop rule.
+// Pinned host staging of a handle's per-call copies (descriptor up, loop state and
+// statistics down).
+struct PinStage {
+    glgpu::Inst inst;
+    glgpu::InstState st;
+    glgpu::LoopState loop;
+};
+
 struct glgpu_batch {
     int dtype = 4, device = 0, ninst = 0;
     std::vector<glgpu_handle*> hs;
@@ -222,6 +231,9 @@ struct glgpu_batch {
     glgpu::LoopState* loop = nullptr;
     glgpu::InstState* gather = nullptr;
     std::vector<glgpu::InstState> gather_h;
+    glgpu::InstState* gather_pin = nullptr;  // pinned host copies of the per-call transfers
+    glgpu::LoopState* loop_pin = nullptr;
+    glgpu::Inst* insts_pin = nullptr;
     int ntiles = 0, nitems = 0, psi_grid = 0, strip_rows = 0;
     std::vector<int> inst_items;         // psi sweep items of each instance (at strip_rows)
     cudaGraphExec_t td_exec[glgpu::kTDGraphs] = {};

@@ -660,6 +660,195 @@ k_conv_tma_persist(const __grid_constant__ CUtensorMap ta1, const __grid_constan
 }
 
 // ---------------------------------------------------------------------------
+// k_conv_tma_persist with the B operand resident: a CTA works on one output-channel
+// tile (n-tile = blockIdx.x % NT) and loops over pixel tiles; it loads the n-tile's
+// weights (all 9 taps x input-channel chunks, 8 KB each) into shared memory once,
+// and only the shifted activation boxes (16 KB per chunk) stream through the ring.
+// This removes the weight re-reads, a third of the bytes that move from L2 into the
+// SMs.  Used when the weights of an n-tile fit (at most two 64-channel input
+// chunks); the same MMAs in the same order, so the same values bitwise.
+// ---------------------------------------------------------------------------
+constexpr int BR_MAX_CHUNKS = 18;  // 9 taps x 2 input-channel chunks
+__host__ __device__ constexpr int br_smem_bytes(int nk) {
+    return P_STAGES * A_BYTES + nk * B_BYTES + 1024 + (2 * P_STAGES + 5) * 8 + 16;
+}
+static_assert(br_smem_bytes(BR_MAX_CHUNKS) <= 227 * 1024, "resident-weight conv exceeds shared memory");
+
+template <int MODE, int RELU>
+__global__ void __launch_bounds__(P_THREADS)
+k_conv_tma_bres(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ CUtensorMap ta2,
+                const __grid_constant__ CUtensorMap tb, const float* __restrict__ bias, bf16* __restrict__ y, int Cout,
+                bf16* __restrict__ o2, int Co2, int C1, int C2, int H, int W, int nmt, int NT, int* err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int nck = (C1 + C2) / TK, nk = 9 * nck;
+    unsigned char* bres = smem + P_STAGES * A_BYTES;
+    uint64_t* full = (uint64_t*)(bres + nk * B_BYTES);
+    uint64_t* empty = full + P_STAGES;
+    uint64_t* acc_full = empty + P_STAGES;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* b_full = acc_empty + 2;
+    uint32_t* tslot = (uint32_t*)(b_full + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int cpn = gridDim.x / NT;  // CTAs per n-tile
+    const int nt = blockIdx.x % NT, mt0 = blockIdx.x / NT, n0 = nt * TN;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)),
+                     "r"(kTmemColsP)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int q = 0; q < P_STAGES; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(full + q)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(empty + q)) : "memory");
+        }
+        for (int q = 0; q < 2; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(acc_full + q)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(saddr(acc_empty + q)) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(b_full)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // the n-tile's weights, once
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(b_full)),
+                         "r"((uint32_t)(nk * B_BYTES))
+                         : "memory");
+            for (int kc = 0; kc < nk; ++kc) {
+                const int tap = kc / nck, c = (kc - tap * nck) * TK;
+                const uint32_t b_dst = saddr(bres + kc * B_BYTES);
+                if (MODE == 0) tma_load_2d(b_dst, &tb, tap * (C1 + C2) + c, n0, saddr(b_full));
+                else tma_load_3d(b_dst, &tb, c, n0, tap, saddr(b_full));
+            }
+            int g = 0;
+            for (int mt = mt0; mt < nmt && ok; mt += cpn) {
+                const int m0 = mt * TM;
+                const int img = m0 / (H * W), rem = m0 - img * H * W, y0 = rem / W, x0 = rem - y0 * W;
+                for (int kc = 0; kc < nk; ++kc, ++g) {
+                    const int st = g % P_STAGES, use = g / P_STAGES;
+                    if (use > 0 && !wait_parity(saddr(empty + st), (uint32_t)((use + 1) & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    const int tap = kc / nck, cc = kc - tap * nck;
+                    const int sgn = MODE == 0 ? 1 : -1;
+                    const int dy = sgn * (tap / 3 - 1), dx = sgn * (tap % 3 - 1);
+                    const int c = cc * TK;
+                    const uint32_t a_dst = saddr(smem + st * A_BYTES);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(full + st)),
+                                 "r"((uint32_t)A_BYTES)
+                                 : "memory");
+                    if (c < C1) tma_load_4d(a_dst, &ta1, c, x0 + dx, y0 + dy, img, saddr(full + st));
+                    else tma_load_4d(a_dst, &ta2, c - C1, x0 + dx, y0 + dy, img, saddr(full + st));
+                }
+            }
+            // copies still in flight land before the CTA leaves (bounded waits)
+            wait_parity(saddr(b_full), 0u);
+            for (int q = 0; q < P_STAGES && q < g; ++q) {
+                const int gg = g - 1 - q, st = gg % P_STAGES, use = gg / P_STAGES;
+                wait_parity(saddr(full + st), (uint32_t)(use & 1));
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            if (!wait_parity(saddr(b_full), 0u)) ok = false;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            int g = 0, lt = 0;
+            for (int mt = mt0; mt < nmt && ok; mt += cpn, ++lt) {
+                const int acc = lt & 1, ause = lt >> 1;
+                if (ause > 0 && !wait_parity(saddr(acc_empty + acc), (uint32_t)((ause + 1) & 1))) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)(acc * TN);
+                for (int kc = 0; kc < nk; ++kc, ++g) {
+                    const int st = g % P_STAGES, use = g / P_STAGES;
+                    if (!wait_parity(saddr(full + st), (uint32_t)(use & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t a0 = saddr(smem + st * A_BYTES), b0 = saddr(bres + kc * B_BYTES);
+#pragma unroll
+                    for (int j = 0; j < TK / 16; ++j)
+                        mma_f16(d, smem_desc_sw128(a0 + 32 * j), smem_desc_sw128(b0 + 32 * j), kIdesc,
+                                (kc > 0 || j > 0) ? 1u : 0u);
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                     saddr(empty + st))
+                                 : "memory");
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 saddr(acc_full + acc))
+                             : "memory");
+            }
+        }
+        __syncwarp();
+    } else {
+        const int quarter = warp & 3;
+        int lt = 0;
+        for (int mt = mt0; mt < nmt; mt += cpn, ++lt) {
+            const int acc = lt & 1, ause = lt >> 1;
+            const bool got = wait_parity(saddr(acc_full + acc), (uint32_t)(ause & 1));
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (!got) {
+                ok = false;
+                break;
+            }
+            const int p = mt * TM + quarter * 32 + lane;
+#pragma unroll
+            for (int c = 0; c < TN; c += 16) {
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                    : "r"(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TN + c))
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (MODE == 0) {
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        const int col = n0 + c + q;
+                        float v0 = __uint_as_float(r[q]) + bias[col], v1 = __uint_as_float(r[q + 1]) + bias[col + 1];
+                        if (RELU) {
+                            v0 = fmaxf(v0, 0.f);
+                            v1 = fmaxf(v1, 0.f);
+                        }
+                        *(__nv_bfloat162*)(y + (size_t)p * Cout + col) = __floats2bfloat162_rn(v0, v1);
+                    }
+                } else {
+                    bf16* out = n0 < Cout ? y + (size_t)p * Cout + n0 : o2 + (size_t)p * Co2 + (n0 - Cout);
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2)
+                        *(__nv_bfloat162*)(out + c + q) =
+                            __floats2bfloat162_rn(__uint_as_float(r[q]), __uint_as_float(r[q + 1]));
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(saddr(acc_empty + acc)) : "memory");
+        }
+    }
+    if (!ok) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemColsP) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Weight gradient on tcgen05 with TMA operands: dW[co][tap][ci] =
 // sum_p dy'[p][co] x[p + off(tap)][ci] (dy' = dy * relu'(y), formed by
 // k_relu_mask_dy beforehand), as D[m][co] = sum_k A[m][k] B[k][co] with
@@ -925,6 +1114,24 @@ template <int MODE, int RELU> static cudaError_t conv_persist_smem_attr() {
     return e;
 }
 
+template <int MODE, int RELU> static cudaError_t conv_bres_smem_attr() {
+    static cudaError_t e = cudaFuncSetAttribute(k_conv_tma_bres<MODE, RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                br_smem_bytes(BR_MAX_CHUNKS));
+    return e;
+}
+
+// grid of the resident-weight kernel: NT x (CTAs per n-tile), the CTAs that fit on
+// all SMs at this shared-memory size, at most one per pixel tile of an n-tile
+template <int MODE, int RELU> static int bres_grid(int NT, int nmt, int smem) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv_tma_bres<MODE, RELU>, P_THREADS, smem);
+    int cpn = (sms > 0 ? sms : 152) * (per > 0 ? per : 1) / NT;
+    cpn = cpn < 1 ? 1 : (cpn > nmt ? nmt : cpn);
+    return NT * cpn;
+}
+
 // grid of the persistent kernel: its resident CTAs on every SM, at most one per tile
 static int persist_grid(int ntiles) {
     static int ctas = 0;
@@ -946,6 +1153,13 @@ static int conv_bwd_data_tma(const void* dy, const void* wt, void* dx1, int c1, 
     CUtensorMap ta, tb;
     if (!act_map(&ta, dy, cout, n, h, w) || !weight_t_map(&tb, wt, c1 + c2, cout)) return 0;
     const long long P = (long long)n * h * w;
+    if (g_conv_tma == 2 && 9 * (cout / TK) <= BR_MAX_CHUNKS) {
+        if (conv_bres_smem_attr<1, 0>() != cudaSuccess) return 0;
+        const int nmt = (int)(P / TM), NT = (c1 + c2) / TN, smem = br_smem_bytes(9 * (cout / TK));
+        k_conv_tma_bres<1, 0><<<bres_grid<1, 0>(NT, nmt, smem), P_THREADS, smem, s>>>(
+            ta, ta, tb, nullptr, (bf16*)dx1, c1, (bf16*)dx2, c2, cout, 0, h, w, nmt, NT, err);
+        return 1;
+    }
     if (g_conv_tma == 2) {
         if (conv_persist_smem_attr<1, 0>() != cudaSuccess) return 0;
         const int nmt = (int)(P / TM), ntiles = nmt * ((c1 + c2) / TN);
@@ -973,6 +1187,17 @@ static int conv_fwd_tma(const void* x1, int c1, const void* x2, int c2, const vo
     }
     if (!weight_map(&tb, wb, 9LL * (c1 + c2), cout)) return 0;
     const long long P = (long long)n * h * w;
+    if (g_conv_tma == 2 && 9 * ((c1 + c2) / TK) <= BR_MAX_CHUNKS) {
+        if ((relu ? conv_bres_smem_attr<0, 1>() : conv_bres_smem_attr<0, 0>()) != cudaSuccess) return 0;
+        const int nmt = (int)(P / TM), NT = cout / TN, smem = br_smem_bytes(9 * ((c1 + c2) / TK));
+        if (relu)
+            k_conv_tma_bres<0, 1><<<bres_grid<0, 1>(NT, nmt, smem), P_THREADS, smem, s>>>(
+                t1, t2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2, h, w, nmt, NT, err);
+        else
+            k_conv_tma_bres<0, 0><<<bres_grid<0, 0>(NT, nmt, smem), P_THREADS, smem, s>>>(
+                t1, t2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2, h, w, nmt, NT, err);
+        return 1;
+    }
     if (g_conv_tma == 2) {
         if ((relu ? conv_persist_smem_attr<0, 1>() : conv_persist_smem_attr<0, 0>()) != cudaSuccess) return 0;
         const int nmt = (int)(P / TM), ntiles = nmt * (cout / TN);

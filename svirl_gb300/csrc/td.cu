@@ -1604,7 +1604,17 @@ __global__ void k_bench_prep(const Inst* __restrict__ insts, int ninst, LoopStat
 }
 
 // Per-call counters of every instance back to zero.
-__global__ void k_reset_counters(const Inst* __restrict__ insts, int ninst) {
+// With `loop`, also the time loop's state for a call of Nt steps (written here rather
+// than copied from the host, which saves a transfer per call).
+__global__ void k_reset_counters(const Inst* __restrict__ insts, int ninst, LoopState* loop, int Nt, int guard) {
+    if (loop && blockIdx.x == 0 && threadIdx.x == 0) {
+        LoopState ls;
+        memset(&ls, 0, sizeof(ls));
+        ls.Nt = Nt;
+        ls.ninst = ninst;
+        ls.guard = guard;
+        *loop = ls;
+    }
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ninst; q += gridDim.x * blockDim.x) {
         InstState* st = insts[q].st;
         st->nan_seen = 0;
@@ -1738,25 +1748,21 @@ struct TDOutcome {
 // One TD call over the instances of L: per-call counters reset, the graph (built
 // once per eqn mode and kappa mix) or the host-driven loop, then the instances'
 // loop states gathered to the host.
+// gather_host and hl: pinned host memory (the call's last copies are asynchronous)
 static TDOutcome td_core(cudaStream_t s, const TDLaunch& L, int Nt, int eqn, cudaGraphExec_t* execs, bool* graph_failed,
-                         bool use_graphs, int guard, bool timed, InstState* gather_dev, InstState* gather_host) {
+                         bool use_graphs, int guard, bool timed, InstState* gather_dev, InstState* gather_host,
+                         LoopState* hl_pinned) {
     TDOutcome o = {cudaSuccess, 0, 0, 0, 0.f, 0};
-    k_reset_counters<<<(L.ninst + 127) / 128, 128, 0, s>>>(L.insts, L.ninst);
+    k_reset_counters<<<(L.ninst + 127) / 128, 128, 0, s>>>(L.insts, L.ninst, Nt > 0 ? L.loop : nullptr, Nt,
+                                                           guard > 0 ? guard : kLoopGuard);
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (timed) {
         cudaEventCreate(&ev0);
         cudaEventCreate(&ev1);
     }
-    LoopState hl;
+    LoopState& hl = *hl_pinned;
     memset(&hl, 0, sizeof(hl));
     if (Nt > 0) {
-        LoopState ls;
-        memset(&ls, 0, sizeof(ls));
-        ls.Nt = Nt;
-        ls.ninst = L.ninst;
-        ls.guard = guard > 0 ? guard : kLoopGuard;
-        o.err = cudaMemcpyAsync(L.loop, &ls, sizeof(ls), cudaMemcpyHostToDevice, s);
-        if (o.err != cudaSuccess) return o;
         const int slot = eqn * 4 + (L.any_solveA ? 2 : 0) + (L.any_fv ? 1 : 0);
         if (use_graphs && !*graph_failed) {
             if (execs[slot] == nullptr) {
@@ -1781,7 +1787,7 @@ static TDOutcome td_core(cudaStream_t s, const TDLaunch& L, int Nt, int eqn, cud
     }
     k_gather_states<<<(L.ninst + 127) / 128, 128, 0, s>>>(L.insts, L.ninst, gather_dev);
     o.err = cudaMemcpyAsync(gather_host, gather_dev, sizeof(InstState) * (size_t)L.ninst, cudaMemcpyDeviceToHost, s);
-    if (o.err == cudaSuccess) o.err = cudaMemcpyAsync(&hl, L.loop, sizeof(hl), cudaMemcpyDeviceToHost, s);
+    if (o.err == cudaSuccess) o.err = cudaMemcpyAsync(hl_pinned, L.loop, sizeof(hl), cudaMemcpyDeviceToHost, s);
     if (o.err == cudaSuccess) o.err = cudaStreamSynchronize(s);
     if (ev0) {
         if (o.err == cudaSuccess && Nt > 0) cudaEventElapsedTime(&o.ms, ev0, ev1);
@@ -1818,7 +1824,11 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     // dt of the order-parameter iterator; the A kernel also receives it (td.py:278)
     h->inst_h.dt = dt;
     h->inst_h.fdt = (float)dt;
-    cudaError_t e = cudaMemcpyAsync(h->inst, &h->inst_h, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
+    // pinned staging: the descriptor upload and the statistics download of a call are
+    // asynchronous copies (the stream is synchronised before td_core returns)
+    PinStage* ps = (PinStage*)h->pin;
+    ps->inst = h->inst_h;
+    cudaError_t e = cudaMemcpyAsync(h->inst, &ps->inst, sizeof(Inst), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return cuda_check(h, e, "td: write descriptor");
     TDLaunch L;
     L.insts = h->inst; L.tiles = h->tiles; L.items = h->items; L.loop = h->loop;
@@ -1828,10 +1838,10 @@ int td_run(glgpu_handle* h, double dt, int Nt, int eqn, glgpu_td_stats* stats, d
     L.psi_cn = h->psi_scheme;
     L.any_solveA = h->inst_h.solveA != 0;
     L.any_fv = h->vpi != nullptr || h->lock_n > 0;
-    InstState hs;
     TDOutcome o = td_core(h->stream, L, Nt, eqn, h->td_exec, &h->td_graph_failed, h->use_graphs, h->loop_guard,
                           elapsed_ms != nullptr,
-                          h->st_gather, &hs);
+                          h->st_gather, &ps->st, &ps->loop);
+    const InstState hs = ps->st;
     if (o.err != cudaSuccess) return cuda_check(h, o.err, "td");
     if (elapsed_ms) *elapsed_ms = o.ms;
     h->p.rand_t = hs.rand_t;
@@ -1859,7 +1869,8 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
         any_solveA = any_solveA || h->inst_h.solveA != 0;
         any_fv = any_fv || h->vpi != nullptr || h->lock_n > 0;
     }
-    cudaError_t e = cudaMemcpyAsync(b->insts, insts.data(), sizeof(Inst) * insts.size(), cudaMemcpyHostToDevice, b->stream);
+    memcpy(b->insts_pin, insts.data(), sizeof(Inst) * insts.size());
+    cudaError_t e = cudaMemcpyAsync(b->insts, b->insts_pin, sizeof(Inst) * insts.size(), cudaMemcpyHostToDevice, b->stream);
     if (e != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_td: ") + cudaGetErrorString(e));
     TDLaunch L;
     L.insts = b->insts; L.tiles = b->tiles; L.items = b->items; L.loop = b->loop;
@@ -1871,7 +1882,8 @@ int batch_td(glgpu_batch* b, double dt, int Nt, int eqn, glgpu_td_stats* stats, 
     L.any_fv = any_fv;
     TDOutcome o = td_core(b->stream, L, Nt, eqn, b->td_exec, &b->td_graph_failed, b->use_graphs, b->loop_guard,
                           elapsed_ms != nullptr,
-                          b->gather, b->gather_h.data());
+                          b->gather, b->gather_pin, b->loop_pin);
+    if (o.err == cudaSuccess) memcpy(b->gather_h.data(), b->gather_pin, sizeof(InstState) * (size_t)b->ninst);
     if (o.err != cudaSuccess) return batch_error(b, GLGPU_E_CUDA, std::string("batch_td: ") + cudaGetErrorString(o.err));
     if (elapsed_ms) *elapsed_ms = o.ms;
     int nan = 0;

@@ -6,7 +6,9 @@ tolerance of the other convolution tests (2e-2 of the output's max: bfloat16
 outputs), and against the thread-gather kernel on the same inputs (bitwise: the
 same products accumulated in the same order); on the shapes the TMA path takes:
 whole-row tiles (w = 128, 256), groups of rows (w = 16, 32), channel concatenation,
-several output tiles.  No bounded wait may run out."""
+several output tiles; mode 2 keeps the weights resident in shared memory for up to
+two 64-channel input chunks and streams them for more (the last shape).  No
+bounded wait may run out."""
 import numpy as np
 import pytest
 
@@ -35,7 +37,7 @@ def _fwd(L, x1, x2, W, b, relu, mode):
 
 
 @pytest.mark.parametrize("shape", [(2, 16, 16, 64, 0, 64), (1, 32, 128, 64, 64, 128), (1, 8, 256, 128, 0, 64),
-                                   (4, 8, 32, 64, 64, 64)])
+                                   (4, 8, 32, 64, 64, 64), (1, 8, 128, 128, 64, 64)])
 @pytest.mark.parametrize("relu", [0, 1])
 @pytest.mark.parametrize("mode", [1, 2])
 def test_tma_forward_matches_reference_and_gather(shape, relu, mode):

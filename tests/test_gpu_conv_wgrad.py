@@ -41,7 +41,8 @@ def _grads(L, x1, x2, W, b, dy, relu, mode):
 
 
 @pytest.mark.parametrize("shape", [(2, 16, 16, 64, 0, 64), (1, 32, 128, 64, 64, 128), (1, 8, 64, 128, 0, 64),
-                                   (4, 8, 32, 64, 64, 64), (1, 2, 32, 64, 0, 64), (8, 64, 64, 64, 0, 64)])
+                                   (4, 8, 32, 64, 64, 64), (1, 2, 32, 64, 0, 64), (8, 64, 64, 64, 0, 64),
+                                   (1, 8, 64, 64, 0, 192)])
 @pytest.mark.parametrize("relu", [0, 1])
 def test_tcgen05_weight_gradient(shape, relu):
     from svirl_gb300 import learned as L
