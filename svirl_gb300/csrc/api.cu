@@ -75,6 +75,7 @@ void upload_inst(glgpu_handle* h) {
     }
     I.tile0 = 0;
     I.ntiles = h->ntiles;
+    I.natiles = h->natiles;
     I.nitems = strip_items(h->g.Nx, h->g.Ny, h->strip_rows);  // strips (the table also has empty items)
     I.solveA = finite_kappa(h->p) ? 1 : 0;
     I.fepsilon = (float)I.epsilon;
@@ -113,7 +114,7 @@ static void free_all(glgpu_handle* h) {
         if (h->dir_psi[q]) cudaFree(h->dir_psi[q]);
         if (h->dir_A[q]) cudaFree(h->dir_A[q]);
     }
-    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->code, h->dinv, h->st, h->inst, h->tiles, h->items, h->loop, h->partials, h->counter,
+    void* ptrs[] = {h->abei, h->mt, h->eps_sp, h->U, h->code, h->dinv, h->st, h->inst, h->tiles, h->atiles, h->items, h->loop, h->partials, h->counter,
                     h->dscal, h->out, h->vort, h->vort_n, h->flush};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -169,6 +170,8 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     ok = ok && cudaMalloc(&h->st_gather, sizeof(InstState)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->inst, sizeof(Inst)) == cudaSuccess;
     ok = ok && cudaMalloc(&h->tiles, sizeof(Tile) * (size_t)h->ntiles) == cudaSuccess;
+    h->natiles = atiles_of(h->g.Nx, h->g.Ny);
+    ok = ok && cudaMalloc(&h->atiles, sizeof(ATile) * (size_t)h->natiles) == cudaSuccess;
     {
         const Geo* gp = &h->g;
         h->strip_rows = choose_strip_rows(h->dtype, &gp, 1);
@@ -196,7 +199,12 @@ int glgpu_create(const glgpu_grid* grid, int32_t device, glgpu_handle** out) {
     InstState st;
     memset(&st, 0, sizeof(st));
     st.rand_t = h->p.rand_t;
+    std::vector<ATile> atiles;
+    for (int j0 = 0; j0 < h->g.Ny; j0 += kATY)
+        for (int i0 = 0; i0 < h->g.Nx; i0 += kATX) atiles.push_back(ATile{0, i0, j0, 0});
     e = cudaMemcpyAsync(h->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->atiles, atiles.data(), sizeof(ATile) * atiles.size(), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->items, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->st, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->counter, 0, sizeof(unsigned) * 4, h->stream);
@@ -544,6 +552,7 @@ int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** ou
     b->hs.assign(handles, handles + n);
     cudaSetDevice(b->device);
     std::vector<Tile> tiles;
+    std::vector<ATile> atiles;
     std::vector<Item> items;
     std::vector<const Geo*> geos(n);
     for (int q = 0; q < n; ++q) geos[q] = &handles[q]->g;
@@ -551,11 +560,14 @@ int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** ou
     b->inst_items.resize(n);
     for (int q = 0; q < n; ++q) {
         for (int k = 0; k < handles[q]->ntiles; ++k) tiles.push_back(Tile{q, k * kThreads});
+        for (int j0 = 0; j0 < handles[q]->g.Ny; j0 += kATY)
+            for (int i0 = 0; i0 < handles[q]->g.Nx; i0 += kATX) atiles.push_back(ATile{q, i0, j0, 0});
         const std::vector<Item> it = make_items(handles[q]->g, q, b->strip_rows);
         b->inst_items[q] = strip_items(handles[q]->g.Nx, handles[q]->g.Ny, b->strip_rows);
         items.insert(items.end(), it.begin(), it.end());
     }
     b->ntiles = (int)tiles.size();
+    b->natiles = (int)atiles.size();
     b->nitems = (int)items.size();
     b->psi_grid = psi_sweep_grid(psi_kind(b->dtype, 0), b->strip_rows, b->nitems);
     b->gather_h.resize(n);
@@ -563,6 +575,7 @@ int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** ou
     ok = ok && cudaMalloc(&b->insts, sizeof(Inst) * (size_t)n) == cudaSuccess;
     ok = ok && cudaMalloc(&b->gather, sizeof(InstState) * (size_t)n) == cudaSuccess;
     ok = ok && cudaMalloc(&b->tiles, sizeof(Tile) * tiles.size()) == cudaSuccess;
+    ok = ok && cudaMalloc(&b->atiles, sizeof(ATile) * atiles.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&b->items, sizeof(Item) * items.size()) == cudaSuccess;
     ok = ok && cudaMalloc(&b->loop, sizeof(LoopState)) == cudaSuccess;
     ok = ok && cudaMallocHost(&b->gather_pin, sizeof(InstState) * (size_t)n) == cudaSuccess;
@@ -570,6 +583,8 @@ int glgpu_batch_create(glgpu_handle* const* handles, int32_t n, glgpu_batch** ou
     ok = ok && cudaMallocHost(&b->insts_pin, sizeof(Inst) * (size_t)n) == cudaSuccess;
     cudaError_t e = ok ? cudaSuccess : cudaErrorMemoryAllocation;
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->atiles, atiles.data(), sizeof(ATile) * atiles.size(), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->items, items.data(), sizeof(Item) * items.size(), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) {
@@ -588,7 +603,7 @@ int glgpu_batch_destroy(glgpu_batch* b) {
     for (int q = 0; q < kTDGraphs; ++q)
         if (b->td_exec[q]) cudaGraphExecDestroy(b->td_exec[q]);
     if (b->cg_exec) cudaGraphExecDestroy(b->cg_exec);
-    void* ptrs[] = {b->insts, b->gather, b->tiles, b->items, b->loop, b->cg_partials, b->cg_loop, b->cg_tiles};
+    void* ptrs[] = {b->insts, b->gather, b->tiles, b->atiles, b->items, b->loop, b->cg_partials, b->cg_loop, b->cg_tiles};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* pins[] = {b->gather_pin, b->loop_pin, b->insts_pin};

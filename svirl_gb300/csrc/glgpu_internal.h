@@ -91,6 +91,7 @@ struct Inst {
     void* dpsi[2];
     void* dA[2];
     int tile0, ntiles;        // this instance's range in the tile table
+    int natiles;              // its A-sweep tiles (ATile)
     int nitems;               // number of warp-strip items of this instance
     int solveA;               // finite kappa
     int cg_exact;             // batched device CG: exact dF/dA on boundary links
@@ -118,6 +119,13 @@ constexpr int kErrCopyWait = 2;  // a wait for a bulk copy into shared memory ra
 struct Tile {
     int inst, n0;
 };
+
+// A tile of the A sweep: kATX x kATY nodes of one instance from node (i0, j0).
+constexpr int kATX = 32, kATY = 32;
+struct ATile {
+    int inst, i0, j0, pad;
+};
+inline int atiles_of(int Nx, int Ny) { return ((Nx + kATX - 1) / kATX) * ((Ny + kATY - 1) / kATY); }
 
 // Work item of the warp-strip psi sweep: kStripCols output columns (x0..) by
 // `rows` rows (j0..) of one instance, processed by one warp whose 32 lanes also
@@ -169,6 +177,8 @@ struct glgpu_handle {
     glgpu::Inst* inst = nullptr;        // device copy of the descriptor
     glgpu::Inst inst_h;                 // host copy of the descriptor
     glgpu::Tile* tiles = nullptr;
+    glgpu::ATile* atiles = nullptr;     // A-sweep tiles
+    int natiles = 0;
     glgpu::Item* items = nullptr;
     int nitems = 0;
     int strip_rows = 0;                 // strip height of the psi sweep items
@@ -227,6 +237,8 @@ struct glgpu_batch {
     cudaStream_t stream = nullptr;
     glgpu::Inst* insts = nullptr;
     glgpu::Tile* tiles = nullptr;
+    glgpu::ATile* atiles = nullptr;     // A-sweep tiles
+    int natiles = 0;
     glgpu::Item* items = nullptr;
     glgpu::LoopState* loop = nullptr;
     glgpu::InstState* gather = nullptr;
