@@ -849,6 +849,214 @@ k_conv_tma_bres(const __grid_constant__ CUtensorMap ta1, const __grid_constant__
 }
 
 // ---------------------------------------------------------------------------
+// k_conv_tma_bres with each input row loaded once: for 128-pixel tiles that lie in
+// one image row (w a multiple of 128), a stage holds one tap row dy of the tile, i.e.
+// for every input-channel chunk one box of 130 pixels (the tile and a one-pixel halo
+// on each side, zeros outside the image) x 64 channels.  The three taps dx of that row
+// read the same box from pixel 0, 1 or 2: the A descriptor starts 0, 128 or 256 bytes
+// into the 1024-byte swizzle atom (see smem_desc_sw128_at).  The activation bytes
+// moved from L2 per tile fall from 9 x 16 KB to 3 x 16.25 KB per channel chunk.  The
+// MMAs run in the order of the other kernels (tap-major, channel chunk inner), so
+// the results are the same bitwise.
+// ---------------------------------------------------------------------------
+constexpr int HALO_PX = TM + 2;                        // 130 pixels per box
+constexpr int HALO_BOX = HALO_PX * TK * 2;             // 16,640 bytes
+constexpr int HALO_SLOT = 17 * 1024;                   // a box's 1024-aligned slot
+__host__ __device__ constexpr int halo_stages(int nck) { return nck == 1 ? 3 : 2; }
+__host__ __device__ constexpr int halo_smem_bytes(int nck) {
+    return halo_stages(nck) * nck * HALO_SLOT + 9 * nck * B_BYTES + 1024 + (2 * 3 + 5) * 8 + 16;
+}
+static_assert(halo_smem_bytes(1) <= 227 * 1024 && halo_smem_bytes(2) <= 227 * 1024, "halo conv exceeds shared memory");
+
+// A view starting 128 or 256 bytes into a swizzle atom: the MMA applies the 128-byte
+// swizzle by the absolute shared-memory address bits, as the TMA copy that wrote the
+// box did, so the descriptor is the plain one (its base-offset field stays 0; set to
+// (start >> 7) & 7 it gave wrong products, measured).
+__device__ __forceinline__ uint64_t smem_desc_sw128_at(uint32_t start) { return smem_desc_sw128(start); }
+
+template <int MODE, int RELU>
+__global__ void __launch_bounds__(P_THREADS)
+k_conv_tma_halo(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ CUtensorMap ta2,
+                const __grid_constant__ CUtensorMap tb, const float* __restrict__ bias, bf16* __restrict__ y, int Cout,
+                bf16* __restrict__ o2, int Co2, int C1, int C2, int H, int W, int nmt, int NT, int* err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int nck = (C1 + C2) / TK, nk = 9 * nck, S = halo_stages(nck);
+    const int stage_bytes = nck * HALO_SLOT;
+    unsigned char* bres = smem + S * stage_bytes;
+    uint64_t* full = (uint64_t*)(bres + nk * B_BYTES);
+    uint64_t* empty = full + 3;
+    uint64_t* acc_full = empty + 3;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* b_full = acc_empty + 2;
+    uint32_t* tslot = (uint32_t*)(b_full + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int cpn = gridDim.x / NT;
+    const int nt = blockIdx.x % NT, mt0 = blockIdx.x / NT, n0 = nt * TN;
+    const int sgn = MODE == 0 ? 1 : -1;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)),
+                     "r"(kTmemColsP)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int q = 0; q < S; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(full + q)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(empty + q)) : "memory");
+        }
+        for (int q = 0; q < 2; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(acc_full + q)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(saddr(acc_empty + q)) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(b_full)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(b_full)),
+                         "r"((uint32_t)(nk * B_BYTES))
+                         : "memory");
+            for (int kc = 0; kc < nk; ++kc) {
+                const int tap = kc / nck, c = (kc - tap * nck) * TK;
+                const uint32_t b_dst = saddr(bres + kc * B_BYTES);
+                if (MODE == 0) tma_load_2d(b_dst, &tb, tap * (C1 + C2) + c, n0, saddr(b_full));
+                else tma_load_3d(b_dst, &tb, c, n0, tap, saddr(b_full));
+            }
+            int g = 0;  // stages filled, across tiles
+            for (int mt = mt0; mt < nmt && ok; mt += cpn) {
+                const int m0 = mt * TM;
+                const int img = m0 / (H * W), rem = m0 - img * H * W, y0 = rem / W, x0 = rem - y0 * W;
+                for (int ty = 0; ty < 3; ++ty, ++g) {
+                    const int st = g % S, use = g / S;
+                    if (use > 0 && !wait_parity(saddr(empty + st), (uint32_t)((use + 1) & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(full + st)),
+                                 "r"((uint32_t)(nck * HALO_BOX))
+                                 : "memory");
+                    const int yy = y0 + sgn * (ty - 1);
+                    for (int cc = 0; cc < nck; ++cc) {
+                        const int c = cc * TK;
+                        const uint32_t dst = saddr(smem + st * stage_bytes + cc * HALO_SLOT);
+                        if (c < C1) tma_load_4d(dst, &ta1, c, x0 - 1, yy, img, saddr(full + st));
+                        else tma_load_4d(dst, &ta2, c - C1, x0 - 1, yy, img, saddr(full + st));
+                    }
+                }
+            }
+            wait_parity(saddr(b_full), 0u);
+            for (int q = 0; q < S && q < g; ++q) {
+                const int gg = g - 1 - q, st = gg % S, use = gg / S;
+                wait_parity(saddr(full + st), (uint32_t)(use & 1));
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            if (!wait_parity(saddr(b_full), 0u)) ok = false;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            int g = 0, lt = 0;
+            for (int mt = mt0; mt < nmt && ok; mt += cpn, ++lt) {
+                const int acc = lt & 1, ause = lt >> 1;
+                if (ause > 0 && !wait_parity(saddr(acc_empty + acc), (uint32_t)((ause + 1) & 1))) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)(acc * TN);
+                for (int ty = 0; ty < 3; ++ty, ++g) {
+                    const int st = g % S, use = g / S;
+                    if (!wait_parity(saddr(full + st), (uint32_t)(use & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    for (int tx = 0; tx < 3; ++tx) {
+                        // pixel offset of the view in the box: +tx-1 (forward) or -(tx-1) (data gradient)
+                        const int off = MODE == 0 ? tx : 2 - tx;
+                        for (int cc = 0; cc < nck; ++cc) {
+                            const int kc = (ty * 3 + tx) * nck + cc;
+                            const uint32_t a0 = saddr(smem + st * stage_bytes + cc * HALO_SLOT) + 128u * off;
+                            const uint32_t b0 = saddr(bres + kc * B_BYTES);
+#pragma unroll
+                            for (int j = 0; j < TK / 16; ++j)
+                                mma_f16(d, smem_desc_sw128_at(a0 + 32 * j), smem_desc_sw128(b0 + 32 * j), kIdesc,
+                                        (kc > 0 || j > 0) ? 1u : 0u);
+                        }
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                     saddr(empty + st))
+                                 : "memory");
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 saddr(acc_full + acc))
+                             : "memory");
+            }
+        }
+        __syncwarp();
+    } else {
+        const int quarter = warp & 3;
+        int lt = 0;
+        for (int mt = mt0; mt < nmt; mt += cpn, ++lt) {
+            const int acc = lt & 1, ause = lt >> 1;
+            const bool got = wait_parity(saddr(acc_full + acc), (uint32_t)(ause & 1));
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (!got) {
+                ok = false;
+                break;
+            }
+            const int p = mt * TM + quarter * 32 + lane;
+#pragma unroll
+            for (int c = 0; c < TN; c += 16) {
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                    : "r"(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TN + c))
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (MODE == 0) {
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2) {
+                        const int col = n0 + c + q;
+                        float v0 = __uint_as_float(r[q]) + bias[col], v1 = __uint_as_float(r[q + 1]) + bias[col + 1];
+                        if (RELU) {
+                            v0 = fmaxf(v0, 0.f);
+                            v1 = fmaxf(v1, 0.f);
+                        }
+                        *(__nv_bfloat162*)(y + (size_t)p * Cout + col) = __floats2bfloat162_rn(v0, v1);
+                    }
+                } else {
+                    bf16* out = n0 < Cout ? y + (size_t)p * Cout + n0 : o2 + (size_t)p * Co2 + (n0 - Cout);
+#pragma unroll
+                    for (int q = 0; q < 16; q += 2)
+                        *(__nv_bfloat162*)(out + c + q) =
+                            __floats2bfloat162_rn(__uint_as_float(r[q]), __uint_as_float(r[q + 1]));
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(saddr(acc_empty + acc)) : "memory");
+        }
+    }
+    if (!ok) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemColsP) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Weight gradient on tcgen05 with TMA operands: dW[co][tap][ci] =
 // sum_p dy'[p][co] x[p + off(tap)][ci] (dy' = dy * relu'(y), formed by
 // k_relu_mask_dy beforehand), as D[m][co] = sum_k A[m][k] B[k][co] with
@@ -1070,6 +1278,20 @@ static bool act_map(CUtensorMap* m, const void* base, int c, int n, int h, int w
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// activations [n][h][w][c] (bf16), box = 64 channels x 130 pixels of one row (a
+// 128-pixel tile with a one-pixel halo on each side)
+static bool act_map_halo(CUtensorMap* m, const void* base, int c, int n, int h, int w) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)w * c * 2, (cuuint64_t)h * w * c * 2};
+    cuuint32_t box[4] = {(cuuint32_t)TK, (cuuint32_t)HALO_PX, 1u, 1u};
+    cuuint32_t es[4] = {1u, 1u, 1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // weights [rows][k] (bf16, k contiguous), box = 64 k x 64 rows
 static bool weight_map(CUtensorMap* m, const void* base, long long k, long long rows) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
@@ -1120,6 +1342,23 @@ template <int MODE, int RELU> static cudaError_t conv_bres_smem_attr() {
     return e;
 }
 
+template <int MODE, int RELU> static cudaError_t conv_halo_smem_attr() {
+    static cudaError_t e = cudaFuncSetAttribute(k_conv_tma_halo<MODE, RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                halo_smem_bytes(2));
+    return e;
+}
+template <int MODE, int RELU> static int halo_grid(int NT, int nmt, int smem) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv_tma_halo<MODE, RELU>, P_THREADS, smem);
+    int cpn = (sms > 0 ? sms : 152) * (per > 0 ? per : 1) / NT;
+    cpn = cpn < 1 ? 1 : (cpn > nmt ? nmt : cpn);
+    return NT * cpn;
+}
+// the halo kernel takes 128-pixel tiles inside one image row and at most two input chunks
+static bool halo_ok(int w, int nck) { return g_conv_tma == 2 && w % TM == 0 && nck >= 1 && nck <= 2; }
+
 // grid of the resident-weight kernel: NT x (CTAs per n-tile), the CTAs that fit on
 // all SMs at this shared-memory size, at most one per pixel tile of an n-tile
 template <int MODE, int RELU> static int bres_grid(int NT, int nmt, int smem) {
@@ -1153,6 +1392,14 @@ static int conv_bwd_data_tma(const void* dy, const void* wt, void* dx1, int c1, 
     CUtensorMap ta, tb;
     if (!act_map(&ta, dy, cout, n, h, w) || !weight_t_map(&tb, wt, c1 + c2, cout)) return 0;
     const long long P = (long long)n * h * w;
+    if (halo_ok(w, cout / TK)) {
+        CUtensorMap th;
+        if (!act_map_halo(&th, dy, cout, n, h, w) || conv_halo_smem_attr<1, 0>() != cudaSuccess) return 0;
+        const int nmt = (int)(P / TM), NT = (c1 + c2) / TN, smem = halo_smem_bytes(cout / TK);
+        k_conv_tma_halo<1, 0><<<halo_grid<1, 0>(NT, nmt, smem), P_THREADS, smem, s>>>(
+            th, th, tb, nullptr, (bf16*)dx1, c1, (bf16*)dx2, c2, cout, 0, h, w, nmt, NT, err);
+        return 1;
+    }
     if (g_conv_tma == 2 && 9 * (cout / TK) <= BR_MAX_CHUNKS) {
         if (conv_bres_smem_attr<1, 0>() != cudaSuccess) return 0;
         const int nmt = (int)(P / TM), NT = (c1 + c2) / TN, smem = br_smem_bytes(9 * (cout / TK));
@@ -1187,6 +1434,24 @@ static int conv_fwd_tma(const void* x1, int c1, const void* x2, int c2, const vo
     }
     if (!weight_map(&tb, wb, 9LL * (c1 + c2), cout)) return 0;
     const long long P = (long long)n * h * w;
+    if (halo_ok(w, (c1 + c2) / TK)) {
+        CUtensorMap h1, h2;
+        if (!act_map_halo(&h1, x1, c1, n, h, w)) return 0;
+        if (c2 > 0) {
+            if (!act_map_halo(&h2, x2, c2, n, h, w)) return 0;
+        } else {
+            h2 = h1;
+        }
+        if ((relu ? conv_halo_smem_attr<0, 1>() : conv_halo_smem_attr<0, 0>()) != cudaSuccess) return 0;
+        const int nmt = (int)(P / TM), NT = cout / TN, smem = halo_smem_bytes((c1 + c2) / TK);
+        if (relu)
+            k_conv_tma_halo<0, 1><<<halo_grid<0, 1>(NT, nmt, smem), P_THREADS, smem, s>>>(
+                h1, h2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2, h, w, nmt, NT, err);
+        else
+            k_conv_tma_halo<0, 0><<<halo_grid<0, 0>(NT, nmt, smem), P_THREADS, smem, s>>>(
+                h1, h2, tb, bias, (bf16*)y, cout, nullptr, 0, c1, c2, h, w, nmt, NT, err);
+        return 1;
+    }
     if (g_conv_tma == 2 && 9 * ((c1 + c2) / TK) <= BR_MAX_CHUNKS) {
         if ((relu ? conv_bres_smem_attr<0, 1>() : conv_bres_smem_attr<0, 0>()) != cudaSuccess) return 0;
         const int nmt = (int)(P / TM), NT = cout / TN, smem = br_smem_bytes(9 * ((c1 + c2) / TK));
