@@ -1,15 +1,14 @@
 """Learned CG warm start: a convolutional encoder-decoder that predicts a
 near-minimum (psi, A) of an instance from (material mask, H, 1/kappa, initial
-psi), used as the starting point of the CG.  The CG stays the judge: a
-prediction only counts once the CG from it reaches the energy and gradient
-tolerances.  No counterpart in the reference (its only minimiser is the CG of
+psi), used as the starting point of the CG.  The CG decides: a prediction only
+counts once the CG from it reaches the energy and gradient tolerances.  No counterpart in the reference (its only minimiser is the CG of
 svirl/solvers/cg.py).
 
 Compute: every convolution, pooling/upsampling, the loss and the optimiser step
 run in the hand-written kernels of ``include/glgpu_nn.h`` (BF16 implicit GEMMs
 on the tensor cores with FP32 accumulation: tcgen05 with tensor memory, the
-operands of the forward pass and the weight gradient loaded by TMA; mma.sync for
-weight gradients of shapes the tcgen05 kernel does not take); PyTorch
+operands of the forward pass and of both gradients loaded by TMA; thread-gather and
+mma.sync kernels for shapes the TMA kernels do not take); PyTorch
 supplies device tensors, the stream and the autograd bookkeeping
 (``torch.autograd.Function`` wrappers).
 
