@@ -741,8 +741,11 @@ __device__ __forceinline__ void step_tile(const Inst& I, int n0, int rep, T ap, 
 // owners store, so the energy equals that of the stored state bit for bit.  The
 // last CTA of the launch counts the active instances and sets the WHILE
 // condition.
+#ifndef GLGPU_CG_MINB_STEP
+#define GLGPU_CG_MINB_STEP 1
+#endif
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB_STEP : 1)
 kb_step(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double* __restrict__ partials, CGLoop* loop,
         cudaGraphConditionalHandle cond, int use_cond) {
     const CGTile t = tiles[blockIdx.x];

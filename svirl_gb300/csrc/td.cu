@@ -854,8 +854,12 @@ k_psi_sweep_cn(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, L
 // atomics per 1,024 nodes (per 256 they made each CTA's life a chain of dependent
 // loads and atomics; that version took 0.202 ms per sweep at 2049^2, 0.125 ms with
 // four tiles per CTA).  The arithmetic of a link is unchanged.
+// resident CTAs per SM asked of the compiler for the FP32 A sweep (caps its registers)
+#ifndef GLGPU_A_MINB
+#define GLGPU_A_MINB 8
+#endif
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_A_MINB : 1)
 k_A_sweep(const Inst* __restrict__ insts, const ATile* __restrict__ atiles, LoopState* loop,
           cudaGraphConditionalHandle cond, int use_cond) {
     const int tid = threadIdx.x;
