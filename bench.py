@@ -322,59 +322,103 @@ def states_instances(count, first_seed=1000):
     return out
 
 
-def run_states(args):
+def states_instances_bounded(count, max_side, first_seed=1000):
+    """The first `count` instances of the field sweep (instance k drawn exactly as
+    states_instances draws it) whose side is at most `max_side`."""
+    from svirl_gb300 import learned as L
+    out, k = [], 0
+    while len(out) < count:
+        rng = np.random.default_rng(first_seed + k)
+        n = STATE_SIZES[int(rng.integers(len(STATE_SIZES)))]
+        if n <= max_side:
+            out.append(L.Instance.sample(n, rng, H_range=(0.02, 0.5), kappa_range=(4.0, 4.0), hole_frac=(0.0, 0.05),
+                                         radius=(2.0, 6.0)))
+        k += 1
+    return out
+
+
+def measure_states(insts, cg_iters, gtol, plain_sample):
     """The batched pipeline (FP32 stencils, FP64 reductions, exact-boundary gradient,
-    device-decided steps) on `args.instances` instances, against F* from a tight FP64
-    relaxation of the same instances from the same start; the plain single-instance
-    CG (the reference's algorithm, step length on the host, FP64) timed on a sample."""
+    device-decided steps) on `insts`, timed with its loads and fetches, against F*
+    from a tight FP64 relaxation of the same instances from the same start (untimed);
+    the plain single-instance CG (one instance at a time, FP64, the same device CG and
+    stop rule) timed on the first `plain_sample` instances.  A state counts when
+    |F - F*|/|F*| <= 1e-6."""
     from svirl_gb300 import relax as RX
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    insts = states_instances(args.instances)
     cache = RX.HandleCache()
-    nodes = sum(it.n * it.n for it in insts)
-    # warm-up: a few small instances through the same path
-    RX.relax(states_instances(4, first_seed=1), cache, np.float32, n_iter=50, gtol=1e-3)
-    t0 = time.perf_counter()
-    out, states, _ = RX.relax(insts, cache, np.float32, n_iter=args.cg_iters, gtol=args.gtol)
-    wall = time.perf_counter() - t0
-    # validation (untimed): tight FP64 relaxation from the same start, energies in FP64
-    ref, _, _ = RX.relax(insts, cache, np.float64, n_iter=2 * args.cg_iters, gtol=args.gtol * 1e-2, fetch=False)
-    E = RX.energies_fp64(insts, states, cache)
-    Estar = ref["energy"]
-    rel = (E - Estar) / np.abs(Estar)
-    ok = np.abs(rel) <= 1e-6
-    value = float(ok.sum()) / wall
-    # plain single-instance CG on a sample: one instance at a time, FP64, no
-    # batching, same device CG and the same stop rule, counted by the same criterion
-    sample = insts[:args.plain_sample]
-    t_plain, ok_plain = 0.0, 0
-    for q, it in enumerate(sample):
-        t1 = time.perf_counter()
-        o1, st1, _ = RX.relax([it], cache, np.float64, n_iter=args.cg_iters, gtol=args.gtol)
-        t_plain += time.perf_counter() - t1
-        E1 = RX.energies_fp64([it], st1, cache)[0]
-        ok_plain += int(abs(E1 - Estar[q]) / abs(Estar[q]) <= 1e-6)
+    try:
+        # warm-up: a few small instances through the same path
+        RX.relax(states_instances(4, first_seed=1), cache, np.float32, n_iter=50, gtol=1e-3)
+        t0 = time.perf_counter()
+        out, states, _ = RX.relax(insts, cache, np.float32, n_iter=cg_iters, gtol=gtol)
+        wall = time.perf_counter() - t0
+        ref, _, _ = RX.relax(insts, cache, np.float64, n_iter=2 * cg_iters, gtol=gtol * 1e-2, fetch=False)
+        E = RX.energies_fp64(insts, states, cache)
+        Estar = ref["energy"]
+        rel = (E - Estar) / np.abs(Estar)
+        ok = np.abs(rel) <= 1e-6
+        value = float(ok.sum()) / wall
+        sample = insts[:plain_sample]
+        t_plain, ok_plain = 0.0, 0
+        for q, it in enumerate(sample):
+            t1 = time.perf_counter()
+            o1, st1, _ = RX.relax([it], cache, np.float64, n_iter=cg_iters, gtol=gtol)
+            t_plain += time.perf_counter() - t1
+            E1 = RX.energies_fp64([it], st1, cache)[0]
+            ok_plain += int(abs(E1 - Estar[q]) / abs(Estar[q]) <= 1e-6)
+    finally:
+        cache.close()
     plain_rate = ok_plain / t_plain if t_plain > 0 else 0.0
-    line = {"metric": STATES_METRIC, "value": value, "unit": "states/s", "n_gpus": 1, "steps": 1, "warmup": 1,
-            "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 stencils, f64 reductions", "data": "synthetic (seeded)",
-            "config": {"workload": "batched_field_sweep", "instances": len(insts), "sizes": list(STATE_SIZES),
-                       "kappa": 4.0, "H": "U[0.02,0.5]", "holes": "fraction U[0,0.05], radius U[2,6]",
-                       "nodes_total": nodes, "cg_iters_cap": args.cg_iters, "gtol_abs": args.gtol,
-                       "criterion": "|F - F*|/|F*| <= 1e-6, F* = FP64 relaxation of the same instance from the same "
-                                    "start (gradient tolerance gtol/100, twice the iteration cap)"},
-            "states_ok": int(ok.sum()), "states_lower_energy": int((rel < -1e-6).sum()), "rel_err_quantiles": np.quantile(rel, [0, 0.5, 0.9, 1]).tolist(),
+    return {"value": value, "wall_s": wall, "states_ok": int(ok.sum()), "instances": len(insts),
+            "states_lower_energy": int((rel < -1e-6).sum()),
+            "rel_err_quantiles": np.quantile(rel, [0, 0.5, 0.9, 1]).tolist(),
             "cg_device_ms": out["ms"], "cg_iters": {"mean": float(out["iters"].mean()), "max": int(out["iters"].max())},
             "plain": {"states_per_s": plain_rate, "sample": len(sample), "met_criterion": ok_plain, "wall_s": t_plain,
                       "how": "the same device CG on one instance at a time, FP64, no batching"},
             "speedup_vs_plain": value / plain_rate if plain_rate > 0 else None,
-            "e2e": {"value": value, "unit": "states/s", "h2d_bytes_per_step": int(sum(it.n * it.n * 4 * 4 for it in insts)),
-                    "d2h_bytes_per_step": int(sum(it.n * it.n * 4 * 4 for it in insts)),
+            "h2d_bytes": int(sum(it.n * it.n * 4 * 4 for it in insts))}
+
+
+STATES_CRITERION = ("|F - F*|/|F*| <= 1e-6, F* = FP64 relaxation of the same instance from the same start "
+                    "(gradient tolerance gtol/100, twice the iteration cap)")
+
+
+def run_states(args):
+    """States/s of the batched field sweep (`args.instances` instances) against the
+    plain single-instance CG (measure_states)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    insts = states_instances(args.instances)
+    nodes = sum(it.n * it.n for it in insts)
+    m = measure_states(insts, args.cg_iters, args.gtol, args.plain_sample)
+    value = m["value"]
+    line = {"metric": STATES_METRIC, "value": value, "unit": "states/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1e3 * m["wall_s"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 stencils, f64 reductions", "data": "synthetic (seeded)",
+            "config": {"workload": "batched_field_sweep", "instances": len(insts), "sizes": list(STATE_SIZES),
+                       "kappa": 4.0, "H": "U[0.02,0.5]", "holes": "fraction U[0,0.05], radius U[2,6]",
+                       "nodes_total": nodes, "cg_iters_cap": args.cg_iters, "gtol_abs": args.gtol,
+                       "criterion": STATES_CRITERION},
+            "states_ok": m["states_ok"], "states_lower_energy": m["states_lower_energy"],
+            "rel_err_quantiles": m["rel_err_quantiles"], "cg_device_ms": m["cg_device_ms"], "cg_iters": m["cg_iters"],
+            "plain": m["plain"], "speedup_vs_plain": m["speedup_vs_plain"],
+            "e2e": {"value": value, "unit": "states/s", "h2d_bytes_per_step": m["h2d_bytes"],
+                    "d2h_bytes_per_step": m["h2d_bytes"],
                     "how": "wall time of load (H2D) + batched CG + fetch (D2H) of every instance"}}
     print(json.dumps(line), flush=True)
-    cache.close()
+
+
+def states_sample_line(count=48, max_side=257, cg_iters=12000, gtol=1e-4, plain_sample=8):
+    """A bounded sample of the states/s comparison for the default bench line: the
+    first `count` instances of the field sweep with side <= `max_side` (the larger
+    sides take minutes in the FP64 validation), the field sweep's cap and stop rule."""
+    insts = states_instances_bounded(count, max_side)
+    m = measure_states(insts, cg_iters, gtol, plain_sample)
+    m.update({"metric": STATES_METRIC, "unit": "states/s", "criterion": STATES_CRITERION,
+              "sample": "the first %d instances of the seeded field sweep with side <= %d (sides %s), cap %d, "
+                        "absolute gradient %g" % (count, max_side, sorted({it.n for it in insts}), cg_iters, gtol)})
+    return m
 
 
 def run_cg(args):
@@ -672,6 +716,8 @@ def main():
     ap.add_argument("--cg-iters", type=int, default=12000)
     ap.add_argument("--gtol", type=float, default=1e-4)
     ap.add_argument("--plain-sample", type=int, default=8)
+    ap.add_argument("--no-states-sample", action="store_true",
+                    help="leave out the bounded states/s sample of the default line")
     ap.add_argument("--learned-cap", type=int, default=4000,
                     help="CG iteration cap of both arms of the learned + batched states/s comparison")
     args = ap.parse_args()
@@ -850,6 +896,11 @@ def main():
         }
         if a_sweep is not None:
             line["A_sweep"] = a_sweep
+        if dtype == np.float32 and kinf and not args.no_states_sample:
+            try:  # a side measurement after the timed region, like fp32_vs_fp64
+                line["states_sample"] = states_sample_line()
+            except Exception as e:  # noqa: BLE001
+                line["states_sample"] = {"error": "%s: %s" % (type(e).__name__, e)}
         print(json.dumps(line), flush=True)
     gl.close()
     if dist is not None:
