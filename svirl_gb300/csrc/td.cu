@@ -1143,33 +1143,102 @@ k_A_sweep(const Inst* __restrict__ insts, const ATile* __restrict__ atiles, Loop
 // its own unscaled factors in link order before each run), and per node the Winecki-Adams
 // link weights as a bit code (bit 0: left link r_m0, 1: right r_p0, 2: lower
 // r_0m, 3: upper r_0p; a node is updated iff it has a left or a right link).
+// Tiles per CTA of the per-call kernels k_link_U and k_canonical_copy.  With one
+// 256-node tile per CTA (16,401 CTAs at 2049^2) each CTA's life is a chain of
+// dependent loads (tile, instance, state word, data) and the launch is bound by
+// that latency; a CTA that takes kCallTiles consecutive tiles of one instance
+// loads the instance and state once and issues the data loads of its kCallTiles
+// nodes per thread together.  Tiles of several instances (a batch's boundaries)
+// are taken one after the other.  Results do not depend on it.
+constexpr int kCallTiles = 4;
+static inline unsigned call_grid(int ntiles) { return (unsigned)((ntiles + kCallTiles - 1) / kCallTiles); }
+
+// the tiles of CTA blockIdx.x (inst = -1 past the end); true when all of them
+// that exist belong to one instance
+__device__ __forceinline__ bool call_tiles(const Tile* __restrict__ tiles, int ntiles, Tile (&t)[kCallTiles]) {
+#pragma unroll
+    for (int q = 0; q < kCallTiles; ++q) {
+        const int b = (int)blockIdx.x * kCallTiles + q;
+        t[q] = b < ntiles ? tiles[b] : Tile{-1, 0};
+    }
+    bool same = true;
+#pragma unroll
+    for (int q = 1; q < kCallTiles; ++q) same = same && (t[q].inst < 0 || t[q].inst == t[0].inst);
+    return same;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int only_solveA) {
-    const Tile t = tiles[blockIdx.x];
-    const Inst& I = insts[t.inst];
-    // A of a kappa=inf instance does not change, unless fixed vortices add to it
-    if (only_solveA && !I.solveA && !I.vpi) return;
+__device__ __forceinline__ void link_U_nodes(const Inst& I, const int (&n)[kCallTiles], int nq) {
     const Geo g = I.g;
-    const int n = t.n0 + threadIdx.x;
-    if (n >= g.N) return;
-    const int i = n % g.Nx, j = n / g.Nx;
-    const unsigned cb = cell_bits(g, I.mt, i, j);
-    const unsigned rm0 = (GL_MM(cb) || GL_MP(cb)) ? 1u : 0u, rp0 = (GL_PM(cb) || GL_PP(cb)) ? 1u : 0u;
-    const unsigned r0m = (GL_MM(cb) || GL_PM(cb)) ? 1u : 0u, r0p = (GL_MP(cb) || GL_PP(cb)) ? 1u : 0u;
-    I.code[n] = (uint8_t)(rm0 | (rp0 << 1) | (r0m << 2) | (r0p << 3));
     const T* A = (const T*)I.ab[*(volatile int*)&I.st->rhsA];
     C2<T>* U = (C2<T>*)I.U;
-    const C2<T> z = cmk<T>(T(0), T(0));
     const T dt = gsel<T>(I.dt, I.fdt), sx = dt * GT(g, idx2), sy = dt * GT(g, idy2);
-    C2<T> ua = z, ub = z;
-    if (i < g.Nx - 1 && rp0) ua = cscale(sx, link_U<T>(GT(g, dx) * A[i + (g.Nx - 1) * j]));
-    if (j < g.Ny - 1 && r0p) ub = cscale(sy, link_U<T>(GT(g, dy) * A[g.Na + i + g.Nx * j]));
-    if constexpr (sizeof(T) == 4) {
-        ((float4*)U)[n] = make_float4(ua.x, ua.y, ub.x, ub.y);
+    unsigned cbq[kCallTiles];
+    T aa[kCallTiles], ab[kCallTiles];
+    // loads of all the thread's nodes first ...
+#pragma unroll
+    for (int q = 0; q < kCallTiles; ++q) {
+        cbq[q] = 0u;
+        aa[q] = T(0);
+        ab[q] = T(0);
+        if (q < nq && n[q] < g.N) {
+            const int i = n[q] % g.Nx, j = n[q] / g.Nx;
+            cbq[q] = cell_bits(g, I.mt, i, j);
+            if (i < g.Nx - 1) aa[q] = A[i + (g.Nx - 1) * j];
+            if (j < g.Ny - 1) ab[q] = A[g.Na + i + g.Nx * j];
+        }
+    }
+    // ... then the factors and the stores
+#pragma unroll
+    for (int q = 0; q < kCallTiles; ++q) {
+        if (q >= nq || n[q] >= g.N) continue;
+        const int i = n[q] % g.Nx, j = n[q] / g.Nx;
+        const unsigned cb = cbq[q];
+        const unsigned rm0 = (GL_MM(cb) || GL_MP(cb)) ? 1u : 0u, rp0 = (GL_PM(cb) || GL_PP(cb)) ? 1u : 0u;
+        const unsigned r0m = (GL_MM(cb) || GL_PM(cb)) ? 1u : 0u, r0p = (GL_MP(cb) || GL_PP(cb)) ? 1u : 0u;
+        I.code[n[q]] = (uint8_t)(rm0 | (rp0 << 1) | (r0m << 2) | (r0p << 3));
+        const C2<T> z = cmk<T>(T(0), T(0));
+        C2<T> ua = z, ub = z;
+        if (i < g.Nx - 1 && rp0) ua = cscale(sx, link_U<T>(GT(g, dx) * aa[q]));
+        if (j < g.Ny - 1 && r0p) ub = cscale(sy, link_U<T>(GT(g, dy) * ab[q]));
+        if constexpr (sizeof(T) == 4) {
+            ((float4*)U)[n[q]] = make_float4(ua.x, ua.y, ub.x, ub.y);
+        } else {
+            U[2 * n[q]] = ua;
+            U[2 * n[q] + 1] = ub;
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_link_U(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int ntiles, int only_solveA) {
+    Tile t[kCallTiles];
+    const bool same = call_tiles(tiles, ntiles, t);
+    auto skip = [&](const Inst& I) {
+        // A of a kappa=inf instance does not change, unless fixed vortices add to it
+        return only_solveA && !I.solveA && !I.vpi;
+    };
+    if (same) {
+        if (t[0].inst < 0) return;
+        const Inst& I = insts[t[0].inst];
+        if (skip(I)) return;
+        int n[kCallTiles];
+        int nq = 0;
+#pragma unroll
+        for (int q = 0; q < kCallTiles; ++q) {
+            n[q] = t[q].n0 + threadIdx.x;
+            if (t[q].inst >= 0) nq = q + 1;
+        }
+        link_U_nodes<T>(I, n, nq);
     } else {
-        U[2 * n] = ua;
-        U[2 * n + 1] = ub;
+        for (int q = 0; q < kCallTiles; ++q) {
+            if (t[q].inst < 0) break;
+            const Inst& I = insts[t[q].inst];
+            if (skip(I)) continue;
+            int n[kCallTiles] = {t[q].n0 + (int)threadIdx.x};
+            link_U_nodes<T>(I, n, 1);
+        }
     }
 }
 
@@ -1294,21 +1363,66 @@ __global__ void k_step_end(const Inst* __restrict__ insts, int ninst, LoopState*
     }
 }
 
-// After a TD call: move psi and A back into buffer 0.
+// After a TD call: move psi and A back into buffer 0 (kCallTiles tiles per CTA,
+// all of a thread's loads before its stores).
+template <typename T>
+__device__ __forceinline__ void canonical_nodes(const Inst& I, const int (&n)[kCallTiles], int nq) {
+    const Geo g = I.g;
+    const int R = *(volatile int*)&I.st->rhs, RA = *(volatile int*)&I.st->rhsA;
+    if (R != 0) {
+        const C2<T>* src = (const C2<T>*)I.psi[R];
+        C2<T>* dst = (C2<T>*)I.psi[0];
+        C2<T> v[kCallTiles];
+#pragma unroll
+        for (int q = 0; q < kCallTiles; ++q)
+            if (q < nq && n[q] < g.N) v[q] = src[n[q]];
+#pragma unroll
+        for (int q = 0; q < kCallTiles; ++q)
+            if (q < nq && n[q] < g.N) dst[n[q]] = v[q];
+    }
+    if (RA != 0) {
+        const T* src = (const T*)I.ab[RA];
+        T* dst = (T*)I.ab[0];
+        T va[kCallTiles], vb[kCallTiles];
+        int la[kCallTiles], lb[kCallTiles];
+#pragma unroll
+        for (int q = 0; q < kCallTiles; ++q) {
+            la[q] = -1;
+            lb[q] = -1;
+            if (q < nq && n[q] < g.N) {
+                const int i = n[q] % g.Nx, j = n[q] / g.Nx;
+                if (i < g.Nx - 1) { la[q] = i + (g.Nx - 1) * j; va[q] = src[la[q]]; }
+                if (j < g.Ny - 1) { lb[q] = g.Na + i + g.Nx * j; vb[q] = src[lb[q]]; }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kCallTiles; ++q) {
+            if (la[q] >= 0) dst[la[q]] = va[q];
+            if (lb[q] >= 0) dst[lb[q]] = vb[q];
+        }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_canonical_copy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles) {
-    const Tile t = tiles[blockIdx.x];
-    const Inst& I = insts[t.inst];
-    const Geo g = I.g;
-    const int n = t.n0 + threadIdx.x;
-    if (n >= g.N) return;
-    const int R = *(volatile int*)&I.st->rhs, RA = *(volatile int*)&I.st->rhsA;
-    if (R != 0) ((C2<T>*)I.psi[0])[n] = ((const C2<T>*)I.psi[R])[n];
-    if (RA != 0) {
-        const int i = n % g.Nx, j = n / g.Nx;
-        if (i < g.Nx - 1) { int na = i + (g.Nx - 1) * j; ((T*)I.ab[0])[na] = ((const T*)I.ab[RA])[na]; }
-        if (j < g.Ny - 1) { int nb = g.Na + i + g.Nx * j; ((T*)I.ab[0])[nb] = ((const T*)I.ab[RA])[nb]; }
+k_canonical_copy(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, int ntiles) {
+    Tile t[kCallTiles];
+    if (call_tiles(tiles, ntiles, t)) {
+        if (t[0].inst < 0) return;
+        int n[kCallTiles];
+        int nq = 0;
+#pragma unroll
+        for (int q = 0; q < kCallTiles; ++q) {
+            n[q] = t[q].n0 + threadIdx.x;
+            if (t[q].inst >= 0) nq = q + 1;
+        }
+        canonical_nodes<T>(insts[t[0].inst], n, nq);
+    } else {
+        for (int q = 0; q < kCallTiles; ++q) {
+            if (t[q].inst < 0) break;
+            int n[kCallTiles] = {t[q].n0 + (int)threadIdx.x};
+            canonical_nodes<T>(insts[t[q].inst], n, 1);
+        }
     }
 }
 
@@ -1426,7 +1540,7 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
     Tile const* tiles = L.tiles;
     Item const* items = L.items;
     LoopState* loop = L.loop;
-    int ninst = L.ninst, nitems = L.nitems;
+    int ninst = L.ninst, nitems = L.nitems, ntiles = L.ntiles;
     // appends a kernel node after `prev` in graph `g`
     auto chain = [&](cudaGraph_t g, void* fn, dim3 grid, dim3 block, void** a) -> cudaError_t {
         cudaError_t e = add_kernel(g, &nd, prev ? &prev : nullptr, prev ? 1 : 0, fn, grid, block, a);
@@ -1441,8 +1555,8 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         GCHK(chain(top, fv_psi_pre_fn(L.dtype), gt, bt, a));
     }
     if (do_psi) {
-        void* a[] = {&insts, &tiles, &zero};
-        GCHK(chain(top, link_fn(L.dtype), gt, bt, a));
+        void* a[] = {&insts, &tiles, &ntiles, &zero};
+        GCHK(chain(top, link_fn(L.dtype), dim3(call_grid(ntiles)), bt, a));
     }
     GCHK(add_while(top, &n_out, prev ? &prev : nullptr, prev ? 1 : 0, hout, &obody));
     prev = nullptr;
@@ -1453,8 +1567,8 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
             GCHK(chain(obody, fv_psi_pre_fn(L.dtype), gt, bt, a));
         }
         if (L.any_solveA || L.any_fv) {
-            void* a[] = {&insts, &tiles, &one};
-            GCHK(chain(obody, link_fn(L.dtype), gt, bt, a));
+            void* a[] = {&insts, &tiles, &ntiles, &one};
+            GCHK(chain(obody, link_fn(L.dtype), dim3(call_grid(ntiles)), bt, a));
         }
         {
             void* a[] = {&insts, &ninst, &loop, &hpsi, &one, &zero};
@@ -1519,9 +1633,9 @@ static cudaError_t build_td_graph(const TDLaunch& L, int eqn, cudaGraphExec_t* e
         GCHK(chain(obody, (void*)k_step_end, g1, b1, a));
     }
     {
-        void* a[] = {&insts, &tiles};
+        void* a[] = {&insts, &tiles, &ntiles};
         void* fn = L.dtype == 8 ? (void*)k_canonical_copy<double> : (void*)k_canonical_copy<float>;
-        GCHK(add_kernel(top, &n_cc, &n_out, 1, fn, gt, bt, a));
+        GCHK(add_kernel(top, &n_cc, &n_out, 1, fn, dim3(call_grid(ntiles)), bt, a));
         void* b[] = {&insts, &ninst};
         GCHK(add_kernel(top, &n_cr, &n_cc, 1, (void*)k_canonical_reset, g1, b1, b));
     }
@@ -1535,8 +1649,8 @@ fail:
 }
 
 static void launch_link_U(const TDLaunch& L, int only_solveA, cudaStream_t s) {
-    if (L.dtype == 8) k_link_U<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, only_solveA);
-    else k_link_U<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles, only_solveA);
+    if (L.dtype == 8) k_link_U<double><<<call_grid(L.ntiles), kThreads, 0, s>>>(L.insts, L.tiles, L.ntiles, only_solveA);
+    else k_link_U<float><<<call_grid(L.ntiles), kThreads, 0, s>>>(L.insts, L.tiles, L.ntiles, only_solveA);
 }
 
 // Host-driven fallback: the same kernels, the loop decided on the host after
@@ -1597,8 +1711,8 @@ static cudaError_t run_host_loop(const TDLaunch& L, int eqn, int Nt, cudaStream_
         }
         k_step_end<<<1, 32, 0, s>>>(L.insts, L.ninst, L.loop, none, 0);
     }
-    if (L.dtype == 8) k_canonical_copy<double><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
-    else k_canonical_copy<float><<<L.ntiles, kThreads, 0, s>>>(L.insts, L.tiles);
+    if (L.dtype == 8) k_canonical_copy<double><<<call_grid(L.ntiles), kThreads, 0, s>>>(L.insts, L.tiles, L.ntiles);
+    else k_canonical_copy<float><<<call_grid(L.ntiles), kThreads, 0, s>>>(L.insts, L.tiles, L.ntiles);
     k_canonical_reset<<<1, 32, 0, s>>>(L.insts, L.ninst);
     return cudaGetLastError();
 }
@@ -1667,8 +1781,8 @@ int time_sweeps(glgpu_handle* h, int which, int nrep, double* avg_ms) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaGraphConditionalHandle none = 0;
-    if (h->dtype == 8) k_link_U<double><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, 0);
-    else k_link_U<float><<<h->ntiles, kThreads, 0, h->stream>>>(h->inst, h->tiles, 0);
+    if (h->dtype == 8) k_link_U<double><<<call_grid(h->ntiles), kThreads, 0, h->stream>>>(h->inst, h->tiles, h->ntiles, 0);
+    else k_link_U<float><<<call_grid(h->ntiles), kThreads, 0, h->stream>>>(h->inst, h->tiles, h->ntiles, 0);
     double total = 0.0;
     // A sweeps come in pairs (sweep 0 computes the links' fixed parts, sweep 1 reuses
     // them), so an A repetition times both and the average is over sweeps
