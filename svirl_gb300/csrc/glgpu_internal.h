@@ -120,8 +120,18 @@ struct Tile {
     int inst, n0;
 };
 
-// A tile of the A sweep: kATX x kATY nodes of one instance from node (i0, j0).
-constexpr int kATX = 32, kATY = 32;
+// A tile of the A sweep: kATX x kATY nodes of one instance from node (i0, j0)
+// (a CTA of 256 threads covers 256 / kATX rows of the tile per pass).  64 x 32:
+// 0.084 ms per sweep at 2049^2 and kappa = 4; 32 x 32, 64 x 16 and 128 x 8 tiles
+// 0.090-0.091 ms, 32 x 64 and 128 x 16 0.084-0.085.
+#ifndef GLGPU_ATX
+#define GLGPU_ATX 64
+#endif
+#ifndef GLGPU_ATY
+#define GLGPU_ATY 32
+#endif
+constexpr int kATX = GLGPU_ATX, kATY = GLGPU_ATY;
+static_assert(256 % kATX == 0 && kATY % (256 / kATX) == 0, "A tile: whole rows per pass, whole passes per tile");
 struct ATile {
     int inst, i0, j0, pad;
 };

@@ -851,9 +851,9 @@ k_psi_sweep_cn(const Inst* __restrict__ insts, const Tile* __restrict__ tiles, L
 // of rows j0-1 .. j0+kATY-1 and columns i0-1 .. i0+kATX) into shared memory with
 // coalesced row loads; the twelve neighbour values of a node's two link updates
 // then come from shared memory.  One prologue, one block reduction and one set of
-// atomics per 1,024 nodes (per 256 they made each CTA's life a chain of dependent
-// loads and atomics; that version took 0.202 ms per sweep at 2049^2, 0.125 ms with
-// four tiles per CTA).  The arithmetic of a link is unchanged.
+// atomics per tile (2,048 nodes; per 256 they made each CTA's life a chain of
+// dependent loads and atomics; that version took 0.202 ms per sweep at 2049^2,
+// 0.125 ms with four 256-node tiles per CTA).  The arithmetic of a link is unchanged.
 // resident CTAs per SM asked of the compiler for the FP32 A sweep (caps its registers)
 #ifndef GLGPU_A_MINB
 #define GLGPU_A_MINB 8
