@@ -22,6 +22,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include "glgpu_bulk.cuh"
 #include "glgpu_internal.h"
@@ -926,25 +927,122 @@ k_A_sweep(const Inst* __restrict__ insts, const ATile* __restrict__ atiles, Loop
             T* Gc = Xc + g.Nab;
             T res = T(0);
             bool nan = false;
-            for (int q = 0; q < kATY / (kThreads / kATX); ++q) {
-                const int ti = t.i0 + (tid % kATX), tj = t.j0 + tid / kATX + (kThreads / kATX) * q;
-                const bool in = ti < g.Nx && tj < g.Ny;
-                const int n = in ? ti + g.Nx * tj : g.N;
-                T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
-                bool has_a = false, has_b = false;
-                int na = 0, nb = 0;
-                if constexpr (kDelta) {
-                    // The same Jacobi iteration as the FP64 branch, written for delta: with
-                    // A^(k) = A^(0) + delta^(k) the update of a link is
-                    //   delta' = (noise + dt rho (js + rh) + dt rho k2 (dd nbs(A^(0)) - 2 d^-2 A^(0))
-                    //            + dt rho k2 dd nbs(delta^(k))) / D,
-                    // and the stop rule's |A^(k+1) - A^(k)| = |delta^(k+1) - delta^(k)|.  In FP32 the
-                    // iterates of A itself differ by whole units in the last place once |A| > 8
-                    // (the Landau gauge reaches H L), which the absolute stop rule of 1e-6
-                    // (svirl/solvers/td.py:53-57) never accepts; delta is small, so the loop
-                    // converges.  The supercurrent phase is that of A^(0) + delta^(2 floor(k/2)).
-                    // The division by a link's constant diagonal is a multiplication by
-                    // its reciprocal here; FP64 divides as the reference does.
+            // the node loop compiled twice, for the sweeps that compute the fixed parts and
+            // for those that read them back, so that the second keeps only its own values
+            // in registers
+            auto sweep_nodes = [&](auto fresh_tag) {
+                constexpr bool kFresh = decltype(fresh_tag)::value;
+                for (int q = 0; q < kATY / (kThreads / kATX); ++q) {
+                    const int ti = t.i0 + (tid % kATX), tj = t.j0 + tid / kATX + (kThreads / kATX) * q;
+                    const bool in = ti < g.Nx && tj < g.Ny;
+                    const int n = in ? ti + g.Nx * tj : g.N;
+                    T va = T(0), vb = T(0), ca = T(0), cbv = T(0);
+                    bool has_a = false, has_b = false;
+                    int na = 0, nb = 0;
+                    if constexpr (kDelta) {
+                        // The same Jacobi iteration as the FP64 branch, written for delta: with
+                        // A^(k) = A^(0) + delta^(k) the update of a link is
+                        //   delta' = (noise + dt rho (js + rh) + dt rho k2 (dd nbs(A^(0)) - 2 d^-2 A^(0))
+                        //            + dt rho k2 dd nbs(delta^(k))) / D,
+                        // and the stop rule's |A^(k+1) - A^(k)| = |delta^(k+1) - delta^(k)|.  In FP32 the
+                        // iterates of A itself differ by whole units in the last place once |A| > 8
+                        // (the Landau gauge reaches H L), which the absolute stop rule of 1e-6
+                        // (svirl/solvers/td.py:53-57) never accepts; delta is small, so the loop
+                        // converges.  The supercurrent phase is that of A^(0) + delta^(2 floor(k/2)).
+                        // The division by a link's constant diagonal is a multiplication by
+                        // its reciprocal here; FP64 divides as the reference does.
+                        if (n < g.N) {
+                            const int i = ti, j = tj;
+                            const int Nxa = g.Nx - 1, Na = g.Na;
+                            has_a = i < g.Nx - 1;
+                            has_b = j < g.Ny - 1;
+                            na = i + Nxa * j;
+                            nb = Na + i + g.Nx * j;
+                            auto dlx = [&](int ii, int jj) -> T { return cur ? cx(ii, jj) : T(0); };
+                            auto dly = [&](int ii, int jj) -> T { return cur ? cy(ii, jj) : T(0); };
+                            const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
+                            const T k2 = I.fkappa2;
+                            const T dt_rho_k2 = I.fdt * I.frho * k2;
+                            T xa = T(0), xb = T(0);
+                            if constexpr (kFresh) {
+                                const T* al = (I.vpi || k < 2) ? nullptr : (const T*)I.ab[(R + 2) % 3];  // delta of the phase
+                                const T ph_a = has_a ? (I.vpi ? abi[na] : rhs[na] + (al ? al[na] : T(0))) : T(0);
+                                const T ph_b = has_b ? (I.vpi ? abi[nb] : rhs[nb] + (al ? al[nb] : T(0))) : T(0);
+                                const unsigned cb = cell_bits(g, I.mt, i, j);
+                                const C2<T> psi0 = psi[n];
+                                const T dx = GT(g, dx), dy = GT(g, dy);
+                                const T idx = GT(g, idx), idy = GT(g, idy);
+                                const T H = I.fH;
+                                const T dt_rho = I.fdt * I.frho;
+                                const T lc = I.flang_A;
+                                const bool lang = I.lang_A_on != 0;
+                                if (has_a) {
+                                    const T noise = lang ? lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5)) : T(0);
+                                    T rh = T(0), dd = T(1);
+                                    if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
+                                    else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
+                                    T jl = T(0);
+                                    if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
+                                    T ga;
+                                    if (k == 0) {
+                                        T nr = T(0);
+                                        if (j > 0)
+                                            nr += idy2 * rhs[i + Nxa * (j - 1)] - idxy * rhs[Na + i + g.Nx * (j - 1)] +
+                                                  idxy * rhs[Na + i + 1 + g.Nx * (j - 1)];
+                                        if (j < g.Ny - 1)
+                                            nr += idy2 * rhs[i + Nxa * (j + 1)] + idxy * rhs[Na + i + g.Nx * j] - idxy * rhs[Na + i + 1 + g.Nx * j];
+                                        ga = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idy2 * rhs[na]);
+                                        Gc[na] = ga;
+                                    } else {
+                                        ga = Gc[na];
+                                    }
+                                    xa = noise + dt_rho * (jl + rh) + ga;
+                                    Xc[na] = xa;
+                                }
+                                if (has_b) {
+                                    const T noise = lang ? lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5)) : T(0);
+                                    T rh = T(0), dd = T(1);
+                                    if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
+                                    else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
+                                    T jl = T(0);
+                                    if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
+                                    T gb;
+                                    if (k == 0) {
+                                        T nr = T(0);
+                                        if (i > 0)
+                                            nr += idx2 * rhs[Na + (i - 1) + g.Nx * j] - idxy * rhs[(i - 1) + Nxa * j] + idxy * rhs[(i - 1) + Nxa * (j + 1)];
+                                        if (i < g.Nx - 1)
+                                            nr += idx2 * rhs[Na + (i + 1) + g.Nx * j] + idxy * rhs[i + Nxa * j] - idxy * rhs[i + Nxa * (j + 1)];
+                                        gb = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idx2 * rhs[nb]);
+                                        Gc[nb] = gb;
+                                    } else {
+                                        gb = Gc[nb];
+                                    }
+                                    xb = noise + dt_rho * (jl + rh) + gb;
+                                    Xc[nb] = xb;
+                                }
+                            } else {
+                                if (has_a) xa = Xc[na];
+                                if (has_b) xb = Xc[nb];
+                            }
+                            if (has_a) {
+                                const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
+                                T nd = T(0);
+                                if (j > 0) nd += idy2 * dlx(i, j - 1) - idxy * dly(i, j - 1) + idxy * dly(i + 1, j - 1);
+                                if (j < g.Ny - 1) nd += idy2 * dlx(i, j + 1) + idxy * dly(i, j) - idxy * dly(i + 1, j);
+                                va = (xa + dt_rho_k2 * dd * nd) * (T(1) / (T(1) + T(2) * dt_rho_k2 * idy2));
+                                ca = dlx(i, j);
+                            }
+                            if (has_b) {
+                                const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
+                                T nd = T(0);
+                                if (i > 0) nd += idx2 * dly(i - 1, j) - idxy * dlx(i - 1, j) + idxy * dlx(i - 1, j + 1);
+                                if (i < g.Nx - 1) nd += idx2 * dly(i + 1, j) + idxy * dlx(i, j) - idxy * dlx(i, j + 1);
+                                vb = (xb + dt_rho_k2 * dd * nd) * (T(1) / (T(1) + T(2) * dt_rho_k2 * idx2));
+                                cbv = dly(i, j);
+                            }
+                        }
+                    } else
                     if (n < g.N) {
                         const int i = ti, j = tj;
                         const int Nxa = g.Nx - 1, Na = g.Na;
@@ -952,67 +1050,42 @@ k_A_sweep(const Inst* __restrict__ insts, const ATile* __restrict__ atiles, Loop
                         has_b = j < g.Ny - 1;
                         na = i + Nxa * j;
                         nb = Na + i + g.Nx * j;
-                        auto dlx = [&](int ii, int jj) -> T { return cur ? cx(ii, jj) : T(0); };
-                        auto dly = [&](int ii, int jj) -> T { return cur ? cy(ii, jj) : T(0); };
                         const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
-                        const T k2 = I.fkappa2;
-                        const T dt_rho_k2 = I.fdt * I.frho * k2;
+                        const T k2 = gsel<T>(I.kappa2, I.fkappa2);
+                        const T dt_rho = gsel<T>(I.dt, I.fdt) * gsel<T>(I.rho, I.frho);
+                        const T dt_rho_k2 = dt_rho * k2;
                         T xa = T(0), xb = T(0);
-                        if (fresh) {
-                            const T* al = (I.vpi || k < 2) ? nullptr : (const T*)I.ab[(R + 2) % 3];  // delta of the phase
-                            const T ph_a = has_a ? (I.vpi ? abi[na] : rhs[na] + (al ? al[na] : T(0))) : T(0);
-                            const T ph_b = has_b ? (I.vpi ? abi[nb] : rhs[nb] + (al ? al[nb] : T(0))) : T(0);
+                        if constexpr (kFresh) {
+                            // read the supercurrent phases before anything is stored (aliasing, see top)
+                            const T ph_a = has_a ? abi[na] : T(0);
+                            const T ph_b = has_b ? abi[nb] : T(0);
                             const unsigned cb = cell_bits(g, I.mt, i, j);
                             const C2<T> psi0 = psi[n];
                             const T dx = GT(g, dx), dy = GT(g, dy);
                             const T idx = GT(g, idx), idy = GT(g, idy);
-                            const T H = I.fH;
-                            const T dt_rho = I.fdt * I.frho;
-                            const T lc = I.flang_A;
+                            const T H = gsel<T>(I.H, I.fH);
+                            const T lc = gsel<T>(I.lang_A, I.flang_A);
                             const bool lang = I.lang_A_on != 0;
                             if (has_a) {
-                                const T noise = lang ? lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5)) : T(0);
-                                T rh = T(0), dd = T(1);
-                                if (j == 0) { rh = T(2) * k2 * H * idy; dd = T(2); }
-                                else if (j == g.Ny - 1) { rh = -T(2) * k2 * H * idy; dd = T(2); }
+                                T r = rhs[na];
+                                if (lang) r += lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5));
+                                T rh = T(0);
+                                if (j == 0) rh = T(2) * k2 * H * idy;
+                                else if (j == g.Ny - 1) rh = -T(2) * k2 * H * idy;
                                 T jl = T(0);
                                 if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
-                                T ga;
-                                if (k == 0) {
-                                    T nr = T(0);
-                                    if (j > 0)
-                                        nr += idy2 * rhs[i + Nxa * (j - 1)] - idxy * rhs[Na + i + g.Nx * (j - 1)] +
-                                              idxy * rhs[Na + i + 1 + g.Nx * (j - 1)];
-                                    if (j < g.Ny - 1)
-                                        nr += idy2 * rhs[i + Nxa * (j + 1)] + idxy * rhs[Na + i + g.Nx * j] - idxy * rhs[Na + i + 1 + g.Nx * j];
-                                    ga = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idy2 * rhs[na]);
-                                    Gc[na] = ga;
-                                } else {
-                                    ga = Gc[na];
-                                }
-                                xa = noise + dt_rho * (jl + rh) + ga;
+                                xa = r + dt_rho * (jl + rh);
                                 Xc[na] = xa;
                             }
                             if (has_b) {
-                                const T noise = lang ? lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5)) : T(0);
-                                T rh = T(0), dd = T(1);
-                                if (i == 0) { rh = -T(2) * k2 * H * idx; dd = T(2); }
-                                else if (i == g.Nx - 1) { rh = T(2) * k2 * H * idx; dd = T(2); }
+                                T r = rhs[nb];
+                                if (lang) r += lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5));
+                                T rh = T(0);
+                                if (i == 0) rh = -T(2) * k2 * H * idx;
+                                else if (i == g.Nx - 1) rh = T(2) * k2 * H * idx;
                                 T jl = T(0);
                                 if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
-                                T gb;
-                                if (k == 0) {
-                                    T nr = T(0);
-                                    if (i > 0)
-                                        nr += idx2 * rhs[Na + (i - 1) + g.Nx * j] - idxy * rhs[(i - 1) + Nxa * j] + idxy * rhs[(i - 1) + Nxa * (j + 1)];
-                                    if (i < g.Nx - 1)
-                                        nr += idx2 * rhs[Na + (i + 1) + g.Nx * j] + idxy * rhs[i + Nxa * j] - idxy * rhs[i + Nxa * (j + 1)];
-                                    gb = mul_rn<T>(dt_rho_k2, dd * nr - T(2) * idx2 * rhs[nb]);
-                                    Gc[nb] = gb;
-                                } else {
-                                    gb = Gc[nb];
-                                }
-                                xb = noise + dt_rho * (jl + rh) + gb;
+                                xb = r + dt_rho * (jl + rh);
                                 Xc[nb] = xb;
                             }
                         } else {
@@ -1021,101 +1094,37 @@ k_A_sweep(const Inst* __restrict__ insts, const ATile* __restrict__ atiles, Loop
                         }
                         if (has_a) {
                             const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
-                            T nd = T(0);
-                            if (j > 0) nd += idy2 * dlx(i, j - 1) - idxy * dly(i, j - 1) + idxy * dly(i + 1, j - 1);
-                            if (j < g.Ny - 1) nd += idy2 * dlx(i, j + 1) + idxy * dly(i, j) - idxy * dly(i + 1, j);
-                            va = (xa + dt_rho_k2 * dd * nd) * (T(1) / (T(1) + T(2) * dt_rho_k2 * idy2));
-                            ca = dlx(i, j);
+                            T nbs = T(0);
+                            if (j > 0) nbs += idy2 * cx(i, j - 1) - idxy * cy(i, j - 1) + idxy * cy(i + 1, j - 1);
+                            if (j < g.Ny - 1) nbs += idy2 * cx(i, j + 1) + idxy * cy(i, j) - idxy * cy(i + 1, j);
+                            va = (xa + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idy2);
+                            ca = cx(i, j);
                         }
                         if (has_b) {
                             const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
-                            T nd = T(0);
-                            if (i > 0) nd += idx2 * dly(i - 1, j) - idxy * dlx(i - 1, j) + idxy * dlx(i - 1, j + 1);
-                            if (i < g.Nx - 1) nd += idx2 * dly(i + 1, j) + idxy * dlx(i, j) - idxy * dlx(i, j + 1);
-                            vb = (xb + dt_rho_k2 * dd * nd) * (T(1) / (T(1) + T(2) * dt_rho_k2 * idx2));
-                            cbv = dly(i, j);
+                            T nbs = T(0);
+                            if (i > 0) nbs += idx2 * cy(i - 1, j) - idxy * cx(i - 1, j) + idxy * cx(i - 1, j + 1);
+                            if (i < g.Nx - 1) nbs += idx2 * cy(i + 1, j) + idxy * cx(i, j) - idxy * cx(i, j + 1);
+                            vb = (xb + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idx2);
+                            cbv = cy(i, j);
                         }
                     }
-                } else
-                if (n < g.N) {
-                    const int i = ti, j = tj;
-                    const int Nxa = g.Nx - 1, Na = g.Na;
-                    has_a = i < g.Nx - 1;
-                    has_b = j < g.Ny - 1;
-                    na = i + Nxa * j;
-                    nb = Na + i + g.Nx * j;
-                    const T idx2 = GT(g, idx2), idy2 = GT(g, idy2), idxy = GT(g, idxy);
-                    const T k2 = gsel<T>(I.kappa2, I.fkappa2);
-                    const T dt_rho = gsel<T>(I.dt, I.fdt) * gsel<T>(I.rho, I.frho);
-                    const T dt_rho_k2 = dt_rho * k2;
-                    T xa = T(0), xb = T(0);
-                    if (fresh) {
-                        // read the supercurrent phases before anything is stored (aliasing, see top)
-                        const T ph_a = has_a ? abi[na] : T(0);
-                        const T ph_b = has_b ? abi[nb] : T(0);
-                        const unsigned cb = cell_bits(g, I.mt, i, j);
-                        const C2<T> psi0 = psi[n];
-                        const T dx = GT(g, dx), dy = GT(g, dy);
-                        const T idx = GT(g, idx), idy = GT(g, idy);
-                        const T H = gsel<T>(I.H, I.fH);
-                        const T lc = gsel<T>(I.lang_A, I.flang_A);
-                        const bool lang = I.lang_A_on != 0;
+                    if (n < g.N) {
                         if (has_a) {
-                            T r = rhs[na];
-                            if (lang) r += lc * (rand_1<T>((uint32_t)na, s_rt) - T(0.5));
-                            T rh = T(0);
-                            if (j == 0) rh = T(2) * k2 * H * idy;
-                            else if (j == g.Ny - 1) rh = -T(2) * k2 * H * idy;
-                            T jl = T(0);
-                            if (GL_PM(cb) || GL_PP(cb)) jl = idx * js_of<T>(psi0, dx * ph_a, psi[n + 1]);
-                            xa = r + dt_rho * (jl + rh);
-                            Xc[na] = xa;
+                            nxt[na] = va;
+                            T d = fabs(va - ca);
+                            if (d == d) { if (d > res) res = d; } else nan = true;
                         }
                         if (has_b) {
-                            T r = rhs[nb];
-                            if (lang) r += lc * (rand_2<T>((uint32_t)nb, s_rt) - T(0.5));
-                            T rh = T(0);
-                            if (i == 0) rh = -T(2) * k2 * H * idx;
-                            else if (i == g.Nx - 1) rh = T(2) * k2 * H * idx;
-                            T jl = T(0);
-                            if (GL_MP(cb) || GL_PP(cb)) jl = idy * js_of<T>(psi0, dy * ph_b, psi[n + g.Nx]);
-                            xb = r + dt_rho * (jl + rh);
-                            Xc[nb] = xb;
+                            nxt[nb] = vb;
+                            T d = fabs(vb - cbv);
+                            if (d == d) { if (d > res) res = d; } else nan = true;
                         }
-                    } else {
-                        if (has_a) xa = Xc[na];
-                        if (has_b) xb = Xc[nb];
-                    }
-                    if (has_a) {
-                        const T dd = (j == 0 || j == g.Ny - 1) ? T(2) : T(1);
-                        T nbs = T(0);
-                        if (j > 0) nbs += idy2 * cx(i, j - 1) - idxy * cy(i, j - 1) + idxy * cy(i + 1, j - 1);
-                        if (j < g.Ny - 1) nbs += idy2 * cx(i, j + 1) + idxy * cy(i, j) - idxy * cy(i + 1, j);
-                        va = (xa + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idy2);
-                        ca = cx(i, j);
-                    }
-                    if (has_b) {
-                        const T dd = (i == 0 || i == g.Nx - 1) ? T(2) : T(1);
-                        T nbs = T(0);
-                        if (i > 0) nbs += idx2 * cy(i - 1, j) - idxy * cx(i - 1, j) + idxy * cx(i - 1, j + 1);
-                        if (i < g.Nx - 1) nbs += idx2 * cy(i + 1, j) + idxy * cx(i, j) - idxy * cx(i, j + 1);
-                        vb = (xb + dt_rho_k2 * dd * nbs) / (T(1) + T(2) * dt_rho_k2 * idx2);
-                        cbv = cy(i, j);
                     }
                 }
-                if (n < g.N) {
-                    if (has_a) {
-                        nxt[na] = va;
-                        T d = fabs(va - ca);
-                        if (d == d) { if (d > res) res = d; } else nan = true;
-                    }
-                    if (has_b) {
-                        nxt[nb] = vb;
-                        T d = fabs(vb - cbv);
-                        if (d == d) { if (d > res) res = d; } else nan = true;
-                    }
-                }
-            }
+            };
+            if (fresh) sweep_nodes(std::true_type{});
+            else sweep_nodes(std::false_type{});
             T bmax = block_max_res<T>(res, nan);
             if (tid == 0) {
                 if (bmax < T(0)) {
