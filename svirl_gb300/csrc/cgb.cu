@@ -22,6 +22,7 @@
 // A call starts from a zero direction and beta = 0.
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "glgpu_internal.h"
 #include "glgpu_phys.cuh"
@@ -308,7 +309,7 @@ __device__ __forceinline__ void step_prefetch(const Inst& I, const Geo& g, int n
 }
 
 // gradient (new buffer), Polak-Ribiere sums and |g|^2 of one tile
-template <typename T>
+template <typename T, bool SA>
 __device__ __forceinline__ void grad_tile(const Inst& I, int n0, int rep, const C2<T>* __restrict__ psi,
                                           const T* __restrict__ ab, const T* __restrict__ abei,
                                           const C2<T>* __restrict__ U, C2<T>* __restrict__ G,
@@ -333,7 +334,7 @@ __device__ __forceinline__ void grad_tile(const Inst& I, int n0, int rep, const 
             T ga[2] = {T(0), T(0)};
             const bool has[2] = {i < g.Nx - 1, j < g.Ny - 1};
             const int l[2] = {i + (g.Nx - 1) * j, g.Na + i + g.Nx * j};
-            if (I.solveA) {
+            if (SA) {
 #pragma unroll
                 for (int dir = 0; dir < 2; ++dir) {
                     if (!has[dir]) continue;
@@ -345,7 +346,7 @@ __device__ __forceinline__ void grad_tile(const Inst& I, int n0, int rep, const 
                 }
             }
             G[n] = gv;
-            if (I.solveA)
+            if (SA)
 #pragma unroll
                 for (int dir = 0; dir < 2; ++dir)
                     if (has[dir]) GA[l[dir]] = ga[dir];
@@ -362,9 +363,13 @@ kb_grad(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double
     if (*(volatile const int*)&cs->done) return;
     const int gi = cs->gi, pi = cs->pi;
     T v[5] = {T(0), T(0), T(0), T(0), T(0)};
-    grad_tile<T>(I, t.n0, t.rep, (const C2<T>*)I.psi[pi], (const T*)I.ab[I.solveA ? pi : 0], (const T*)I.abei,
-                 (const C2<T>*)I.U, (C2<T>*)I.gpsi[1 - gi], (const C2<T>*)I.gpsi[gi], (T*)I.gA[1 - gi],
-                 (const T*)I.gA[gi], v);
+    auto run = [&](auto sa) {
+        grad_tile<T, decltype(sa)::value>(I, t.n0, t.rep, (const C2<T>*)I.psi[pi], (const T*)I.ab[I.solveA ? pi : 0],
+                                          (const T*)I.abei, (const C2<T>*)I.U, (C2<T>*)I.gpsi[1 - gi],
+                                          (const C2<T>*)I.gpsi[gi], (T*)I.gA[1 - gi], (const T*)I.gA[gi], v);
+    };
+    if (I.solveA) run(std::true_type{});
+    else run(std::false_type{});
     double vs[5];
     block_sum<5>(v, vs);
     if (threadIdx.x == 0) store_partials<T>(vs, 5, partials + (size_t)blockIdx.x * kPart);
@@ -586,7 +591,7 @@ __device__ __noinline__ void inst_alpha(const Inst& I, CGState* cs, const double
 }
 
 // new direction (written) and the line-search coefficients of one tile
-template <typename T>
+template <typename T, bool SA>
 __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, int rep, T bp, T bA, const C2<T>* __restrict__ psi,
                                               const T* __restrict__ ab, const T* __restrict__ abei,
                                               const C2<T>* __restrict__ U, const C2<T>* __restrict__ G,
@@ -610,7 +615,7 @@ __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, int rep, T 
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
             const unsigned cb = I.cbits[n];
-            if (I.solveA) {
+            if (SA) {
                 coef_node<T, 17>(g, gsel<T>(I.kappa2, I.fkappa2), eps0, (const T*)I.eps_sp, H, psi_at, phase, ab, lk,
                                  n, i, j, cb, dpsi, dA, c);
             } else {
@@ -620,7 +625,7 @@ __device__ __forceinline__ void dir_coef_tile(const Inst& I, int n0, int rep, T 
                 c[0] += c5[0]; c[5] += c5[1]; c[10] += c5[2]; c[15] += c5[3]; c[16] += c5[4];
             }
             dN[n] = dpsi(n);
-            if (I.solveA) {
+            if (SA) {
                 if (i < g.Nx - 1) { const int na = i + (g.Nx - 1) * j; dAN[na] = dA(na); }
                 if (j < g.Ny - 1) { const int nb = g.Na + i + g.Nx * j; dAN[nb] = dA(nb); }
             }
@@ -640,10 +645,14 @@ kb_dir_coef(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, do
     T c[17];
 #pragma unroll
     for (int k = 0; k < 17; ++k) c[k] = T(0);
-    dir_coef_tile<T>(I, t.n0, t.rep, (T)cs->beta_psi, (T)cs->beta_A, (const C2<T>*)I.psi[pi],
-                     (const T*)I.ab[I.solveA ? pi : 0], (const T*)I.abei, (const C2<T>*)I.U,
-                     (const C2<T>*)I.gpsi[gi], (const T*)I.gA[gi], (const C2<T>*)I.dpsi[di], (const T*)I.dA[di],
-                     (C2<T>*)I.dpsi[1 - di], (T*)I.dA[1 - di], c);
+    auto run = [&](auto sa) {
+        dir_coef_tile<T, decltype(sa)::value>(I, t.n0, t.rep, (T)cs->beta_psi, (T)cs->beta_A, (const C2<T>*)I.psi[pi],
+                                              (const T*)I.ab[I.solveA ? pi : 0], (const T*)I.abei, (const C2<T>*)I.U,
+                                              (const C2<T>*)I.gpsi[gi], (const T*)I.gA[gi], (const C2<T>*)I.dpsi[di],
+                                              (const T*)I.dA[di], (C2<T>*)I.dpsi[1 - di], (T*)I.dA[1 - di], c);
+    };
+    if (I.solveA) run(std::true_type{});
+    else run(std::false_type{});
     double cs17[17];
     block_sum<17>(c, cs17);
     if (threadIdx.x == 0) store_partials<T>(cs17, 17, partials + (size_t)blockIdx.x * kPart);
@@ -689,7 +698,7 @@ __device__ __noinline__ void inst_energy_stop(const Inst& I, CGState* cs, const 
 }
 
 // step and energy of the new state of one tile
-template <typename T>
+template <typename T, bool SA>
 __device__ __forceinline__ void step_tile(const Inst& I, int n0, int rep, T ap, T aA, const C2<T>* __restrict__ psi,
                                           C2<T>* __restrict__ psiN, const C2<T>* __restrict__ dpsi,
                                           const T* __restrict__ ab, T* __restrict__ abN, const T* __restrict__ dA,
@@ -712,7 +721,7 @@ __device__ __forceinline__ void step_tile(const Inst& I, int n0, int rep, T ap, 
         cg_prefetch_ahead(r, rep, [&](int q) { step_prefetch<T>(I, g, n0 + threadIdx.x + q * kThreads, psi, dpsi, ab, dA); });
         if (n < g.N) {
             const int i = n % g.Nx, j = n / g.Nx;
-            if (I.solveA) {
+            if (SA) {
                 if (i < g.Nx - 1) {
                     const int na = i + (g.Nx - 1) * j;
                     const T a = ab_new(na);
@@ -728,7 +737,7 @@ __device__ __forceinline__ void step_tile(const Inst& I, int n0, int rep, T ap, 
             }
             // the node's own links' factors were written above by this thread
             v[0] += energy_density_f<T>(g, k2, eps0, (const T*)I.eps_sp, H, (unsigned)I.cbits[n], psi_new, abei,
-                                        I.solveA != 0, ab_new, lk, n, i, j);
+                                        SA, ab_new, lk, n, i, j);
             psiN[n] = psi_new(n);
         }
     }
@@ -754,9 +763,14 @@ kb_step(const Inst* __restrict__ insts, const CGTile* __restrict__ tiles, double
     if (!*(volatile const int*)&cs->done) {
         const int pi = cs->pi, di = cs->di;
         T v[1] = {T(0)};
-        step_tile<T>(I, t.n0, t.rep, (T)cs->alpha_psi, (T)cs->alpha_A, (const C2<T>*)I.psi[pi], (C2<T>*)I.psi[1 - pi],
-                     (const C2<T>*)I.dpsi[di], (const T*)I.ab[I.solveA ? pi : 0], I.solveA ? (T*)I.ab[1 - pi] : nullptr,
-                     (const T*)I.dA[di], (const T*)I.abei, (C2<T>*)I.U, v);
+        auto run = [&](auto sa) {
+            step_tile<T, decltype(sa)::value>(I, t.n0, t.rep, (T)cs->alpha_psi, (T)cs->alpha_A, (const C2<T>*)I.psi[pi],
+                                              (C2<T>*)I.psi[1 - pi], (const C2<T>*)I.dpsi[di],
+                                              (const T*)I.ab[I.solveA ? pi : 0], I.solveA ? (T*)I.ab[1 - pi] : nullptr,
+                                              (const T*)I.dA[di], (const T*)I.abei, (C2<T>*)I.U, v);
+        };
+        if (I.solveA) run(std::true_type{});
+        else run(std::false_type{});
         double vs[1];
         block_sum<1>(v, vs);
         if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kPart] = vs[0];
