@@ -51,13 +51,18 @@ static int cg_rep_of(int N) {
         if ((N + kThreads * r - 1) / (kThreads * r) >= kCGMinTiles) return r;
     return 2;
 }
-// Resident CTAs per SM asked of the compiler for the two stencil-heavy FP32 CG
-// kernels (caps their registers at 65536 / (kThreads * minimum CTAs)), per kernel.
+// Resident CTAs per SM asked of the compiler for the FP32 CG kernels (caps their
+// registers at 65536 / (kThreads * minimum CTAs)), per kernel.  Measured on the
+// 64-instance field sweep (ms per iteration, grad / coef / step caps; one box):
+// 5/4/4 0.694, 4/4/4 0.702 (the step kernel fits 64 registers without spilling),
+// 6/4/4 0.702, 5/3/4 0.710, 4/4/1 0.715; on another box 4/4/1 0.708, 5/4/1 0.701,
+// 4/4/3 0.715, 5/5/1 0.724; earlier 6/6, 8/4, 4/8 and 8/8 0.79-1.09, 3/3 and 2/2
+// 0.82-0.94.
 #ifndef GLGPU_CG_MINB
 #define GLGPU_CG_MINB 4
 #endif
 #ifndef GLGPU_CG_MINB_GRAD
-#define GLGPU_CG_MINB_GRAD GLGPU_CG_MINB
+#define GLGPU_CG_MINB_GRAD 5
 #endif
 #ifndef GLGPU_CG_MINB_COEF
 #define GLGPU_CG_MINB_COEF GLGPU_CG_MINB
@@ -751,7 +756,7 @@ __device__ __forceinline__ void step_tile(const Inst& I, int n0, int rep, T ap, 
 // last CTA of the launch counts the active instances and sets the WHILE
 // condition.
 #ifndef GLGPU_CG_MINB_STEP
-#define GLGPU_CG_MINB_STEP 1
+#define GLGPU_CG_MINB_STEP 4
 #endif
 template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? GLGPU_CG_MINB_STEP : 1)
