@@ -1145,13 +1145,6 @@ k_A_sweep(const Inst* __restrict__ insts, const ATile* __restrict__ atiles, Loop
     }
 }
 
-// Per-step tables of the psi Jacobi loop, during which A is fixed: the link
-// factors U = exp(-i d a) of the current A times dt/d^2 (0 on links whose
-// weight is 0), stored per node as the pair (x link, y link) that starts there,
-// so a lane loads both with one 16-byte load (the CG fills the same buffer with
-// its own unscaled factors in link order before each run), and per node the Winecki-Adams
-// link weights as a bit code (bit 0: left link r_m0, 1: right r_p0, 2: lower
-// r_0m, 3: upper r_0p; a node is updated iff it has a left or a right link).
 // Tiles per CTA of the per-call kernels k_link_U and k_canonical_copy.  With one
 // 256-node tile per CTA (16,401 CTAs at 2049^2) each CTA's life is a chain of
 // dependent loads (tile, instance, state word, data) and the launch is bound by
@@ -1176,6 +1169,13 @@ __device__ __forceinline__ bool call_tiles(const Tile* __restrict__ tiles, int n
     return same;
 }
 
+// Per-step tables of the psi Jacobi loop, during which A is fixed: the link
+// factors U = exp(-i d a) of the current A times dt/d^2 (0 on links whose
+// weight is 0), stored per node as the pair (x link, y link) that starts there,
+// so a lane loads both with one 16-byte load (the CG fills the same buffer with
+// its own unscaled factors in link order before each run), and per node the Winecki-Adams
+// link weights as a bit code (bit 0: left link r_m0, 1: right r_p0, 2: lower
+// r_0m, 3: upper r_0p; a node is updated iff it has a left or a right link).
 template <typename T>
 __device__ __forceinline__ void link_U_nodes(const Inst& I, const int (&n)[kCallTiles], int nq) {
     const Geo g = I.g;
