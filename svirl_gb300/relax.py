@@ -75,6 +75,31 @@ def relax(insts, cache, dtype=np.float32, starts=None, n_iter=4000, gtol=1e-4, g
             cache.put(h)
 
 
+def polish_fp64(insts, states, cache, n_iter, gtol, window=0, window_tol=0.0):
+    """Finish FP32-relaxed states in float64: each (psi, ab) state goes into a
+    float64 handle and one batched device CG (exact-boundary gradient, absolute
+    gradient tolerance gtol, at most n_iter iterations) runs from it.  A state
+    stored in FP32 cannot meet an absolute gradient tolerance below the gradient
+    of its own rounding; the FP64 iterations remove that.  Returns (cg dict with
+    'ms', [(psi, ab)] in float64)."""
+    hs = [cache.get(it.n, np.float64) for it in insts]
+    try:
+        for it, h, (psi, ab) in zip(insts, hs, states):
+            it.load_into(h, psi=np.asarray(psi, np.complex128), ab=np.asarray(ab, np.float64))
+        batch = HandleBatch(hs)
+        try:
+            if window > 0:
+                batch.set_cg_window(window, window_tol)
+            out = batch.cg_device(n_iter=n_iter, rtol=0.0, gtol=gtol, exact_boundary=True, gtol_abs=True,
+                                  timed=True)
+        finally:
+            batch.close()
+        return out, [(h.get_psi(), h.get_ab()) for h in hs]
+    finally:
+        for h in hs:
+            cache.put(h)
+
+
 def energies_fp64(insts, states, cache):
     """Free energy of each (psi, ab) state evaluated in float64."""
     E = np.empty(len(insts))
@@ -86,3 +111,24 @@ def energies_fp64(insts, states, cache):
         finally:
             cache.put(h)
     return E
+
+
+def gradient_ok_fp64(insts, states, cache, gtol):
+    """Whether each (psi, ab) state meets the device CG's absolute gradient
+    tolerance |grad F| <= gtol (exact-boundary gradient), evaluated in float64:
+    the state is loaded into a float64 handle and a one-iteration CG stops at
+    iteration 0 with status 1 exactly when the tolerance holds."""
+    ok = np.zeros(len(insts), dtype=bool)
+    for q, (it, (psi, ab)) in enumerate(zip(insts, states)):
+        h = cache.get(it.n, np.float64)
+        try:
+            it.load_into(h, psi=np.asarray(psi, np.complex128), ab=np.asarray(ab, np.float64))
+            b = HandleBatch([h])
+            try:
+                out = b.cg_device(n_iter=1, rtol=0.0, gtol=gtol, exact_boundary=True, gtol_abs=True)
+            finally:
+                b.close()
+            ok[q] = int(out["status"][0]) == 1 and int(out["iters"][0]) == 0
+        finally:
+            cache.put(h)
+    return ok
